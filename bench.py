@@ -1,0 +1,424 @@
+"""Benchmark: DyCuckoo find on a large static table (one GB300).
+
+Workload (the large static table of the measurement plan): a 4-subtable
+table of uint32 keys / uint32 values holding 2^28 unique keys at load factor
+0.90 (about 2.4 GB); find batches of 2^26 keys. One step = one find batch
+(one kernel). The headline line is the uniform, 100%-hit mix; the other
+three mixes (uniform 10% hit, Zipf(0.99) 100% and 10% hit) are reported under
+"variants". Inputs (table 2.4 GB, batch 256 MB) are larger than the 129 MB
+L2, so no flush runs between steps.
+
+Keys are synthetic and seeded: key(i) = P(i) for a fixed bijection P of the
+32-bit integers (multiply-xorshift rounds), so inserted keys (i < 2^28) and
+miss keys (i >= 2^28) are disjoint by construction; 0 and 2^32-1 are
+excluded. Zipf ranks use the continuous inverse-CDF approximation.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--log2-keys 28] [--log2-batch 26] [--skip-cpu]
+
+--impl reference times the reference's algorithm on the host cores (the
+oracle's restatement of GPU/dyhash: 16-slot buckets, the reference's hash
+functions and eviction rule), the only CPU form the reference's path has.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+M32 = 0xFFFFFFFF
+SECTOR = 32
+
+
+def perm32(i, torch):
+    """Bijection of [0, 2^32): odd multiplies and xorshifts (all invertible)."""
+    x = (i ^ 0x5BD1E995) & M32
+    x = (x * 0x9E3779B1) & M32
+    x = x ^ (x >> 16)
+    x = (x * 0x85EBCA6B) & M32
+    x = x ^ (x >> 13)
+    x = (x * 0xC2B2AE35) & M32
+    x = x ^ (x >> 16)
+    return x
+
+
+def make_keys(lo, hi, torch, device):
+    i = torch.arange(lo, hi, dtype=torch.int64, device=device)
+    k = perm32(i, torch)
+    bad = (k == 0) | (k == M32)
+    if bool(bad.any()):
+        # replacements come from an index range no workload uses
+        j = torch.arange(1 << 31, (1 << 31) + 64, dtype=torch.int64, device=device)
+        r = perm32(j, torch)
+        r = r[(r != 0) & (r != M32)]
+        idx = torch.nonzero(bad).flatten()
+        k[idx] = r[: idx.numel()] + 0  # distinct from all P(i), i < 2^31
+    return k
+
+
+def as_i32(k64, torch):
+    return (k64 - ((k64 >> 31) << 32)).to(torch.int32)  # same 32 bits, signed view
+
+
+def zipf_ranks(n, N, s, gen, torch, device):
+    u = torch.rand(n, generator=gen, device=device, dtype=torch.float64)
+    a = 1.0 - s
+    x = torch.pow(1.0 + u * (float(N) ** a - 1.0), 1.0 / a)
+    r = x.floor().to(torch.int64) - 1
+    return r.clamp_(0, N - 1)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="dyc_clocks_", suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "20"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.1)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self, t0, t1):
+        """Median SM clock and active throttle reasons of the samples taken
+        between host times t0 and t1 (the timed region)."""
+        import datetime
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        os.unlink(self.path)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        parsed = []
+        for r in rows:
+            try:
+                ts = datetime.datetime.strptime(r[0].strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                parsed.append((ts, float(r[2]), float(r[3]),
+                               [n for n, v in zip(names, r[6:10]) if v.strip().lower() == "active"]))
+            except (ValueError, IndexError):
+                continue
+        inside = [p for p in parsed if t0 <= p[0] <= t1]
+        use = inside if inside else [p for p in parsed if p[0] >= t0][:1]
+        reasons = sorted({n for p in use for n in p[3]})
+        return {"sm_mhz": statistics.median([p[1] for p in use]) if use else None,
+                "sm_max_mhz": use[0][2] if use else None, "reasons": reasons,
+                "samples": len(inside)}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_setup():
+    import torch
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_table_and_sample(keys_dev, log2_keys, sample, threads, torch):
+    """The reference algorithm's table on the host: hashAPI(N/0.9) sizing,
+    16-slot buckets, MAX_ITER 15 (GPU/dyhash/dy_hash.h:32-37), built with the
+    exchange chain on all host threads."""
+    from oracle import oracle as orc
+    N = 1 << log2_keys
+    keys = keys_dev.cpu().numpy().astype(np.uint32)
+    vals = np.arange(1, N + 1, dtype=np.uint32)
+    t = orc.RefCuckoo(int(N / 0.9), 4, 16, 15)
+    t0 = time.perf_counter()
+    dropped = t.insert(keys, vals, threads=threads)
+    build_s = time.perf_counter() - t0
+    rng = np.random.default_rng(7)
+    idx = rng.integers(0, N, sample)
+    q = np.ascontiguousarray(keys[idx])
+    exp = vals[idx]
+    return t, q, exp, dropped, build_s
+
+
+def time_cpu_find(t, q, threads, reps=1):
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out = t.find(q, threads=threads)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return best, out
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm on the host cores."""
+    import torch
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    N = 1 << args.log2_keys
+    keys = make_keys(0, N, torch, "cpu")
+    sample = 1 << args.log2_cpu_sample
+    t, q, exp, dropped, build_s = cpu_table_and_sample(keys, args.log2_keys, sample, threads, torch)
+    for _ in range(args.warmup):
+        t.find(q, threads=threads)
+    times = []
+    for _ in range(args.steps):
+        dt, out = time_cpu_find(t, q, threads)
+        times.append(dt)
+    total = sum(times)
+    value = args.steps * sample / total / 1e6
+    line = {
+        "metric": "find Mops/s", "impl": "reference", "value": round(value, 2), "unit": "Mops/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": workload_config(args, lf=None),
+        "cpu_baseline": {"value": round(value, 2), "unit": "Mops/s", "cores": threads,
+                         "kind": "port",
+                         "sample": "%d uniform 100%%-hit finds per step on the full %d-key table "
+                                   "(reference algorithm: 16-slot buckets, MAX_ITER 15; %d of %d "
+                                   "keys dropped by its eviction bound; build %.1f s)"
+                                   % (sample, N, dropped, N, build_s)},
+        "e2e": {"value": round(value, 2), "unit": "Mops/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "mismatches_vs_expected": int((out != exp).sum()),
+    }
+    print(json.dumps(line))
+
+
+def workload_config(args, lf):
+    return {
+        "workload": "large static table find: u32 keys/values, 4 subtables, 2^%d unique keys "
+                    "at load factor 0.90, find batches of 2^%d" % (args.log2_keys, args.log2_batch),
+        "keys": 1 << args.log2_keys, "batch": 1 << args.log2_batch,
+        "load_factor": lf, "query_mix": "uniform, 100% hit",
+        "bucket_bytes": args.bucket_bytes, "subtables": 4,
+        "l2": "inputs larger than L2 (table ~2.4 GB, batch 256 MB); no flush",
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--log2-keys", type=int, default=28)
+    ap.add_argument("--log2-batch", type=int, default=26)
+    ap.add_argument("--log2-cpu-sample", type=int, default=24)
+    ap.add_argument("--bucket-bytes", type=int, default=32)
+    ap.add_argument("--max-evictions", type=int, default=256)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-variants", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    import databases_gpu_gb300 as dg
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    N = 1 << args.log2_keys
+    Q = 1 << args.log2_batch
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(10327)
+
+    # ---- table (untimed set-up)
+    keys64 = make_keys(0, N, torch, dev)
+    keys = as_i32(keys64, torch)
+    vals = torch.arange(1, N + 1, dtype=torch.int32, device=dev)
+    t = dg.DyCuckoo(int(N / 0.9), bucket_bytes=args.bucket_bytes, auto_resize=False,
+                    max_evictions=args.max_evictions, device=local)
+    torch.cuda.synchronize()
+    tb = time.perf_counter()
+    st = t.insert(keys, vals, unique=True, new_keys=True)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - tb
+    lf = t.size / t.capacity
+    assert t.size == N, (t.size, N)
+
+    # ---- query batches: 2 of each mix, alternated between steps
+    def batch(mix):
+        if mix.startswith("uniform"):
+            idx = torch.randint(0, N, (Q,), generator=gen, device=dev)
+        else:
+            idx = zipf_ranks(Q, N, 0.99, gen, torch, dev)
+        q = keys64[idx].clone()
+        expv = (idx + 1).to(torch.int32)
+        hit = torch.ones(Q, dtype=torch.bool, device=dev)
+        if mix.endswith("10"):
+            nm = Q - Q // 10
+            pos = torch.randperm(Q, generator=gen, device=dev)[:nm]
+            mi = torch.randint(N, N + (1 << 27), (nm,), generator=gen, device=dev)
+            q[pos] = perm32(mi, torch)  # indices >= N: never inserted
+            expv[pos] = 0
+            hit[pos] = False
+        return as_i32(q, torch), expv, hit
+
+    mixes = ["uniform100"] if args.skip_variants else ["uniform100", "uniform10", "zipf100", "zipf10"]
+    out = torch.empty(Q, dtype=torch.int32, device=dev)
+    bits = torch.empty(Q // 32, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+    peak, peak_kind = load_peaks()
+    results = {}
+    clocks = None
+    for mix in mixes:
+        qs = [batch(mix) for _ in range(2)]
+        for w in range(args.warmup):
+            t.find(qs[w % 2][0], out=out, hit_bits=bits, stream=stream)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        cm = Clocks(local) if mix == "uniform100" else None
+        if cm:
+            cm.__enter__()
+        h0 = time.time()
+        e0.record(stream)
+        for s in range(args.steps):
+            t.find(qs[s % 2][0], out=out, hit_bits=bits, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        h1 = time.time()
+        if cm:
+            cm.__exit__(None, None, None)
+            clocks = cm.summary(h0, h1)
+        ms = e0.elapsed_time(e1)
+        ms = barrier_max(ms, ws)
+        # correctness of the last step's results
+        q, expv, hit = qs[(args.steps - 1) % 2]
+        bad_v = int((out != expv).sum())
+        got_hit = torch.from_numpy(dg.unpack_bits(bits, Q)).to(dev)
+        bad_h = int((got_hit != hit).sum())
+        hit_frac = float(hit.float().mean())
+        bytes_per_op = hit_frac * (SECTOR + 8) + (1 - hit_frac) * (2 * SECTOR + 8)
+        mops = ws * args.steps * Q / (ms / 1e3) / 1e6
+        per_launch_s = ms / 1e3 / args.steps
+        achieved = Q * bytes_per_op / per_launch_s / 1e9
+        results[mix] = {"mops": round(mops, 1), "ms_per_batch": round(ms / args.steps, 4),
+                        "alg_bytes_per_op": round(bytes_per_op, 2),
+                        "achieved_gbs": round(achieved, 1), "frac": round(achieved / peak, 4),
+                        "mismatches": bad_v + bad_h}
+
+    # ---- e2e: host buffers through the C ABI (dyc_find_host), pinned memory
+    q0 = qs_e2e = batch("uniform100")
+    qh = q0[0].cpu().pin_memory()
+    outh = torch.empty(Q, dtype=torch.int32).pin_memory()
+    bitsh = torch.empty(Q // 32, dtype=torch.int32).pin_memory()
+    import ctypes as C
+    L = dg.lib()
+    for _ in range(2):
+        L.dyc_find_host(t.handle, C.c_void_p(qh.data_ptr()), C.c_void_p(outh.data_ptr()),
+                        C.c_void_p(bitsh.data_ptr()), Q)
+    e2e_steps = max(3, min(args.steps, 20))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        rc = L.dyc_find_host(t.handle, C.c_void_p(qh.data_ptr()), C.c_void_p(outh.data_ptr()),
+                             C.c_void_p(bitsh.data_ptr()), Q)
+        assert rc == 0, L.dyc_last_error()
+    e2e_s = barrier_max(time.perf_counter() - t0, ws)
+    e2e_bad = int((outh.to(dev) != qs_e2e[1]).sum())
+    e2e_mops = ws * e2e_steps * Q / e2e_s / 1e6
+
+    # ---- CPU baseline: reference algorithm on the host cores (rank 0, N=1)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        threads = os.cpu_count() or 1
+        sample = 1 << args.log2_cpu_sample
+        ct, cq, cexp, dropped, cbuild = cpu_table_and_sample(keys64, args.log2_keys, sample,
+                                                             threads, torch)
+        dt, cout = time_cpu_find(ct, cq, threads, reps=3)
+        cpu = {"value": round(sample / dt / 1e6, 2), "unit": "Mops/s", "cores": threads,
+               "kind": "port",
+               "sample": "%d uniform 100%%-hit finds on the full 2^%d-key table, best of 3 "
+                         "(reference algorithm: 16-slot buckets, MAX_ITER 15; %d keys dropped "
+                         "by its eviction bound; %d mismatches)"
+                         % (sample, args.log2_keys, dropped, int((cout != cexp).sum()))}
+        ct.close()
+
+    head = results["uniform100"]
+    line = {
+        "metric": "find Mops/s", "value": head["mops"], "unit": "Mops/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_batch"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded bijective key permutation; Zipf by inverse CDF)",
+        "config": workload_config(args, round(lf, 4)),
+        "e2e": {"value": round(e2e_mops, 1), "unit": "Mops/s",
+                "h2d_bytes_per_step": Q * 4, "d2h_bytes_per_step": Q * 4 + Q // 8,
+                "api": "dyc_find_host (pinned host buffers)", "mismatches": e2e_bad},
+        "roofline": {"bound": "hbm", "achieved": head["achieved_gbs"], "peak": peak,
+                     "unit": "GB/s", "frac": head["frac"], "traffic": None,
+                     "peak_kind": peak_kind,
+                     "alg_bytes_per_op": head["alg_bytes_per_op"]},
+        "cpu_baseline": cpu,
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "variants": results,
+        "build": {"seconds": round(build_s, 3), "evict_steps": st["evict_steps"],
+                  "overflowed": st["overflowed"], "capacity": t.capacity},
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    t.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,117 @@
+"""ctypes binding of libdycuckoo.so (the C ABI in include/dycuckoo.h).
+
+Loading builds the library in-tree when it is missing or stale and nvcc is
+available; otherwise it raises. There is no CPU fallback: every table
+operation runs the CUDA kernels of the library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+DYC_OK, DYC_ENOMEM, DYC_EINVAL, DYC_EOVERFLOW, DYC_ETIMEOUT, DYC_ECUDA, DYC_ENOTSUP = range(7)
+FLAG_UNIQUE, FLAG_NEW_KEYS, FLAG_NO_RESIZE = 1, 2, 4
+
+
+class DycConfig(C.Structure):
+    _fields_ = [
+        ("key_bytes", C.c_uint32),
+        ("value_bytes", C.c_uint32),
+        ("num_subtables", C.c_uint32),
+        ("bucket_bytes", C.c_uint32),
+        ("max_evictions", C.c_uint32),
+        ("auto_resize", C.c_uint32),
+        ("initial_size", C.c_uint64),
+        ("upper_load", C.c_double),
+        ("lower_load", C.c_double),
+        ("min_downsize_capacity", C.c_uint64),
+        ("device", C.c_int32),
+        ("reserved", C.c_uint32 * 7),
+    ]
+
+
+class DycOpStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "inserted", "updated", "erased", "rejected", "superseded", "evict_steps",
+        "overflowed", "resizes_up", "resizes_down")]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+EXPORTS = [
+    "dyc_config_default", "dyc_create", "dyc_destroy", "dyc_insert", "dyc_find", "dyc_erase",
+    "dyc_resize_up", "dyc_resize_down", "dyc_size", "dyc_capacity", "dyc_layout",
+    "dyc_subtable", "dyc_export", "dyc_last_stats", "dyc_insert_host", "dyc_find_host",
+    "dyc_erase_host", "dyc_status_string", "dyc_last_error",
+]
+
+_lock = threading.Lock()
+_lib = None
+
+
+def _declare(L):
+    vp, u64, u32 = C.c_void_p, C.c_uint64, C.c_uint32
+    st = C.c_int
+    T = C.c_void_p
+    sig = {
+        "dyc_config_default": (None, [C.POINTER(DycConfig)]),
+        "dyc_create": (st, [C.POINTER(DycConfig), C.POINTER(C.c_void_p)]),
+        "dyc_destroy": (st, [T]),
+        "dyc_insert": (st, [T, vp, vp, u64, u32, vp]),
+        "dyc_find": (st, [T, vp, vp, vp, u64, vp]),
+        "dyc_erase": (st, [T, vp, u64, vp, C.POINTER(u64), u32, vp]),
+        "dyc_resize_up": (st, [T, vp]),
+        "dyc_resize_down": (st, [T, vp]),
+        "dyc_size": (st, [T, C.POINTER(u64)]),
+        "dyc_capacity": (st, [T, C.POINTER(u64)]),
+        "dyc_layout": (st, [T, C.POINTER(u32), C.POINTER(u32)]),
+        "dyc_subtable": (st, [T, u32, C.POINTER(vp), C.POINTER(u64)]),
+        "dyc_export": (st, [T, vp, vp, u64, C.POINTER(u64), vp]),
+        "dyc_last_stats": (st, [T, C.POINTER(DycOpStats)]),
+        "dyc_insert_host": (st, [T, vp, vp, u64, u32]),
+        "dyc_find_host": (st, [T, vp, vp, vp, u64]),
+        "dyc_erase_host": (st, [T, vp, u64, vp, C.POINTER(u64)]),
+        "dyc_status_string": (C.c_char_p, [st]),
+        "dyc_last_error": (C.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def lib(path: str | None = None):
+    """Load (building first if needed) and return the C library."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or _build.LIB
+        if not os.path.exists(p) or not _build.up_to_date(p):
+            _build.build()
+        L = C.CDLL(p)
+        _declare(L)
+        _lib = L
+        return L
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+class DycError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        L = lib()
+        msg = L.dyc_last_error().decode(errors="replace")
+        name = L.dyc_status_string(status).decode()
+        super().__init__("%s failed: %s (%d): %s" % (where, name, status, msg))
+        self.status = status
+
+
+def check(status: int, where: str) -> None:
+    if status != DYC_OK:
+        raise DycError(status, where)

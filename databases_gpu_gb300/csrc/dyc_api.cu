@@ -1,0 +1,673 @@
+// dyc_api.cu -- the C ABI of include/dycuckoo.h: table lifetime, sizing and
+// resize policy (GPU/dyhash/api.cpp), batch chunking, the no-loss overflow
+// loop, and the host-buffer forms of the hashAPI calls.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "dycuckoo.h"
+#include "dyc_device.cuh"
+#include "dyc_internal.h"
+
+using dyc::Counters;
+using dyc::Desc;
+using dyc::LaunchCtx;
+using dyc::Ops;
+using dyc::Scratch;
+
+namespace {
+
+thread_local std::string g_err;
+
+dyc_status fail(dyc_status s, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return s;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(e_ == cudaErrorMemoryAllocation ? DYC_ENOMEM : DYC_ECUDA,         \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+#define TRY(expr)                       \
+    do {                                \
+        dyc_status s_ = (expr);         \
+        if (s_ != DYC_OK) return s_;    \
+    } while (0)
+
+// --- sizing: isPrime / nextPrime / buckets per subtable (api.cpp:4-22, :46-56)
+bool is_prime_ref(int32_t num) {
+    if (num == 2 || num == 3) return true;
+    if (num % 6 != 1 && num % 6 != 5) return false;
+    for (int32_t i = 5; (int64_t)i * i <= num; i += 6)
+        if (num % i == 0 || num % (i + 2) == 0) return false;
+    return true;
+}
+uint32_t next_prime_ref(uint32_t n) {
+    while (!is_prime_ref((int32_t)n)) ++n;
+    return n;
+}
+
+// resize target choice (api.cpp:115-122 and :147-153)
+uint32_t pick_up(const uint32_t *nb, uint32_t d) {
+    for (uint32_t i = 0; i + 1 < d; ++i)
+        if (nb[i] == 2u * nb[i + 1]) return i + 1;
+    return 0;
+}
+uint32_t pick_down(const uint32_t *nb, uint32_t d) {
+    for (uint32_t i = 0; i + 1 < d; ++i)
+        if (nb[i] > nb[i + 1]) return i;
+    return d - 1;
+}
+
+uint64_t next_pow2(uint64_t x) {
+    uint64_t p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+constexpr uint64_t kChunkDefault = 1ull << 22;  // ops per insert/erase pass
+constexpr int kMaxOverflowRounds = 24;
+
+}  // namespace
+
+struct dyc_table {
+    dyc_config cfg;
+    int kb, vb, sb, slot_bytes, slots;
+    int device, sms;
+    Desc D;
+    Counters *d_ctr = nullptr;
+    Counters *h_ctr = nullptr;
+    // scratch for one chunk
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    Scratch S{};
+    uint64_t chunk = kChunkDefault;
+    // host-form staging
+    cudaStream_t io_stream = nullptr;
+    void *d_io = nullptr;
+    size_t d_io_bytes = 0;
+    uint64_t size = 0, capacity = 0;
+    dyc_op_stats last{};
+};
+
+namespace {
+
+dyc_status set_device(dyc_table *t) {
+    int cur = -1;
+    CK(cudaGetDevice(&cur));
+    if (cur != t->device) CK(cudaSetDevice(t->device));
+    return DYC_OK;
+}
+
+LaunchCtx ctx(dyc_table *t, void *stream) { return LaunchCtx{t->sms, (cudaStream_t)stream}; }
+
+// dispatch on key width
+#define KB_CALL(t, fn, ...) ((t)->kb == 4 ? Ops<4>::fn(__VA_ARGS__) : Ops<8>::fn(__VA_ARGS__))
+
+// Make the scratch lists hold `n` ops (grow only).
+dyc_status ensure_scratch(dyc_table *t, uint64_t n) {
+    const uint64_t cap = next_pow2(2 * (n < 16 ? 16 : n));
+    const size_t dedup_bytes = (size_t)cap * 8;
+    const size_t idx_bytes = t->kb == 8 ? (size_t)cap * 4 : 0;
+    const size_t list_bytes = (size_t)n * t->slot_bytes;
+    const size_t need = dedup_bytes + idx_bytes + 2 * list_bytes + 3 * 256;
+    if (t->scratch && t->scratch_bytes >= need && t->S.list_cap >= n && t->S.dedup_cap >= cap)
+        return DYC_OK;
+    if (t->scratch) {
+        CK(cudaDeviceSynchronize());
+        CK(cudaFree(t->scratch));
+        t->scratch = nullptr;
+    }
+    CK(cudaMalloc(&t->scratch, need));
+    t->scratch_bytes = need;
+    char *p = (char *)t->scratch;
+    auto carve = [&](size_t bytes) {
+        char *r = p;
+        p += (bytes + 255) & ~(size_t)255;
+        return (void *)r;
+    };
+    t->S.dedup = carve(dedup_bytes);
+    t->S.dedup_idx = idx_bytes ? (uint32_t *)carve(idx_bytes) : nullptr;
+    t->S.dedup_cap = cap;
+    t->S.list_a = carve(list_bytes);
+    t->S.list_b = carve(list_bytes);
+    t->S.list_cap = n;
+    return DYC_OK;
+}
+
+dyc_status reset_call_counters(dyc_table *t, cudaStream_t s) {
+    CK(cudaMemsetAsync(&t->d_ctr->inserted, 0, sizeof(Counters) - sizeof(unsigned long long), s));
+    return DYC_OK;
+}
+
+dyc_status read_counters(dyc_table *t, cudaStream_t s) {
+    CK(cudaMemcpyAsync(t->h_ctr, t->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (t->h_ctr->spill)
+        return fail(DYC_EOVERFLOW, "internal list overflow (%llu entries)",
+                    (unsigned long long)t->h_ctr->spill);
+    t->size = t->h_ctr->size;
+    return DYC_OK;
+}
+
+// Double subtable pick_up(): allocate 2nb buckets, stream the old buckets
+// into their two images, retire the old buffer (all stream-ordered).
+dyc_status resize_up_impl(dyc_table *t, cudaStream_t s) {
+    const uint32_t ti = pick_up(t->D.nb, t->D.d);
+    const uint32_t onb = t->D.nb[ti];
+    if ((uint64_t)onb * 2 > 0xFFFFFFFFull) return fail(DYC_EINVAL, "subtable %u too large", ti);
+    const uint32_t nnb = onb * 2;
+    void *nw = nullptr;
+    CK(cudaMallocAsync(&nw, (size_t)nnb * t->sb, s));
+    void *old = t->D.sub[ti];
+    cudaError_t e = KB_CALL(t, resize_up, ctx(t, s), t->sb, ti, old, onb, nw);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(nw, s);
+        return fail(DYC_ECUDA, "resize_up kernel: %s", cudaGetErrorString(e));
+    }
+    t->D.sub[ti] = nw;
+    t->D.nb[ti] = nnb;
+    t->D.magic[ti] = dyc::fastmod_magic(nnb);
+    CK(cudaFreeAsync(old, s));
+    t->capacity += (uint64_t)onb * t->slots;
+    t->last.resizes_up++;
+    return DYC_OK;
+}
+
+// Place the entries of list `src` (count in counter *src_ctr) by eviction
+// walks; leftovers go to `dst`. Repeats with an upsize in between until
+// nothing is left. count_new: successes are new keys (insert) rather than
+// moved ones (downsize).
+dyc_status drain(dyc_table *t, cudaStream_t s, void *src, unsigned long long *src_ctr,
+                 void *dst, unsigned long long *dst_ctr, uint64_t cap, bool count_new,
+                 bool first_upsize) {
+    for (int round = 0; round < kMaxOverflowRounds; ++round) {
+        if (round > 0 || first_upsize) {
+            // grow to the upper load bound for everything placed or pending,
+            // and by at least one subtable
+            const unsigned long long left = *(src_ctr == &t->d_ctr->pending ? &t->h_ctr->pending
+                                                                           : &t->h_ctr->overflow);
+            int guard = 0;
+            do {
+                TRY(resize_up_impl(t, s));
+            } while ((double)(t->size + left) > t->cfg.upper_load * (double)t->capacity &&
+                     ++guard < 64);
+        }
+        CK(cudaMemsetAsync(dst_ctr, 0, sizeof(unsigned long long), s));
+        cudaError_t e = KB_CALL(t, walk, ctx(t, s), t->D, t->sb, src, src_ctr, dst, dst_ctr, cap,
+                                t->cfg.max_evictions, count_new, t->d_ctr, cap);
+        if (e != cudaSuccess) return fail(DYC_ECUDA, "walk kernel: %s", cudaGetErrorString(e));
+        TRY(read_counters(t, s));
+        const unsigned long long left =
+            dst_ctr == &t->d_ctr->pending ? t->h_ctr->pending : t->h_ctr->overflow;
+        if (left == 0) return DYC_OK;
+        std::swap(src, dst);
+        std::swap(src_ctr, dst_ctr);
+    }
+    return fail(DYC_EOVERFLOW, "eviction overflow persisted after %d upsizes", kMaxOverflowRounds);
+}
+
+dyc_status insert_chunk(dyc_table *t, const void *keys, const void *vals, uint64_t n,
+                        uint32_t flags, cudaStream_t s) {
+    const bool use_dedup = !(flags & DYC_FLAG_UNIQUE) && n > 1;
+    const bool new_keys = (flags & DYC_FLAG_NEW_KEYS) != 0;
+    TRY(reset_call_counters(t, s));
+    if (use_dedup) {
+        CK(cudaMemsetAsync(t->S.dedup, 0, (size_t)t->S.dedup_cap * 8, s));
+        if (t->S.dedup_idx) CK(cudaMemsetAsync(t->S.dedup_idx, 0, (size_t)t->S.dedup_cap * 4, s));
+        cudaError_t e = KB_CALL(t, dedup, ctx(t, s), t->S, keys, n, dyc::kKeepLast);
+        if (e != cudaSuccess) return fail(DYC_ECUDA, "dedup kernel: %s", cudaGetErrorString(e));
+    }
+    cudaError_t e = KB_CALL(t, place, ctx(t, s), t->D, t->sb, t->S, use_dedup, new_keys, keys,
+                            vals, (uint32_t)t->vb, n, t->d_ctr);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "place kernel: %s", cudaGetErrorString(e));
+    // walks for the ops whose buckets were full: list_a -> list_b
+    e = KB_CALL(t, walk, ctx(t, s), t->D, t->sb, t->S.list_a, &t->d_ctr->pending, t->S.list_b,
+                &t->d_ctr->overflow, t->S.list_cap, t->cfg.max_evictions, true, t->d_ctr,
+                t->S.list_cap);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "walk kernel: %s", cudaGetErrorString(e));
+    TRY(read_counters(t, s));
+    const Counters c = *t->h_ctr;
+    dyc_op_stats &L = t->last;
+    L.inserted += c.inserted;
+    L.updated += c.updated;
+    L.rejected += c.rejected;
+    L.superseded += c.superseded;
+    L.evict_steps += c.evict_steps;
+    L.overflowed += c.overflow;
+    if (c.overflow) {
+        TRY(drain(t, s, t->S.list_b, &t->d_ctr->overflow, t->S.list_a, &t->d_ctr->pending,
+                  t->S.list_cap, true, true));
+        L.inserted += t->h_ctr->inserted - c.inserted;
+        L.evict_steps += t->h_ctr->evict_steps - c.evict_steps;
+    }
+    return DYC_OK;
+}
+
+dyc_status erase_chunk(dyc_table *t, const void *keys, uint64_t n, uint32_t *bits,
+                       uint32_t flags, cudaStream_t s) {
+    const bool use_dedup = !(flags & DYC_FLAG_UNIQUE) && n > 1;
+    TRY(reset_call_counters(t, s));
+    if (use_dedup) {
+        CK(cudaMemsetAsync(t->S.dedup, 0, (size_t)t->S.dedup_cap * 8, s));
+        if (t->S.dedup_idx) CK(cudaMemsetAsync(t->S.dedup_idx, 0xFF, (size_t)t->S.dedup_cap * 4, s));
+        cudaError_t e = KB_CALL(t, dedup, ctx(t, s), t->S, keys, n, dyc::kKeepFirst);
+        if (e != cudaSuccess) return fail(DYC_ECUDA, "dedup kernel: %s", cudaGetErrorString(e));
+    }
+    cudaError_t e = KB_CALL(t, erase, ctx(t, s), t->D, t->sb, t->S, use_dedup, keys, n, bits,
+                            t->d_ctr);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "erase kernel: %s", cudaGetErrorString(e));
+    TRY(read_counters(t, s));
+    t->last.erased += t->h_ctr->erased;
+    t->last.superseded += t->h_ctr->superseded;
+    return DYC_OK;
+}
+
+// Halve subtable pick_down(). Even bucket counts merge bucket j with j+nb/2;
+// odd counts rehash the whole subtable into ceil(nb/2) buckets. Entries that
+// do not fit are placed by eviction walks (upsizing another subtable if
+// needed), so nothing is dropped.
+dyc_status resize_down_impl(dyc_table *t, cudaStream_t s) {
+    const uint32_t ti = pick_down(t->D.nb, t->D.d);
+    const uint32_t onb = t->D.nb[ti];
+    if (onb < 2) return fail(DYC_EINVAL, "subtable %u has %u bucket(s); cannot halve", ti, onb);
+    const bool even = (onb % 2u) == 0;
+    const uint32_t nnb = even ? onb / 2 : (onb + 1) / 2;
+    const uint64_t list_cap = even ? (uint64_t)nnb * t->slots : (uint64_t)onb * t->slots;
+    void *nw = nullptr, *la = nullptr, *lb = nullptr;
+    CK(cudaMallocAsync(&nw, (size_t)nnb * t->sb, s));
+    CK(cudaMallocAsync(&la, (size_t)list_cap * t->slot_bytes, s));
+    CK(cudaMallocAsync(&lb, (size_t)list_cap * t->slot_bytes, s));
+    TRY(reset_call_counters(t, s));
+    void *old = t->D.sub[ti];
+    cudaError_t e;
+    if (even) {
+        e = KB_CALL(t, resize_down, ctx(t, s), t->sb, old, onb, nw, la, &t->d_ctr->pending,
+                    list_cap, &t->d_ctr->spill);
+    } else {
+        CK(cudaMemsetAsync(nw, 0, (size_t)nnb * t->sb, s));
+        e = KB_CALL(t, collect, ctx(t, s), t->sb, old, onb, la, &t->d_ctr->pending, list_cap,
+                    &t->d_ctr->spill);
+    }
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "downsize kernel: %s", cudaGetErrorString(e));
+    t->D.sub[ti] = nw;
+    t->D.nb[ti] = nnb;
+    t->D.magic[ti] = dyc::fastmod_magic(nnb);
+    t->capacity -= (uint64_t)(onb - nnb) * t->slots;
+    CK(cudaFreeAsync(old, s));
+    t->last.resizes_down++;
+    dyc_status st = drain(t, s, la, &t->d_ctr->pending, lb, &t->d_ctr->overflow, list_cap, false,
+                          false);
+    cudaFreeAsync(la, s);
+    cudaFreeAsync(lb, s);
+    return st;
+}
+
+bool valid_config(const dyc_config *c, char *why, size_t n) {
+    if (c->key_bytes != 4 && c->key_bytes != 8) return snprintf(why, n, "key_bytes must be 4 or 8"), false;
+    if (c->value_bytes != 4 && c->value_bytes != 8) return snprintf(why, n, "value_bytes must be 4 or 8"), false;
+    if (c->key_bytes == 4 && c->value_bytes != 4)
+        return snprintf(why, n, "4-byte keys take 4-byte values"), false;
+    if (c->num_subtables < 2 || c->num_subtables > 6)
+        return snprintf(why, n, "num_subtables must be 2..6"), false;
+    if (c->bucket_bytes != 32 && c->bucket_bytes != 64 && c->bucket_bytes != 128)
+        return snprintf(why, n, "bucket_bytes must be 32, 64 or 128"), false;
+    if (c->max_evictions < 1 || c->max_evictions > 100000)
+        return snprintf(why, n, "max_evictions must be 1..100000"), false;
+    if (!(c->upper_load > 0.0 && c->upper_load <= 1.0) || !(c->lower_load >= 0.0 && c->lower_load < c->upper_load))
+        return snprintf(why, n, "need 0 <= lower_load < upper_load <= 1"), false;
+    return true;
+}
+
+}  // namespace
+
+// =============================================================================
+extern "C" {
+
+void dyc_config_default(dyc_config *cfg) {
+    if (!cfg) return;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->key_bytes = 4;
+    cfg->value_bytes = 4;
+    cfg->num_subtables = 4;
+    cfg->bucket_bytes = 32;
+    cfg->max_evictions = 64;
+    cfg->auto_resize = 1;
+    cfg->initial_size = 1024;
+    cfg->upper_load = 0.8;
+    cfg->lower_load = 0.5;
+    cfg->min_downsize_capacity = (uint64_t)(4 * 1024 * 1024 * 1.2);
+    cfg->device = 0;
+}
+
+const char *dyc_status_string(dyc_status s) {
+    switch (s) {
+    case DYC_OK: return "ok";
+    case DYC_ENOMEM: return "out of memory";
+    case DYC_EINVAL: return "invalid argument";
+    case DYC_EOVERFLOW: return "eviction overflow";
+    case DYC_ETIMEOUT: return "device wait timed out";
+    case DYC_ECUDA: return "CUDA error";
+    case DYC_ENOTSUP: return "not supported";
+    }
+    return "unknown status";
+}
+
+const char *dyc_last_error(void) { return g_err.c_str(); }
+
+dyc_status dyc_create(const dyc_config *cfg, dyc_table **out) {
+    if (!cfg || !out) return fail(DYC_EINVAL, "null argument");
+    *out = nullptr;
+    char why[128];
+    if (!valid_config(cfg, why, sizeof(why))) return fail(DYC_EINVAL, "%s", why);
+    dyc_table *t = new (std::nothrow) dyc_table();
+    if (!t) return fail(DYC_ENOMEM, "host allocation");
+    t->cfg = *cfg;
+    t->kb = (int)cfg->key_bytes;
+    t->vb = (int)cfg->value_bytes;
+    t->sb = (int)cfg->bucket_bytes;
+    t->slot_bytes = t->kb == 4 ? 8 : 16;
+    t->slots = t->sb / t->slot_bytes;
+    t->device = cfg->device;
+    auto undo = [&](dyc_status s) {
+        dyc_destroy(t);
+        return s;
+    };
+    {
+        cudaError_t e = cudaSetDevice(t->device);
+        if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "cudaSetDevice(%d): %s", t->device, cudaGetErrorString(e)));
+        e = cudaDeviceGetAttribute(&t->sms, cudaDevAttrMultiProcessorCount, t->device);
+        if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "device attribute: %s", cudaGetErrorString(e)));
+    }
+    // hashAPI::hashAPI sizing (api.cpp:47-54) with this table's slots/bucket
+    const uint64_t per = (uint64_t)cfg->num_subtables * t->slots;
+    const uint64_t s0 = cfg->initial_size / per;
+    if (s0 >= 0x7FFFFFF0ull) return undo(fail(DYC_EINVAL, "initial_size too large"));
+    uint32_t s = next_prime_ref((uint32_t)s0);
+    const uint32_t nb = (s & 1u) ? s + 1u : s;
+    memset(&t->D, 0, sizeof(t->D));
+    t->D.d = cfg->num_subtables;
+    for (uint32_t i = 0; i < t->D.d; ++i) {
+        cudaError_t e = cudaMalloc(&t->D.sub[i], (size_t)nb * t->sb);
+        if (e != cudaSuccess) return undo(fail(DYC_ENOMEM, "subtable %u: %s", i, cudaGetErrorString(e)));
+        e = cudaMemset(t->D.sub[i], 0, (size_t)nb * t->sb);
+        if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "memset: %s", cudaGetErrorString(e)));
+        t->D.nb[i] = nb;
+        t->D.magic[i] = dyc::fastmod_magic(nb);
+        t->capacity += (uint64_t)nb * t->slots;
+    }
+    cudaError_t e = cudaMalloc(&t->d_ctr, sizeof(Counters));
+    if (e == cudaSuccess) e = cudaMemset(t->d_ctr, 0, sizeof(Counters));
+    if (e == cudaSuccess) e = cudaMallocHost(&t->h_ctr, sizeof(Counters));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&t->io_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "table setup: %s", cudaGetErrorString(e)));
+    memset(t->h_ctr, 0, sizeof(Counters));
+    *out = t;
+    return DYC_OK;
+}
+
+dyc_status dyc_destroy(dyc_table *t) {
+    if (!t) return DYC_OK;
+    cudaSetDevice(t->device);
+    cudaDeviceSynchronize();
+    for (uint32_t i = 0; i < dyc::kMaxSub; ++i)
+        if (t->D.sub[i]) cudaFree(t->D.sub[i]);
+    if (t->d_ctr) cudaFree(t->d_ctr);
+    if (t->h_ctr) cudaFreeHost(t->h_ctr);
+    if (t->scratch) cudaFree(t->scratch);
+    if (t->d_io) cudaFree(t->d_io);
+    if (t->io_stream) cudaStreamDestroy(t->io_stream);
+    delete t;
+    return DYC_OK;
+}
+
+dyc_status dyc_insert(dyc_table *t, const void *d_keys, const void *d_vals, uint64_t n,
+                      uint32_t flags, void *stream) {
+    if (!t) return fail(DYC_EINVAL, "null table");
+    if (n == 0) return DYC_OK;
+    if (!d_keys || !d_vals) return fail(DYC_EINVAL, "null key or value array");
+    TRY(set_device(t));
+    cudaStream_t s = (cudaStream_t)stream;
+    t->last = dyc_op_stats{};
+    const uint64_t chunk = t->chunk;
+    TRY(ensure_scratch(t, n < chunk ? n : chunk));
+    for (uint64_t off = 0; off < n; off += chunk) {
+        const uint64_t m = (n - off) < chunk ? (n - off) : chunk;
+        // projected-size check before the batch (api.cpp:359-369)
+        if (t->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE)) {
+            int guard = 0;
+            while ((double)(t->size + m) > t->cfg.upper_load * (double)t->capacity && guard++ < 64)
+                TRY(resize_up_impl(t, s));
+        }
+        TRY(insert_chunk(t, (const char *)d_keys + off * t->kb,
+                         (const char *)d_vals + off * t->vb, m, flags, s));
+    }
+    return DYC_OK;
+}
+
+dyc_status dyc_find(dyc_table *t, const void *d_keys, void *d_vals_out, uint32_t *d_hit_bits_out,
+                    uint64_t n, void *stream) {
+    if (!t) return fail(DYC_EINVAL, "null table");
+    if (n == 0) return DYC_OK;
+    if (!d_keys || !d_vals_out) return fail(DYC_EINVAL, "null key or value array");
+    TRY(set_device(t));
+    cudaError_t e = KB_CALL(t, find, ctx(t, stream), t->D, t->sb, d_keys, d_vals_out,
+                            (uint32_t)t->vb, d_hit_bits_out, n);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "find kernel: %s", cudaGetErrorString(e));
+    return DYC_OK;
+}
+
+dyc_status dyc_erase(dyc_table *t, const void *d_keys, uint64_t n, uint32_t *d_erased_bits_out,
+                     uint64_t *h_erased_count, uint32_t flags, void *stream) {
+    if (!t) return fail(DYC_EINVAL, "null table");
+    if (h_erased_count) *h_erased_count = 0;
+    if (n == 0) return DYC_OK;
+    if (!d_keys) return fail(DYC_EINVAL, "null key array");
+    TRY(set_device(t));
+    cudaStream_t s = (cudaStream_t)stream;
+    t->last = dyc_op_stats{};
+    const uint64_t chunk = t->chunk;
+    TRY(ensure_scratch(t, n < chunk ? n : chunk));
+    for (uint64_t off = 0; off < n; off += chunk) {
+        const uint64_t m = (n - off) < chunk ? (n - off) : chunk;
+        TRY(erase_chunk(t, (const char *)d_keys + off * t->kb, m,
+                        d_erased_bits_out ? d_erased_bits_out + off / 32 : nullptr, flags, s));
+    }
+    if (h_erased_count) *h_erased_count = t->last.erased;
+    // downsize check after the batch (api.cpp:494-505)
+    if (t->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE) &&
+        (double)t->size < t->cfg.lower_load * (double)t->capacity &&
+        t->capacity > t->cfg.min_downsize_capacity) {
+        const dyc_op_stats keep = t->last;
+        dyc_status st = resize_down_impl(t, s);
+        if (st != DYC_OK && st != DYC_EINVAL) return st;
+        const uint64_t downs = t->last.resizes_down, ups = t->last.resizes_up;
+        t->last = keep;
+        t->last.resizes_down = downs;
+        t->last.resizes_up = ups;
+    }
+    return DYC_OK;
+}
+
+dyc_status dyc_resize_up(dyc_table *t, void *stream) {
+    if (!t) return fail(DYC_EINVAL, "null table");
+    TRY(set_device(t));
+    t->last = dyc_op_stats{};
+    TRY(resize_up_impl(t, (cudaStream_t)stream));
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
+    return DYC_OK;
+}
+
+dyc_status dyc_resize_down(dyc_table *t, void *stream) {
+    if (!t) return fail(DYC_EINVAL, "null table");
+    TRY(set_device(t));
+    t->last = dyc_op_stats{};
+    return resize_down_impl(t, (cudaStream_t)stream);
+}
+
+dyc_status dyc_size(dyc_table *t, uint64_t *size) {
+    if (!t || !size) return fail(DYC_EINVAL, "null argument");
+    *size = t->size;
+    return DYC_OK;
+}
+
+dyc_status dyc_capacity(dyc_table *t, uint64_t *capacity) {
+    if (!t || !capacity) return fail(DYC_EINVAL, "null argument");
+    *capacity = t->capacity;
+    return DYC_OK;
+}
+
+dyc_status dyc_layout(dyc_table *t, uint32_t *nbuckets_out, uint32_t *num_subtables) {
+    if (!t) return fail(DYC_EINVAL, "null table");
+    if (num_subtables) *num_subtables = t->D.d;
+    if (nbuckets_out)
+        for (uint32_t i = 0; i < t->D.d; ++i) nbuckets_out[i] = t->D.nb[i];
+    return DYC_OK;
+}
+
+dyc_status dyc_subtable(dyc_table *t, uint32_t i, void **d_ptr, uint64_t *bytes) {
+    if (!t || i >= t->D.d) return fail(DYC_EINVAL, "bad table or subtable index");
+    if (d_ptr) *d_ptr = t->D.sub[i];
+    if (bytes) *bytes = (uint64_t)t->D.nb[i] * t->sb;
+    return DYC_OK;
+}
+
+dyc_status dyc_export(dyc_table *t, void *d_keys_out, void *d_vals_out, uint64_t capacity,
+                      uint64_t *n_out, void *stream) {
+    if (!t) return fail(DYC_EINVAL, "null table");
+    if (capacity && (!d_keys_out || !d_vals_out)) return fail(DYC_EINVAL, "null output array");
+    TRY(set_device(t));
+    cudaStream_t s = (cudaStream_t)stream;
+    CK(cudaMemsetAsync(&t->d_ctr->pad[0], 0, sizeof(unsigned long long), s));
+    cudaError_t e = KB_CALL(t, export_all, ctx(t, s), t->D, t->sb, d_keys_out, d_vals_out,
+                            (uint32_t)t->vb, capacity, &t->d_ctr->pad[0]);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "export kernel: %s", cudaGetErrorString(e));
+    unsigned long long cnt = 0;
+    CK(cudaMemcpyAsync(t->h_ctr, t->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    cnt = t->h_ctr->pad[0];
+    if (n_out) *n_out = cnt;
+    return DYC_OK;
+}
+
+dyc_status dyc_last_stats(dyc_table *t, dyc_op_stats *out) {
+    if (!t || !out) return fail(DYC_EINVAL, "null argument");
+    *out = t->last;
+    return DYC_OK;
+}
+
+// ---- host-buffer forms (hashAPI::hash_insert / hash_search / hash_delete) ----
+namespace {
+constexpr uint64_t kIoChunk = 1ull << 22;  // ops staged per round trip
+
+dyc_status ensure_io(dyc_table *t, size_t bytes) {
+    if (t->d_io && t->d_io_bytes >= bytes) return DYC_OK;
+    if (t->d_io) {
+        CK(cudaStreamSynchronize(t->io_stream));
+        CK(cudaFree(t->d_io));
+        t->d_io = nullptr;
+    }
+    CK(cudaMalloc(&t->d_io, bytes));
+    t->d_io_bytes = bytes;
+    return DYC_OK;
+}
+}  // namespace
+
+dyc_status dyc_insert_host(dyc_table *t, const void *h_keys, const void *h_vals, uint64_t n,
+                           uint32_t flags) {
+    if (!t) return fail(DYC_EINVAL, "null table");
+    if (n == 0) return DYC_OK;
+    if (!h_keys || !h_vals) return fail(DYC_EINVAL, "null key or value array");
+    TRY(set_device(t));
+    const uint64_t c = n < kIoChunk ? n : kIoChunk;
+    TRY(ensure_io(t, (size_t)c * (t->kb + t->vb) + 256));
+    char *dk = (char *)t->d_io;
+    char *dv = dk + (((size_t)c * t->kb + 255) & ~(size_t)255);
+    dyc_op_stats total{};
+    for (uint64_t off = 0; off < n; off += c) {
+        const uint64_t m = (n - off) < c ? (n - off) : c;
+        CK(cudaMemcpyAsync(dk, (const char *)h_keys + off * t->kb, m * t->kb, cudaMemcpyHostToDevice, t->io_stream));
+        CK(cudaMemcpyAsync(dv, (const char *)h_vals + off * t->vb, m * t->vb, cudaMemcpyHostToDevice, t->io_stream));
+        TRY(dyc_insert(t, dk, dv, m, flags, t->io_stream));
+        total.inserted += t->last.inserted;
+        total.updated += t->last.updated;
+        total.rejected += t->last.rejected;
+        total.superseded += t->last.superseded;
+        total.evict_steps += t->last.evict_steps;
+        total.overflowed += t->last.overflowed;
+        total.resizes_up += t->last.resizes_up;
+    }
+    t->last = total;
+    return DYC_OK;
+}
+
+dyc_status dyc_find_host(dyc_table *t, const void *h_keys, void *h_vals_out,
+                         uint32_t *h_hit_bits_out, uint64_t n) {
+    if (!t) return fail(DYC_EINVAL, "null table");
+    if (n == 0) return DYC_OK;
+    if (!h_keys || !h_vals_out) return fail(DYC_EINVAL, "null key or value array");
+    TRY(set_device(t));
+    const uint64_t c = n < kIoChunk ? n : kIoChunk;
+    const size_t kbytes = (((size_t)c * t->kb) + 255) & ~(size_t)255;
+    const size_t vbytes = (((size_t)c * t->vb) + 255) & ~(size_t)255;
+    TRY(ensure_io(t, kbytes + vbytes + (c / 32 + 1) * 4 + 256));
+    char *dk = (char *)t->d_io;
+    char *dv = dk + kbytes;
+    uint32_t *db = (uint32_t *)(dv + vbytes);
+    for (uint64_t off = 0; off < n; off += c) {
+        const uint64_t m = (n - off) < c ? (n - off) : c;
+        CK(cudaMemcpyAsync(dk, (const char *)h_keys + off * t->kb, m * t->kb, cudaMemcpyHostToDevice, t->io_stream));
+        TRY(dyc_find(t, dk, dv, h_hit_bits_out ? db : nullptr, m, t->io_stream));
+        CK(cudaMemcpyAsync((char *)h_vals_out + off * t->vb, dv, m * t->vb, cudaMemcpyDeviceToHost, t->io_stream));
+        if (h_hit_bits_out)
+            CK(cudaMemcpyAsync(h_hit_bits_out + off / 32, db, ((m + 31) / 32) * 4, cudaMemcpyDeviceToHost, t->io_stream));
+    }
+    CK(cudaStreamSynchronize(t->io_stream));
+    return DYC_OK;
+}
+
+dyc_status dyc_erase_host(dyc_table *t, const void *h_keys, uint64_t n,
+                          uint32_t *h_erased_bits_out, uint64_t *erased_count) {
+    if (!t) return fail(DYC_EINVAL, "null table");
+    if (erased_count) *erased_count = 0;
+    if (n == 0) return DYC_OK;
+    if (!h_keys) return fail(DYC_EINVAL, "null key array");
+    TRY(set_device(t));
+    const uint64_t c = n < kIoChunk ? n : kIoChunk;
+    const size_t kbytes = (((size_t)c * t->kb) + 255) & ~(size_t)255;
+    TRY(ensure_io(t, kbytes + (c / 32 + 1) * 4 + 256));
+    char *dk = (char *)t->d_io;
+    uint32_t *db = (uint32_t *)(dk + kbytes);
+    uint64_t total = 0;
+    dyc_op_stats agg{};
+    for (uint64_t off = 0; off < n; off += c) {
+        const uint64_t m = (n - off) < c ? (n - off) : c;
+        CK(cudaMemcpyAsync(dk, (const char *)h_keys + off * t->kb, m * t->kb, cudaMemcpyHostToDevice, t->io_stream));
+        uint64_t got = 0;
+        TRY(dyc_erase(t, dk, m, h_erased_bits_out ? db : nullptr, &got, 0, t->io_stream));
+        total += got;
+        agg.erased += t->last.erased;
+        agg.superseded += t->last.superseded;
+        agg.resizes_down += t->last.resizes_down;
+        agg.resizes_up += t->last.resizes_up;
+        if (h_erased_bits_out)
+            CK(cudaMemcpyAsync(h_erased_bits_out + off / 32, db, ((m + 31) / 32) * 4, cudaMemcpyDeviceToHost, t->io_stream));
+    }
+    CK(cudaStreamSynchronize(t->io_stream));
+    t->last = agg;
+    if (erased_count) *erased_count = total;
+    return DYC_OK;
+}
+
+}  // extern "C"

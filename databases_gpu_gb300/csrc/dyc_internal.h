@@ -1,0 +1,94 @@
+// dyc_internal.h -- shared between the kernels and the host side of the
+// C ABI: the device-side table descriptor, the per-table counters and the
+// kernel launchers.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace dyc {
+
+// The reference's modulus before the bucket modulo, written as in
+// GPU/dyhash/dy_hash.h:24 (294967291, not the prime 4294967291).
+constexpr uint32_t kPrime = 294967291u;
+constexpr int kMaxSub = 6;
+
+// Table descriptor passed by value to every kernel (the reference keeps one
+// in __constant__ memory, cuckoo.cu:16, which limits a process to one table).
+struct Desc {
+    void *sub[kMaxSub];       // subtable base addresses
+    uint64_t magic[kMaxSub];  // fastmod reciprocals of nb[]
+    uint32_t nb[kMaxSub];     // buckets per subtable
+    uint32_t d;               // subtable count
+};
+
+// Per-table device counters (one 128-byte block). `size` persists; the rest
+// are per-call and reset before each insert / erase / resize.
+struct Counters {
+    unsigned long long size;
+    unsigned long long inserted, updated, erased, rejected, superseded;
+    unsigned long long pending, overflow, evict_steps;
+    unsigned long long spill;  // pending entries a list could not hold (must stay 0)
+    unsigned long long pad[6];
+};
+static_assert(sizeof(Counters) == 128, "Counters is one 128-byte block");
+
+enum DedupMode { kKeepLast = 0, kKeepFirst = 1 };
+
+// Scratch lists used by one insert / erase / resize chunk.
+struct Scratch {
+    void *dedup;            // open-addressing table of (key, op index)
+    uint32_t *dedup_idx;    // op index array for 8-byte keys
+    uint64_t dedup_cap;     // power of two
+    void *list_a;           // pending entries (slots)
+    void *list_b;           // overflow entries (slots)
+    uint64_t list_cap;      // entries per list
+};
+
+// Launch parameters picked once per kernel from the occupancy calculator.
+struct LaunchCtx {
+    int sms;
+    cudaStream_t stream;
+};
+
+// Kernel launchers, one set per key width; `sb` = bucket bytes (32/64/128).
+// All return cudaGetLastError() of their launches.
+template <int KB> struct Ops {
+    static cudaError_t find(const LaunchCtx &L, const Desc &D, int sb, const void *keys,
+                            void *vals, uint32_t vb, uint32_t *hits, uint64_t n);
+    static cudaError_t dedup(const LaunchCtx &L, const Scratch &S, const void *keys, uint64_t n,
+                             DedupMode mode);
+    // insert: place or update every op; ops whose two buckets are full go to
+    // list_a (counted in pending). new_keys = caller promises absent keys.
+    static cudaError_t place(const LaunchCtx &L, const Desc &D, int sb, const Scratch &S,
+                             bool use_dedup, bool new_keys, const void *keys, const void *vals,
+                             uint32_t vb, uint64_t n, Counters *ctr);
+    // eviction walks for the entries of `src` (count at *src_count); entries
+    // that reach the bound go to `dst` (count at *dst_count). count_new adds
+    // successes to ctr->inserted and ctr->size.
+    static cudaError_t walk(const LaunchCtx &L, const Desc &D, int sb, const void *src,
+                            const unsigned long long *src_count, void *dst,
+                            unsigned long long *dst_count, uint64_t dst_cap, uint32_t max_evict,
+                            bool count_new, Counters *ctr, uint64_t max_entries);
+    static cudaError_t erase(const LaunchCtx &L, const Desc &D, int sb, const Scratch &S,
+                             bool use_dedup, const void *keys, uint64_t n, uint32_t *bits,
+                             Counters *ctr);
+    static cudaError_t resize_up(const LaunchCtx &L, int sb, uint32_t t, const void *old_sub,
+                                 uint32_t old_nb, void *new_sub);
+    // halve an even subtable: merged buckets to new_sub, leftovers to list
+    static cudaError_t resize_down(const LaunchCtx &L, int sb, const void *old_sub,
+                                   uint32_t old_nb, void *new_sub, void *list,
+                                   unsigned long long *list_count, uint64_t list_cap,
+                                   unsigned long long *spill);
+    // every live slot of one subtable to list (general rehash)
+    static cudaError_t collect(const LaunchCtx &L, int sb, const void *sub, uint32_t nb,
+                               void *list, unsigned long long *list_count, uint64_t list_cap,
+                               unsigned long long *spill);
+    static cudaError_t export_all(const LaunchCtx &L, const Desc &D, int sb, void *keys,
+                                  void *vals, uint32_t vb, uint64_t cap,
+                                  unsigned long long *count);
+};
+
+}  // namespace dyc

@@ -1,0 +1,168 @@
+// dyc_ops.cuh -- host launchers for the kernels of one key width. Included by
+// dyc_ops4.cu and dyc_ops8.cu, which instantiate Ops<4> and Ops<8>, so the
+// two widths compile as separate translation units in parallel.
+#pragma once
+
+#include <mutex>
+#include <unordered_map>
+
+#include "dyc_kernels.cuh"
+
+namespace dyc {
+
+// Grid size for a grid-stride kernel: enough blocks for `work` threads, at
+// most one full wave of resident blocks (occupancy x SM count).
+inline int grid_for(const void *kernel, const LaunchCtx &L, uint64_t work, int block = 256) {
+    static std::mutex mu;
+    static std::unordered_map<const void *, int> occ;
+    int per_sm;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = occ.find(kernel);
+        if (it == occ.end()) {
+            int v = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, block, 0) != cudaSuccess ||
+                v < 1)
+                v = 1;
+            occ[kernel] = v;
+            per_sm = v;
+        } else {
+            per_sm = it->second;
+        }
+    }
+    const uint64_t need = (work + block - 1) / block;
+    const uint64_t wave = (uint64_t)per_sm * (uint64_t)(L.sms > 0 ? L.sms : 1);
+    uint64_t g = need < wave ? need : wave;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+#define DYC_SB_DISPATCH(sb, ...)                              \
+    switch (sb) {                                             \
+    case 32: { constexpr int SB = 32; __VA_ARGS__; } break;   \
+    case 64: { constexpr int SB = 64; __VA_ARGS__; } break;   \
+    case 128: { constexpr int SB = 128; __VA_ARGS__; } break; \
+    default: return cudaErrorInvalidValue;                    \
+    }
+
+template <int KB>
+cudaError_t Ops<KB>::find(const LaunchCtx &L, const Desc &D, int sb, const void *keys, void *vals,
+                          uint32_t vb, uint32_t *hits, uint64_t n) {
+    if (n == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_find<KB, SB>;
+        k<<<grid_for((const void *)k, L, n), 256, 0, L.stream>>>(D, keys, vals, vb, hits, n);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::dedup(const LaunchCtx &L, const Scratch &S, const void *keys, uint64_t n,
+                           DedupMode mode) {
+    if (n == 0) return cudaSuccess;
+    auto k = k_dedup<KB>;
+    k<<<grid_for((const void *)k, L, n), 256, 0, L.stream>>>(S, keys, n, mode);
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::place(const LaunchCtx &L, const Desc &D, int sb, const Scratch &S,
+                           bool use_dedup, bool new_keys, const void *keys, const void *vals,
+                           uint32_t vb, uint64_t n, Counters *ctr) {
+    if (n == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_place<KB, SB>;
+        k<<<grid_for((const void *)k, L, n), 256, 0, L.stream>>>(
+            D, S, use_dedup ? 1 : 0, new_keys ? 1 : 0, keys, vals, vb, n, ctr);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::walk(const LaunchCtx &L, const Desc &D, int sb, const void *src,
+                          const unsigned long long *src_count, void *dst,
+                          unsigned long long *dst_count, uint64_t dst_cap, uint32_t max_evict,
+                          bool count_new, Counters *ctr, uint64_t max_entries) {
+    if (max_entries == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_walk<KB, SB>;
+        k<<<grid_for((const void *)k, L, max_entries), 256, 0, L.stream>>>(
+            D, src, src_count, dst, dst_count, dst_cap, max_evict, count_new ? 1 : 0, ctr,
+            max_entries);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::erase(const LaunchCtx &L, const Desc &D, int sb, const Scratch &S,
+                           bool use_dedup, const void *keys, uint64_t n, uint32_t *bits,
+                           Counters *ctr) {
+    if (n == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_erase<KB, SB>;
+        k<<<grid_for((const void *)k, L, n), 256, 0, L.stream>>>(D, S, use_dedup ? 1 : 0, keys,
+                                                                 n, bits, ctr);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::resize_up(const LaunchCtx &L, int sb, uint32_t t, const void *old_sub,
+                               uint32_t old_nb, void *new_sub) {
+    if (old_nb == 0) return cudaSuccess;
+    const uint32_t new_nb = 2u * old_nb;
+    const uint64_t magic = fastmod_magic(new_nb);
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_resize_up<KB, SB>;
+        k<<<grid_for((const void *)k, L, old_nb), 256, 0, L.stream>>>(
+            t, (const char *)old_sub, old_nb, (char *)new_sub, magic, new_nb);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::resize_down(const LaunchCtx &L, int sb, const void *old_sub,
+                                 uint32_t old_nb, void *new_sub, void *list,
+                                 unsigned long long *list_count, uint64_t list_cap,
+                                 unsigned long long *spill) {
+    const uint32_t new_nb = old_nb / 2u;
+    if (new_nb == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_resize_down<KB, SB>;
+        k<<<grid_for((const void *)k, L, new_nb), 256, 0, L.stream>>>(
+            (const char *)old_sub, new_nb, (char *)new_sub, list, list_count, list_cap, spill);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::collect(const LaunchCtx &L, int sb, const void *sub, uint32_t nb, void *list,
+                             unsigned long long *list_count, uint64_t list_cap,
+                             unsigned long long *spill) {
+    if (nb == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_collect<KB, SB>;
+        k<<<grid_for((const void *)k, L, nb), 256, 0, L.stream>>>((const char *)sub, nb, list,
+                                                                  list_count, list_cap, spill);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::export_all(const LaunchCtx &L, const Desc &D, int sb, void *keys, void *vals,
+                                uint32_t vb, uint64_t cap, unsigned long long *count) {
+    for (uint32_t t = 0; t < D.d; ++t) {
+        const uint32_t nb = D.nb[t];
+        if (nb == 0) continue;
+        DYC_SB_DISPATCH(sb, {
+            auto k = k_export<KB, SB>;
+            k<<<grid_for((const void *)k, L, nb), 256, 0, L.stream>>>(
+                (const char *)D.sub[t], nb, keys, vals, vb, cap, count);
+        });
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace dyc

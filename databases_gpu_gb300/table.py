@@ -1,0 +1,375 @@
+"""Host-side mirror of the reference's DyCuckoo interface over the C ABI.
+
+``DyCuckoo`` is the device-buffer handle (the reference's gpu_lp_* launch
+wrappers, GPU/dyhash/cuckoo.h:99-114): keys, values and results are CUDA
+tensors. ``hashAPI`` keeps the reference's class surface
+(GPU/dyhash/api.h:9-54) with host arrays: hash_insert / hash_search /
+hash_delete / resize_up / resize_low and the batch-pool calls.
+
+PyTorch is used only for device memory and streams; every operation is a
+call into libdycuckoo.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import FLAG_NEW_KEYS, FLAG_NO_RESIZE, FLAG_UNIQUE, check
+
+# test_uilt.h:1-5 of the reference
+UPPER_BOUND = 0.8
+LOWER_BOUND = 0.5
+BATCH_NUM = 1000
+BATCH_SIZE = 100000
+MIN_DOWNSIZE_CAPACITY = int(4 * 1024 * 1024 * 1.2)  # api.cpp:496
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _ptr(t, what: str, elem_bytes: int | None = None):
+    if t is None:
+        return None
+    torch = _torch()
+    if not isinstance(t, torch.Tensor):
+        raise TypeError("%s must be a CUDA tensor" % what)
+    if not t.is_cuda:
+        raise ValueError("%s must live on a CUDA device" % what)
+    if not t.is_contiguous():
+        raise ValueError("%s must be contiguous" % what)
+    if elem_bytes is not None and t.element_size() != elem_bytes:
+        raise ValueError("%s must have %d-byte elements, got %s" % (what, elem_bytes, t.dtype))
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return C.c_void_p(_torch().cuda.current_stream().cuda_stream)
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
+    return C.c_void_p(stream.cuda_stream)
+
+
+class DyCuckoo:
+    """A GB300 DyCuckoo table; all arrays are CUDA tensors.
+
+    size: number of keys to size the table for (the hashAPI(size) argument).
+    """
+
+    def __init__(self, size: int, key_bytes: int = 4, value_bytes: int | None = None,
+                 num_subtables: int = 4, bucket_bytes: int = 32, max_evictions: int = 64,
+                 auto_resize: bool = True, upper_load: float = UPPER_BOUND,
+                 lower_load: float = LOWER_BOUND,
+                 min_downsize_capacity: int = MIN_DOWNSIZE_CAPACITY, device: int = 0):
+        L = _lib.lib()
+        cfg = _lib.DycConfig()
+        L.dyc_config_default(C.byref(cfg))
+        cfg.key_bytes = key_bytes
+        cfg.value_bytes = value_bytes if value_bytes is not None else key_bytes
+        cfg.num_subtables = num_subtables
+        cfg.bucket_bytes = bucket_bytes
+        cfg.max_evictions = max_evictions
+        cfg.auto_resize = 1 if auto_resize else 0
+        cfg.initial_size = int(size)
+        cfg.upper_load = upper_load
+        cfg.lower_load = lower_load
+        cfg.min_downsize_capacity = int(min_downsize_capacity)
+        cfg.device = device
+        h = C.c_void_p()
+        check(L.dyc_create(C.byref(cfg), C.byref(h)), "dyc_create")
+        self._h = h
+        self.L = L
+        self.cfg = cfg
+        self.key_bytes = cfg.key_bytes
+        self.value_bytes = cfg.value_bytes
+        self.device = device
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            self.L.dyc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- dtypes
+    def key_dtype(self):
+        torch = _torch()
+        return torch.int32 if self.key_bytes == 4 else torch.int64
+
+    def value_dtype(self):
+        torch = _torch()
+        return torch.int32 if self.value_bytes == 4 else torch.int64
+
+    # -- batch ops
+    def insert(self, keys, values, unique: bool = False, new_keys: bool = False,
+               no_resize: bool = False, stream=None) -> dict:
+        n = keys.numel()
+        if values.numel() != n:
+            raise ValueError("keys and values differ in length")
+        flags = (FLAG_UNIQUE if unique else 0) | (FLAG_NEW_KEYS if new_keys else 0) | \
+            (FLAG_NO_RESIZE if no_resize else 0)
+        check(self.L.dyc_insert(self._h, _ptr(keys, "keys", self.key_bytes),
+                                _ptr(values, "values", self.value_bytes), n, flags,
+                                _stream_ptr(stream)), "dyc_insert")
+        return self.stats()
+
+    def find(self, keys, out=None, hit_bits=None, want_hits: bool = True, stream=None):
+        torch = _torch()
+        n = keys.numel()
+        if out is None:
+            out = torch.empty(n, dtype=self.value_dtype(), device=keys.device)
+        if hit_bits is None and want_hits:
+            hit_bits = torch.empty((n + 31) // 32, dtype=torch.int32, device=keys.device)
+        check(self.L.dyc_find(self._h, _ptr(keys, "keys", self.key_bytes),
+                              _ptr(out, "out", self.value_bytes),
+                              _ptr(hit_bits, "hit_bits", 4) if hit_bits is not None else None,
+                              n, _stream_ptr(stream)), "dyc_find")
+        return out, hit_bits
+
+    def erase(self, keys, erased_bits=None, unique: bool = False, no_resize: bool = False,
+              stream=None) -> int:
+        n = keys.numel()
+        cnt = C.c_uint64(0)
+        flags = (FLAG_UNIQUE if unique else 0) | (FLAG_NO_RESIZE if no_resize else 0)
+        check(self.L.dyc_erase(self._h, _ptr(keys, "keys", self.key_bytes), n,
+                               _ptr(erased_bits, "erased_bits", 4) if erased_bits is not None else None,
+                               C.byref(cnt), flags, _stream_ptr(stream)), "dyc_erase")
+        return int(cnt.value)
+
+    def resize_up(self, stream=None) -> None:
+        check(self.L.dyc_resize_up(self._h, _stream_ptr(stream)), "dyc_resize_up")
+
+    def resize_down(self, stream=None) -> None:
+        check(self.L.dyc_resize_down(self._h, _stream_ptr(stream)), "dyc_resize_down")
+
+    # -- introspection
+    @property
+    def size(self) -> int:
+        v = C.c_uint64()
+        check(self.L.dyc_size(self._h, C.byref(v)), "dyc_size")
+        return int(v.value)
+
+    @property
+    def capacity(self) -> int:
+        v = C.c_uint64()
+        check(self.L.dyc_capacity(self._h, C.byref(v)), "dyc_capacity")
+        return int(v.value)
+
+    def layout(self):
+        nb = (C.c_uint32 * 6)()
+        d = C.c_uint32()
+        check(self.L.dyc_layout(self._h, nb, C.byref(d)), "dyc_layout")
+        return [int(nb[i]) for i in range(d.value)]
+
+    def stats(self) -> dict:
+        s = _lib.DycOpStats()
+        check(self.L.dyc_last_stats(self._h, C.byref(s)), "dyc_last_stats")
+        return s.as_dict()
+
+    def subtable(self, i: int):
+        """Subtable i as a (buckets, slots) array of raw slots on the host."""
+        torch = _torch()
+        p = C.c_void_p()
+        nbytes = C.c_uint64()
+        check(self.L.dyc_subtable(self._h, i, C.byref(p), C.byref(nbytes)), "dyc_subtable")
+        torch.cuda.synchronize(self.device)
+        host = np.empty(nbytes.value // 8, np.uint64)
+        cudart = C.CDLL("libcudart.so.13")
+        cudart.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+        rc = cudart.cudaMemcpy(host.ctypes.data, p, nbytes.value, 2)
+        if rc != 0:
+            raise RuntimeError("cudaMemcpy of subtable failed: %d" % rc)
+        slot_words = 1 if self.key_bytes == 4 else 2
+        slots = self.cfg.bucket_bytes // (8 * slot_words)
+        nb = self.layout()[i]
+        return host.reshape(nb, slots, slot_words) if slot_words == 2 else host.reshape(nb, slots)
+
+    def export(self, stream=None):
+        """All live (key, value) pairs as CUDA tensors, sorted by key."""
+        torch = _torch()
+        n = self.size
+        cap = max(n, 1)
+        k = torch.empty(cap, dtype=self.key_dtype(), device="cuda:%d" % self.device)
+        v = torch.empty(cap, dtype=self.value_dtype(), device="cuda:%d" % self.device)
+        got = C.c_uint64()
+        check(self.L.dyc_export(self._h, _ptr(k, "keys"), _ptr(v, "vals"), cap, C.byref(got),
+                                _stream_ptr(stream)), "dyc_export")
+        m = int(got.value)
+        if m > cap:
+            raise RuntimeError("export found %d live entries but size is %d" % (m, n))
+        k, v = k[:m], v[:m]
+        # sort as unsigned
+        if self.key_bytes == 4:
+            order = torch.argsort(k.to(torch.int64) & 0xFFFFFFFF)
+        else:
+            kk = k.cpu().numpy().view(np.uint64)
+            order = torch.from_numpy(np.argsort(kk, kind="stable")).to(k.device)
+        return k[order], v[order]
+
+    # -- host-buffer forms (reference-facing C ABI with host memory)
+    def insert_host(self, keys: np.ndarray, values: np.ndarray, flags: int = 0) -> None:
+        keys = np.ascontiguousarray(keys)
+        values = np.ascontiguousarray(values)
+        check(self.L.dyc_insert_host(self._h, keys.ctypes.data, values.ctypes.data,
+                                     keys.size, flags), "dyc_insert_host")
+
+    def find_host(self, keys: np.ndarray, out: np.ndarray, hit_bits: np.ndarray | None = None):
+        keys = np.ascontiguousarray(keys)
+        check(self.L.dyc_find_host(self._h, keys.ctypes.data, out.ctypes.data,
+                                   hit_bits.ctypes.data if hit_bits is not None else None,
+                                   keys.size), "dyc_find_host")
+
+    def erase_host(self, keys: np.ndarray, erased_bits: np.ndarray | None = None) -> int:
+        keys = np.ascontiguousarray(keys)
+        cnt = C.c_uint64()
+        check(self.L.dyc_erase_host(self._h, keys.ctypes.data, keys.size,
+                                    erased_bits.ctypes.data if erased_bits is not None else None,
+                                    C.byref(cnt)), "dyc_erase_host")
+        return int(cnt.value)
+
+
+def unpack_bits(bits, n: int) -> np.ndarray:
+    """Hit / erased bit words (ceil(n/32) uint32) -> bool array of n."""
+    if hasattr(bits, "cpu"):
+        bits = bits.cpu().numpy()
+    w = np.asarray(bits).view(np.uint32)
+    b = np.unpackbits(w.view(np.uint8), bitorder="little")
+    return b[:n].astype(bool)
+
+
+class hashAPI:  # noqa: N801 -- the reference's class name
+    """The reference's hashAPI (GPU/dyhash/api.h:9-54, api.cpp) on GB300.
+
+    Host arrays in, host arrays out, like the reference. Differences, all
+    deliberate: no memory pool and no leaked buffers; any number of live
+    tables; sizes are exact counts (the reference's num_size counts nominal
+    batch sizes, api.cpp:371, :490); insert is an upsert and no entry is ever
+    dropped (the reference drops entries at the end of long eviction chains,
+    cuckoo.cu:422-431).
+    """
+
+    def __init__(self, size: int, **cfg):
+        cfg.setdefault("auto_resize", False)  # hash_insert has the check compiled out (api.cpp:185)
+        self.t = DyCuckoo(int(size), **cfg)
+        self._pool_k = None
+        self._pool_v = None
+        self.batch_num_to_op = 0
+        self.batch_del_num_to_op = 0
+        self.batch_search_num_to_op = 0
+
+    def close(self):
+        self.t.close()
+
+    @property
+    def table_size(self) -> int:
+        return self.t.capacity
+
+    @property
+    def num_size(self) -> int:
+        return self.t.size
+
+    # api.cpp:184-265
+    def hash_insert(self, k: np.ndarray, v: np.ndarray, size: int) -> None:
+        kd = np.uint32 if self.t.key_bytes == 4 else np.uint64
+        vd = np.uint32 if self.t.value_bytes == 4 else np.uint64
+        self.t.insert_host(np.ascontiguousarray(k[:size], kd), np.ascontiguousarray(v[:size], vd))
+
+    # api.cpp:267-285: ans[i] = value, 0 on a miss
+    def hash_search(self, k: np.ndarray, ans: np.ndarray, size: int) -> None:
+        kd = np.uint32 if self.t.key_bytes == 4 else np.uint64
+        vd = np.uint32 if self.t.value_bytes == 4 else np.uint64
+        out = np.empty(size, vd)
+        self.t.find_host(np.ascontiguousarray(k[:size], kd), out)
+        ans[:size] = out
+
+    # api.cpp:289-303: the reference returns zeros in ans; this returns the
+    # number of keys removed as well
+    def hash_delete(self, k: np.ndarray, ans: np.ndarray, size: int) -> int:
+        kd = np.uint32 if self.t.key_bytes == 4 else np.uint64
+        n = self.t.erase_host(np.ascontiguousarray(k[:size], kd))
+        ans[:size] = 0
+        return n
+
+    # api.cpp:112-141, :143-173
+    def resize_up(self) -> None:
+        self.t.resize_up()
+
+    def resize_low(self) -> None:
+        self.t.resize_down()
+
+    # ---- batch pool (api.cpp:309-506)
+    def set_data_to_gpu(self, key: np.ndarray, value: np.ndarray, size: int) -> bool:
+        torch = _torch()
+        if size > (1 << 30) // 8:
+            raise ValueError("set data error size of kv out of 2G")
+        kd = torch.int32 if self.t.key_bytes == 4 else torch.int64
+        vd = torch.int32 if self.t.value_bytes == 4 else torch.int64
+        dev = "cuda:%d" % self.t.device
+        self._pool_k = torch.from_numpy(np.ascontiguousarray(key[:size]).view(
+            np.int32 if kd == torch.int32 else np.int64)).to(dev)
+        self._pool_v = torch.from_numpy(np.ascontiguousarray(value[:size]).view(
+            np.int32 if vd == torch.int32 else np.int64)).to(dev)
+        self._check = torch.zeros(BATCH_SIZE, dtype=vd, device=dev)
+        return True
+
+    def batch_reset(self) -> None:
+        self.batch_num_to_op = 0
+        self.batch_del_num_to_op = 0
+        self.batch_search_num_to_op = 0
+
+    def _batch(self, i: int):
+        lo = i * BATCH_SIZE
+        return self._pool_k[lo:lo + BATCH_SIZE], self._pool_v[lo:lo + BATCH_SIZE]
+
+    def hash_insert_batch(self) -> None:
+        if self.batch_num_to_op >= BATCH_NUM:
+            raise IndexError("batch_num_to_op >= BATCH_NUM")
+        k, v = self._batch(self.batch_num_to_op)
+        self._insert_with_policy(k, v)
+        self.batch_num_to_op += 1
+
+    def hash_search_batch(self) -> None:
+        if self.batch_search_num_to_op >= BATCH_NUM:
+            raise IndexError("batch_search_num_to_op >= BATCH_NUM")
+        k, _ = self._batch(self.batch_search_num_to_op)
+        self.t.find(k, out=self._check[:k.numel()], want_hits=False)
+        self.batch_search_num_to_op += 1
+
+    def hash_delete_batch(self) -> None:
+        if self.batch_del_num_to_op >= BATCH_NUM:
+            raise IndexError("batch_del_num_to_op >= BATCH_NUM")
+        k, _ = self._batch(self.batch_del_num_to_op)
+        self._erase_with_policy(k)
+        self.batch_del_num_to_op += 1
+
+    def _insert_with_policy(self, k, v):
+        # projected-size upsize loop of hash_insert_batch (api.cpp:359-369)
+        while self.t.size + k.numel() > UPPER_BOUND * self.t.capacity:
+            self.t.resize_up()
+        self.t.insert(k, v, no_resize=True)
+
+    def _erase_with_policy(self, k):
+        self.t.erase(k, no_resize=True)
+        # one downsize after a delete batch (api.cpp:494-505)
+        if self.t.size < LOWER_BOUND * self.t.capacity and \
+                self.t.capacity > MIN_DOWNSIZE_CAPACITY:
+            self.t.resize_down()

@@ -1,0 +1,179 @@
+/*
+ * dycuckoo.h -- C ABI of the GB300 DyCuckoo dynamic hash table.
+ *
+ * A DyCuckoo table holds d subtables (2..6, default 4) of fixed-size buckets.
+ * A key lives in one of two buckets: the pair of subtables chosen by the
+ * reference's "two-layer" pair map, at the bucket given by the reference's
+ * per-subtable hash functions. Batches of inserts, finds and erases run as
+ * sm_103a kernels; a subtable grows or shrinks by a factor of two on its own
+ * (upsize / downsize), driven by load-factor thresholds.
+ *
+ * Reference: pauline-ly/databases_gpu, GPU/dyhash. Each entry point below
+ * names the reference interface it replaces. The reference's surface is the
+ * C++ class hashAPI (GPU/dyhash/api.h:9-54) over device-pointer launch
+ * wrappers (GPU/dyhash/cuckoo.h:99-114); this header is the C form of both,
+ * and include/dycuckoo_hashapi.hpp restores the hashAPI class on top of it.
+ *
+ * Conventions
+ *   - Every function returns a dyc_status; dyc_last_error() holds a message
+ *     for the calling thread after a failure (the reference has no return
+ *     codes: api.cpp uses checkCudaErrors and gtest EXPECT_* instead).
+ *   - `d_` pointers are device pointers, `h_` pointers host pointers.
+ *     Keys are uint32 or uint64 (key_bytes), values uint32 or uint64
+ *     (value_bytes); arrays are dense.
+ *   - `stream` is a cudaStream_t passed as void*. Calls on one table are
+ *     ordered on the stream given; a table must not be used from two host
+ *     threads at once. Different tables may be used from different threads.
+ *   - Key 0 is the empty-slot sentinel (as in the reference): an insert of
+ *     key 0 is rejected and counted, a find or erase of key 0 misses.
+ *
+ * Semantics (fixed by this library; the reference leaves them undefined)
+ *   - insert is an upsert. Within one insert batch a repeated key keeps the
+ *     value of its last occurrence (batch index order).
+ *   - find writes the value (0 on a miss) and one hit bit per key.
+ *   - erase removes present keys and reports how many it removed; within one
+ *     erase batch only the first occurrence of a repeated key removes it.
+ *   - no entry is ever dropped: an eviction chain that reaches its bound
+ *     parks its entry, the table upsizes and the entry is placed again.
+ */
+#ifndef DYCUCKOO_H
+#define DYCUCKOO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum dyc_status {
+    DYC_OK = 0,
+    DYC_ENOMEM = 1,    /* device or pinned-host allocation failed */
+    DYC_EINVAL = 2,    /* bad argument or unsupported configuration */
+    DYC_EOVERFLOW = 3, /* eviction overflow persisted after repeated upsizes */
+    DYC_ETIMEOUT = 4,  /* a bounded device-side wait gave up */
+    DYC_ECUDA = 5,     /* a CUDA runtime call failed */
+    DYC_ENOTSUP = 6    /* valid request this build does not support */
+} dyc_status;
+
+typedef struct dyc_table dyc_table;
+
+/* Table configuration. Reference: compile-time macros of GPU/dyhash/dy_hash.h
+ * (TABLE_NUM :32, MAX_ITER :33, ELEM_NUM_P_gpu :34) and test_uilt.h:1-2
+ * (Upper_Bound / Lower_Bound), made runtime fields. */
+typedef struct dyc_config {
+    uint32_t key_bytes;      /* 4 or 8 */
+    uint32_t value_bytes;    /* 4 or 8 (4-byte keys take 4-byte values) */
+    uint32_t num_subtables;  /* d, 2..6; default 4 */
+    uint32_t bucket_bytes;   /* 32, 64 or 128; default 32 (one DRAM sector) */
+    uint32_t max_evictions;  /* eviction chain bound; default 64 */
+    uint32_t auto_resize;    /* 1: apply upper/lower load thresholds */
+    uint64_t initial_size;   /* the hashAPI(size) argument: keys to size for */
+    double upper_load;       /* upsize when size would exceed this; default 0.8 */
+    double lower_load;       /* downsize below this after erase; default 0.5 */
+    uint64_t min_downsize_capacity; /* no downsize at or below this capacity */
+    int32_t device;          /* CUDA device ordinal; default 0 */
+    uint32_t reserved[7];
+} dyc_config;
+
+/* Per-call flags. */
+#define DYC_FLAG_UNIQUE 1u    /* caller promises no key repeats in this batch */
+#define DYC_FLAG_NEW_KEYS 2u  /* insert: caller promises no key of the batch is in the table */
+#define DYC_FLAG_NO_RESIZE 4u /* skip the load-factor policy for this call */
+
+/* Counters of the last insert / erase / resize call on a table. */
+typedef struct dyc_op_stats {
+    uint64_t inserted;    /* new keys placed */
+    uint64_t updated;     /* existing keys whose value was replaced */
+    uint64_t erased;      /* keys removed */
+    uint64_t rejected;    /* ops on key 0 */
+    uint64_t superseded;  /* repeated keys resolved by the batch-order rule */
+    uint64_t evict_steps; /* eviction exchanges performed */
+    uint64_t overflowed;  /* chains that reached the bound and were re-placed */
+    uint64_t resizes_up;
+    uint64_t resizes_down;
+} dyc_op_stats;
+
+/* Defaults: 4-byte keys and values, d = 4, 32-byte buckets, bound 64,
+ * thresholds 0.8 / 0.5, downsize guard 4*1M*1.2 slots (api.cpp:496). */
+void dyc_config_default(dyc_config *cfg);
+
+/* Replaces hashAPI::hashAPI(size) (GPU/dyhash/api.cpp:26-91): subtables of
+ * nextPrime(size / (d * slots)) buckets, rounded up to even (api.cpp:46-56);
+ * no memory pool, no __constant__ descriptor, any number of live tables. */
+dyc_status dyc_create(const dyc_config *cfg, dyc_table **out);
+
+/* Replaces hashAPI::~hashAPI (api.cpp:93-109). */
+dyc_status dyc_destroy(dyc_table *t);
+
+/* Replaces gpu_lp_insert / cuckoo_insert (GPU/dyhash/cuckoo.cu:858-877,
+ * :324-432) and the resize-before-insert check of hashAPI::hash_insert_batch
+ * (api.cpp:359-369). Returns after the batch is in the table (it reads the
+ * overflow counters back). */
+dyc_status dyc_insert(dyc_table *t, const void *d_keys, const void *d_vals, uint64_t n,
+                      uint32_t flags, void *stream);
+
+/* Replaces gpu_lp_search / cuckoo_search (cuckoo.cu:881-899, :460-520).
+ * d_hit_bits_out (optional) receives ceil(n/32) words, bit i%32 of word i/32
+ * set when key i was found. Asynchronous on `stream`. */
+dyc_status dyc_find(dyc_table *t, const void *d_keys, void *d_vals_out,
+                    uint32_t *d_hit_bits_out, uint64_t n, void *stream);
+
+/* Replaces gpu_lp_delete / cuckoo_delete (cuckoo.cu:901-916, :524-587) and the
+ * downsize-after-delete check of hash_delete_batch (api.cpp:494-505).
+ * d_erased_bits_out (optional) as for find; h_erased_count (optional)
+ * receives the number of keys removed. Returns after the erase is complete. */
+dyc_status dyc_erase(dyc_table *t, const void *d_keys, uint64_t n,
+                     uint32_t *d_erased_bits_out, uint64_t *h_erased_count,
+                     uint32_t flags, void *stream);
+
+/* Replaces hashAPI::resize_up + GPU_cuckoo_resize_up (api.cpp:112-141,
+ * cuckoo.cu:731-758, kernel :600-627): doubles the subtable the reference
+ * would pick. */
+dyc_status dyc_resize_up(dyc_table *t, void *stream);
+
+/* Replaces hashAPI::resize_low + GPU_cuckoo_resize_down (api.cpp:143-173,
+ * cuckoo.cu:762-788, kernel :638-728): halves the subtable the reference
+ * would pick; entries that no longer fit are placed again, never dropped. */
+dyc_status dyc_resize_down(dyc_table *t, void *stream);
+
+/* Live key count (hashAPI::num_size, exact here) and slot capacity
+ * (hashAPI::table_size). */
+dyc_status dyc_size(dyc_table *t, uint64_t *size);
+dyc_status dyc_capacity(dyc_table *t, uint64_t *capacity);
+
+/* Buckets per subtable (cuckoo.h:39-51 Lsize >> 4) and the subtable count. */
+dyc_status dyc_layout(dyc_table *t, uint32_t *nbuckets_out, uint32_t *num_subtables);
+
+/* Device address and byte size of subtable i (the reference's
+ * table.table[i], cuckoo.h:42). Slots are bucket_bytes/slot_bytes per
+ * bucket; a 4-byte-key slot is key | value << 32, an 8-byte-key slot is
+ * {key, value} (16 bytes). */
+dyc_status dyc_subtable(dyc_table *t, uint32_t i, void **d_ptr, uint64_t *bytes);
+
+/* Every live (key, value) into d_keys_out / d_vals_out (no order), at most
+ * `capacity` of them; *n_out = number of live entries. The reference has no
+ * export; its debug dump is show_table (cuckoo.cu:795-816). */
+dyc_status dyc_export(dyc_table *t, void *d_keys_out, void *d_vals_out, uint64_t capacity,
+                      uint64_t *n_out, void *stream);
+
+/* Counters of the last insert / erase / resize call. */
+dyc_status dyc_last_stats(dyc_table *t, dyc_op_stats *out);
+
+/* Host-buffer forms: the signatures of hashAPI::hash_insert / hash_search /
+ * hash_delete (api.cpp:184-303). They stage through pinned buffers owned by
+ * the table and return when the results are in host memory. */
+dyc_status dyc_insert_host(dyc_table *t, const void *h_keys, const void *h_vals, uint64_t n,
+                           uint32_t flags);
+dyc_status dyc_find_host(dyc_table *t, const void *h_keys, void *h_vals_out,
+                         uint32_t *h_hit_bits_out, uint64_t n);
+dyc_status dyc_erase_host(dyc_table *t, const void *h_keys, uint64_t n,
+                          uint32_t *h_erased_bits_out, uint64_t *erased_count);
+
+const char *dyc_status_string(dyc_status s);
+const char *dyc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DYCUCKOO_H */

@@ -1,0 +1,96 @@
+"""CPU-only checks of the C ABI: the library builds, loads, exports every
+symbol include/dycuckoo.h declares, and its structs match the header."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+import databases_gpu_gb300 as dg
+from databases_gpu_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "dycuckoo.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(dyc_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_header_declares_the_exported_surface():
+    decl = declared_functions()
+    assert decl == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol():
+    L = dg.lib()
+    for name in declared_functions():
+        assert hasattr(L, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", dg.library_path()],
+                         capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r" T (dyc_\w+)", out))
+    assert set(declared_functions()) <= exported
+
+
+def test_struct_layout_matches_header(tmp_path):
+    prog = tmp_path / "layout.c"
+    prog.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "dycuckoo.h"\n'
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(dyc_config),"
+        " offsetof(dyc_config, initial_size), offsetof(dyc_config, upper_load),"
+        " offsetof(dyc_config, device), sizeof(dyc_op_stats),"
+        " offsetof(dyc_op_stats, resizes_down));return 0;}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(prog), "-o", str(exe)],
+                   check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    D = _lib.DycConfig
+    S = _lib.DycOpStats
+    assert got == [C.sizeof(D), D.initial_size.offset, D.upper_load.offset, D.device.offset,
+                   C.sizeof(S), S.resizes_down.offset]
+
+
+def test_config_defaults():
+    L = dg.lib()
+    cfg = _lib.DycConfig()
+    L.dyc_config_default(C.byref(cfg))
+    assert (cfg.key_bytes, cfg.value_bytes, cfg.num_subtables, cfg.bucket_bytes) == (4, 4, 4, 32)
+    assert cfg.upper_load == 0.8 and cfg.lower_load == 0.5
+    assert cfg.min_downsize_capacity == int(4 * 1024 * 1024 * 1.2)
+    assert cfg.auto_resize == 1
+
+
+@pytest.mark.parametrize("field,value", [("key_bytes", 3), ("value_bytes", 2),
+                                         ("num_subtables", 7), ("num_subtables", 1),
+                                         ("bucket_bytes", 48), ("max_evictions", 0)])
+def test_invalid_config_rejected_before_any_device_call(field, value):
+    L = dg.lib()
+    cfg = _lib.DycConfig()
+    L.dyc_config_default(C.byref(cfg))
+    setattr(cfg, field, value)
+    h = C.c_void_p()
+    assert L.dyc_create(C.byref(cfg), C.byref(h)) == _lib.DYC_EINVAL
+    assert not h.value
+    assert L.dyc_last_error()
+
+
+def test_null_arguments_rejected():
+    L = dg.lib()
+    assert L.dyc_insert(None, None, None, 1, 0, None) == _lib.DYC_EINVAL
+    assert L.dyc_find(None, None, None, None, 1, None) == _lib.DYC_EINVAL
+    assert L.dyc_erase(None, None, 1, None, None, 0, None) == _lib.DYC_EINVAL
+    assert L.dyc_destroy(None) == _lib.DYC_OK
+    assert L.dyc_status_string(_lib.DYC_EOVERFLOW) == b"eviction overflow"
+
+
+def test_four_byte_keys_need_four_byte_values():
+    L = dg.lib()
+    cfg = _lib.DycConfig()
+    L.dyc_config_default(C.byref(cfg))
+    cfg.value_bytes = 8
+    h = C.c_void_p()
+    assert L.dyc_create(C.byref(cfg), C.byref(h)) == _lib.DYC_EINVAL

@@ -1,0 +1,309 @@
+"""GPU parity: the CUDA table through the C ABI against the oracle.
+
+Every check is exact: find values and hit bits, erase counts and erased
+bits, and the table's full key->value contents after every batch equal the
+oracle's map semantics (upsert; last occurrence wins within an insert batch;
+first occurrence removes within an erase batch; key 0 is never stored).
+The placement test also checks that every resident key sits in a bucket the
+reference's hash functions give it (GPU/dyhash/cuckoo.cu:76-90, :190-213).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.helpers import (assert_same_contents, find_and_compare, first_probe_table, to_dev,
+                           unique_u32, unique_u64)
+
+pytestmark = pytest.mark.gpu
+
+
+def _dg():
+    import databases_gpu_gb300 as dg
+    return dg
+
+
+def _bits_np(bits, n):
+    return _dg().unpack_bits(bits, n)
+
+
+# ---------------------------------------------------------------- config 1
+def test_config1_insert_find_erase_refind():
+    """2^20 unique u32 keys at load factor 0.85, 2^20 finds (50% hits),
+    2^19 erases, re-find; contents checked after every batch."""
+    n = 1 << 20
+    pool = unique_u32(2 * n, seed=10327)
+    keys, miss = pool[:n], pool[n:]
+    vals = (np.arange(n, dtype=np.uint32) * 3 + 4) & 0x7FFFFFFF
+    t = _dg().DyCuckoo(int(n / 0.85), auto_resize=False)
+    m = O.Map(n)
+    st = t.insert(to_dev(keys), to_dev(vals))
+    m.insert(keys, vals)
+    assert st["inserted"] == n and st["updated"] == 0
+    assert_same_contents(t, m, "after insert")
+    mt = O.MT19937(4242)
+    q = mt.queries(n, 0.5, np.concatenate([keys, miss]).copy())
+    hits = find_and_compare(t, m, q, "find 50%")
+    assert hits.sum() == n // 2
+    er = keys[: n // 2].copy()
+    mt.shuffle(er)
+    bits = __import__("torch").zeros(n // 2 // 32, dtype=__import__("torch").int32, device="cuda")
+    cnt = t.erase(to_dev(er), erased_bits=bits)
+    _, oh = m.erase(er)
+    assert cnt == n // 2 == int(oh.sum())
+    assert np.array_equal(_bits_np(bits, n // 2), oh)
+    assert_same_contents(t, m, "after erase")
+    find_and_compare(t, m, q, "re-find")
+    t.close()
+
+
+# ------------------------------------------------------ batch-order rules
+def test_repeated_keys_last_insert_wins():
+    rng = np.random.default_rng(1)
+    n = 200_000
+    keys = rng.integers(1, 5000, n, dtype=np.uint32)
+    vals = np.arange(n, dtype=np.uint32)
+    t = _dg().DyCuckoo(20000)
+    m = O.Map()
+    st = t.insert(to_dev(keys), to_dev(vals))
+    m.insert(keys, vals)
+    assert st["superseded"] == n - np.unique(keys).size
+    assert_same_contents(t, m, "dup insert")
+    # second batch: upserts of present keys plus new ones
+    k2 = rng.integers(1, 10000, n, dtype=np.uint32)
+    v2 = np.arange(n, dtype=np.uint32) + 7
+    st = t.insert(to_dev(k2), to_dev(v2))
+    m.insert(k2, v2)
+    assert st["updated"] > 0 and st["inserted"] > 0
+    assert_same_contents(t, m, "upsert batch")
+    t.close()
+
+
+def test_repeated_keys_first_erase_removes():
+    import torch
+    rng = np.random.default_rng(2)
+    keys = unique_u32(50_000, seed=7)
+    t = _dg().DyCuckoo(100_000)
+    m = O.Map()
+    t.insert(to_dev(keys), to_dev(keys))
+    m.insert(keys, keys)
+    er = np.concatenate([rng.choice(keys, 30_000), rng.integers(1, 1 << 32, 2000, dtype=np.uint64).astype(np.uint32)])
+    rng.shuffle(er)
+    bits = torch.zeros((er.size + 31) // 32, dtype=torch.int32, device="cuda")
+    cnt = t.erase(to_dev(er), erased_bits=bits, no_resize=True)
+    _, oh = m.erase(er)
+    assert cnt == int(oh.sum())
+    assert np.array_equal(_bits_np(bits, er.size), oh)
+    assert_same_contents(t, m, "dup erase")
+    t.close()
+
+
+def test_key_zero_is_never_stored():
+    keys = np.array([0, 5, 0, 9, 11], np.uint32)
+    vals = np.array([1, 2, 3, 4, 5], np.uint32)
+    t = _dg().DyCuckoo(1000)
+    m = O.Map()
+    st = t.insert(to_dev(keys), to_dev(vals))
+    m.insert(keys, vals)
+    assert st["rejected"] == 2 and st["inserted"] == 3
+    assert_same_contents(t, m)
+    find_and_compare(t, m, np.array([0, 5, 9, 11, 12], np.uint32))
+    assert t.erase(to_dev(np.array([0, 0], np.uint32))) == 0
+    t.close()
+
+
+def test_empty_and_ragged_batches():
+    t = _dg().DyCuckoo(1000)
+    m = O.Map()
+    import torch
+    e = torch.empty(0, dtype=torch.int32, device="cuda")
+    t.insert(e, e)
+    out, _ = t.find(e)
+    assert out.numel() == 0
+    for n in (1, 31, 33, 1000, 4097):
+        k = unique_u32(n, seed=n)
+        t.insert(to_dev(k), to_dev(k + 1))
+        m.insert(k, k + 1)
+        find_and_compare(t, m, k, "ragged %d" % n)
+    assert_same_contents(t, m)
+    t.close()
+
+
+# ---------------------------------------------------------------- structure
+@pytest.mark.parametrize("bucket_bytes", [32, 64, 128])
+@pytest.mark.parametrize("d", [2, 3, 4, 5, 6])
+def test_placement_follows_reference_hashes(bucket_bytes, d):
+    n = 60_000
+    keys = unique_u32(n, seed=d * 131 + bucket_bytes)
+    t = _dg().DyCuckoo(int(n / 0.8), num_subtables=d, bucket_bytes=bucket_bytes, auto_resize=False)
+    m = O.Map()
+    t.insert(to_dev(keys), to_dev(keys ^ np.uint32(0x5A5A5A5A)))
+    m.insert(keys, keys ^ np.uint32(0x5A5A5A5A))
+    assert_same_contents(t, m, "d=%d sb=%d" % (d, bucket_bytes))
+    nb = t.layout()
+    seen = 0
+    for s in range(d):
+        sub = t.subtable(s)  # (buckets, slots) of key | value << 32
+        kk = (sub & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+        b_idx, _ = np.nonzero(kk)
+        rk = kk[kk != 0]
+        seen += rk.size
+        t1, b1, t2, b2 = O.hash_batch(rk, d, nb)
+        in1 = (t1 == s) & (b1 == b_idx)
+        in2 = (t2 == s) & (b2 == b_idx)
+        assert np.all(in1 | in2), "subtable %d holds keys outside their buckets" % s
+    assert seen == n
+    find_and_compare(t, m, keys[:5000])
+    t.close()
+
+
+def test_first_probe_serves_most_hits():
+    """Finds probe the first subtable of the pair first; the insert policy
+    keeps most keys there (so a hit costs one sector)."""
+    n = 1 << 18
+    keys = unique_u32(n, seed=99)
+    t = _dg().DyCuckoo(int(n / 0.9), auto_resize=False)
+    t.insert(to_dev(keys), to_dev(keys))
+    nb = t.layout()
+    first = 0
+    for s in range(4):
+        sub = t.subtable(s)
+        kk = (sub & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+        rk = kk[kk != 0]
+        first += int((first_probe_table(rk, 4, nb) == s).sum())
+    frac = first / n
+    assert frac > 0.75, frac
+    t.close()
+
+
+# ---------------------------------------------------------------- resizing
+def test_resize_sequence_matches_reference_policy():
+    n = 100_000
+    keys = unique_u32(n, seed=5)
+    vals = np.arange(n, dtype=np.uint32)
+    t = _dg().DyCuckoo(n * 2, auto_resize=False)
+    ref = O.RefCuckoo(n * 2, 4, 4)  # same bucket-count rule: 4 slots per 32-byte bucket
+    m = O.Map()
+    t.insert(to_dev(keys), to_dev(vals))
+    m.insert(keys, vals)
+    for step in range(5):
+        t.resize_up()
+        ref.resize_up()
+        assert t.layout() == list(ref.layout()), "up %d" % step
+        assert_same_contents(t, m, "after up %d" % step)
+        find_and_compare(t, m, keys[::7], "find after up %d" % step)
+    for step in range(7):
+        t.resize_down()
+        ref.resize_down()
+        assert t.layout() == [int(x) for x in ref.layout()], "down %d" % step
+        assert_same_contents(t, m, "after down %d" % step)
+        find_and_compare(t, m, keys[::7], "find after down %d" % step)
+    t.close()
+
+
+def test_downsize_into_full_subtables_never_drops():
+    """Halve subtables of a dense table: merged buckets overflow and the
+    leftovers are walked into other subtables (the reference drops them,
+    cuckoo.cu:714-722); an upsize happens when even that fails."""
+    n = 150_000
+    keys = unique_u32(n, seed=77)
+    t = _dg().DyCuckoo(int(n / 0.75), auto_resize=False)
+    m = O.Map()
+    t.insert(to_dev(keys), to_dev(keys + 3))
+    m.insert(keys, keys + 3)
+    for _ in range(3):
+        t.resize_down()
+        assert_same_contents(t, m, "dense downsize")
+    find_and_compare(t, m, keys, "after dense downsizes")
+    t.close()
+
+
+def test_eviction_overflow_upsizes_and_keeps_everything():
+    n = 50_000
+    keys = unique_u32(n, seed=8)
+    t = _dg().DyCuckoo(64, max_evictions=1, auto_resize=False)
+    m = O.Map()
+    cap0 = t.capacity
+    st = t.insert(to_dev(keys), to_dev(keys * np.uint32(3)))
+    m.insert(keys, keys * np.uint32(3))
+    assert st["overflowed"] > 0 and st["resizes_up"] > 0
+    assert t.capacity > cap0
+    assert_same_contents(t, m, "overflow")
+    t.close()
+
+
+def test_auto_resize_thresholds():
+    n = 1 << 16
+    keys = unique_u32(4 * n, seed=12)
+    t = _dg().DyCuckoo(n, auto_resize=True, min_downsize_capacity=0)
+    m = O.Map()
+    for i in range(4):
+        k = keys[i * n:(i + 1) * n]
+        t.insert(to_dev(k), to_dev(k))
+        m.insert(k, k)
+        assert t.size <= 0.8 * t.capacity + 1
+    assert_same_contents(t, m, "grown")
+    for i in range(4):
+        k = keys[i * n:(i + 1) * n]
+        t.erase(to_dev(k))
+        m.erase(k)
+        assert_same_contents(t, m, "shrinking %d" % i)
+    assert t.size == 0
+    t.close()
+
+
+# ---------------------------------------------------------------- 8-byte keys
+@pytest.mark.parametrize("value_bytes", [8, 4])
+@pytest.mark.parametrize("bucket_bytes", [32, 64, 128])
+def test_u64_keys(value_bytes, bucket_bytes):
+    import torch
+    n = 100_000
+    keys = unique_u64(n, seed=bucket_bytes + value_bytes)
+    vmask = np.uint64(0xFFFFFFFF) if value_bytes == 4 else np.uint64(0xFFFFFFFFFFFFFFFF)
+    vals = (keys * np.uint64(3)) & vmask
+    vals_dev = vals.astype(np.uint32) if value_bytes == 4 else vals
+    t = _dg().DyCuckoo(int(n / 0.8), key_bytes=8, value_bytes=value_bytes,
+                       bucket_bytes=bucket_bytes, auto_resize=False)
+    m = O.Map()
+    t.insert(to_dev(keys), to_dev(vals_dev))
+    m.insert(keys, vals)
+    assert_same_contents(t, m, "u64 insert")
+    q = np.concatenate([keys[: n // 2], unique_u64(n // 2, seed=991)])
+    find_and_compare(t, m, q, "u64 find")
+    er = keys[::3]
+    bits = torch.zeros((er.size + 31) // 32, dtype=torch.int32, device="cuda")
+    cnt = t.erase(to_dev(er), erased_bits=bits)
+    _, oh = m.erase(er)
+    assert cnt == int(oh.sum())
+    assert_same_contents(t, m, "u64 erase")
+    t.resize_up()
+    t.resize_down()
+    t.resize_down()
+    assert_same_contents(t, m, "u64 resizes")
+    # keys that share their low or high halves (fold collisions)
+    k2 = np.array([(1 << 32) | 5, (2 << 32) | 5, 5, (5 << 32), (7 << 32) | 7], np.uint64)
+    v2 = np.arange(5, dtype=np.uint64) + 1
+    t.insert(to_dev(k2), to_dev(v2.astype(np.uint32) if value_bytes == 4 else v2))
+    m.insert(k2, v2)
+    assert_same_contents(t, m, "u64 fold collisions")
+    t.close()
+
+
+# ------------------------------------------------ host-buffer C ABI forms
+def test_host_forms_match_device_forms():
+    n = 300_000
+    keys = unique_u32(2 * n, seed=21)
+    t = _dg().DyCuckoo(n * 2)
+    m = O.Map()
+    t.insert_host(keys[:n], keys[:n] + 1)
+    m.insert(keys[:n], keys[:n] + 1)
+    out = np.zeros(2 * n, np.uint32)
+    bits = np.zeros((2 * n + 31) // 32, np.uint32)
+    t.find_host(keys, out, bits)
+    ov, oh = m.find(keys)
+    assert np.array_equal(out.astype(np.uint64), ov)
+    assert np.array_equal(_bits_np(bits, 2 * n), oh)
+    cnt = t.erase_host(keys[n // 2: n + n // 2])
+    _, eh = m.erase(keys[n // 2: n + n // 2])
+    assert cnt == int(eh.sum())
+    assert_same_contents(t, m, "host forms")
+    t.close()
