@@ -257,7 +257,7 @@ def main():
     ap.add_argument("--log2-batch", type=int, default=26)
     ap.add_argument("--log2-cpu-sample", type=int, default=24)
     ap.add_argument("--bucket-bytes", type=int, default=32)
-    ap.add_argument("--max-evictions", type=int, default=256)
+    ap.add_argument("--max-evictions", type=int, default=2048)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-variants", action="store_true")
     args = ap.parse_args()
