@@ -46,7 +46,7 @@ EXPORTS = [
     "dyc_config_default", "dyc_create", "dyc_destroy", "dyc_insert", "dyc_find", "dyc_erase",
     "dyc_resize_up", "dyc_resize_down", "dyc_size", "dyc_capacity", "dyc_layout",
     "dyc_subtable", "dyc_export", "dyc_last_stats", "dyc_insert_host", "dyc_find_host",
-    "dyc_erase_host", "dyc_status_string", "dyc_last_error",
+    "dyc_erase_host", "dyc_status_string", "dyc_last_error", "dyc_erase_noalloc",
 ]
 
 _lock = threading.Lock()
@@ -75,6 +75,7 @@ def _declare(L):
         "dyc_insert_host": (st, [T, vp, vp, u64, u32]),
         "dyc_find_host": (st, [T, vp, vp, vp, u64]),
         "dyc_erase_host": (st, [T, vp, u64, vp, C.POINTER(u64)]),
+        "dyc_erase_noalloc": (st, [T, vp, u64, vp, C.POINTER(u64), u32, vp]),
         "dyc_status_string": (C.c_char_p, [st]),
         "dyc_last_error": (C.c_char_p, []),
     }

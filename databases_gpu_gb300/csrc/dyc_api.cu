@@ -671,3 +671,81 @@ dyc_status dyc_erase_host(dyc_table *t, const void *h_keys, uint64_t n,
 }
 
 }  // extern "C"
+
+// =============================================================================
+// dyc_erase_noalloc: erase whose batch-dedup table lives in a fixed device
+// array compiled into this file, for callers that must not allocate device
+// memory during the call (see include/dycuckoo.h).
+// =============================================================================
+#include <mutex>
+
+namespace {
+
+constexpr uint64_t kNoAllocMaxKeys = 1ull << 18;         // keys per call
+constexpr uint64_t kNoAllocCells = 2 * kNoAllocMaxKeys;  // dedup cells, a power of two
+// key cells (8 bytes each) followed by the op-index cells 8-byte keys need
+constexpr size_t kNoAllocBytes = (size_t)kNoAllocCells * 8 + (size_t)kNoAllocCells * 4;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+constexpr int kNoAllocMaxDevices = 256;
+void *g_noalloc_addr[kNoAllocMaxDevices];  // device address of the array, per device
+
+// One-time per-device set-up, with that device current: the array's name is
+// only a host-side stand-in, so kernels get the address the runtime reports.
+dyc_status noalloc_scratch(int device, void **out) {
+    if (device < 0 || device >= kNoAllocMaxDevices)
+        return fail(DYC_EINVAL, "device %d out of range for the no-alloc scratch", device);
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(DYC_ECUDA, "cudaGetSymbolAddress(no-alloc scratch) on device %d: %s",
+                        device, cudaGetErrorString(e));
+        g_noalloc_addr[device] = p;
+    }
+    *out = g_noalloc_addr[device];
+    return DYC_OK;
+}
+
+}  // namespace
+
+extern "C" dyc_status dyc_erase_noalloc(dyc_table *t, const void *d_keys, uint64_t n,
+                                        uint32_t *d_erased_bits_out, uint64_t *h_erased_count,
+                                        uint32_t flags, void *stream) {
+    if (!t) return fail(DYC_EINVAL, "null table");
+    if (h_erased_count) *h_erased_count = 0;
+    if (n > kNoAllocMaxKeys)
+        return fail(DYC_EINVAL, "dyc_erase_noalloc takes at most %llu keys per call, got %llu",
+                    (unsigned long long)kNoAllocMaxKeys, (unsigned long long)n);
+    if (n == 0) return DYC_OK;
+    if (!d_keys) return fail(DYC_EINVAL, "null key array");
+    TRY(set_device(t));
+    void *base = nullptr;
+    TRY(noalloc_scratch(t->device, &base));
+    cudaStream_t s = (cudaStream_t)stream;
+    Scratch S{};
+    S.dedup = base;
+    S.dedup_cap = kNoAllocCells;
+    S.dedup_idx = t->kb == 8 ? (uint32_t *)((char *)base + kNoAllocCells * 8) : nullptr;
+    const bool use_dedup = !(flags & DYC_FLAG_UNIQUE) && n > 1;
+    t->last = dyc_op_stats{};
+    TRY(reset_call_counters(t, s));
+    if (use_dedup) {
+        // the array keeps the previous call's cells: clear the ones used
+        CK(cudaMemsetAsync(S.dedup, 0, (size_t)kNoAllocCells * 8, s));
+        if (S.dedup_idx) CK(cudaMemsetAsync(S.dedup_idx, 0xFF, (size_t)kNoAllocCells * 4, s));
+        cudaError_t e = KB_CALL(t, dedup, ctx(t, s), S, d_keys, n, dyc::kKeepFirst);
+        if (e != cudaSuccess) return fail(DYC_ECUDA, "dedup kernel: %s", cudaGetErrorString(e));
+    }
+    cudaError_t e = KB_CALL(t, erase, ctx(t, s), t->D, t->sb, S, use_dedup, d_keys, n,
+                            d_erased_bits_out, t->d_ctr);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "erase kernel: %s", cudaGetErrorString(e));
+    TRY(read_counters(t, s));
+    t->last.erased = t->h_ctr->erased;
+    t->last.superseded = t->h_ctr->superseded;
+    if (h_erased_count) *h_erased_count = t->h_ctr->erased;
+    return DYC_OK;
+}

@@ -170,6 +170,32 @@ dyc_status dyc_find_host(dyc_table *t, const void *h_keys, void *h_vals_out,
 dyc_status dyc_erase_host(dyc_table *t, const void *h_keys, uint64_t n,
                           uint32_t *h_erased_bits_out, uint64_t *erased_count);
 
+/* Erase that allocates nothing. It has no counterpart in the reference.
+ *
+ * For callers that must not allocate device memory while they run: a host
+ * engine whose own allocator owns every byte of HBM (a buffer pool sized to
+ * the device, or an admission budget that counts each allocation), or a
+ * latency-bound request path that cannot take the device-wide
+ * synchronisation cudaMalloc/cudaFree may cause. dyc_erase takes its
+ * batch-dedup table from scratch the table allocates on demand; this form
+ * takes it from one fixed device array compiled into the library instead
+ * (6 MiB, held on every device that loads the library until the process
+ * exits), and it never downsizes (a downsize allocates).
+ *
+ *   - at most 262144 keys per call; a larger n returns DYC_EINVAL and does
+ *     nothing;
+ *   - the first call on a device looks up the array's device address (a
+ *     one-time set-up per device); make that first call before any stream
+ *     capture;
+ *   - every call shares the one array and clears what it needs first, so
+ *     calls that overlap on the GPU (on different streams or host threads,
+ *     for any tables) race and must be serialised by the caller;
+ *   - results, erased bits, count and flags are as for dyc_erase, with
+ *     DYC_FLAG_NO_RESIZE always in effect. */
+dyc_status dyc_erase_noalloc(dyc_table *t, const void *d_keys, uint64_t n,
+                             uint32_t *d_erased_bits_out, uint64_t *h_erased_count,
+                             uint32_t flags, void *stream);
+
 const char *dyc_status_string(dyc_status s);
 const char *dyc_last_error(void);
 
