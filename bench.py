@@ -256,10 +256,12 @@ def main():
     ap.add_argument("--log2-keys", type=int, default=28)
     ap.add_argument("--log2-batch", type=int, default=26)
     ap.add_argument("--log2-cpu-sample", type=int, default=24)
-    ap.add_argument("--bucket-bytes", type=int, default=32)
+    ap.add_argument("--bucket-bytes", type=int, default=128)
     ap.add_argument("--max-evictions", type=int, default=2048)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-variants", action="store_true")
+    ap.add_argument("--mixes", default="uniform100,uniform10,zipf100,zipf10",
+                    help="query mixes to time; the first is the headline")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -309,7 +311,8 @@ def main():
             hit[pos] = False
         return as_i32(q, torch), expv, hit
 
-    mixes = ["uniform100"] if args.skip_variants else ["uniform100", "uniform10", "zipf100", "zipf10"]
+    mixes = ["uniform100"] if args.skip_variants else args.mixes.split(",")
+    assert mixes[0] == "uniform100", "the headline mix is uniform100"
     out = torch.empty(Q, dtype=torch.int32, device=dev)
     bits = torch.empty(Q // 32, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream()

@@ -86,13 +86,16 @@ def _declare(L):
 
 
 def lib(path: str | None = None):
-    """Load (building first if needed) and return the C library."""
+    """Load (building first if needed) and return the C library.
+
+    DYCUCKOO_LIB names a prebuilt libdycuckoo.so to load instead of the
+    in-tree one (for example a build with other launch parameters)."""
     global _lib
     with _lock:
         if _lib is not None:
             return _lib
-        p = path or _build.LIB
-        if not os.path.exists(p) or not _build.up_to_date(p):
+        p = path or os.environ.get("DYCUCKOO_LIB") or _build.LIB
+        if p == _build.LIB and (not os.path.exists(p) or not _build.up_to_date(p)):
             _build.build()
         L = C.CDLL(p)
         _declare(L)
@@ -101,7 +104,7 @@ def lib(path: str | None = None):
 
 
 def library_path() -> str:
-    return _build.LIB
+    return os.environ.get("DYCUCKOO_LIB") or _build.LIB
 
 
 class DycError(RuntimeError):

@@ -298,6 +298,9 @@ dyc_status resize_down_impl(dyc_table *t, cudaStream_t s) {
         CK(cudaMemsetAsync(nw, 0, (size_t)nnb * t->sb, s));
         e = KB_CALL(t, collect, ctx(t, s), t->sb, old, onb, la, &t->d_ctr->pending, list_cap,
                     &t->d_ctr->spill);
+        // keys of other subtables may have had their first-probe bucket here:
+        // start every new bucket with its overflow bit set
+        if (e == cudaSuccess) e = KB_CALL(t, mark_all, ctx(t, s), t->sb, nw, nnb);
     }
     if (e != cudaSuccess) return fail(DYC_ECUDA, "downsize kernel: %s", cudaGetErrorString(e));
     t->D.sub[ti] = nw;
@@ -340,7 +343,7 @@ void dyc_config_default(dyc_config *cfg) {
     cfg->key_bytes = 4;
     cfg->value_bytes = 4;
     cfg->num_subtables = 4;
-    cfg->bucket_bytes = 32;
+    cfg->bucket_bytes = 128;
     cfg->max_evictions = 64;
     cfg->auto_resize = 1;
     cfg->initial_size = 1024;
@@ -377,7 +380,8 @@ dyc_status dyc_create(const dyc_config *cfg, dyc_table **out) {
     t->vb = (int)cfg->value_bytes;
     t->sb = (int)cfg->bucket_bytes;
     t->slot_bytes = t->kb == 4 ? 8 : 16;
-    t->slots = t->sb / t->slot_bytes;
+    // 128-byte buckets keep their last slot as the metadata word
+    t->slots = t->sb / t->slot_bytes - (t->sb == 128 ? 1 : 0);
     t->device = cfg->device;
     auto undo = [&](dyc_status s) {
         dyc_destroy(t);

@@ -66,13 +66,15 @@ __host__ __device__ __forceinline__ uint64_t fastmod_magic(uint32_t d) {
 __device__ __forceinline__ uint32_t fastmod(uint32_t a, uint64_t magic, uint32_t d) {
     return (uint32_t)__umul64hi(magic * a, d);
 }
+// Branch-free: lanes of a warp ask for different subtables, and a switch on
+// t would run all four hash paths one after another. All four are computed
+// (the compiler shares them between the two buckets of a key) and one is
+// selected; hash3 already ends in % kPrime, so the common % is a no-op for it.
 __device__ __forceinline__ uint32_t subtable_hash(uint32_t hk, uint32_t t) {
-    switch (t & 3u) {
-    case 0: return hash1(hk) % kPrime;
-    case 1: return hash2(hk) % kPrime;
-    case 2: return hash3(hk);
-    default: return hash4(hk) % kPrime;
-    }
+    const uint32_t a = hash1(hk), b = hash2(hk), c = hash3(hk), e = hash4(hk);
+    const uint32_t lo = (t & 1u) ? b : a;
+    const uint32_t hi = (t & 1u) ? e : c;
+    return ((t & 2u) ? hi : lo) % kPrime;
 }
 
 // 64-bit keys fold to the 32-bit hash input; equality uses all 64 bits.
@@ -245,29 +247,61 @@ __device__ __forceinline__ void st_v8(void *p, const uint32_t (&w)[8]) {
                  : "memory");
 }
 
-// A whole bucket in registers.
+__device__ __forceinline__ void ld_ca(const void *p, uint32_t (&w)[8]) {
+    asm volatile("ld.global.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]),
+                   "=r"(w[6]), "=r"(w[7])
+                 : "l"(p));
+}
+
+// ----------------------------------------------------------------------------
+// Bucket geometry. A bucket of SB bytes is SB/32 chunks of 32 bytes. A group
+// of kG = SB/32 lanes reads one bucket with one 256-bit load per lane (lane r
+// of the group reads chunk r), so a warp instruction fetches 32/kG whole
+// buckets and every DRAM line it touches is used in full.
+//
+// A 128-byte bucket keeps its last slot as a metadata word; bit 0 (the
+// overflow bit) is set once any key whose first-probe bucket this is has been
+// stored in its second bucket. While it is clear, a key missing from this
+// bucket is missing from the table, and a find or erase stops after one
+// probe. Bits are only ever set (erase leaves them), so a set bit is a hint
+// that costs one extra probe, never a wrong answer.
+// ----------------------------------------------------------------------------
+constexpr unsigned long long kOverflowBit = 1ull;
+
+template <int KB, int SB> struct Geo {
+    using T = SlotT<KB>;
+    static constexpr int kG = SB / 32;             // lanes per bucket
+    static constexpr int kRoundOps = 32 / kG;      // buckets per warp instruction
+    static constexpr int kSPC = 32 / T::kBytes;    // slots per 32-byte chunk
+    static constexpr int kTotal = SB / T::kBytes;  // slots including the metadata slot
+    static constexpr int kMeta = SB == 128 ? 1 : 0;
+    static constexpr int kSlots = kTotal - kMeta;  // slots that hold entries
+};
+
+template <int KB, int SB>
+__device__ __forceinline__ unsigned long long *meta_ptr(char *bucket) {
+    return reinterpret_cast<unsigned long long *>(bucket + (Geo<KB, SB>::kTotal - 1) * SlotT<KB>::kBytes);
+}
+
+// A whole bucket in one thread's registers (streaming kernels: resize, export).
 template <int KB, int SB> struct Bucket {
     using T = SlotT<KB>;
     using S = typename T::S;
-    static constexpr int kSlots = SB / T::kBytes;
+    using G = Geo<KB, SB>;
+    static constexpr int kSlots = G::kSlots;
     static constexpr int kChunks = SB / 32;
-    static constexpr int kPerChunk = 32 / T::kBytes;
-    S s[kSlots];
+    static constexpr int kPerChunk = G::kSPC;
+    S s[G::kTotal];
 
-    __device__ __forceinline__ void load_nc(const void *p) {
+    template <int MODE>  // 0: default caching, 1: read-only no-allocate, 2: L2 only
+    __device__ __forceinline__ void load(const void *p) {
 #pragma unroll
         for (int c = 0; c < kChunks; ++c) {
             uint32_t w[8];
-            ld_nc((const char *)p + 32 * c, w);
-#pragma unroll
-            for (int j = 0; j < kPerChunk; ++j) T::from_words(w + j * (T::kBytes / 4), s[c * kPerChunk + j]);
-        }
-    }
-    __device__ __forceinline__ void load_cg(const void *p) {
-#pragma unroll
-        for (int c = 0; c < kChunks; ++c) {
-            uint32_t w[8];
-            ld_cg((const char *)p + 32 * c, w);
+            if (MODE == 0) ld_ca((const char *)p + 32 * c, w);
+            else if (MODE == 1) ld_nc((const char *)p + 32 * c, w);
+            else ld_cg((const char *)p + 32 * c, w);
 #pragma unroll
             for (int j = 0; j < kPerChunk; ++j) T::from_words(w + j * (T::kBytes / 4), s[c * kPerChunk + j]);
         }
@@ -281,20 +315,18 @@ template <int KB, int SB> struct Bucket {
             st_v8((char *)p + 32 * c, w);
         }
     }
-    // slot index holding key k, or -1
-    __device__ __forceinline__ int find(typename T::K k) const {
-        int at = -1;
-#pragma unroll
-        for (int j = kSlots - 1; j >= 0; --j)
-            if (T::key(s[j]) == k) at = j;
-        return at;
-    }
     __device__ __forceinline__ unsigned empty_mask() const {
         unsigned m = 0;
 #pragma unroll
         for (int j = 0; j < kSlots; ++j)
             if (T::is_empty(s[j])) m |= 1u << j;
         return m;
+    }
+    __device__ __forceinline__ unsigned long long meta() const {
+        if (!G::kMeta) return 0ull;
+        uint32_t w[4];
+        T::to_words(s[G::kTotal - 1], w);
+        return (unsigned long long)w[0] | ((unsigned long long)w[1] << 32);
     }
 };
 

@@ -86,6 +86,8 @@ template <int KB> struct Ops {
     static cudaError_t collect(const LaunchCtx &L, int sb, const void *sub, uint32_t nb,
                                void *list, unsigned long long *list_count, uint64_t list_cap,
                                unsigned long long *spill);
+    // set the overflow bit of every bucket of a subtable
+    static cudaError_t mark_all(const LaunchCtx &L, int sb, void *sub, uint32_t nb);
     static cudaError_t export_all(const LaunchCtx &L, const Desc &D, int sb, void *keys,
                                   void *vals, uint32_t vb, uint64_t cap,
                                   unsigned long long *count);

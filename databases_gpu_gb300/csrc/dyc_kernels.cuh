@@ -2,25 +2,33 @@
 // key width KB (4 or 8 bytes) and bucket size SB (32, 64 or 128 bytes).
 //
 // Design (GB300):
-//   * One thread per op; a bucket is one to four 32-byte sectors read with
-//     256-bit loads, so a probe costs exactly the sectors of its bucket.
-//     (The reference uses 16-lane groups over 128-byte buckets:
-//     GPU/dyhash/cuckoo.cu:365-520.)
-//   * Loops are warp-uniform (every lane of a warp runs the same iterations),
-//     so ballots and warp-aggregated counters always use the full mask.
+//   * A random DRAM access on this part moves a whole 128-byte line and the
+//     part sustains about 5e10 of them per second whatever their size, so a
+//     128-byte bucket (one line) costs the same as a 32-byte one and holds 4x
+//     the entries. A bucket is read by a group of SB/32 lanes, one 256-bit
+//     load each; a warp instruction therefore fetches whole lines (a single
+//     thread issuing four loads to one line runs four times slower).
+//   * Every lane owns one op; probe() serves the ops of a warp round by
+//     round and hands each owner the facts about its bucket (matching slot,
+//     empty slots, metadata word). Reads need cooperation; the atomics that
+//     follow are per-owner.
+//   * Loops are warp-uniform (all 32 lanes run the same iterations), so
+//     shuffles and ballots always use the full mask.
 //   * Insert runs in phases separated by kernel boundaries: (1) resolve
 //     repeated keys of the batch, (2) update present keys / claim empty
 //     slots -- nothing moves while keys are being searched, (3) eviction
 //     walks for the ops whose two buckets were full. Phase 3 only places keys
-//     known to be absent, so a concurrently evicted entry can never be
-//     mistaken for a missing key.
-//   * Every loop is bounded: probe loops by the table size, eviction walks by
-//     max_evict. Nothing spins on another thread.
+//     known to be absent, so an entry in flight can never be mistaken for a
+//     missing key.
+//   * Every loop is bounded: probe loops by the table size, walks by the
+//     eviction bound. Nothing spins on another thread.
 #pragma once
 
 #include "dyc_device.cuh"
 
 namespace dyc {
+
+constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ uint64_t warp_base() {
     return (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) << 5;
@@ -29,48 +37,321 @@ __device__ __forceinline__ uint64_t warp_stride() {
     return ((uint64_t)gridDim.x * blockDim.x) & ~31ull;
 }
 
-// Slot j of a register bucket, selected without dynamic register indexing.
-template <int KB, int SB>
-__device__ __forceinline__ typename SlotT<KB>::S slot_at(const Bucket<KB, SB> &b, int j) {
-    typename SlotT<KB>::S r = SlotT<KB>::empty();
-#pragma unroll
-    for (int q = 0; q < Bucket<KB, SB>::kSlots; ++q)
-        if (q == j) r = b.s[q];
-    return r;
-}
-
 template <int KB, int SB>
 __device__ __forceinline__ typename SlotT<KB>::S *slot_ptr(char *bucket, int j) {
     return reinterpret_cast<typename SlotT<KB>::S *>(bucket + j * SlotT<KB>::kBytes);
 }
 
-// Value of key k in bucket b; returns whether it was there.
-template <int KB, int SB>
-__device__ __forceinline__ bool bucket_get(const Bucket<KB, SB> &b, typename SlotT<KB>::K k,
-                                           uint64_t &v) {
-    bool hit = false;
-#pragma unroll
-    for (int q = 0; q < Bucket<KB, SB>::kSlots; ++q)
-        if (SlotT<KB>::key(b.s[q]) == k) {
-            hit = true;
-            v = SlotT<KB>::val(b.s[q]);
-        }
-    return hit;
+__device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src) {
+    return __shfl_sync(kFull, v, src);
+}
+__device__ __forceinline__ unsigned long long shfl_slot(unsigned long long v, int src) {
+    return shfl64(v, src);
+}
+__device__ __forceinline__ u128 shfl_slot(u128 v, int src) {
+    return {shfl64(v.lo, src), shfl64(v.hi, src)};
 }
 
-// Claim an empty slot of the bucket at p (snapshot b) for e with CAS.
+// Claim the first empty slot of `mask` in the bucket at p for e (CAS).
 template <int KB, int SB>
-__device__ __forceinline__ bool try_empty(char *p, const Bucket<KB, SB> &b,
-                                          const typename SlotT<KB>::S &e) {
+__device__ __forceinline__ bool claim_empty(char *p, unsigned mask, const typename SlotT<KB>::S &e) {
     using T = SlotT<KB>;
-#pragma unroll
-    for (int q = 0; q < Bucket<KB, SB>::kSlots; ++q) {
-        if (T::is_empty(b.s[q])) {
-            typename T::S old = T::cas(slot_ptr<KB, SB>(p, q), T::empty(), e);
-            if (T::same(old, T::empty())) return true;
-        }
+#pragma unroll 1
+    while (mask) {
+        const int j = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const typename T::S old = T::cas(slot_ptr<KB, SB>(p, j), T::empty(), e);
+        if (T::same(old, T::empty())) return true;
     }
     return false;
+}
+
+// The first-probe bucket of an entry's key.
+template <int KB, int SB>
+__device__ __forceinline__ char *first_bucket(const Desc &D, typename SlotT<KB>::K k, Pair &pr,
+                                              uint32_t &hk) {
+    hk = fold(k);
+    pr = pair_of(hk, D.d);
+    return bucket_ptr<KB, SB>(D, pr.first, bucket_index(D, pr.first, hk));
+}
+
+// Mark the entry's first-probe bucket before storing it anywhere else.
+template <int KB, int SB>
+__device__ __forceinline__ void mark_overflow(char *first) {
+    if (Geo<KB, SB>::kMeta) atomicOr(meta_ptr<KB, SB>(first), kOverflowBit);
+}
+
+// ----------------------------------------------------------------------------
+// Cooperative bucket probe. Each lane owns one op: bucket pointer p, key
+// `key`, flag `act`, and the subtable `t` the bucket belongs to. The ops of
+// a warp are served in kG rounds; in round q the group of kG lanes g reads
+// the bucket of op q*(32/kG)+g, one 32-byte chunk per lane. The group
+// combines its per-lane facts with an xor butterfly (log2 kG shuffles) and
+// the owner collects them:
+//   match / mslot : lowest slot holding `key` (-1 if none) and its content
+//   empty         : mask of empty entry slots            (WANT_EMPTY)
+//   pref          : mask of slots whose resident's first-probe subtable is
+//                   not t, i.e. residents in their second bucket (WANT_PREF)
+//   meta          : the bucket's metadata word (0 without one)
+// MODE 1 reads through the read-only path (nobody writes the table during
+// the kernel), MODE 2 through L2 (other lanes update it with atomics).
+// All 32 lanes must call it.
+// ----------------------------------------------------------------------------
+template <int KB> struct ProbeOut {
+    int match;
+    typename SlotT<KB>::S mslot;
+    unsigned empty, pref;
+    unsigned long long meta;
+};
+
+// Position of the n-th (0-based) set bit of m; m must have more than n bits.
+__host__ __device__ __forceinline__ int nth_set(unsigned m, int n) {
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const unsigned low = m & ((1u << w) - 1u);
+#ifdef __CUDA_ARCH__
+        const int cnt = __popc(low);
+#else
+        const int cnt = __builtin_popcount(low);
+#endif
+        if (n >= cnt) {
+            n -= cnt;
+            m >>= w;
+            pos += w;
+        } else {
+            m = low;
+        }
+    }
+    return pos;
+}
+
+template <int G> __device__ __forceinline__ unsigned group_or(unsigned v) {
+#pragma unroll
+    for (int off = 1; off < G; off <<= 1) v |= __shfl_xor_sync(kFull, v, off);
+    return v;
+}
+
+template <int KB, int SB, int MODE, bool WANT_EMPTY, bool WANT_PREF>
+__device__ __forceinline__ ProbeOut<KB> probe(const char *p, typename SlotT<KB>::K key, bool act,
+                                              uint32_t t, uint32_t d) {
+    using T = SlotT<KB>;
+    using Sl = typename T::S;
+    using K = typename T::K;
+    using Gm = Geo<KB, SB>;
+    constexpr int G = Gm::kG, RO = Gm::kRoundOps, SPC = Gm::kSPC, WPS = T::kBytes / 4;
+    const int lane = threadIdx.x & 31;
+    const int g = lane / G, r = lane % G;  // group and chunk this lane serves
+    // Active ops are served in compacted order: op with rank c (among the
+    // active lanes) is read in round c / RO by group c % RO, so a probe with
+    // few active ops costs few rounds.
+    const unsigned am = __ballot_sync(kFull, act);
+    const bool all = am == kFull;
+    const int nact = __popc(am);
+    const int rounds = (nact + RO - 1) / RO;
+    const int c = all ? lane : __popc(am & ((1u << lane) - 1u));
+    const int my_q = act ? c / RO : -1, my_g = c % RO;
+
+    ProbeOut<KB> out;
+    out.match = -1;
+    out.mslot = T::empty();
+    out.empty = 0u;
+    out.pref = 0u;
+    out.meta = 0ull;
+    // one round's loads per batch: fewer registers, more resident warps, and
+    // more lines in flight per SM than batching rounds (measured on GB300)
+    constexpr int QB = 1;
+#pragma unroll 1
+    for (int q0 = 0; q0 < rounds; q0 += QB) {
+        uint32_t w[QB][8];
+        int src[QB];
+#pragma unroll
+        for (int qq = 0; qq < QB; ++qq) {
+            const int ci = (q0 + qq) * RO + g;  // rank of the op this group reads
+            const bool have = ci < nact;
+            src[qq] = all ? ci : (have ? nth_set(am, ci) : lane);
+            const unsigned long long pq = shfl64((unsigned long long)p, src[qq]);
+            if (have) {
+                const char *cp = (const char *)pq + r * 32;
+                if (MODE == 1) ld_nc(cp, w[qq]);
+                else ld_cg(cp, w[qq]);
+            } else {
+#pragma unroll
+                for (int x = 0; x < 8; ++x) w[qq][x] = 0u;
+            }
+        }
+#pragma unroll
+        for (int qq = 0; qq < QB; ++qq) {
+            const int q = q0 + qq;
+            if (q >= rounds) break;  // uniform across the warp
+            const bool have = q * RO + g < nact;
+            const K kq = (KB == 4) ? (K)__shfl_sync(kFull, (uint32_t)key, src[qq])
+                                   : (K)shfl64((unsigned long long)key, src[qq]);
+            Sl s[SPC];
+#pragma unroll
+            for (int j = 0; j < SPC; ++j) T::from_words(w[qq] + j * WPS, s[j]);
+            unsigned mb = 0u, eb = 0u, pb = 0u;
+            uint32_t tq = 0u;
+            if (WANT_PREF) tq = __shfl_sync(kFull, t, src[qq]);
+#pragma unroll
+            for (int j = 0; j < SPC; ++j) {
+                const int idx = r * SPC + j;
+                if (idx < Gm::kSlots) {
+                    if (T::key(s[j]) == kq) mb |= 1u << idx;
+                    if (WANT_EMPTY && T::is_empty(s[j])) eb |= 1u << idx;
+                    if (WANT_PREF && !T::is_empty(s[j]) &&
+                        pair_of(fold(T::key(s[j])), d).first != tq)
+                        pb |= 1u << idx;
+                }
+            }
+            if (!have) mb = eb = pb = 0u;
+            const unsigned gmb = group_or<G>(mb);  // the group's match mask
+            // content of the group's lowest matching slot, from the lane holding it
+            const int jm = gmb ? __ffs(gmb) - 1 : 0;
+            const int lj = jm % SPC;
+            Sl sel = s[0];
+#pragma unroll
+            for (int j = 1; j < SPC; ++j)
+                if (j == lj) sel = s[j];
+            const Sl gslot = shfl_slot(sel, g * G + jm / SPC);
+            // deliver to the owners served in round q (from their group's lead)
+            const int lead = my_g * G;
+            const unsigned omb = __shfl_sync(kFull, gmb, lead);
+            const Sl oslot = shfl_slot(gslot, lead);
+            unsigned oe = 0u, op = 0u;
+            if (WANT_EMPTY) oe = __shfl_sync(kFull, group_or<G>(eb), lead);
+            if (WANT_PREF) op = __shfl_sync(kFull, group_or<G>(pb), lead);
+            unsigned long long ometa = 0ull;
+            if (Gm::kMeta) {
+                uint32_t mw[4];
+                T::to_words(s[SPC - 1], mw);
+                ometa = shfl64((unsigned long long)mw[0] | ((unsigned long long)mw[1] << 32),
+                               lead + G - 1);
+            }
+            if (my_q == q) {
+                if (omb) {
+                    out.match = __ffs(omb) - 1;
+                    out.mslot = oslot;
+                }
+                out.empty = oe;
+                out.pref = op;
+                out.meta = ometa;
+            }
+        }
+    }
+    return out;
+}
+
+// ----------------------------------------------------------------------------
+// Staged probe for find and erase. The buckets of a warp's ops are copied
+// into a warp-private shared-memory stage with cp.async (the destination is
+// shared memory, so no registers are held while the loads are in flight and
+// all rounds are in flight at once); then every lane scans its own bucket.
+// Global reads stay line-shaped: in round q the group of kG lanes g copies
+// the bucket of op q*(32/kG)+g, lane r the 16-byte pieces r and r+kG, so one
+// instruction fetches the first half of 32/kG buckets and the next the
+// second half. The 16-byte pieces of a bucket are XOR-swizzled by the
+// owner's lane so that the scan's 16-byte shared loads are conflict-free.
+// ----------------------------------------------------------------------------
+struct KvOut {
+    int match;
+    uint64_t value;
+    bool overflow;
+};
+
+constexpr int kBlockThreads = 256;
+constexpr int kWarpsPerBlock = kBlockThreads / 32;
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+
+template <int SB> __device__ __forceinline__ uint32_t piece_off(int o, int s) {
+    constexpr int P = SB / 16;  // 16-byte pieces per bucket
+    return (uint32_t)(o * SB + ((s ^ (o & (P - 1))) * 16));
+}
+
+// Copy the bucket at p of every active lane into stage (lane-indexed).
+// ALL: every lane is active; otherwise active lanes are served in rank order
+// so few active lanes cost few rounds.
+template <int SB, bool ALL>
+__device__ __forceinline__ void stage_rounds(const char *p, unsigned am, unsigned char *stage) {
+    constexpr int G = SB / 32, RO = 32 / G;
+    const int lane = threadIdx.x & 31, g = lane / G, r = lane % G;
+    const int nact = ALL ? 32 : __popc(am);
+    const int rounds = ALL ? G : (nact + RO - 1) / RO;
+    const uint32_t base = (uint32_t)__cvta_generic_to_shared(stage);
+#pragma unroll 1
+    for (int q = 0; q < rounds; ++q) {
+        const int ci = q * RO + g;
+        const bool have = ALL ? true : ci < nact;
+        const int o = ALL ? ci : (have ? nth_set(am, ci) : lane);
+        const unsigned long long pq = shfl64((unsigned long long)p, o);
+        if (have) {
+            cp_async16(base + piece_off<SB>(o, r), (const char *)pq + r * 16);
+            cp_async16(base + piece_off<SB>(o, r + G), (const char *)pq + (r + G) * 16);
+        }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncwarp();  // other lanes' copies are visible after the warp barrier
+}
+
+template <int KB, int SB>
+__device__ __forceinline__ KvOut probe_staged(const char *p, typename SlotT<KB>::K key, bool act,
+                                              unsigned char *stage) {
+    using T = SlotT<KB>;
+    using Gm = Geo<KB, SB>;
+    constexpr int P = SB / 16, SPP = 16 / T::kBytes > 0 ? 16 / T::kBytes : 1;
+    const unsigned am = __ballot_sync(kFull, act);
+    __syncwarp();  // the previous use of the stage is finished in every lane
+    if (am == kFull) stage_rounds<SB, true>(p, am, stage);
+    else if (am) stage_rounds<SB, false>(p, am, stage);
+    KvOut out{-1, 0ull, false};
+    if (!act) return out;
+    const int lane = threadIdx.x & 31;
+    const uint32_t base = (uint32_t)__cvta_generic_to_shared(stage);
+#pragma unroll
+    for (int s = 0; s < P; ++s) {
+        uint32_t v[4];
+        asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];"
+                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
+                     : "r"(base + piece_off<SB>(lane, s)));
+#pragma unroll
+        for (int j = 0; j < SPP; ++j) {
+            const int idx = s * SPP + j;
+            typename T::S sl;
+            T::from_words(v + j * (T::kBytes / 4), sl);
+            if (idx < Gm::kSlots) {
+                if (out.match < 0 && T::key(sl) == key) {
+                    out.match = idx;
+                    out.value = T::val(sl);
+                }
+            } else if (Gm::kMeta && idx == Gm::kTotal - 1) {
+                out.overflow = (v[j * (T::kBytes / 4)] & 1u) != 0u;
+            }
+        }
+    }
+    return out;
+}
+
+// Key/value probe used by find and erase: staged for 64- and 128-byte
+// buckets; 32-byte buckets (one lane per bucket, a single 256-bit load) read
+// straight into registers, since staging them would split each sector over
+// two 16-byte copies.
+template <int KB, int SB, int MODE>
+__device__ __forceinline__ KvOut kv_probe(const char *p, typename SlotT<KB>::K key, bool act,
+                                          unsigned char *stage) {
+    if constexpr (SB >= 64) {
+        return probe_staged<KB, SB>(p, key, act, stage);
+    } else {
+        const ProbeOut<KB> r = probe<KB, SB, MODE, false, false>(p, key, act, 0u, 0u);
+        KvOut o;
+        o.match = r.match;
+        o.value = SlotT<KB>::val(r.mslot);
+        o.overflow = false;
+        return o;
+    }
 }
 
 // ----------------------------------------------------------------------------
@@ -140,8 +421,9 @@ template <> struct Dedup<8> {
 };
 
 template <int KB>
-__global__ void __launch_bounds__(256) k_dedup(const __grid_constant__ Scratch S, const void *__restrict__ keys,
-                                               uint64_t n, DedupMode mode) {
+__global__ void __launch_bounds__(256) k_dedup(const __grid_constant__ Scratch S,
+                                               const void *__restrict__ keys, uint64_t n,
+                                               DedupMode mode) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         typename SlotT<KB>::K k = load_key<KB>(keys, i);
@@ -150,100 +432,112 @@ __global__ void __launch_bounds__(256) k_dedup(const __grid_constant__ Scratch S
 }
 
 // ----------------------------------------------------------------------------
-// find: probe the first subtable of the key's pair, then the second
-// (cuckoo_search, cuckoo.cu:460-520). Writes the value (0 on a miss) and one
-// hit bit per key.
+// find (cuckoo_search, cuckoo.cu:460-520): probe the first-probe bucket; probe
+// the second one only on a miss whose first bucket has its overflow bit set
+// (32/64-byte buckets carry no metadata and always probe both on a miss).
+// Writes the value (0 on a miss) and one hit bit per key. (Queueing second
+// probes per warp, or prefetching the next tile's keys, measured slower.)
 // ----------------------------------------------------------------------------
 template <int KB, int SB>
-__global__ void __launch_bounds__(256) k_find(const __grid_constant__ Desc D, const void *__restrict__ keys,
+__global__ void __launch_bounds__(256) k_find(const __grid_constant__ Desc D,
+                                              const void *__restrict__ keys,
                                               void *__restrict__ vals, uint32_t vb,
                                               uint32_t *__restrict__ hits, uint64_t n) {
     using T = SlotT<KB>;
+    using Gm = Geo<KB, SB>;
+    __shared__ __align__(128) unsigned char s_stage[kWarpsPerBlock][32 * SB];
+    unsigned char *stage = s_stage[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t step = warp_stride();
     for (uint64_t base = warp_base(); base < n; base += step) {
         const uint64_t i = base + lane;
         typename T::K k = 0;
         if (i < n) k = load_key<KB>(keys, i);
-        bool hit = false;
-        uint64_t v = 0;
-        if (k != 0) {
-            const uint32_t hk = fold(k);
-            const Pair p = pair_of(hk, D.d);
-            Bucket<KB, SB> b;
-            b.load_nc(bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk)));
-            hit = bucket_get(b, k, v);
-            if (!hit) {
-                b.load_nc(bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk)));
-                hit = bucket_get(b, k, v);
+        const bool act = k != 0;
+        const uint32_t hk = fold(k);
+        const Pair p = pair_of(hk, D.d);
+        const char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
+        const KvOut r1 = kv_probe<KB, SB, 1>(p1, k, act, stage);
+        bool hit = act && r1.match >= 0;
+        uint64_t v = hit ? r1.value : 0ull;
+        const bool need2 = act && !hit && (!Gm::kMeta || r1.overflow);
+        if (__any_sync(kFull, need2)) {
+            const char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
+            const KvOut r2 = kv_probe<KB, SB, 1>(p2, k, need2, stage);
+            if (need2 && r2.match >= 0) {
+                hit = true;
+                v = r2.value;
             }
         }
         if (i < n) store_val(vals, vb, i, v);
-        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        const unsigned m = __ballot_sync(kFull, hit);
         if (hits != nullptr && lane == 0) hits[base >> 5] = m;
     }
 }
 
 // ----------------------------------------------------------------------------
 // insert phase 2: update present keys in place, else claim an empty slot in
-// the first or second bucket; ops with both buckets full go to list_a.
+// the first-probe bucket, else in the second (marking the first bucket's
+// overflow bit first); ops left without a slot go to list_a.
 // ----------------------------------------------------------------------------
 template <int KB, int SB>
-__global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D, const __grid_constant__ Scratch S, int use_dedup,
+__global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
+                                               const __grid_constant__ Scratch S, int use_dedup,
                                                int new_keys, const void *__restrict__ keys,
                                                const void *__restrict__ vals, uint32_t vb,
                                                uint64_t n, Counters *ctr) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
-    const uint32_t lane = threadIdx.x & 31;
+    using Gm = Geo<KB, SB>;
     const uint64_t step = warp_stride();
     uint32_t n_ins = 0, n_upd = 0, n_rej = 0, n_sup = 0;
     for (uint64_t base = warp_base(); base < n; base += step) {
-        const uint64_t i = base + lane;
-        bool pend = false;
+        const uint64_t i = base + (threadIdx.x & 31);
+        typename T::K k = 0;
+        bool act = false;
         Sl e = T::empty();
         if (i < n) {
-            const typename T::K k = load_key<KB>(keys, i);
+            k = load_key<KB>(keys, i);
             if (k == 0) {
                 ++n_rej;
             } else if (use_dedup && !Dedup<KB>::winner(S, k, (uint32_t)i)) {
                 ++n_sup;
             } else {
+                act = true;
                 e = T::make(k, load_val(vals, vb, i));
-                const uint32_t hk = fold(k);
-                const Pair p = pair_of(hk, D.d);
-                char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
-                char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-                Bucket<KB, SB> b1, b2;
-                b1.load_cg(p1);
-                int r = 0;  // 1 updated, 2 inserted
-                if (!new_keys) {
-                    int j = b1.find(k);
-                    if (j >= 0) {
-                        T::exch(slot_ptr<KB, SB>(p1, j), e);
-                        r = 1;
-                    } else {
-                        b2.load_cg(p2);
-                        j = b2.find(k);
-                        if (j >= 0) {
-                            T::exch(slot_ptr<KB, SB>(p2, j), e);
-                            r = 1;
-                        } else if (try_empty<KB, SB>(p1, b1, e) || try_empty<KB, SB>(p2, b2, e)) {
-                            r = 2;
-                        }
-                    }
-                } else {
-                    if (try_empty<KB, SB>(p1, b1, e)) {
-                        r = 2;
-                    } else {
-                        b2.load_cg(p2);
-                        if (try_empty<KB, SB>(p2, b2, e)) r = 2;
-                    }
-                }
-                if (r == 1) ++n_upd;
-                else if (r == 2) ++n_ins;
-                else pend = true;
             }
+        }
+        const uint32_t hk = fold(k);
+        const Pair p = pair_of(hk, D.d);
+        char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
+        char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
+        const ProbeOut<KB> r1 = probe<KB, SB, 2, true, false>(p1, k, act, p.first, D.d);
+        const bool found1 = act && r1.match >= 0;
+        // the second bucket is needed to look for the key (upsert, unless the
+        // first bucket's overflow bit rules it out) or for an empty slot
+        const bool check2 =
+            act && !found1 &&
+            ((!new_keys && (!Gm::kMeta || (r1.meta & kOverflowBit))) || r1.empty == 0u);
+        ProbeOut<KB> r2;
+        r2.match = -1;
+        r2.empty = 0u;
+        r2.mslot = T::empty();
+        if (__any_sync(kFull, check2)) r2 = probe<KB, SB, 2, true, false>(p2, k, check2, p.second, D.d);
+        bool pend = false;
+        if (found1) {
+            T::exch(slot_ptr<KB, SB>(p1, r1.match), e);
+            ++n_upd;
+        } else if (check2 && !new_keys && r2.match >= 0) {
+            T::exch(slot_ptr<KB, SB>(p2, r2.match), e);
+            ++n_upd;
+        } else if (act) {
+            bool ok = claim_empty<KB, SB>(p1, r1.empty, e);
+            if (!ok && check2 && r2.empty) {
+                mark_overflow<KB, SB>(p1);
+                ok = claim_empty<KB, SB>(p2, r2.empty, e);
+            }
+            if (ok) ++n_ins;
+            else pend = true;
         }
         __syncwarp();
         const unsigned long long at = agg_inc(&ctr->pending, pend);
@@ -259,82 +553,95 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D, c
     agg_add(&ctr->superseded, n_sup);
 }
 
-// Victim choice when a bucket is full: prefer a resident that sits in the
-// second subtable of its own pair (evicting it moves it back to its first,
-// where finds look first); rotate the start so chains do not cycle.
+// Victim when a bucket is full: prefer a resident sitting in its second
+// bucket (evicting it sends it back to its first-probe bucket); the start
+// rotates with the step so chains do not cycle.
 template <int KB, int SB>
-__device__ __forceinline__ int pick_victim(const Bucket<KB, SB> &b, uint32_t t, uint32_t d,
-                                           uint32_t rot) {
-    constexpr int B = Bucket<KB, SB>::kSlots;
-    unsigned pref = 0;
-#pragma unroll
-    for (int q = 0; q < B; ++q) {
-        const Pair pr = pair_of(fold(SlotT<KB>::key(b.s[q])), d);
-        if (pr.first != t) pref |= 1u << q;
-    }
-    rot &= (B - 1);
+__device__ __forceinline__ int pick_victim(unsigned pref, uint32_t rot) {
+    constexpr int B = Geo<KB, SB>::kSlots;
+    rot %= (uint32_t)B;
     if (!pref) return (int)rot;
-    const unsigned rotated = ((pref >> rot) | (pref << (B - rot))) & ((1u << B) - 1u);
-    return (int)((__ffs(rotated) - 1 + rot) & (B - 1));
+    const unsigned all = (B == 32) ? kFull : ((1u << B) - 1u);
+    const unsigned rotated = ((pref >> rot) | (pref << ((B - rot) & 31))) & all;
+    return (int)((__ffs(rotated) - 1 + rot) % (uint32_t)B);
 }
 
-// One bounded eviction walk; on failure `e` holds the entry left over.
+// ----------------------------------------------------------------------------
+// insert phase 3: eviction walks (warp_insert, cuckoo.cu:365-432). Each
+// entry of `src` first tries the empty slots of its first-probe bucket, then
+// of its second, then walks: exchange into the current bucket, carry the
+// resident to the other bucket of its own pair. An entry whose walk reaches
+// max_evict exchanges goes to `dst` for the host to place after an upsize.
+// ----------------------------------------------------------------------------
 template <int KB, int SB>
-__device__ __forceinline__ bool walk_one(const Desc &D, typename SlotT<KB>::S &e,
-                                         uint32_t max_evict, uint32_t &steps) {
-    using T = SlotT<KB>;
-    uint32_t hk = fold(T::key(e));
-    Pair p = pair_of(hk, D.d);
-    char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
-    char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-    Bucket<KB, SB> b;
-    b.load_cg(p1);
-    if (try_empty<KB, SB>(p1, b, e)) return true;
-    b.load_cg(p2);
-    if (try_empty<KB, SB>(p2, b, e)) return true;
-    uint32_t t = p.first;
-    char *bp = p1;
-    const uint32_t seed = hk;
-    for (uint32_t s = 0; s < max_evict; ++s) {
-        b.load_cg(bp);
-        if (try_empty<KB, SB>(bp, b, e)) return true;
-        const int j = pick_victim<KB, SB>(b, t, D.d, seed + s);
-        typename T::S old = T::exch(slot_ptr<KB, SB>(bp, j), e);
-        ++steps;
-        if (T::is_empty(old)) return true;
-        e = old;
-        hk = fold(T::key(e));
-        p = pair_of(hk, D.d);
-        t = other_of(p, t);
-        bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
-    }
-    return false;
-}
-
-// insert phase 3: eviction walks. Entries come from `src`; an entry whose
-// walk reaches max_evict goes to `dst` for the host to place after an upsize.
-template <int KB, int SB>
-__global__ void __launch_bounds__(256) k_walk(const __grid_constant__ Desc D, const void *__restrict__ src,
+__global__ void __launch_bounds__(256) k_walk(const __grid_constant__ Desc D,
+                                              const void *__restrict__ src,
                                               const unsigned long long *src_count, void *dst,
                                               unsigned long long *dst_count, uint64_t dst_cap,
                                               uint32_t max_evict, int count_new, Counters *ctr,
                                               uint64_t max_entries) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
-    const uint32_t lane = threadIdx.x & 31;
     uint64_t n = *src_count;
     if (n > max_entries) n = max_entries;
     const uint64_t step = warp_stride();
     uint32_t n_ok = 0, n_steps = 0;
+    const uint32_t max_iter = 2u * max_evict + 8u;
     for (uint64_t base = warp_base(); base < n; base += step) {
-        const uint64_t i = base + lane;
+        const uint64_t i = base + (threadIdx.x & 31);
+        bool live = i < n;
+        Sl e = live ? ((const Sl *)src)[i] : T::empty();
+        uint32_t hk = 0;
+        Pair pe{0u, 0u};
+        char *fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);  // first bucket of e
+        uint32_t t = pe.first;
+        char *bp = fb;
+        int mode = 0;  // 0: empties of the first bucket, 1: of the second, 2: walking
+        uint32_t evictions = 0;
         bool fail = false;
-        Sl e = T::empty();
-        if (i < n) {
-            e = ((const Sl *)src)[i];
-            if (walk_one<KB, SB>(D, e, max_evict, n_steps)) ++n_ok;
-            else fail = true;
+        for (uint32_t it = 0; it < max_iter; ++it) {
+            if (!__any_sync(kFull, live)) break;
+            const ProbeOut<KB> r = probe<KB, SB, 2, true, true>(bp, T::key(e), live, t, D.d);
+            if (!live) continue;
+            bool placed = false;
+            if (r.empty) {
+                if (t != pe.first) mark_overflow<KB, SB>(fb);
+                placed = claim_empty<KB, SB>(bp, r.empty, e);
+            }
+            if (placed) {
+                live = false;
+                ++n_ok;
+            } else if (mode == 0) {
+                mode = 1;
+                t = pe.second;
+                bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
+            } else if (mode == 1) {
+                mode = 2;
+                t = pe.first;
+                bp = fb;
+            } else if (r.empty) {
+                // every empty slot was taken by another lane: look again
+            } else if (evictions >= max_evict) {
+                live = false;
+                fail = true;
+            } else {
+                const int j = pick_victim<KB, SB>(r.pref, hk + evictions);
+                if (t != pe.first) mark_overflow<KB, SB>(fb);
+                const Sl old = T::exch(slot_ptr<KB, SB>(bp, j), e);
+                ++evictions;
+                ++n_steps;
+                if (T::is_empty(old)) {
+                    live = false;
+                    ++n_ok;
+                } else {
+                    e = old;
+                    fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);
+                    t = other_of(pe, t);
+                    bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
+                }
+            }
         }
+        if (live) fail = true;  // iteration bound reached
         __syncwarp();
         const unsigned long long at = agg_inc(dst_count, fail);
         if (fail) {
@@ -350,53 +657,60 @@ __global__ void __launch_bounds__(256) k_walk(const __grid_constant__ Desc D, co
 }
 
 // ----------------------------------------------------------------------------
-// erase: probe both buckets; the slot holding the key is cleared with a CAS
-// (the reference clears with a plain store and returns nothing,
-// cuckoo.cu:524-587).
+// erase (cuckoo_delete, cuckoo.cu:524-587): the slot holding the key is
+// cleared with a CAS; the second bucket is only probed when the first one's
+// overflow bit allows the key to be there.
 // ----------------------------------------------------------------------------
 template <int KB, int SB>
-__global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D, const __grid_constant__ Scratch S, int use_dedup,
+__global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D,
+                                               const __grid_constant__ Scratch S, int use_dedup,
                                                const void *__restrict__ keys, uint64_t n,
                                                uint32_t *__restrict__ bits, Counters *ctr) {
     using T = SlotT<KB>;
+    using Gm = Geo<KB, SB>;
+    __shared__ __align__(128) unsigned char s_stage[kWarpsPerBlock][32 * SB];
+    unsigned char *stage = s_stage[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t step = warp_stride();
     uint32_t n_del = 0, n_sup = 0;
     for (uint64_t base = warp_base(); base < n; base += step) {
         const uint64_t i = base + lane;
-        bool erased = false;
+        typename T::K k = 0;
+        bool act = false;
         if (i < n) {
-            const typename T::K k = load_key<KB>(keys, i);
+            k = load_key<KB>(keys, i);
             if (k != 0) {
-                if (use_dedup && !Dedup<KB>::winner(S, k, (uint32_t)i)) {
-                    ++n_sup;
-                } else {
-                    const uint32_t hk = fold(k);
-                    const Pair p = pair_of(hk, D.d);
-#pragma unroll 1
-                    for (int r = 0; r < 2 && !erased; ++r) {
-                        const uint32_t t = r ? p.second : p.first;
-                        char *bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
-                        Bucket<KB, SB> b;
-                        b.load_cg(bp);
-                        const int j = b.find(k);
-                        if (j >= 0) {
-                            const typename T::S cur = slot_at(b, j);
-                            const typename T::S old = T::cas(slot_ptr<KB, SB>(bp, j), cur, T::empty());
-                            erased = T::same(old, cur);
-                            break;
-                        }
-                    }
-                }
+                if (use_dedup && !Dedup<KB>::winner(S, k, (uint32_t)i)) ++n_sup;
+                else act = true;
             }
         }
-        const unsigned m = __ballot_sync(0xffffffffu, erased);
+        const uint32_t hk = fold(k);
+        const Pair p = pair_of(hk, D.d);
+        char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
+        const KvOut r1 = kv_probe<KB, SB, 2>(p1, k, act, stage);
+        bool erased = false;
+        if (act && r1.match >= 0) {
+            const typename T::S cur = T::make(k, r1.value);
+            const typename T::S old = T::cas(slot_ptr<KB, SB>(p1, r1.match), cur, T::empty());
+            erased = T::same(old, cur);
+        }
+        const bool need2 = act && r1.match < 0 && (!Gm::kMeta || r1.overflow);
+        if (__any_sync(kFull, need2)) {
+            char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
+            const KvOut r2 = kv_probe<KB, SB, 2>(p2, k, need2, stage);
+            if (need2 && r2.match >= 0) {
+                const typename T::S cur = T::make(k, r2.value);
+                const typename T::S old = T::cas(slot_ptr<KB, SB>(p2, r2.match), cur, T::empty());
+                erased = T::same(old, cur);
+            }
+        }
+        const unsigned m = __ballot_sync(kFull, erased);
         if (bits != nullptr && lane == 0) bits[base >> 5] = m;
         n_del += erased ? 1u : 0u;
     }
     // loops are warp-uniform, so every lane of the warp is here
-    const uint32_t del = __reduce_add_sync(0xffffffffu, n_del);
-    const uint32_t sup = __reduce_add_sync(0xffffffffu, n_sup);
+    const uint32_t del = __reduce_add_sync(kFull, n_del);
+    const uint32_t sup = __reduce_add_sync(kFull, n_sup);
     if (lane == 0) {
         if (del) {
             atomicAdd(&ctr->erased, (unsigned long long)del);
@@ -411,38 +725,51 @@ __global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D, c
 // old bucket b is b or b+nb, so every slot keeps its index and each old
 // bucket writes exactly two new buckets: a pure stream, read S / write 2S,
 // no zero-fill pass and no atomics (cuckoo_resize_up, cuckoo.cu:600-627).
+// One thread per 32-byte chunk; the metadata word is copied to both halves
+// (keys displaced from old bucket b now have b or b+nb as first bucket).
 // ----------------------------------------------------------------------------
 template <int KB, int SB>
 __global__ void __launch_bounds__(256) k_resize_up(uint32_t t, const char *__restrict__ old_sub,
                                                    uint32_t old_nb, char *__restrict__ new_sub,
                                                    uint64_t new_magic, uint32_t new_nb) {
     using T = SlotT<KB>;
-    constexpr int B = Bucket<KB, SB>::kSlots;
+    using Gm = Geo<KB, SB>;
+    constexpr int G = Gm::kG, SPC = Gm::kSPC, WPS = T::kBytes / 4;
+    const uint64_t chunks = (uint64_t)old_nb * G;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < old_nb; b += stride) {
-        Bucket<KB, SB> src, lo, hi;
-        src.load_nc(old_sub + b * SB);
+    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < chunks; x += stride) {
+        const uint64_t b = x / G;
+        const int r = (int)(x % G);
+        uint32_t w[8], lo[8], hi[8];
+        ld_nc(old_sub + x * 32, w);
 #pragma unroll
-        for (int q = 0; q < B; ++q) {
-            lo.s[q] = T::empty();
-            hi.s[q] = T::empty();
-            if (!T::is_empty(src.s[q])) {
-                const uint32_t nbk =
-                    fastmod(subtable_hash(fold(T::key(src.s[q])), t), new_magic, new_nb);
-                if (nbk == (uint32_t)b) lo.s[q] = src.s[q];
-                else hi.s[q] = src.s[q];
+        for (int j = 0; j < SPC; ++j) {
+            typename T::S s;
+            T::from_words(w + j * WPS, s);
+            const int idx = r * SPC + j;
+            const bool is_meta = Gm::kMeta && idx == Gm::kTotal - 1;
+            bool to_lo = is_meta, to_hi = is_meta;
+            if (!is_meta && !T::is_empty(s)) {
+                const uint32_t nbk = fastmod(subtable_hash(fold(T::key(s)), t), new_magic, new_nb);
+                to_lo = nbk == (uint32_t)b;
+                to_hi = !to_lo;
+            }
+#pragma unroll
+            for (int x2 = 0; x2 < WPS; ++x2) {
+                lo[j * WPS + x2] = to_lo ? w[j * WPS + x2] : 0u;
+                hi[j * WPS + x2] = to_hi ? w[j * WPS + x2] : 0u;
             }
         }
-        lo.store(new_sub + b * SB);
-        hi.store(new_sub + (b + old_nb) * SB);
+        st_v8(new_sub + b * SB + r * 32, lo);
+        st_v8(new_sub + (b + old_nb) * SB + r * 32, hi);
     }
 }
 
 // ----------------------------------------------------------------------------
 // downsize of an even subtable: new bucket j = old buckets j and j+nb/2
-// merged; entries that do not fit are listed for eviction walks
-// (cuckoo_resize_down, cuckoo.cu:638-728, which drops the ones its walks
-// cannot place).
+// merged, metadata OR-ed; entries that do not fit are listed for eviction
+// walks (cuckoo_resize_down, cuckoo.cu:638-728, drops the ones its walks
+// cannot place). Thread per new bucket.
 // ----------------------------------------------------------------------------
 template <int KB, int SB>
 __global__ void __launch_bounds__(256) k_resize_down(const char *__restrict__ old_sub,
@@ -452,12 +779,13 @@ __global__ void __launch_bounds__(256) k_resize_down(const char *__restrict__ ol
                                                      unsigned long long *spill) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
-    constexpr int B = Bucket<KB, SB>::kSlots;
+    using Gm = Geo<KB, SB>;
+    constexpr int B = Gm::kSlots;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < new_nb; j += stride) {
         Bucket<KB, SB> a, c;
-        a.load_nc(old_sub + j * SB);
-        c.load_nc(old_sub + (j + new_nb) * SB);
+        a.template load<0>(old_sub + j * SB);
+        c.template load<0>(old_sub + (j + new_nb) * SB);
         unsigned freem = a.empty_mask();
 #pragma unroll
         for (int q = 0; q < B; ++q) {
@@ -474,6 +802,11 @@ __global__ void __launch_bounds__(256) k_resize_down(const char *__restrict__ ol
                 else atomicAdd(spill, 1ull);
             }
         }
+        if (Gm::kMeta) {
+            const unsigned long long m = a.meta() | c.meta();
+            uint32_t mw[4] = {(uint32_t)m, (uint32_t)(m >> 32), 0u, 0u};
+            T::from_words(mw, a.s[Gm::kTotal - 1]);
+        }
         a.store(new_sub + j * SB);
     }
 }
@@ -485,12 +818,12 @@ __global__ void __launch_bounds__(256) k_collect(const char *__restrict__ sub, u
                                                  uint64_t list_cap, unsigned long long *spill) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
-    constexpr int B = Bucket<KB, SB>::kSlots;
+    constexpr int B = Geo<KB, SB>::kSlots;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nb; j += stride) {
         Bucket<KB, SB> a;
-        a.load_nc(sub + j * SB);
-        const unsigned live = ((1u << B) - 1u) & ~a.empty_mask();
+        a.template load<0>(sub + j * SB);
+        const unsigned live = ((B == 32) ? kFull : ((1u << B) - 1u)) & ~a.empty_mask();
         if (!live) continue;
         unsigned long long at = atomicAdd(list_count, (unsigned long long)__popc(live));
 #pragma unroll
@@ -503,18 +836,27 @@ __global__ void __launch_bounds__(256) k_collect(const char *__restrict__ sub, u
     }
 }
 
+// set the overflow bit of every bucket of a subtable (after an odd-size
+// downsize the bits of the old buckets no longer map onto the new ones)
+template <int KB, int SB>
+__global__ void __launch_bounds__(256) k_mark_all(char *__restrict__ sub, uint32_t nb) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nb; j += stride)
+        if (Geo<KB, SB>::kMeta) *meta_ptr<KB, SB>(sub + j * SB) = kOverflowBit;
+}
+
 // every live (key, value) of one subtable
 template <int KB, int SB>
 __global__ void __launch_bounds__(256) k_export(const char *__restrict__ sub, uint32_t nb,
                                                 void *keys, void *vals, uint32_t vb, uint64_t cap,
                                                 unsigned long long *count) {
     using T = SlotT<KB>;
-    constexpr int B = Bucket<KB, SB>::kSlots;
+    constexpr int B = Geo<KB, SB>::kSlots;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nb; j += stride) {
         Bucket<KB, SB> a;
-        a.load_nc(sub + j * SB);
-        const unsigned live = ((1u << B) - 1u) & ~a.empty_mask();
+        a.template load<0>(sub + j * SB);
+        const unsigned live = ((B == 32) ? kFull : ((1u << B) - 1u)) & ~a.empty_mask();
         if (!live) continue;
         unsigned long long at = atomicAdd(count, (unsigned long long)__popc(live));
 #pragma unroll

@@ -3,6 +3,7 @@
 // two widths compile as separate translation units in parallel.
 #pragma once
 
+#include <algorithm>
 #include <mutex>
 #include <unordered_map>
 
@@ -51,7 +52,12 @@ cudaError_t Ops<KB>::find(const LaunchCtx &L, const Desc &D, int sb, const void 
     if (n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_find<KB, SB>;
-        k<<<grid_for((const void *)k, L, n), 256, 0, L.stream>>>(D, keys, vals, vb, hits, n);
+        // eight 32-key tiles per warp and as many blocks as that takes: block
+        // turnover keeps the SMs' fetch phases out of step, which sustains
+        // more random line reads than a persistent grid (on GB300, 2^26
+        // finds: 39.3 G/s vs 34.2 G/s for one wave of resident blocks)
+        const int g = (int)std::min<uint64_t>((n + 2047) / 2048, 0x7fffffffull);
+        k<<<g, 256, 0, L.stream>>>(D, keys, vals, vb, hits, n);
     });
     return cudaGetLastError();
 }
@@ -114,7 +120,7 @@ cudaError_t Ops<KB>::resize_up(const LaunchCtx &L, int sb, uint32_t t, const voi
     const uint64_t magic = fastmod_magic(new_nb);
     DYC_SB_DISPATCH(sb, {
         auto k = k_resize_up<KB, SB>;
-        k<<<grid_for((const void *)k, L, old_nb), 256, 0, L.stream>>>(
+        k<<<grid_for((const void *)k, L, (uint64_t)old_nb * (SB / 32)), 256, 0, L.stream>>>(
             t, (const char *)old_sub, old_nb, (char *)new_sub, magic, new_nb);
     });
     return cudaGetLastError();
@@ -144,6 +150,16 @@ cudaError_t Ops<KB>::collect(const LaunchCtx &L, int sb, const void *sub, uint32
         auto k = k_collect<KB, SB>;
         k<<<grid_for((const void *)k, L, nb), 256, 0, L.stream>>>((const char *)sub, nb, list,
                                                                   list_count, list_cap, spill);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::mark_all(const LaunchCtx &L, int sb, void *sub, uint32_t nb) {
+    if (nb == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_mark_all<KB, SB>;
+        k<<<grid_for((const void *)k, L, nb), 256, 0, L.stream>>>((char *)sub, nb);
     });
     return cudaGetLastError();
 }

@@ -61,7 +61,7 @@ class DyCuckoo:
     """
 
     def __init__(self, size: int, key_bytes: int = 4, value_bytes: int | None = None,
-                 num_subtables: int = 4, bucket_bytes: int = 32, max_evictions: int = 64,
+                 num_subtables: int = 4, bucket_bytes: int = 128, max_evictions: int = 64,
                  auto_resize: bool = True, upper_load: float = UPPER_BOUND,
                  lower_load: float = LOWER_BOUND,
                  min_downsize_capacity: int = MIN_DOWNSIZE_CAPACITY, device: int = 0):
@@ -185,8 +185,10 @@ class DyCuckoo:
         check(self.L.dyc_last_stats(self._h, C.byref(s)), "dyc_last_stats")
         return s.as_dict()
 
-    def subtable(self, i: int):
-        """Subtable i as a (buckets, slots) array of raw slots on the host."""
+    def subtable(self, i: int, with_meta: bool = False):
+        """Subtable i on the host: (buckets, slots) raw 64-bit slots for
+        4-byte keys, (buckets, slots, 2) for 8-byte keys. 128-byte buckets end
+        with a metadata slot, dropped unless with_meta."""
         torch = _torch()
         p = C.c_void_p()
         nbytes = C.c_uint64()
@@ -201,7 +203,10 @@ class DyCuckoo:
         slot_words = 1 if self.key_bytes == 4 else 2
         slots = self.cfg.bucket_bytes // (8 * slot_words)
         nb = self.layout()[i]
-        return host.reshape(nb, slots, slot_words) if slot_words == 2 else host.reshape(nb, slots)
+        a = host.reshape(nb, slots, slot_words) if slot_words == 2 else host.reshape(nb, slots)
+        if self.cfg.bucket_bytes == 128 and not with_meta:
+            a = a[:, :-1]
+        return a
 
     def export(self, stream=None):
         """All live (key, value) pairs as CUDA tensors, sorted by key."""

@@ -65,7 +65,7 @@ typedef struct dyc_config {
     uint32_t key_bytes;      /* 4 or 8 */
     uint32_t value_bytes;    /* 4 or 8 (4-byte keys take 4-byte values) */
     uint32_t num_subtables;  /* d, 2..6; default 4 */
-    uint32_t bucket_bytes;   /* 32, 64 or 128; default 32 (one DRAM sector) */
+    uint32_t bucket_bytes;   /* 32, 64 or 128; default 128 (one DRAM line) */
     uint32_t max_evictions;  /* eviction chain bound; default 64 */
     uint32_t auto_resize;    /* 1: apply upper/lower load thresholds */
     uint64_t initial_size;   /* the hashAPI(size) argument: keys to size for */
@@ -94,7 +94,7 @@ typedef struct dyc_op_stats {
     uint64_t resizes_down;
 } dyc_op_stats;
 
-/* Defaults: 4-byte keys and values, d = 4, 32-byte buckets, bound 64,
+/* Defaults: 4-byte keys and values, d = 4, 128-byte buckets, bound 64,
  * thresholds 0.8 / 0.5, downsize guard 4*1M*1.2 slots (api.cpp:496). */
 void dyc_config_default(dyc_config *cfg);
 
@@ -148,7 +148,9 @@ dyc_status dyc_layout(dyc_table *t, uint32_t *nbuckets_out, uint32_t *num_subtab
 /* Device address and byte size of subtable i (the reference's
  * table.table[i], cuckoo.h:42). Slots are bucket_bytes/slot_bytes per
  * bucket; a 4-byte-key slot is key | value << 32, an 8-byte-key slot is
- * {key, value} (16 bytes). */
+ * {key, value} (16 bytes). In 128-byte buckets the last slot is a metadata
+ * word, not an entry (bit 0: some key whose first-probe bucket this is lives
+ * in its second bucket). */
 dyc_status dyc_subtable(dyc_table *t, uint32_t i, void **d_ptr, uint64_t *bytes);
 
 /* Every live (key, value) into d_keys_out / d_vals_out (no order), at most

@@ -58,7 +58,7 @@ def test_config_defaults():
     L = dg.lib()
     cfg = _lib.DycConfig()
     L.dyc_config_default(C.byref(cfg))
-    assert (cfg.key_bytes, cfg.value_bytes, cfg.num_subtables, cfg.bucket_bytes) == (4, 4, 4, 32)
+    assert (cfg.key_bytes, cfg.value_bytes, cfg.num_subtables, cfg.bucket_bytes) == (4, 4, 4, 128)
     assert cfg.upper_load == 0.8 and cfg.lower_load == 0.5
     assert cfg.min_downsize_capacity == int(4 * 1024 * 1024 * 1.2)
     assert cfg.auto_resize == 1

@@ -156,12 +156,13 @@ def test_placement_follows_reference_hashes(bucket_bytes, d):
     t.close()
 
 
-def test_first_probe_serves_most_hits():
-    """Finds probe the first subtable of the pair first; the insert policy
-    keeps most keys there (so a hit costs one sector)."""
+@pytest.mark.parametrize("bucket_bytes,floor", [(32, 0.75), (128, 0.9)])
+def test_first_probe_serves_most_hits(bucket_bytes, floor):
+    """Finds probe the first-probe bucket first; the insert policy keeps most
+    keys there (so a hit costs one bucket read)."""
     n = 1 << 18
     keys = unique_u32(n, seed=99)
-    t = _dg().DyCuckoo(int(n / 0.9), auto_resize=False)
+    t = _dg().DyCuckoo(int(n / 0.9), bucket_bytes=bucket_bytes, auto_resize=False)
     t.insert(to_dev(keys), to_dev(keys))
     nb = t.layout()
     first = 0
@@ -171,30 +172,85 @@ def test_first_probe_serves_most_hits():
         rk = kk[kk != 0]
         first += int((first_probe_table(rk, 4, nb) == s).sum())
     frac = first / n
-    assert frac > 0.75, frac
+    assert frac > floor, frac
+    t.close()
+
+
+def _check_overflow_bits(t, d=4):
+    """Every key stored in its second bucket has the overflow bit set on its
+    first-probe bucket (128-byte buckets)."""
+    nb = t.layout()
+    metas = [t.subtable(s, with_meta=True)[:, -1] for s in range(d)]
+    bad = 0
+    for s in range(d):
+        sub = t.subtable(s)
+        kk = (sub & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+        b_idx, _ = np.nonzero(kk)
+        rk = kk[kk != 0]
+        t1, b1, t2, b2 = O.hash_batch(rk, d, nb)
+        first_t = first_probe_table(rk, d, nb)
+        first_b = np.where(first_t == t1, b1, b2)
+        second = first_t != s
+        for ft in range(d):
+            sel = second & (first_t == ft)
+            if sel.any():
+                bits = metas[ft][first_b[sel]] & np.uint64(1)
+                bad += int((bits == 0).sum())
+    return bad
+
+
+def test_overflow_bits_cover_every_displaced_key():
+    n = 1 << 18
+    keys = unique_u32(2 * n, seed=4321)
+    t = _dg().DyCuckoo(int(n / 0.9), auto_resize=False)
+    m = O.Map()
+    t.insert(to_dev(keys[:n]), to_dev(keys[:n]))
+    m.insert(keys[:n], keys[:n])
+    assert _check_overflow_bits(t) == 0
+    t.erase(to_dev(keys[: n // 3]), no_resize=True)
+    m.erase(keys[: n // 3])
+    t.insert(to_dev(keys[n: n + n // 3]), to_dev(keys[n: n + n // 3]))
+    m.insert(keys[n: n + n // 3], keys[n: n + n // 3])
+    assert _check_overflow_bits(t) == 0
+    t.resize_up()
+    assert _check_overflow_bits(t) == 0
+    t.resize_down()
+    t.resize_down()
+    assert _check_overflow_bits(t) == 0
+    assert_same_contents(t, m, "after bit checks")
+    find_and_compare(t, m, keys, "misses skip the second probe only when safe")
     t.close()
 
 
 # ---------------------------------------------------------------- resizing
-def test_resize_sequence_matches_reference_policy():
+@pytest.mark.parametrize("bucket_bytes,slots", [(32, 4), (128, 15)])
+def test_resize_sequence_matches_reference_policy(bucket_bytes, slots):
+    """Initial bucket counts follow the reference sizing rule (api.cpp:46-56)
+    with this table's entry slots per bucket; each resize doubles or halves
+    the subtable the reference's choice rules name (api.cpp:115-122, :147-153,
+    pinned against the reference in test_oracle_golden)."""
     n = 100_000
     keys = unique_u32(n, seed=5)
     vals = np.arange(n, dtype=np.uint32)
-    t = _dg().DyCuckoo(n * 2, auto_resize=False)
-    ref = O.RefCuckoo(n * 2, 4, 4)  # same bucket-count rule: 4 slots per 32-byte bucket
+    t = _dg().DyCuckoo(n * 2, bucket_bytes=bucket_bytes, auto_resize=False)
+    nb = np.array([O.subtable_buckets(n * 2, 4, slots)] * 4, np.uint32)
+    assert t.layout() == [int(x) for x in nb]
+    L = O.lib()
     m = O.Map()
     t.insert(to_dev(keys), to_dev(vals))
     m.insert(keys, vals)
     for step in range(5):
         t.resize_up()
-        ref.resize_up()
-        assert t.layout() == list(ref.layout()), "up %d" % step
+        i = L.orc_pick_up_nb(nb, 4)
+        nb[i] *= 2
+        assert t.layout() == [int(x) for x in nb], "up %d" % step
         assert_same_contents(t, m, "after up %d" % step)
         find_and_compare(t, m, keys[::7], "find after up %d" % step)
     for step in range(7):
         t.resize_down()
-        ref.resize_down()
-        assert t.layout() == [int(x) for x in ref.layout()], "down %d" % step
+        i = L.orc_pick_down_nb(nb, 4)
+        nb[i] = nb[i] // 2 if nb[i] % 2 == 0 else (nb[i] + 1) // 2
+        assert t.layout() == [int(x) for x in nb], "down %d" % step
         assert_same_contents(t, m, "after down %d" % step)
         find_and_compare(t, m, keys[::7], "find after down %d" % step)
     t.close()
