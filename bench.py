@@ -236,6 +236,22 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_line_probe():
+    """Random DRAM line ceiling (databases_gpu_gb300/csrc/dyc_line_probe.cu)."""
+    from databases_gpu_gb300 import build as pkg_build
+    src = os.path.join(pkg_build.CSRC, "dyc_line_probe.cu")
+    exe = os.path.join(pkg_build.BUILD_DIR, "dyc_line_probe")
+    os.makedirs(pkg_build.BUILD_DIR, exist_ok=True)
+    if not os.path.exists(exe) or os.path.getmtime(exe) < os.path.getmtime(src):
+        subprocess.check_call([pkg_build.nvcc()] + pkg_build.ARCH + ["-O3", "-o", exe, src])
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.strip()
+    d = json.loads(out)
+    peak, kind = load_peaks()
+    d["line_bytes_frac_of_%s_hbm" % kind] = round(d["line_bytes_per_s"] / 1e9 / peak, 4)
+    d["find_hit_ceiling_ops_per_s"] = d["random_lines_per_s"]
+    print(json.dumps(d))
+
+
 def workload_config(args, lf):
     return {
         "workload": "large static table find: u32 keys/values, 4 subtables, 2^%d unique keys "
@@ -260,10 +276,14 @@ def main():
     ap.add_argument("--max-evictions", type=int, default=2048)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-variants", action="store_true")
+    ap.add_argument("--line-probe", action="store_true",
+                    help="measure the random 128-byte line ceiling of this GPU and exit")
     ap.add_argument("--mixes", default="uniform100,uniform10,zipf100,zipf10",
                     help="query mixes to time; the first is the headline")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.line_probe:
+        return run_line_probe()
     if args.impl == "reference":
         return run_reference(args)
 

@@ -96,6 +96,10 @@ struct dyc_table {
     cudaStream_t io_stream = nullptr;
     void *d_io = nullptr;
     size_t d_io_bytes = 0;
+    // dyc_find_host pipeline: one stream and one device buffer per stage
+    cudaStream_t pipe_stream[3] = {nullptr, nullptr, nullptr};
+    void *pipe_buf[3] = {nullptr, nullptr, nullptr};
+    size_t pipe_bytes = 0;
     uint64_t size = 0, capacity = 0;
     dyc_op_stats last{};
 };
@@ -432,6 +436,10 @@ dyc_status dyc_destroy(dyc_table *t) {
     if (t->scratch) cudaFree(t->scratch);
     if (t->d_io) cudaFree(t->d_io);
     if (t->io_stream) cudaStreamDestroy(t->io_stream);
+    for (int i = 0; i < 3; ++i) {
+        if (t->pipe_buf[i]) cudaFree(t->pipe_buf[i]);
+        if (t->pipe_stream[i]) cudaStreamDestroy(t->pipe_stream[i]);
+    }
     delete t;
     return DYC_OK;
 }
@@ -616,28 +624,53 @@ dyc_status dyc_insert_host(dyc_table *t, const void *h_keys, const void *h_vals,
     return DYC_OK;
 }
 
+// Three-stage pipeline over chunks: chunk c uses stream and buffer c % 3, so
+// the upload of one chunk, the find kernel of the previous one and the
+// download of the one before that run at the same time (the two copy
+// directions use separate engines). Stream order on each stage keeps a
+// buffer from being refilled before its previous results are downloaded.
 dyc_status dyc_find_host(dyc_table *t, const void *h_keys, void *h_vals_out,
                          uint32_t *h_hit_bits_out, uint64_t n) {
     if (!t) return fail(DYC_EINVAL, "null table");
     if (n == 0) return DYC_OK;
     if (!h_keys || !h_vals_out) return fail(DYC_EINVAL, "null key or value array");
     TRY(set_device(t));
+    constexpr int kStages = 3;
     const uint64_t c = n < kIoChunk ? n : kIoChunk;
     const size_t kbytes = (((size_t)c * t->kb) + 255) & ~(size_t)255;
     const size_t vbytes = (((size_t)c * t->vb) + 255) & ~(size_t)255;
-    TRY(ensure_io(t, kbytes + vbytes + (c / 32 + 1) * 4 + 256));
-    char *dk = (char *)t->d_io;
-    char *dv = dk + kbytes;
-    uint32_t *db = (uint32_t *)(dv + vbytes);
-    for (uint64_t off = 0; off < n; off += c) {
-        const uint64_t m = (n - off) < c ? (n - off) : c;
-        CK(cudaMemcpyAsync(dk, (const char *)h_keys + off * t->kb, m * t->kb, cudaMemcpyHostToDevice, t->io_stream));
-        TRY(dyc_find(t, dk, dv, h_hit_bits_out ? db : nullptr, m, t->io_stream));
-        CK(cudaMemcpyAsync((char *)h_vals_out + off * t->vb, dv, m * t->vb, cudaMemcpyDeviceToHost, t->io_stream));
-        if (h_hit_bits_out)
-            CK(cudaMemcpyAsync(h_hit_bits_out + off / 32, db, ((m + 31) / 32) * 4, cudaMemcpyDeviceToHost, t->io_stream));
+    const size_t need = kbytes + vbytes + (c / 32 + 1) * 4 + 256;
+    if (t->pipe_bytes < need) {
+        for (int i = 0; i < kStages; ++i) {
+            if (t->pipe_stream[i]) CK(cudaStreamSynchronize(t->pipe_stream[i]));
+            if (t->pipe_buf[i]) CK(cudaFree(t->pipe_buf[i]));
+            t->pipe_buf[i] = nullptr;
+        }
+        t->pipe_bytes = 0;
+        for (int i = 0; i < kStages; ++i) {
+            if (!t->pipe_stream[i])
+                CK(cudaStreamCreateWithFlags(&t->pipe_stream[i], cudaStreamNonBlocking));
+            CK(cudaMalloc(&t->pipe_buf[i], need));
+        }
+        t->pipe_bytes = need;
     }
-    CK(cudaStreamSynchronize(t->io_stream));
+    const uint64_t nchunks = (n + c - 1) / c;
+    for (uint64_t ci = 0; ci < nchunks; ++ci) {
+        const int st = (int)(ci % kStages);
+        cudaStream_t s = t->pipe_stream[st];
+        char *dk = (char *)t->pipe_buf[st];
+        char *dv = dk + kbytes;
+        uint32_t *db = (uint32_t *)(dv + vbytes);
+        const uint64_t off = ci * c;
+        const uint64_t m = (n - off) < c ? (n - off) : c;
+        CK(cudaMemcpyAsync(dk, (const char *)h_keys + off * t->kb, m * t->kb, cudaMemcpyHostToDevice, s));
+        TRY(dyc_find(t, dk, dv, h_hit_bits_out ? db : nullptr, m, s));
+        CK(cudaMemcpyAsync((char *)h_vals_out + off * t->vb, dv, m * t->vb, cudaMemcpyDeviceToHost, s));
+        if (h_hit_bits_out)
+            CK(cudaMemcpyAsync(h_hit_bits_out + off / 32, db, ((m + 31) / 32) * 4, cudaMemcpyDeviceToHost, s));
+    }
+    for (int i = 0; i < kStages; ++i)
+        if (t->pipe_stream[i]) CK(cudaStreamSynchronize(t->pipe_stream[i]));
     return DYC_OK;
 }
 
