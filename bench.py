@@ -147,6 +147,19 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+def load_traffic(args):
+    """DRAM bytes per find launch from the committed ncu capture, when it was
+    taken on this exact workload (profiles/k_find_traffic.json)."""
+    p = os.path.join(ROOT, "profiles", "k_find_traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    if (d["keys"], d["batch"], d["bucket_bytes"]) != (1 << args.log2_keys, 1 << args.log2_batch,
+                                                      args.bucket_bytes):
+        return None
+    return d["dram_bytes_read"] + d["dram_bytes_write"]
+
+
 def dist_setup():
     import torch
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -378,6 +391,29 @@ def main():
                         "achieved_gbs": round(achieved, 1), "frac": round(achieved / peak, 4),
                         "mismatches": bad_v + bad_h}
 
+    # ---- insert / erase on the same table (after the finds): erase 2^26
+    # present keys, then upsert them back (dedup + update-or-place path)
+    ops = {}
+    if not args.skip_variants:
+        ek = keys[:Q].contiguous()
+        ev = vals[:Q].contiguous()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        erased = t.erase(ek, no_resize=True, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ops["erase_mops"] = round(Q / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
+        e0.record(stream)
+        ust = t.insert(ek, ev, no_resize=True, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ops["upsert_mops"] = round(Q / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
+        ops["bulk_insert_mops"] = round(N / build_s / 1e6, 1)
+        ops["checks"] = {"erased": erased, "reinserted": ust["inserted"], "size": t.size}
+        assert erased == Q and ust["inserted"] == Q and t.size == N
+
     # ---- e2e: host buffers through the C ABI (dyc_find_host), pinned memory
     q0 = qs_e2e = batch("uniform100")
     qh = q0[0].cpu().pin_memory()
@@ -426,13 +462,14 @@ def main():
                 "h2d_bytes_per_step": Q * 4, "d2h_bytes_per_step": Q * 4 + Q // 8,
                 "api": "dyc_find_host (pinned host buffers)", "mismatches": e2e_bad},
         "roofline": {"bound": "hbm", "achieved": head["achieved_gbs"], "peak": peak,
-                     "unit": "GB/s", "frac": head["frac"], "traffic": None,
+                     "unit": "GB/s", "frac": head["frac"], "traffic": load_traffic(args),
                      "peak_kind": peak_kind,
                      "alg_bytes_per_op": head["alg_bytes_per_op"]},
         "cpu_baseline": cpu,
         "gpu_launches": args.steps,
         "clocks": clocks,
         "variants": results,
+        "ops": ops,
         "build": {"seconds": round(build_s, 3), "evict_steps": st["evict_steps"],
                   "overflowed": st["overflowed"], "capacity": t.capacity},
     }
