@@ -413,6 +413,31 @@ def main():
         ops["bulk_insert_mops"] = round(N / build_s / 1e6, 1)
         ops["checks"] = {"erased": erased, "reinserted": ust["inserted"], "size": t.size}
         assert erased == Q and ust["inserted"] == Q and t.size == N
+        # mixed batch (dyc_apply): 2^26 ops on distinct present keys, 50% find /
+        # 30% upsert (new value) / 20% erase; the table is restored untimed after
+        perm = torch.randperm(N, generator=gen, device=dev)[:Q]
+        mk = keys[perm].contiguous()
+        mv = (vals[perm] + 1).contiguous()
+        u = torch.rand(Q, generator=gen, device=dev)
+        mo = torch.where(u < 0.5, 0, torch.where(u < 0.8, 1, 2)).to(torch.uint8)
+        mout = torch.empty(Q, dtype=torch.int32, device=dev)
+        mbits = torch.empty(Q // 32, dtype=torch.int32, device=dev)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        t.apply(mo, mk, mv, out=mout, bits=mbits, no_resize=True, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ops["mixed_50f_30u_20e_mops"] = round(Q / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
+        mst = t.stats()
+        mbad = int((mout != vals[perm]).sum())  # every key was present: its old value
+        n_er = int((mo == 2).sum())
+        ops["checks"]["mixed"] = {"value_mismatches": mbad, "erased": mst["erased"],
+                                  "expected_erased": n_er, "updated": mst["updated"]}
+        assert mbad == 0 and mst["erased"] == n_er and t.size == N - n_er
+        t.insert(keys[perm].contiguous(), vals[perm].contiguous(), unique=True, no_resize=True,
+                 stream=stream)
+        torch.cuda.synchronize()
+        assert t.size == N
 
     # ---- e2e: host buffers through the C ABI (dyc_find_host), pinned memory
     q0 = qs_e2e = batch("uniform100")

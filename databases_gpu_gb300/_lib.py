@@ -14,6 +14,7 @@ from . import build as _build
 
 DYC_OK, DYC_ENOMEM, DYC_EINVAL, DYC_EOVERFLOW, DYC_ETIMEOUT, DYC_ECUDA, DYC_ENOTSUP = range(7)
 FLAG_UNIQUE, FLAG_NEW_KEYS, FLAG_NO_RESIZE = 1, 2, 4
+OP_FIND, OP_INSERT, OP_ERASE = 0, 1, 2  # dyc_apply op codes
 
 
 class DycConfig(C.Structure):
@@ -46,7 +47,7 @@ EXPORTS = [
     "dyc_config_default", "dyc_create", "dyc_destroy", "dyc_insert", "dyc_find", "dyc_erase",
     "dyc_resize_up", "dyc_resize_down", "dyc_size", "dyc_capacity", "dyc_layout",
     "dyc_subtable", "dyc_export", "dyc_last_stats", "dyc_insert_host", "dyc_find_host",
-    "dyc_erase_host", "dyc_status_string", "dyc_last_error", "dyc_erase_noalloc",
+    "dyc_erase_host", "dyc_status_string", "dyc_last_error", "dyc_erase_noalloc", "dyc_apply",
 ]
 
 _lock = threading.Lock()
@@ -76,6 +77,7 @@ def _declare(L):
         "dyc_find_host": (st, [T, vp, vp, vp, u64]),
         "dyc_erase_host": (st, [T, vp, u64, vp, C.POINTER(u64)]),
         "dyc_erase_noalloc": (st, [T, vp, u64, vp, C.POINTER(u64), u32, vp]),
+        "dyc_apply": (st, [T, vp, vp, vp, u64, vp, vp, u32, vp]),
         "dyc_status_string": (C.c_char_p, [st]),
         "dyc_last_error": (C.c_char_p, []),
     }

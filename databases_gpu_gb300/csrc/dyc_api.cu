@@ -92,6 +92,11 @@ struct dyc_table {
     size_t scratch_bytes = 0;
     Scratch S{};
     uint64_t chunk = kChunkDefault;
+    // mixed-batch scratch (dyc_apply), allocated on first use
+    void *apply_buf = nullptr;
+    size_t apply_bytes = 0;
+    dyc::ApplyScratch A{};
+    unsigned long long *h_actr = nullptr;  // pinned copy of A.ctr
     // host-form staging
     cudaStream_t io_stream = nullptr;
     void *d_io = nullptr;
@@ -434,6 +439,8 @@ dyc_status dyc_destroy(dyc_table *t) {
     if (t->d_ctr) cudaFree(t->d_ctr);
     if (t->h_ctr) cudaFreeHost(t->h_ctr);
     if (t->scratch) cudaFree(t->scratch);
+    if (t->apply_buf) cudaFree(t->apply_buf);
+    if (t->h_actr) cudaFreeHost(t->h_actr);
     if (t->d_io) cudaFree(t->d_io);
     if (t->io_stream) cudaStreamDestroy(t->io_stream);
     for (int i = 0; i < 3; ++i) {
@@ -708,6 +715,159 @@ dyc_status dyc_erase_host(dyc_table *t, const void *h_keys, uint64_t n,
 }
 
 }  // extern "C"
+
+// =============================================================================
+// dyc_apply: mixed batches of finds, inserts and erases in batch order.
+// The kernels (dyc_apply.cuh) group the ops by key, read every distinct key's
+// state before the batch, replay each key's ops in index order, and leave one
+// list of keys to erase and one of keys to upsert; the table's own erase and
+// insert phases apply those lists (unique keys), so placement, eviction walks,
+// overflow handling and the resize policy are the ones dyc_insert/dyc_erase use.
+// =============================================================================
+namespace {
+
+// Carve the mixed-batch scratch for `n` ops per chunk (grow only).
+dyc_status ensure_apply(dyc_table *t, uint64_t n) {
+    const uint64_t ops = n < 64 ? 64 : n;
+    const uint64_t cells = next_pow2(2 * ops);
+    const uint64_t blocks = (ops + dyc::kSortTile - 1) / dyc::kSortTile;
+    const size_t kb = (size_t)t->kb, vb = (size_t)t->vb;
+    const size_t sizes[] = {
+        cells * kb, cells * 4, cells * 4,            // cell_key, cell_cnt, cell_did
+        ops * 4, ops * kb, ops * 4, ops * 4, ops * 4,  // op_cell, dkey, dcnt, doff, dfill
+        ops * 4, ops * vb, (ops / 32 + 1) * 4,       // seg, pre_val, pre_hit
+        ops * kb, ops * vb, ops * kb,                // up_key, up_val, er_key
+        8 * 8, ops * 4,                              // ctr, large
+        ops * 4, ops * 4, ops * 4, ops * 4,          // sort buffers
+        blocks * 256 * 4, ops * 4};                  // hist, seg_start
+    size_t need = 0;
+    for (size_t b : sizes) need += (b + 255) & ~(size_t)255;
+    if (t->apply_buf && t->A.cap_ops >= ops) return DYC_OK;
+    if (t->apply_buf) {
+        CK(cudaDeviceSynchronize());
+        CK(cudaFree(t->apply_buf));
+        t->apply_buf = nullptr;
+        t->A = dyc::ApplyScratch{};
+    }
+    if (!t->h_actr) CK(cudaMallocHost(&t->h_actr, 8 * sizeof(unsigned long long)));
+    CK(cudaMalloc(&t->apply_buf, need));
+    t->apply_bytes = need;
+    char *p = (char *)t->apply_buf;
+    int k = 0;
+    auto carve = [&]() {
+        char *r = p;
+        p += (sizes[k++] + 255) & ~(size_t)255;
+        return (void *)r;
+    };
+    dyc::ApplyScratch &A = t->A;
+    A.cell_key = carve();
+    A.cell_cnt = (uint32_t *)carve();
+    A.cell_did = (uint32_t *)carve();
+    A.op_cell = (uint32_t *)carve();
+    A.dkey = carve();
+    A.dcnt = (uint32_t *)carve();
+    A.doff = (uint32_t *)carve();
+    A.dfill = (uint32_t *)carve();
+    A.seg = (uint32_t *)carve();
+    A.pre_val = carve();
+    A.pre_hit = (uint32_t *)carve();
+    A.up_key = carve();
+    A.up_val = carve();
+    A.er_key = carve();
+    A.ctr = (unsigned long long *)carve();
+    A.large = (uint32_t *)carve();
+    A.sort_key = (uint32_t *)carve();
+    A.sort_val = (uint32_t *)carve();
+    A.sort_key2 = (uint32_t *)carve();
+    A.sort_val2 = (uint32_t *)carve();
+    A.hist = (uint32_t *)carve();
+    A.seg_start = (uint32_t *)carve();
+    A.cap_cells = cells;
+    A.cap_ops = ops;
+    return DYC_OK;
+}
+
+dyc_status read_apply_counters(dyc_table *t, cudaStream_t s) {
+    CK(cudaMemcpyAsync(t->h_actr, t->A.ctr, 8 * sizeof(unsigned long long),
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return DYC_OK;
+}
+
+dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const void *vals,
+                       uint64_t n, void *vals_out, uint32_t *bits_out, uint32_t flags,
+                       cudaStream_t s) {
+    const dyc::ApplyScratch &A = t->A;
+    const LaunchCtx L = ctx(t, s);
+    CK(cudaMemsetAsync(A.cell_key, 0, (size_t)A.cap_cells * t->kb, s));
+    CK(cudaMemsetAsync(A.cell_cnt, 0, (size_t)A.cap_cells * 4, s));
+    CK(cudaMemsetAsync(A.ctr, 0, 8 * sizeof(unsigned long long), s));
+    if (bits_out) CK(cudaMemsetAsync(bits_out, 0, (size_t)((n + 31) / 32) * 4, s));
+    cudaError_t e = KB_CALL(t, apply_group, L, A, keys, n);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "apply group kernels: %s", cudaGetErrorString(e));
+    TRY(read_apply_counters(t, s));
+    const uint64_t nd = t->h_actr[0];
+    e = KB_CALL(t, apply_replay, L, A, t->D, t->sb, ops, keys, vals, (uint32_t)t->vb, vals_out,
+                bits_out, n, nd);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "apply replay kernels: %s", cudaGetErrorString(e));
+    TRY(read_apply_counters(t, s));
+    if (t->h_actr[4]) {
+        e = KB_CALL(t, apply_long, L, A, ops, vals, (uint32_t)t->vb, vals_out, bits_out, n,
+                    t->h_actr[4]);
+        if (e != cudaSuccess)
+            return fail(DYC_ECUDA, "apply long-segment kernels: %s", cudaGetErrorString(e));
+        TRY(read_apply_counters(t, s));
+    }
+    const uint64_t nu = t->h_actr[2], ne = t->h_actr[3];
+    if (ne) TRY(erase_chunk(t, A.er_key, ne, nullptr, DYC_FLAG_UNIQUE, s));
+    if (nu) {
+        if (t->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE)) {
+            int guard = 0;
+            while ((double)(t->size + nu) > t->cfg.upper_load * (double)t->capacity &&
+                   guard++ < 64)
+                TRY(resize_up_impl(t, s));
+        }
+        TRY(insert_chunk(t, A.up_key, A.up_val, nu, DYC_FLAG_UNIQUE, s));
+    }
+    return DYC_OK;
+}
+
+}  // namespace
+
+extern "C" dyc_status dyc_apply(dyc_table *t, const uint8_t *d_ops, const void *d_keys,
+                                const void *d_vals, uint64_t n, void *d_vals_out,
+                                uint32_t *d_bits_out, uint32_t flags, void *stream) {
+    if (!t) return fail(DYC_EINVAL, "null table");
+    if (n == 0) return DYC_OK;
+    if (!d_ops || !d_keys || !d_vals) return fail(DYC_EINVAL, "null op, key or value array");
+    TRY(set_device(t));
+    cudaStream_t s = (cudaStream_t)stream;
+    t->last = dyc_op_stats{};
+    const uint64_t chunk = t->chunk;
+    const uint64_t m0 = n < chunk ? n : chunk;
+    TRY(ensure_apply(t, m0));
+    TRY(ensure_scratch(t, m0));
+    for (uint64_t off = 0; off < n; off += chunk) {
+        const uint64_t m = (n - off) < chunk ? (n - off) : chunk;
+        TRY(apply_chunk(t, d_ops + off, (const char *)d_keys + off * t->kb,
+                        (const char *)d_vals + off * t->vb, m,
+                        d_vals_out ? (char *)d_vals_out + off * t->vb : nullptr,
+                        d_bits_out ? d_bits_out + off / 32 : nullptr, flags, s));
+    }
+    // downsize check after the batch, as after an erase batch (api.cpp:494-505)
+    if (t->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE) &&
+        (double)t->size < t->cfg.lower_load * (double)t->capacity &&
+        t->capacity > t->cfg.min_downsize_capacity) {
+        const dyc_op_stats keep = t->last;
+        dyc_status st = resize_down_impl(t, s);
+        if (st != DYC_OK && st != DYC_EINVAL) return st;
+        const uint64_t downs = t->last.resizes_down, ups = t->last.resizes_up;
+        t->last = keep;
+        t->last.resizes_down = downs;
+        t->last.resizes_up = ups;
+    }
+    return DYC_OK;
+}
 
 // =============================================================================
 // dyc_erase_noalloc: erase whose batch-dedup table lives in a fixed device

@@ -47,6 +47,33 @@ struct Scratch {
     uint64_t list_cap;      // entries per list
 };
 
+// Scratch of one mixed batch of at most `cap_ops` ops.
+struct ApplyScratch {
+    void *cell_key;            // cap_cells keys (4 or 8 bytes), 0 = free
+    uint32_t *cell_cnt;        // ops per cell
+    uint32_t *cell_did;        // distinct id of a cell
+    uint32_t *op_cell;         // cell of each op
+    void *dkey;                // distinct keys
+    uint32_t *dcnt, *doff, *dfill;  // per distinct key: ops, segment start, fill cursor
+    uint32_t *seg;             // op indices grouped by key
+    void *pre_val;             // pre-batch value per distinct key
+    uint32_t *pre_hit;         // pre-batch hit bits per distinct key
+    void *up_key, *up_val;     // upserts to apply
+    void *er_key;              // erases to apply
+    unsigned long long *ctr;   // [0] distinct keys, [1] ops placed, [2] upserts, [3] erases,
+                               // [4] long segments
+    uint32_t *large;           // distinct ids of long segments
+    uint32_t *sort_key, *sort_val, *sort_key2, *sort_val2;  // radix sort buffers
+    uint32_t *hist;            // 256 x blocks digit counts
+    uint32_t *seg_start;       // start of each distinct key in the sorted order
+    uint64_t cap_cells;        // power of two, >= 2 * cap_ops
+    uint64_t cap_ops;
+};
+
+// radix-sort elements per block per pass (256 threads x 16)
+constexpr int kSortTile = 4096;
+
+
 // Launch parameters picked once per kernel from the occupancy calculator.
 struct LaunchCtx {
     int sms;
@@ -86,6 +113,17 @@ template <int KB> struct Ops {
     static cudaError_t collect(const LaunchCtx &L, int sb, const void *sub, uint32_t nb,
                                void *list, unsigned long long *list_count, uint64_t list_cap,
                                unsigned long long *spill);
+    // mixed batches (dyc_apply.cuh): group + compact; scatter + pre-batch
+    // find + replay; the long-segment path
+    static cudaError_t apply_group(const LaunchCtx &L, const ApplyScratch &A, const void *keys,
+                                  uint64_t n);
+    static cudaError_t apply_replay(const LaunchCtx &L, const ApplyScratch &A, const Desc &D,
+                                   int sb, const uint8_t *ops, const void *keys, const void *vals,
+                                   uint32_t vb, void *vals_out, uint32_t *bits_out, uint64_t n,
+                                   uint64_t nd);
+    static cudaError_t apply_long(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
+                                  const void *vals, uint32_t vb, void *vals_out, uint32_t *bits_out,
+                                  uint64_t n, uint64_t nlarge);
     // set the overflow bit of every bucket of a subtable
     static cudaError_t mark_all(const LaunchCtx &L, int sb, void *sub, uint32_t nb);
     static cudaError_t export_all(const LaunchCtx &L, const Desc &D, int sb, void *keys,

@@ -7,6 +7,7 @@
 #include <mutex>
 #include <unordered_map>
 
+#include "dyc_apply.cuh"
 #include "dyc_kernels.cuh"
 
 namespace dyc {
@@ -151,6 +152,61 @@ cudaError_t Ops<KB>::collect(const LaunchCtx &L, int sb, const void *sub, uint32
         k<<<grid_for((const void *)k, L, nb), 256, 0, L.stream>>>((const char *)sub, nb, list,
                                                                   list_count, list_cap, spill);
     });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::apply_group(const LaunchCtx &L, const ApplyScratch &A, const void *keys,
+                                 uint64_t n) {
+    if (n == 0) return cudaSuccess;
+    auto g = k_apply_group<KB>;
+    g<<<grid_for((const void *)g, L, n), 256, 0, L.stream>>>(A, keys, n);
+    auto c = k_apply_compact<KB>;
+    c<<<grid_for((const void *)c, L, A.cap_cells), 256, 0, L.stream>>>(A);
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::apply_replay(const LaunchCtx &L, const ApplyScratch &A, const Desc &D, int sb,
+                                  const uint8_t *ops, const void *keys, const void *vals,
+                                  uint32_t vb, void *vals_out, uint32_t *bits_out, uint64_t n,
+                                  uint64_t nd) {
+    if (n == 0) return cudaSuccess;
+    auto sc = k_apply_scatter<KB>;
+    sc<<<grid_for((const void *)sc, L, n), 256, 0, L.stream>>>(A, n);
+    // state of every distinct key before the batch
+    cudaError_t e = find(L, D, sb, A.dkey, A.pre_val, vb, A.pre_hit, nd);
+    if (e != cudaSuccess) return e;
+    auto r = k_apply_replay<KB>;
+    r<<<grid_for((const void *)r, L, n > nd ? n : nd), 256, 0, L.stream>>>(A, ops, keys, vals, vb,
+                                                                            vals_out, bits_out, n, nd);
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::apply_long(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
+                                const void *vals, uint32_t vb, void *vals_out, uint32_t *bits_out,
+                                uint64_t n, uint64_t nlarge) {
+    if (n == 0 || nlarge == 0) return cudaSuccess;
+    auto si = k_apply_sort_init<KB>;
+    si<<<grid_for((const void *)si, L, n), 256, 0, L.stream>>>(A, n);
+    const unsigned blocks = (unsigned)((n + kSortTile - 1) / kSortTile);
+    uint32_t *k0 = A.sort_key, *v0 = A.sort_val, *k1 = A.sort_key2, *v1 = A.sort_val2;
+    for (int shift = 0; shift < 24; shift += 8) {  // distinct ids fit in 24 bits
+        k_radix_hist<KB><<<blocks, 256, 0, L.stream>>>(k0, n, shift, A.hist);
+        k_scan_exclusive<KB><<<1, 1024, 0, L.stream>>>(A.hist, (uint64_t)blocks * 256);
+        k_radix_scatter<KB><<<blocks, 256, 0, L.stream>>>(k0, v0, n, shift, A.hist, k1, v1);
+        uint32_t *tk = k0, *tv = v0;
+        k0 = k1;
+        v0 = v1;
+        k1 = tk;
+        v1 = tv;
+    }
+    auto ss = k_apply_seg_start<KB>;
+    ss<<<grid_for((const void *)ss, L, n), 256, 0, L.stream>>>(A, k0, n);
+    auto rl = k_apply_replay_long<KB>;
+    rl<<<grid_for((const void *)rl, L, nlarge * 32), 256, 0, L.stream>>>(A, v0, ops, vals, vb,
+                                                                         vals_out, bits_out, nlarge);
     return cudaGetLastError();
 }
 

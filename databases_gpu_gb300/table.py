@@ -155,6 +155,29 @@ class DyCuckoo:
                                C.byref(cnt), flags, _stream_ptr(stream)), "dyc_erase")
         return int(cnt.value)
 
+    def apply(self, ops, keys, values, out=None, bits=None, no_resize: bool = False,
+              stream=None):
+        """Mixed batch (dyc_apply): ops is a uint8 tensor of OP_FIND /
+        OP_INSERT / OP_ERASE, applied in index order. Returns (out, bits):
+        the value each op saw (found / previous / removed, 0 if absent) and
+        one bit per op, set when the key was present before the op."""
+        torch = _torch()
+        n = keys.numel()
+        if ops.numel() != n or values.numel() != n:
+            raise ValueError("ops, keys and values differ in length")
+        if ops.dtype != torch.uint8:
+            raise TypeError("ops must be uint8")
+        if out is None:
+            out = torch.empty(n, dtype=self.value_dtype(), device=keys.device)
+        if bits is None:
+            bits = torch.empty((n + 31) // 32, dtype=torch.int32, device=keys.device)
+        check(self.L.dyc_apply(self._h, _ptr(ops, "ops", 1), _ptr(keys, "keys", self.key_bytes),
+                               _ptr(values, "values", self.value_bytes),
+                               n, _ptr(out, "out", self.value_bytes), _ptr(bits, "bits", 4),
+                               FLAG_NO_RESIZE if no_resize else 0, _stream_ptr(stream)),
+              "dyc_apply")
+        return out, bits
+
     def resize_up(self, stream=None) -> None:
         check(self.L.dyc_resize_up(self._h, _stream_ptr(stream)), "dyc_resize_up")
 

@@ -172,6 +172,31 @@ dyc_status dyc_find_host(dyc_table *t, const void *h_keys, void *h_vals_out,
 dyc_status dyc_erase_host(dyc_table *t, const void *h_keys, uint64_t n,
                           uint32_t *h_erased_bits_out, uint64_t *erased_count);
 
+/* Op codes of dyc_apply. */
+#define DYC_OP_FIND 0u
+#define DYC_OP_INSERT 1u
+#define DYC_OP_ERASE 2u
+
+/* Mixed batch: n ops, op i = (d_ops[i], d_keys[i], d_vals[i]), applied in
+ * batch index order. The reference names this kernel family but never
+ * shipped it (README.md:9-10, "mixed insert/find/delete kernels ... not
+ * uploaded yet"); the semantics are those of the single-op calls, in order:
+ *   - FIND   : d_vals_out[i] = value (0 if absent), bit i = present;
+ *   - INSERT : upsert of d_vals[i]; d_vals_out[i] = previous value (0 if the
+ *              key was absent), bit i = key was present before the op;
+ *   - ERASE  : removes the key; d_vals_out[i] = removed value (0 if absent),
+ *              bit i = key was present before the op.
+ * An op sees the latest earlier op on its key in the batch, else the table
+ * as it was before the call. Ops on key 0 miss and change nothing.
+ * d_vals is read only for INSERT ops but must hold n values; d_vals_out and
+ * d_bits_out (ceil(n/32) words) are optional. Ops other than 0/1/2 are
+ * treated as FIND. Inserts may upsize first (projected load above
+ * upper_load); the batch may downsize after (load below lower_load), unless
+ * DYC_FLAG_NO_RESIZE. Returns after the batch is in the table. */
+dyc_status dyc_apply(dyc_table *t, const uint8_t *d_ops, const void *d_keys, const void *d_vals,
+                     uint64_t n, void *d_vals_out, uint32_t *d_bits_out, uint32_t flags,
+                     void *stream);
+
 /* Erase that allocates nothing. It has no counterpart in the reference.
  *
  * For callers that must not allocate device memory while they run: a host

@@ -725,7 +725,8 @@ void orc_map_apply(orc_map *m, const uint8_t *ops, const uint64_t *k, const uint
         switch (ops[i]) {
         case 1: /* insert */
             if (!key) break;
-            if (found) {
+            if (found) { /* the previous value comes back, as for erase */
+                rv = m->v[h];
                 m->v[h] = v[i];
                 hit = 1;
             } else {

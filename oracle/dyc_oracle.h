@@ -83,7 +83,9 @@ uint64_t orc_ck_export(const orc_ck *t, uint32_t *k, uint32_t *v);
 const uint64_t *orc_ck_subtable(const orc_ck *t, uint32_t i);
 
 /* ---- semantic map (u64 keys and values; key 0 is never stored) ----
- * op codes for orc_map_apply: 0 = find, 1 = insert (upsert), 2 = erase.     */
+ * op codes for orc_map_apply: 0 = find, 1 = insert (upsert), 2 = erase.
+ * Per op, out_v/out_hit = the key's value / presence just before the op
+ * (the value found, replaced or removed; 0 and no hit when absent).        */
 typedef struct orc_map orc_map;
 orc_map *orc_map_new(uint64_t cap_hint);
 void     orc_map_free(orc_map *m);

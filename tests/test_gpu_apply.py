@@ -1,0 +1,151 @@
+"""GPU parity of mixed batches (dyc_apply) against the oracle's map, op by op.
+
+For every op the value it saw (found / replaced / removed, 0 when absent) and
+its hit bit (key present just before the op) must equal the oracle's, which
+runs the same ops one at a time in index order; the table's full contents
+must equal the oracle's after every batch. Cases: unique keys, heavy
+repetition (segments replayed by one thread), keys repeated thousands of
+times (segments replayed by a warp after the radix sort), key 0, u64 keys,
+batches that span several internal chunks, and growth/shrink through the
+resize policy.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.helpers import assert_same_contents, to_dev, to_host, unique_u32, unique_u64
+
+pytestmark = pytest.mark.gpu
+
+
+def _dg():
+    import databases_gpu_gb300 as dg
+    return dg
+
+
+def _apply_and_compare(t, m, ops, keys, vals, label):
+    out, bits = t.apply(to_dev(ops), to_dev(keys), to_dev(vals))
+    gv = to_host(out, t.value_bytes).astype(np.uint64)
+    gh = _dg().unpack_bits(bits, keys.size)
+    ov, oh = m.apply(ops, keys.astype(np.uint64), vals.astype(np.uint64))
+    bad = np.nonzero(gh != oh)[0]
+    assert bad.size == 0, "%s: %d hit bits differ, first op %d (op %d key %d)" % (
+        label, bad.size, bad[0], ops[bad[0]], keys[bad[0]])
+    bad = np.nonzero(gv != ov)[0]
+    assert bad.size == 0, "%s: %d values differ, first op %d (op %d key %d gpu %d oracle %d)" % (
+        label, bad.size, bad[0], ops[bad[0]], keys[bad[0]], gv[bad[0]], ov[bad[0]])
+    assert_same_contents(t, m, label)
+    return gh
+
+
+def _mixed(rng, n, key_pool, p=(0.5, 0.3, 0.2), vdtype=np.uint32):
+    ops = rng.choice(np.array([0, 1, 2], np.uint8), size=n, p=list(p))
+    keys = key_pool[rng.integers(0, key_pool.size, n)]
+    vals = (rng.integers(1, 1 << 31, n)).astype(vdtype)
+    return ops, keys, vals
+
+
+def test_apply_unique_keys_u32():
+    rng = np.random.default_rng(7)
+    pool = unique_u32(1 << 20, seed=99)
+    t = _dg().DyCuckoo(1 << 20)
+    m = O.Map(1 << 20)
+    # preload half, then a mixed batch over all keys, each key once
+    pre = pool[: 1 << 19]
+    t.insert(to_dev(pre), to_dev(pre ^ np.uint32(0x1234)))
+    m.insert(pre, pre ^ np.uint32(0x1234))
+    perm = rng.permutation(pool.size)
+    keys = pool[perm]
+    ops = rng.choice(np.array([0, 1, 2], np.uint8), size=keys.size)
+    vals = rng.integers(1, 1 << 31, keys.size).astype(np.uint32)
+    gh = _apply_and_compare(t, m, ops, keys, vals, "unique mixed")
+    assert 0 < gh.sum() < keys.size
+    t.close()
+
+
+@pytest.mark.parametrize("distinct", [64, 5000, 300_000])
+def test_apply_repeated_keys_u32(distinct):
+    """Ops on few distinct keys: many ops per key in one batch; 64 distinct
+    keys over 2^20 ops gives ~16k ops per key (the long-segment path)."""
+    rng = np.random.default_rng(distinct)
+    pool = unique_u32(distinct, seed=distinct + 1)
+    t = _dg().DyCuckoo(1 << 16)
+    m = O.Map()
+    for b in range(3):
+        ops, keys, vals = _mixed(rng, 1 << 20, pool)
+        _apply_and_compare(t, m, ops, keys, vals, "repeated %d batch %d" % (distinct, b))
+    t.close()
+
+
+def test_apply_segment_length_boundaries():
+    """Keys with exactly 63, 64, 65, 96 and 1000 ops in one batch, interleaved
+    with keys seen once, covering both replay paths and their boundary."""
+    rng = np.random.default_rng(3)
+    heavy = unique_u32(5, seed=5)
+    lengths = [63, 64, 65, 96, 1000]
+    light = unique_u32(20000, seed=6)
+    light = light[~np.isin(light, heavy)]
+    keys = np.concatenate([np.repeat(heavy, lengths), light])
+    keys = keys[rng.permutation(keys.size)]
+    ops = rng.choice(np.array([0, 1, 2], np.uint8), size=keys.size, p=[0.4, 0.4, 0.2])
+    vals = rng.integers(1, 1 << 31, keys.size).astype(np.uint32)
+    t = _dg().DyCuckoo(1 << 16)
+    m = O.Map()
+    t.insert(to_dev(heavy[:3]), to_dev(heavy[:3]))
+    m.insert(heavy[:3], heavy[:3])
+    _apply_and_compare(t, m, ops, keys, vals, "segment boundaries")
+    _apply_and_compare(t, m, ops, keys, vals + np.uint32(1), "segment boundaries again")
+    t.close()
+
+
+def test_apply_key_zero_and_unknown_ops():
+    """Ops on key 0 miss and change nothing; op codes other than 0/1/2 read."""
+    rng = np.random.default_rng(11)
+    pool = np.concatenate([unique_u32(1000, seed=12), np.zeros(1, np.uint32)])
+    ops, keys, vals = _mixed(rng, 100_000, pool)
+    t = _dg().DyCuckoo(4096)
+    m = O.Map()
+    _apply_and_compare(t, m, ops, keys, vals, "key 0")
+    ops2 = ops.copy()
+    ops2[::7] = 9  # treated as find
+    oracle_ops = ops2.copy()
+    oracle_ops[oracle_ops > 2] = 0
+    out, bits = t.apply(to_dev(ops2), to_dev(keys), to_dev(vals))
+    ov, oh = m.apply(oracle_ops, keys.astype(np.uint64), vals.astype(np.uint64))
+    assert np.array_equal(_dg().unpack_bits(bits, keys.size), oh)
+    assert np.array_equal(to_host(out, 4).astype(np.uint64), ov)
+    assert_same_contents(t, m, "unknown op codes")
+    t.close()
+
+
+@pytest.mark.parametrize("distinct", [100, 1 << 18])
+def test_apply_u64_keys(distinct):
+    rng = np.random.default_rng(distinct)
+    pool = unique_u64(distinct, seed=77)
+    t = _dg().DyCuckoo(1 << 16, key_bytes=8, value_bytes=8)
+    m = O.Map()
+    for b in range(2):
+        ops, keys, vals = _mixed(rng, 1 << 19, pool, vdtype=np.uint64)
+        vals = vals * np.uint64(0x100000001)
+        _apply_and_compare(t, m, ops, keys, vals, "u64 %d batch %d" % (distinct, b))
+    t.close()
+
+
+def test_apply_spans_chunks_and_resizes():
+    """A batch longer than one internal chunk (2^22 ops) keeps batch order
+    across the chunk boundary; inserts grow the table, erases shrink it."""
+    rng = np.random.default_rng(21)
+    pool = unique_u32(1 << 21, seed=31)
+    t = _dg().DyCuckoo(1 << 12)
+    m = O.Map()
+    n = (1 << 22) + 12345
+    ops, keys, vals = _mixed(rng, n, pool, p=(0.2, 0.7, 0.1))
+    _apply_and_compare(t, m, ops, keys, vals, "growth across chunks")
+    cap_big = t.capacity
+    # erase most keys: the post-batch policy may downsize
+    present = m.export()[0].astype(np.uint32)
+    er = present[rng.permutation(present.size)[: present.size * 9 // 10]]
+    ops = np.full(er.size, 2, np.uint8)
+    _apply_and_compare(t, m, ops, er, np.zeros(er.size, np.uint32), "mass erase")
+    assert t.capacity <= cap_big
+    t.close()
