@@ -728,7 +728,7 @@ namespace {
 
 // Carve the mixed-batch scratch for `n` ops per chunk (grow only).
 dyc_status ensure_apply(dyc_table *t, uint64_t n) {
-    const uint64_t ops = n < 64 ? 64 : n;
+    const uint64_t ops = n < 128 ? 128 : n;  // cap_cells >= 256: whole blocks
     const uint64_t cells = next_pow2(2 * ops);
     const uint64_t blocks = (ops + dyc::kSortTile - 1) / dyc::kSortTile;
     const size_t kb = (size_t)t->kb, vb = (size_t)t->vb;

@@ -63,6 +63,41 @@ __global__ void __launch_bounds__(256) k_apply_group(const __grid_constant__ App
     }
 }
 
+// Block-wide allocation from a shared counter: thread gets base + the sum of
+// x over the threads before it in the block; one atomic per block (the same
+// address taken once per warp serialised these kernels). Every thread of the
+// block must call it at the same point.
+__device__ __forceinline__ uint32_t block_alloc(unsigned long long *ctr, uint32_t x) {
+    __shared__ uint32_t wsum[32];
+    __shared__ unsigned long long bbase;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        const uint32_t v = lane < nw ? wsum[lane] : 0u;
+        uint32_t vi = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, vi, o);
+            if (lane >= o) vi += y;
+        }
+        if (lane < nw) wsum[lane] = vi - v;
+        if (lane == 31) bbase = vi ? atomicAdd(ctr, (unsigned long long)vi) : 0ull;
+    }
+    __syncthreads();
+    const uint32_t r = (uint32_t)bbase + wsum[w] + incl - x;
+    __syncthreads();  // wsum / bbase are reused by the next call
+    return r;
+}
+
+// The loop steps whole blocks (cap_cells is a multiple of 256), so every
+// thread reaches each block_alloc.
 template <int KB>
 __global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ ApplyScratch A) {
     using K = typename SlotT<KB>::K;
@@ -70,9 +105,9 @@ __global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ A
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < A.cap_cells; c += stride) {
         const uint32_t cnt = A.cell_cnt[c];
+        const uint32_t d = block_alloc(&A.ctr[0], cnt ? 1u : 0u);
+        const uint32_t off = block_alloc(&A.ctr[1], cnt);
         if (!cnt) continue;
-        const uint32_t d = (uint32_t)atomicAdd(&A.ctr[0], 1ull);
-        const uint32_t off = (uint32_t)atomicAdd(&A.ctr[1], (unsigned long long)cnt);
         A.cell_did[c] = d;
         ((K *)A.dkey)[d] = ck[c];
         A.dcnt[d] = cnt;
@@ -110,58 +145,65 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
     // key-0 ops (no cell): miss, output 0
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
         if (A.op_cell[i] == 0xffffffffu && vals_out) store_val(vals_out, vb, i, 0ull);
-    for (uint64_t d = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += stride) {
-        const uint32_t cnt = A.dcnt[d], off = A.doff[d];
-        if (cnt > kShortSeg) {  // replayed by a warp after a stable sort
-            A.large[atomicAdd(&A.ctr[4], 1ull)] = (uint32_t)d;
-            continue;
-        }
-        uint32_t *s = A.seg + off;
-        // insertion sort of the segment by op index (segments are short)
-        for (uint32_t a = 1; a < cnt; ++a) {
-            const uint32_t x = s[a];
-            uint32_t b = a;
-            while (b > 0 && s[b - 1] > x) {
-                s[b] = s[b - 1];
-                --b;
-            }
-            s[b] = x;
-        }
-        const K k = ((const K *)A.dkey)[d];
-        const bool pre_present = (A.pre_hit[d >> 5] >> (d & 31)) & 1u;
-        const uint64_t pre_value = load_val(A.pre_val, vb, d);
-        bool present = pre_present;
-        uint64_t value = pre_value;
-        for (uint32_t a = 0; a < cnt; ++a) {
-            const uint32_t i = s[a];
-            const uint8_t op = ops[i];
-            bool bit = false;
-            uint64_t out = 0ull;
-            if (op == kOpInsert) {
-                bit = present;
-                out = present ? value : 0ull;
-                present = true;
-                value = load_val(vals, vb, i);
-            } else if (op == kOpErase) {
-                bit = present;
-                out = present ? value : 0ull;
-                present = false;
-                value = 0ull;
+    // whole blocks step through the distinct keys so every thread reaches
+    // the block_alloc calls
+    for (uint64_t d0 = (uint64_t)blockIdx.x * blockDim.x; d0 < nd; d0 += stride) {
+        const uint64_t d = d0 + threadIdx.x;
+        bool up = false, er = false, lg = false;
+        K k = 0;
+        uint64_t value = 0ull;
+        if (d < nd) {
+            const uint32_t cnt = A.dcnt[d], off = A.doff[d];
+            if (cnt > kShortSeg) {
+                lg = true;  // replayed by a warp after a stable sort
             } else {
-                bit = present;
-                out = present ? value : 0ull;
+                uint32_t *s = A.seg + off;
+                // insertion sort of the segment by op index (segments are short)
+                for (uint32_t a = 1; a < cnt; ++a) {
+                    const uint32_t x = s[a];
+                    uint32_t b = a;
+                    while (b > 0 && s[b - 1] > x) {
+                        s[b] = s[b - 1];
+                        --b;
+                    }
+                    s[b] = x;
+                }
+                k = ((const K *)A.dkey)[d];
+                const bool pre_present = (A.pre_hit[d >> 5] >> (d & 31)) & 1u;
+                const uint64_t pre_value = load_val(A.pre_val, vb, d);
+                bool present = pre_present;
+                value = pre_value;
+                for (uint32_t a = 0; a < cnt; ++a) {
+                    const uint32_t i = s[a];
+                    const uint8_t op = ops[i];
+                    // every op reports the state just before it
+                    const bool bit = present;
+                    const uint64_t out = present ? value : 0ull;
+                    if (op == kOpInsert) {
+                        present = true;
+                        value = load_val(vals, vb, i);
+                    } else if (op == kOpErase) {
+                        present = false;
+                        value = 0ull;
+                    }
+                    if (vals_out) store_val(vals_out, vb, i, out);
+                    if (bit && bits_out) atomicOr(&bits_out[i >> 5], 1u << (i & 31));
+                }
+                up = present && (!pre_present || value != pre_value);
+                er = !present && pre_present;
             }
-            if (vals_out) store_val(vals_out, vb, i, out);
-            if (bit && bits_out) atomicOr(&bits_out[i >> 5], 1u << (i & 31));
         }
-        if (present && (!pre_present || value != pre_value)) {
-            const uint32_t u = (uint32_t)atomicAdd(&A.ctr[2], 1ull);
+        const uint32_t u = block_alloc(&A.ctr[2], up ? 1u : 0u);
+        const uint32_t e = block_alloc(&A.ctr[3], er ? 1u : 0u);
+        const uint32_t l = block_alloc(&A.ctr[4], lg ? 1u : 0u);
+        if (up) {
             ((K *)A.up_key)[u] = k;
             if (vb == 4) ((uint32_t *)A.up_val)[u] = (uint32_t)value;
             else ((unsigned long long *)A.up_val)[u] = value;
-        } else if (!present && pre_present) {
-            const uint32_t e = (uint32_t)atomicAdd(&A.ctr[3], 1ull);
+        } else if (er) {
             ((K *)A.er_key)[e] = k;
+        } else if (lg) {
+            A.large[l] = (uint32_t)d;
         }
     }
 }
