@@ -265,6 +265,71 @@ def run_line_probe():
     print(json.dumps(d))
 
 
+def unpack_bits_dev(bits, n, torch):
+    sh = torch.arange(32, dtype=torch.int32, device=bits.device)
+    return ((bits.view(-1, 1) >> sh) & 1).flatten()[:n].bool()
+
+
+def run_resize_stream(args, dev, torch, dg):
+    """Dynamic resize stream: u64 keys/values, grow then shrink batches of
+    mixed ops through dyc_apply; per-batch CUDA-event latency, exact checks
+    of table size, find hits and erase counts after every batch."""
+    from databases_gpu_gb300.workloads import ResizeStream
+    B = 1 << args.stream_log2_batch
+    nb = args.stream_batches
+    ws = ResizeStream(B, nb // 2, nb - nb // 2, 1 << args.stream_log2_start,
+                      1 << args.stream_log2_peak, dup=0.05, seed=10327, device=dev)
+    t = dg.DyCuckoo(1 << args.stream_log2_start, key_bytes=8, value_bytes=8, upper_load=0.90,
+                    lower_load=0.35, min_downsize_capacity=0, max_evictions=args.max_evictions,
+                    device=dev.index or 0)
+    k0, v0 = ws.preload()
+    t.insert(k0, v0)
+    del k0, v0
+    stream = torch.cuda.current_stream()
+    out = torch.empty(B, dtype=torch.int64, device=dev)
+    bits = torch.empty((B + 31) // 32, dtype=torch.int32, device=dev)
+    lat = []
+    bad = 0
+    ups = downs = 0
+    peak_cap = 0
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    for b in range(len(ws)):
+        sb = ws.next()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        t.apply(sb.ops, sb.keys, sb.vals, out=out, bits=bits, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        lat.append(e0.elapsed_time(e1))
+        st = t.stats()
+        ups += st["resizes_up"]
+        downs += st["resizes_down"]
+        peak_cap = max(peak_cap, t.capacity)
+        hits = unpack_bits_dev(bits, B, torch)
+        fh = int((hits & (sb.ops == 0)).sum())
+        bad += int(t.size != sb.size_after) + int(fh != sb.find_ops) + \
+            int(st["erased"] != sb.erase_hits)
+    total_ms = sum(lat)
+    lat_sorted = sorted(lat)
+    res = {
+        "workload": "dynamic resize stream: u64 keys/values, 4 subtables, %d batches of 2^%d "
+                    "ops, 60/30/10 insert/find/erase growing 2^%d -> 2^%d keys then 10/30/60 "
+                    "shrinking back; upsize > 0.90, downsize < 0.35; 5%% in-batch repeats"
+                    % (nb, args.stream_log2_batch, args.stream_log2_start, args.stream_log2_peak),
+        "mops": round(nb * B / (total_ms / 1e3) / 1e6, 1),
+        "batch_ms_p50": round(lat_sorted[len(lat) // 2], 3),
+        "batch_ms_p99": round(lat_sorted[min(len(lat) - 1, int(len(lat) * 0.99))], 3),
+        "total_s": round(total_ms / 1e3, 3),
+        "resizes_up": ups, "resizes_down": downs, "peak_capacity": peak_cap,
+        "final_capacity": t.capacity, "final_size": t.size,
+        "check_failures": bad,
+        "api": "dyc_apply (device buffers; resizes inside the timed calls)",
+    }
+    t.close()
+    return res
+
+
 def workload_config(args, lf):
     return {
         "workload": "large static table find: u32 keys/values, 4 subtables, 2^%d unique keys "
@@ -291,6 +356,12 @@ def main():
     ap.add_argument("--skip-variants", action="store_true")
     ap.add_argument("--line-probe", action="store_true",
                     help="measure the random 128-byte line ceiling of this GPU and exit")
+    ap.add_argument("--skip-stream", action="store_true",
+                    help="skip the dynamic resize stream workload")
+    ap.add_argument("--stream-batches", type=int, default=512)
+    ap.add_argument("--stream-log2-batch", type=int, default=22)
+    ap.add_argument("--stream-log2-start", type=int, default=20)
+    ap.add_argument("--stream-log2-peak", type=int, default=27)
     ap.add_argument("--mixes", default="uniform100,uniform10,zipf100,zipf10",
                     help="query mixes to time; the first is the headline")
     args = ap.parse_args()
@@ -439,6 +510,11 @@ def main():
         torch.cuda.synchronize()
         assert t.size == N
 
+    # ---- dynamic resize stream (its own u64 table; the find table is kept)
+    workloads = {}
+    if not args.skip_stream and not args.skip_variants:
+        workloads["resize_stream"] = run_resize_stream(args, dev, torch, dg)
+
     # ---- e2e: host buffers through the C ABI (dyc_find_host), pinned memory
     q0 = qs_e2e = batch("uniform100")
     qh = q0[0].cpu().pin_memory()
@@ -495,6 +571,7 @@ def main():
         "clocks": clocks,
         "variants": results,
         "ops": ops,
+        "workloads": workloads,
         "build": {"seconds": round(build_s, 3), "evict_steps": st["evict_steps"],
                   "overflowed": st["overflowed"], "capacity": t.capacity},
     }

@@ -149,3 +149,39 @@ def test_apply_spans_chunks_and_resizes():
     _apply_and_compare(t, m, ops, er, np.zeros(er.size, np.uint32), "mass erase")
     assert t.capacity <= cap_big
     t.close()
+
+
+def test_resize_stream_u64_matches_oracle_every_batch():
+    """The dynamic resize stream at reduced size: u64 keys and values, mixed
+    batches that grow the table 2^11 -> 2^15 keys (60/30/10) and shrink it
+    back (10/30/60), 5% in-batch repeats, upsize above 0.90 and downsize
+    below 0.35 of capacity; every op result and the full contents equal the
+    oracle after every batch, and the expected counts hold exactly."""
+    from databases_gpu_gb300.workloads import ResizeStream
+    ws = ResizeStream(batch_ops=1 << 14, grow=12, shrink=12, start=1 << 11, peak=1 << 15,
+                      seed=10327)
+    t = _dg().DyCuckoo(1 << 11, key_bytes=8, value_bytes=8, upper_load=0.90, lower_load=0.35,
+                       min_downsize_capacity=0)
+    m = O.Map()
+    k0, v0 = ws.preload()
+    t.insert(k0, v0)
+    m.insert(k0.cpu().numpy().view(np.uint64), v0.cpu().numpy().view(np.uint64))
+    peak_cap = 0
+    ups = downs = 0
+    for b in range(len(ws)):
+        sb = ws.next()
+        ops = sb.ops.cpu().numpy()
+        keys = sb.keys.cpu().numpy().view(np.uint64)
+        vals = sb.vals.cpu().numpy().view(np.uint64)
+        gh = _apply_and_compare(t, m, ops, keys, vals, "stream batch %d (%s)" % (b, sb.phase))
+        st = t.stats()
+        ups += st["resizes_up"]
+        downs += st["resizes_down"]
+        assert t.size == sb.size_after
+        assert int(gh[ops == 0].sum()) == sb.find_ops
+        assert st["erased"] == sb.erase_hits
+        assert t.size <= 0.90 * t.capacity + 1
+        peak_cap = max(peak_cap, t.capacity)
+    assert ups > 0 and downs > 0
+    assert t.capacity < peak_cap
+    t.close()
