@@ -13,7 +13,7 @@ import threading
 from . import build as _build
 
 DYC_OK, DYC_ENOMEM, DYC_EINVAL, DYC_EOVERFLOW, DYC_ETIMEOUT, DYC_ECUDA, DYC_ENOTSUP = range(7)
-FLAG_UNIQUE, FLAG_NEW_KEYS, FLAG_NO_RESIZE = 1, 2, 4
+FLAG_UNIQUE, FLAG_NEW_KEYS, FLAG_NO_RESIZE, FLAG_GRAPH = 1, 2, 4, 8
 OP_FIND, OP_INSERT, OP_ERASE = 0, 1, 2  # dyc_apply op codes
 
 
@@ -48,6 +48,8 @@ EXPORTS = [
     "dyc_resize_up", "dyc_resize_down", "dyc_size", "dyc_capacity", "dyc_layout",
     "dyc_subtable", "dyc_export", "dyc_last_stats", "dyc_insert_host", "dyc_find_host",
     "dyc_erase_host", "dyc_status_string", "dyc_last_error", "dyc_erase_noalloc", "dyc_apply",
+    "dyc_set_create", "dyc_set_destroy", "dyc_set_table", "dyc_set_sizes", "dyc_set_apply",
+    "dyc_set_apply_each", "dyc_set_last_stats",
 ]
 
 _lock = threading.Lock()
@@ -78,6 +80,13 @@ def _declare(L):
         "dyc_erase_host": (st, [T, vp, u64, vp, C.POINTER(u64)]),
         "dyc_erase_noalloc": (st, [T, vp, u64, vp, C.POINTER(u64), u32, vp]),
         "dyc_apply": (st, [T, vp, vp, vp, u64, vp, vp, u32, vp]),
+        "dyc_set_create": (st, [C.POINTER(DycConfig), u32, vp, vp, C.POINTER(C.c_void_p)]),
+        "dyc_set_destroy": (st, [T]),
+        "dyc_set_table": (st, [T, u32, C.POINTER(C.c_void_p)]),
+        "dyc_set_sizes": (st, [T, vp, vp]),
+        "dyc_set_apply": (st, [T, vp, vp, vp, vp, vp, vp, vp, u32, vp]),
+        "dyc_set_apply_each": (st, [T, vp, vp, vp, vp, vp, vp, vp, u32, vp]),
+        "dyc_set_last_stats": (st, [T, C.POINTER(DycOpStats)]),
         "dyc_status_string": (C.c_char_p, [st]),
         "dyc_last_error": (C.c_char_p, []),
     }

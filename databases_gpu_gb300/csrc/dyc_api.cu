@@ -87,6 +87,7 @@ struct dyc_table {
     Desc D;
     Counters *d_ctr = nullptr;
     Counters *h_ctr = nullptr;
+    bool owns_ctr = true;  // false for a member of a table set (the set's arrays)
     // scratch for one chunk
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
@@ -377,7 +378,13 @@ const char *dyc_status_string(dyc_status s) {
 
 const char *dyc_last_error(void) { return g_err.c_str(); }
 
-dyc_status dyc_create(const dyc_config *cfg, dyc_table **out) {
+}  // extern "C"
+
+namespace {
+// Table creation. ext_d / ext_h: counters owned by a table set (the table
+// then allocates none); sync: wait for the zero-fill before returning.
+dyc_status create_impl(const dyc_config *cfg, Counters *ext_d, Counters *ext_h, bool sync,
+                       dyc_table **out) {
     if (!cfg || !out) return fail(DYC_EINVAL, "null argument");
     *out = nullptr;
     char why[128];
@@ -413,21 +420,34 @@ dyc_status dyc_create(const dyc_config *cfg, dyc_table **out) {
     for (uint32_t i = 0; i < t->D.d; ++i) {
         cudaError_t e = cudaMalloc(&t->D.sub[i], (size_t)nb * t->sb);
         if (e != cudaSuccess) return undo(fail(DYC_ENOMEM, "subtable %u: %s", i, cudaGetErrorString(e)));
-        e = cudaMemset(t->D.sub[i], 0, (size_t)nb * t->sb);
+        e = cudaMemsetAsync(t->D.sub[i], 0, (size_t)nb * t->sb, 0);
         if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "memset: %s", cudaGetErrorString(e)));
         t->D.nb[i] = nb;
         t->D.magic[i] = dyc::fastmod_magic(nb);
         t->capacity += (uint64_t)nb * t->slots;
     }
-    cudaError_t e = cudaMalloc(&t->d_ctr, sizeof(Counters));
-    if (e == cudaSuccess) e = cudaMemset(t->d_ctr, 0, sizeof(Counters));
-    if (e == cudaSuccess) e = cudaMallocHost(&t->h_ctr, sizeof(Counters));
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&t->io_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaError_t e = cudaSuccess;
+    if (ext_d) {
+        t->owns_ctr = false;
+        t->d_ctr = ext_d;
+        t->h_ctr = ext_h;
+    } else {
+        e = cudaMalloc(&t->d_ctr, sizeof(Counters));
+        if (e == cudaSuccess) e = cudaMemsetAsync(t->d_ctr, 0, sizeof(Counters), 0);
+        if (e == cudaSuccess) e = cudaMallocHost(&t->h_ctr, sizeof(Counters));
+        if (e == cudaSuccess) memset(t->h_ctr, 0, sizeof(Counters));
+    }
+    if (e == cudaSuccess && sync) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "table setup: %s", cudaGetErrorString(e)));
-    memset(t->h_ctr, 0, sizeof(Counters));
     *out = t;
     return DYC_OK;
+}
+}  // namespace
+
+extern "C" {
+
+dyc_status dyc_create(const dyc_config *cfg, dyc_table **out) {
+    return create_impl(cfg, nullptr, nullptr, true, out);
 }
 
 dyc_status dyc_destroy(dyc_table *t) {
@@ -436,8 +456,8 @@ dyc_status dyc_destroy(dyc_table *t) {
     cudaDeviceSynchronize();
     for (uint32_t i = 0; i < dyc::kMaxSub; ++i)
         if (t->D.sub[i]) cudaFree(t->D.sub[i]);
-    if (t->d_ctr) cudaFree(t->d_ctr);
-    if (t->h_ctr) cudaFreeHost(t->h_ctr);
+    if (t->owns_ctr && t->d_ctr) cudaFree(t->d_ctr);
+    if (t->owns_ctr && t->h_ctr) cudaFreeHost(t->h_ctr);
     if (t->scratch) cudaFree(t->scratch);
     if (t->apply_buf) cudaFree(t->apply_buf);
     if (t->h_actr) cudaFreeHost(t->h_actr);
@@ -591,6 +611,7 @@ namespace {
 constexpr uint64_t kIoChunk = 1ull << 22;  // ops staged per round trip
 
 dyc_status ensure_io(dyc_table *t, size_t bytes) {
+    if (!t->io_stream) CK(cudaStreamCreateWithFlags(&t->io_stream, cudaStreamNonBlocking));
     if (t->d_io && t->d_io_bytes >= bytes) return DYC_OK;
     if (t->d_io) {
         CK(cudaStreamSynchronize(t->io_stream));
@@ -727,39 +748,45 @@ dyc_status dyc_erase_host(dyc_table *t, const void *h_keys, uint64_t n,
 namespace {
 
 // Carve the mixed-batch scratch for `n` ops per chunk (grow only).
-dyc_status ensure_apply(dyc_table *t, uint64_t n) {
-    const uint64_t ops = n < 128 ? 128 : n;  // cap_cells >= 256: whole blocks
-    const uint64_t cells = next_pow2(2 * ops);
+// Carve an ApplyScratch for `ops` ops and `cells` cells out of one device
+// buffer (*buf, grown when too small). ntables > 0 adds the multi-table
+// arrays.
+dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t ntables,
+                       void **buf, size_t *buf_bytes, dyc::ApplyScratch *out) {
     const uint64_t blocks = (ops + dyc::kSortTile - 1) / dyc::kSortTile;
-    const size_t kb = (size_t)t->kb, vb = (size_t)t->vb;
+    const bool multi = ntables > 0;
+    const size_t K = (size_t)kb, V = (size_t)vb;
     const size_t sizes[] = {
-        cells * kb, cells * 4, cells * 4,            // cell_key, cell_cnt, cell_did
-        ops * 4, ops * kb, ops * 4, ops * 4, ops * 4,  // op_cell, dkey, dcnt, doff, dfill
-        ops * 4, ops * vb, (ops / 32 + 1) * 4,       // seg, pre_val, pre_hit
-        ops * kb, ops * vb, ops * kb,                // up_key, up_val, er_key
-        8 * 8, ops * 4,                              // ctr, large
-        ops * 4, ops * 4, ops * 4, ops * 4,          // sort buffers
-        blocks * 256 * 4, ops * 4};                  // hist, seg_start
+        cells * K, cells * 4, cells * 4,              // cell_key, cell_cnt, cell_did
+        ops * 4, ops * K, ops * 4, ops * 4, ops * 4,  // op_cell, dkey, dcnt, doff, dfill
+        ops * 4, ops * V, (ops / 32 + 1) * 4,         // seg, pre_val, pre_hit
+        ops * K, ops * V, ops * K,                    // up_key, up_val, er_key
+        dyc::kCtrSlots * 8, ops * 4, ops * 4,         // ctr, mid, giant
+        ops * 4, ops * 4, ops * 4, ops * 4,           // sort buffers
+        blocks * 256 * 4, ops * 4,                    // hist, seg_start
+        multi ? cells * 4 : 0, multi ? ops * 4 : 0,   // cell_tid, dtid
+        multi ? ops * 4 : 0, multi ? ops * 4 : 0,     // up_tid, er_tid
+        multi ? (size_t)ntables * 4 : 0,              // tnew
+        multi ? ((size_t)ntables + 1) * 4 : 0};       // tcell_off
     size_t need = 0;
     for (size_t b : sizes) need += (b + 255) & ~(size_t)255;
-    if (t->apply_buf && t->A.cap_ops >= ops) return DYC_OK;
-    if (t->apply_buf) {
+    if (*buf && *buf_bytes < need) {
         CK(cudaDeviceSynchronize());
-        CK(cudaFree(t->apply_buf));
-        t->apply_buf = nullptr;
-        t->A = dyc::ApplyScratch{};
+        CK(cudaFree(*buf));
+        *buf = nullptr;
     }
-    if (!t->h_actr) CK(cudaMallocHost(&t->h_actr, 8 * sizeof(unsigned long long)));
-    CK(cudaMalloc(&t->apply_buf, need));
-    t->apply_bytes = need;
-    char *p = (char *)t->apply_buf;
+    if (!*buf) {
+        CK(cudaMalloc(buf, need));
+        *buf_bytes = need;
+    }
+    char *p = (char *)*buf;
     int k = 0;
     auto carve = [&]() {
-        char *r = p;
+        char *r = sizes[k] ? p : nullptr;
         p += (sizes[k++] + 255) & ~(size_t)255;
         return (void *)r;
     };
-    dyc::ApplyScratch &A = t->A;
+    dyc::ApplyScratch A{};
     A.cell_key = carve();
     A.cell_cnt = (uint32_t *)carve();
     A.cell_did = (uint32_t *)carve();
@@ -775,20 +802,38 @@ dyc_status ensure_apply(dyc_table *t, uint64_t n) {
     A.up_val = carve();
     A.er_key = carve();
     A.ctr = (unsigned long long *)carve();
-    A.large = (uint32_t *)carve();
+    A.mid = (uint32_t *)carve();
+    A.giant = (uint32_t *)carve();
     A.sort_key = (uint32_t *)carve();
     A.sort_val = (uint32_t *)carve();
     A.sort_key2 = (uint32_t *)carve();
     A.sort_val2 = (uint32_t *)carve();
     A.hist = (uint32_t *)carve();
     A.seg_start = (uint32_t *)carve();
+    A.cell_tid = (uint32_t *)carve();
+    A.dtid = (uint32_t *)carve();
+    A.up_tid = (uint32_t *)carve();
+    A.er_tid = (uint32_t *)carve();
+    A.tnew = (uint32_t *)carve();
+    A.tcell_off = (uint32_t *)carve();
+    A.ntables = ntables;
     A.cap_cells = cells;
     A.cap_ops = ops;
+    *out = A;
     return DYC_OK;
 }
 
+// Mixed-batch scratch of a single table for `n` ops per chunk (grow only).
+dyc_status ensure_apply(dyc_table *t, uint64_t n) {
+    const uint64_t ops = n < 128 ? 128 : n;  // cap_cells >= 256: whole blocks
+    if (t->apply_buf && t->A.cap_ops >= ops) return DYC_OK;
+    if (!t->h_actr) CK(cudaMallocHost(&t->h_actr, dyc::kCtrSlots * sizeof(unsigned long long)));
+    return carve_apply(t->kb, t->vb, ops, next_pow2(2 * ops), 0, &t->apply_buf, &t->apply_bytes,
+                       &t->A);
+}
+
 dyc_status read_apply_counters(dyc_table *t, cudaStream_t s) {
-    CK(cudaMemcpyAsync(t->h_actr, t->A.ctr, 8 * sizeof(unsigned long long),
+    CK(cudaMemcpyAsync(t->h_actr, t->A.ctr, dyc::kCtrSlots * sizeof(unsigned long long),
                        cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     return DYC_OK;
@@ -799,26 +844,29 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
                        cudaStream_t s) {
     const dyc::ApplyScratch &A = t->A;
     const LaunchCtx L = ctx(t, s);
+    const uint32_t vb = (uint32_t)t->vb;
     CK(cudaMemsetAsync(A.cell_key, 0, (size_t)A.cap_cells * t->kb, s));
     CK(cudaMemsetAsync(A.cell_cnt, 0, (size_t)A.cap_cells * 4, s));
-    CK(cudaMemsetAsync(A.ctr, 0, 8 * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(A.ctr, 0, dyc::kCtrSlots * sizeof(unsigned long long), s));
     if (bits_out) CK(cudaMemsetAsync(bits_out, 0, (size_t)((n + 31) / 32) * 4, s));
     cudaError_t e = KB_CALL(t, apply_group, L, A, keys, n);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "apply group kernels: %s", cudaGetErrorString(e));
     TRY(read_apply_counters(t, s));
-    const uint64_t nd = t->h_actr[0];
-    e = KB_CALL(t, apply_replay, L, A, t->D, t->sb, ops, keys, vals, (uint32_t)t->vb, vals_out,
-                bits_out, n, nd);
+    const uint64_t nd = t->h_actr[dyc::kCtrDistinct];
+    e = KB_CALL(t, apply_scatter, L, A, n);
+    // state of every distinct key before the batch
+    if (e == cudaSuccess) e = KB_CALL(t, find, L, t->D, t->sb, A.dkey, A.pre_val, vb, A.pre_hit, nd);
+    if (e == cudaSuccess) e = KB_CALL(t, apply_replay, L, A, ops, vals, vb, vals_out, bits_out, n, nd);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "apply replay kernels: %s", cudaGetErrorString(e));
     TRY(read_apply_counters(t, s));
-    if (t->h_actr[4]) {
-        e = KB_CALL(t, apply_long, L, A, ops, vals, (uint32_t)t->vb, vals_out, bits_out, n,
-                    t->h_actr[4]);
+    if (t->h_actr[dyc::kCtrGiant]) {
+        e = KB_CALL(t, apply_giant, L, A, ops, vals, vb, vals_out, bits_out, n, nd,
+                    t->h_actr[dyc::kCtrGiant]);
         if (e != cudaSuccess)
-            return fail(DYC_ECUDA, "apply long-segment kernels: %s", cudaGetErrorString(e));
+            return fail(DYC_ECUDA, "apply giant-segment kernels: %s", cudaGetErrorString(e));
         TRY(read_apply_counters(t, s));
     }
-    const uint64_t nu = t->h_actr[2], ne = t->h_actr[3];
+    const uint64_t nu = t->h_actr[dyc::kCtrUp], ne = t->h_actr[dyc::kCtrEr];
     if (ne) TRY(erase_chunk(t, A.er_key, ne, nullptr, DYC_FLAG_UNIQUE, s));
     if (nu) {
         if (t->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE)) {
@@ -946,3 +994,460 @@ extern "C" dyc_status dyc_erase_noalloc(dyc_table *t, const void *d_keys, uint64
     if (h_erased_count) *h_erased_count = t->h_ctr->erased;
     return DYC_OK;
 }
+
+// =============================================================================
+// Table sets: many independent tables whose mixed batches are served by one
+// launch sequence (include/dycuckoo.h, dyc_set_*). Each phase is one
+// grid-stride launch over a work list that spans every table; an item reads
+// its table's descriptor from a device array. Member tables are ordinary
+// dyc_tables whose counters live in one set-owned array, so resizes,
+// overflow handling and single-table calls reuse the code above.
+// =============================================================================
+#include <vector>
+
+struct dyc_set {
+    dyc_config cfg;
+    int kb = 4, vb = 4, sb = 128, sms = 0, device = 0;
+    uint32_t ntables = 0;
+    std::vector<dyc_table *> tables;
+    Counters *d_tctr = nullptr, *h_tctr = nullptr;  // per-table counters
+    Desc *d_desc = nullptr, *h_desc = nullptr;      // per-table descriptors (pinned mirror)
+    Counters *d_gctr = nullptr, *h_gctr = nullptr;  // set-wide counters of one call
+    void *abuf = nullptr;
+    size_t abytes = 0;
+    dyc::ApplyScratch A{};
+    void *lbuf = nullptr;
+    size_t lbytes = 0;
+    void *list_a = nullptr, *list_b = nullptr;
+    uint32_t *tid_a = nullptr, *tid_b = nullptr;
+    uint64_t list_cap = 0;
+    unsigned long long *h_actr = nullptr;  // pinned copy of A.ctr
+    uint32_t *h_tnew = nullptr;            // pinned copy of A.tnew
+    uint32_t *d_bits_tmp = nullptr;        // dyc_set_apply_each: one table's result bits
+    size_t bits_tmp_words = 0;
+    // CUDA graphs of the two launch sequences, for the last call shape
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    std::vector<uintptr_t> gkey;
+    bool gwarm = false;
+    dyc_op_stats last{};
+};
+
+namespace {
+
+void set_drop_graphs(dyc_set *s) {
+    for (auto &g : s->gexec)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    s->gkey.clear();
+    s->gwarm = false;
+}
+
+dyc_status set_push_descs(dyc_set *s, cudaStream_t st) {
+    for (uint32_t t = 0; t < s->ntables; ++t) s->h_desc[t] = s->tables[t]->D;
+    CK(cudaMemcpyAsync(s->d_desc, s->h_desc, sizeof(Desc) * s->ntables, cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));  // the pinned mirror is rewritten by the next push
+    return DYC_OK;
+}
+
+// Push the descriptors again if any member changed since the last push.
+dyc_status set_refresh_descs(dyc_set *s, cudaStream_t st) {
+    for (uint32_t t = 0; t < s->ntables; ++t)
+        if (memcmp(&s->h_desc[t], &s->tables[t]->D, sizeof(Desc)) != 0) return set_push_descs(s, st);
+    return DYC_OK;
+}
+
+// Scratch for batches of up to n ops over the set (grow only).
+dyc_status set_ensure_scratch(dyc_set *s, uint64_t n) {
+    const uint64_t ops = n < 128 ? 128 : n;
+    if (s->abuf && s->A.cap_ops >= ops) return DYC_OK;
+    set_drop_graphs(s);
+    TRY(carve_apply(s->kb, s->vb, ops, 4 * ops, s->ntables, &s->abuf, &s->abytes, &s->A));
+    const size_t slot = s->kb == 4 ? 8 : 16;
+    const size_t lb = ((ops * slot + 255) & ~(size_t)255) * 2 + ((ops * 4 + 255) & ~(size_t)255) * 2;
+    if (s->lbuf) {
+        CK(cudaDeviceSynchronize());
+        CK(cudaFree(s->lbuf));
+        s->lbuf = nullptr;
+    }
+    CK(cudaMalloc(&s->lbuf, lb));
+    s->lbytes = lb;
+    char *p = (char *)s->lbuf;
+    const size_t ls = (ops * slot + 255) & ~(size_t)255, lt = (ops * 4 + 255) & ~(size_t)255;
+    s->list_a = p;
+    s->list_b = p + ls;
+    s->tid_a = (uint32_t *)(p + 2 * ls);
+    s->tid_b = (uint32_t *)(p + 2 * ls + lt);
+    s->list_cap = ops;
+    return DYC_OK;
+}
+
+#define SET_KB_CALL(s, fn, ...) ((s)->kb == 4 ? Ops<4>::fn(__VA_ARGS__) : Ops<8>::fn(__VA_ARGS__))
+
+// Phase A: group, scatter, pre-batch find, replay; counters to the host.
+dyc_status set_phase_a(dyc_set *s, const uint32_t *d_off, const uint8_t *ops, const void *keys,
+                       const void *vals, void *out, uint32_t *bits, uint64_t n, cudaStream_t st) {
+    const dyc::ApplyScratch &A = s->A;
+    const LaunchCtx L{s->sms, st};
+    const uint32_t vb = (uint32_t)s->vb;
+    CK(cudaMemsetAsync(A.ctr, 0, dyc::kCtrSlots * sizeof(unsigned long long), st));
+    if (bits) CK(cudaMemsetAsync(bits, 0, (size_t)((n + 31) / 32) * 4, st));
+    cudaError_t e = SET_KB_CALL(s, set_group, L, A, d_off, keys, n);
+    if (e == cudaSuccess) e = SET_KB_CALL(s, apply_scatter, L, A, n);
+    if (e == cudaSuccess)
+        e = SET_KB_CALL(s, set_find, L, s->d_desc, s->sb, A.dkey, A.dtid, &A.ctr[dyc::kCtrDistinct],
+                        n, A.pre_val, vb, A.pre_hit);
+    if (e == cudaSuccess) e = SET_KB_CALL(s, apply_replay, L, A, ops, vals, vb, out, bits, n, n);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "set phase A kernels: %s", cudaGetErrorString(e));
+    CK(cudaMemcpyAsync(s->h_actr, A.ctr, dyc::kCtrSlots * sizeof(unsigned long long),
+                       cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(s->h_tnew, A.tnew, (size_t)s->ntables * 4, cudaMemcpyDeviceToHost, st));
+    return DYC_OK;
+}
+
+// Phase B: erase list, upsert list, eviction walks; counters to the host.
+dyc_status set_phase_b(dyc_set *s, uint64_t n, cudaStream_t st) {
+    const dyc::ApplyScratch &A = s->A;
+    const LaunchCtx L{s->sms, st};
+    CK(cudaMemsetAsync(s->d_gctr, 0, sizeof(Counters), st));
+    cudaError_t e = SET_KB_CALL(s, set_erase, L, s->d_desc, s->d_tctr, s->sb, A.er_key, A.er_tid,
+                                &A.ctr[dyc::kCtrEr], n, s->d_gctr);
+    if (e == cudaSuccess)
+        e = SET_KB_CALL(s, set_place, L, s->d_desc, s->d_tctr, s->sb, A.up_key, A.up_val,
+                        (uint32_t)s->vb, A.up_tid, &A.ctr[dyc::kCtrUp], n, s->list_a, s->tid_a,
+                        s->list_cap, s->d_gctr);
+    if (e == cudaSuccess)
+        e = SET_KB_CALL(s, set_walk, L, s->d_desc, s->d_tctr, s->sb, s->list_a, s->tid_a,
+                        &s->d_gctr->pending, s->list_b, s->tid_b, &s->d_gctr->overflow,
+                        s->list_cap, s->cfg.max_evictions, s->d_gctr, s->list_cap);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "set phase B kernels: %s", cudaGetErrorString(e));
+    CK(cudaMemcpyAsync(s->h_gctr, s->d_gctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(s->h_tctr, s->d_tctr, sizeof(Counters) * s->ntables,
+                       cudaMemcpyDeviceToHost, st));
+    return DYC_OK;
+}
+
+// Run a phase directly, or through its captured graph when `graph` (captured
+// on the second call with the same shape, after one direct run has warmed the
+// launch-configuration caches).
+template <class F>
+dyc_status set_run(dyc_set *s, int which, bool graph, cudaStream_t st, F &&issue) {
+    if (!graph || !s->gwarm) return issue();
+    if (!s->gexec[which]) {
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        dyc_status r = issue();
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (r != DYC_OK) {
+            if (g) cudaGraphDestroy(g);
+            return r;
+        }
+        if (e != cudaSuccess) return fail(DYC_ECUDA, "stream capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&s->gexec[which], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(DYC_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    }
+    CK(cudaGraphLaunch(s->gexec[which], st));
+    return DYC_OK;
+}
+
+// Entries whose eviction walks reached the bound: place them per table after
+// an upsize of that table (never dropped).
+dyc_status set_overflow(dyc_set *s, uint64_t cnt, cudaStream_t st) {
+    const size_t slot = s->kb == 4 ? 8 : 16;
+    std::vector<unsigned char> ent(cnt * slot);
+    std::vector<uint32_t> tid(cnt);
+    CK(cudaMemcpyAsync(ent.data(), s->list_b, cnt * slot, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(tid.data(), s->tid_b, cnt * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::vector<std::vector<uint64_t>> per(s->ntables);
+    for (uint64_t i = 0; i < cnt; ++i) per[tid[i]].push_back(i);
+    for (uint32_t t = 0; t < s->ntables; ++t) {
+        if (per[t].empty()) continue;
+        dyc_table *m = s->tables[t];
+        const uint64_t c = per[t].size();
+        std::vector<unsigned char> hk(c * s->kb), hv(c * s->vb);
+        for (uint64_t j = 0; j < c; ++j) {
+            const unsigned char *e = ent.data() + per[t][j] * slot;
+            // a 4-byte-key slot is key | value << 32; an 8-byte-key slot is {key, value}
+            memcpy(hk.data() + j * s->kb, e, s->kb);
+            memcpy(hv.data() + j * s->vb, e + (s->kb == 4 ? 4 : 8), s->vb);
+        }
+        TRY(ensure_io(m, c * (s->kb + s->vb) + 256));
+        char *dk = (char *)m->d_io, *dv = dk + ((c * s->kb + 255) & ~(uint64_t)255);
+        CK(cudaMemcpyAsync(dk, hk.data(), c * s->kb, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dv, hv.data(), c * s->vb, cudaMemcpyHostToDevice, st));
+        TRY(ensure_scratch(m, c));
+        int guard = 0;
+        do {
+            TRY(resize_up_impl(m, st));
+        } while ((double)(m->size + c) > m->cfg.upper_load * (double)m->capacity && ++guard < 64);
+        TRY(insert_chunk(m, dk, dv, c, DYC_FLAG_UNIQUE | DYC_FLAG_NEW_KEYS, st));
+        CK(cudaStreamSynchronize(st));  // hk / hv and the io buffer are reused
+        s->last.resizes_up += m->last.resizes_up;
+        m->last = dyc_op_stats{};
+    }
+    return DYC_OK;
+}
+
+__global__ void k_bits_merge(uint32_t *__restrict__ dst, uint64_t dst_bit,
+                             const uint32_t *__restrict__ src, uint64_t m) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride)
+        if ((src[i >> 5] >> (i & 31)) & 1u) {
+            const uint64_t b = dst_bit + i;
+            atomicOr(&dst[b >> 5], 1u << (b & 31));
+        }
+}
+
+bool set_args_ok(const dyc_set *s, const uint32_t *d_off, const uint32_t *h_off,
+                 const uint8_t *ops, const void *keys, const void *vals, uint64_t *n_out) {
+    if (!s || !d_off || !h_off) return (fail(DYC_EINVAL, "null set or offsets"), false);
+    if (h_off[0] != 0) return (fail(DYC_EINVAL, "offsets must start at 0"), false);
+    for (uint32_t t = 0; t < s->ntables; ++t)
+        if (h_off[t + 1] < h_off[t]) return (fail(DYC_EINVAL, "offsets must not decrease"), false);
+    *n_out = h_off[s->ntables];
+    if (*n_out && (!ops || !keys || !vals))
+        return (fail(DYC_EINVAL, "null op, key or value array"), false);
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_t *sizes,
+                          const uint32_t *num_subtables, dyc_set **out) {
+    if (!cfg || !out || !sizes || ntables == 0) return fail(DYC_EINVAL, "null argument or no tables");
+    *out = nullptr;
+    char why[128];
+    if (!valid_config(cfg, why, sizeof(why))) return fail(DYC_EINVAL, "%s", why);
+    dyc_set *s = new (std::nothrow) dyc_set();
+    if (!s) return fail(DYC_ENOMEM, "host allocation");
+    s->cfg = *cfg;
+    s->kb = (int)cfg->key_bytes;
+    s->vb = (int)cfg->value_bytes;
+    s->sb = (int)cfg->bucket_bytes;
+    s->device = cfg->device;
+    s->ntables = ntables;
+    auto undo = [&](dyc_status r) {
+        dyc_set_destroy(s);
+        return r;
+    };
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_tctr, sizeof(Counters) * ntables);
+    if (e == cudaSuccess) e = cudaMemset(s->d_tctr, 0, sizeof(Counters) * ntables);
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_tctr, sizeof(Counters) * ntables);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_desc, sizeof(Desc) * ntables);
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_desc, sizeof(Desc) * ntables);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_gctr, sizeof(Counters));
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_gctr, sizeof(Counters));
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_actr, dyc::kCtrSlots * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_tnew, sizeof(uint32_t) * ntables);
+    if (e != cudaSuccess) return undo(fail(DYC_ENOMEM, "set setup: %s", cudaGetErrorString(e)));
+    memset(s->h_tctr, 0, sizeof(Counters) * ntables);
+    s->tables.assign(ntables, nullptr);
+    for (uint32_t t = 0; t < ntables; ++t) {
+        dyc_config c = *cfg;
+        c.initial_size = sizes[t];
+        if (num_subtables) c.num_subtables = num_subtables[t];
+        dyc_status r = create_impl(&c, s->d_tctr + t, s->h_tctr + t, false, &s->tables[t]);
+        if (r != DYC_OK) return undo(r);
+    }
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "set setup: %s", cudaGetErrorString(e)));
+    dyc_status r = set_push_descs(s, 0);
+    if (r != DYC_OK) return undo(r);
+    *out = s;
+    return DYC_OK;
+}
+
+dyc_status dyc_set_destroy(dyc_set *s) {
+    if (!s) return DYC_OK;
+    cudaSetDevice(s->device);
+    cudaDeviceSynchronize();
+    set_drop_graphs(s);
+    for (dyc_table *t : s->tables)
+        if (t) dyc_destroy(t);
+    if (s->d_tctr) cudaFree(s->d_tctr);
+    if (s->h_tctr) cudaFreeHost(s->h_tctr);
+    if (s->d_desc) cudaFree(s->d_desc);
+    if (s->h_desc) cudaFreeHost(s->h_desc);
+    if (s->d_gctr) cudaFree(s->d_gctr);
+    if (s->h_gctr) cudaFreeHost(s->h_gctr);
+    if (s->h_actr) cudaFreeHost(s->h_actr);
+    if (s->h_tnew) cudaFreeHost(s->h_tnew);
+    if (s->abuf) cudaFree(s->abuf);
+    if (s->lbuf) cudaFree(s->lbuf);
+    if (s->d_bits_tmp) cudaFree(s->d_bits_tmp);
+    delete s;
+    return DYC_OK;
+}
+
+dyc_status dyc_set_table(dyc_set *s, uint32_t i, dyc_table **out) {
+    if (!s || !out || i >= s->ntables) return fail(DYC_EINVAL, "bad set or table index");
+    *out = s->tables[i];
+    return DYC_OK;
+}
+
+dyc_status dyc_set_sizes(dyc_set *s, uint64_t *h_sizes, uint64_t *h_capacities) {
+    if (!s) return fail(DYC_EINVAL, "null set");
+    for (uint32_t t = 0; t < s->ntables; ++t) {
+        if (h_sizes) h_sizes[t] = s->tables[t]->size;
+        if (h_capacities) h_capacities[t] = s->tables[t]->capacity;
+    }
+    return DYC_OK;
+}
+
+dyc_status dyc_set_last_stats(dyc_set *s, dyc_op_stats *out) {
+    if (!s || !out) return fail(DYC_EINVAL, "null argument");
+    *out = s->last;
+    return DYC_OK;
+}
+
+dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *h_offsets,
+                         const uint8_t *d_ops, const void *d_keys, const void *d_vals,
+                         void *d_vals_out, uint32_t *d_bits_out, uint32_t flags, void *stream) {
+    uint64_t n = 0;
+    if (!set_args_ok(s, d_offsets, h_offsets, d_ops, d_keys, d_vals, &n)) return DYC_EINVAL;
+    if (n == 0) return DYC_OK;
+    if (n >= 0xFFFFFFFFull) return fail(DYC_EINVAL, "a set batch takes fewer than 2^32 ops");
+    cudaStream_t st = (cudaStream_t)stream;
+    {
+        int cur = -1;
+        CK(cudaGetDevice(&cur));
+        if (cur != s->device) CK(cudaSetDevice(s->device));
+    }
+    s->last = dyc_op_stats{};
+    for (dyc_table *m : s->tables) m->last = dyc_op_stats{};
+    // single-table calls on members since the last set call may have resized
+    // them: the kernels must see the current subtables
+    TRY(set_refresh_descs(s, st));
+    TRY(set_ensure_scratch(s, n));
+    const bool graph = (flags & DYC_FLAG_GRAPH) != 0;
+    if (graph) {
+        const std::vector<uintptr_t> key = {(uintptr_t)d_offsets, (uintptr_t)d_ops,
+                                            (uintptr_t)d_keys,    (uintptr_t)d_vals,
+                                            (uintptr_t)d_vals_out, (uintptr_t)d_bits_out, n};
+        if (key != s->gkey) {
+            set_drop_graphs(s);
+            s->gkey = key;
+        }
+    }
+    TRY(set_run(s, 0, graph, st, [&] {
+        return set_phase_a(s, d_offsets, d_ops, d_keys, d_vals, d_vals_out, d_bits_out, n, st);
+    }));
+    CK(cudaStreamSynchronize(st));
+    const uint64_t nd = s->h_actr[dyc::kCtrDistinct], ng = s->h_actr[dyc::kCtrGiant];
+    if (ng) {
+        cudaError_t e = SET_KB_CALL(s, apply_giant, LaunchCtx{s->sms, st}, s->A, d_ops, d_vals,
+                                    (uint32_t)s->vb, d_vals_out, d_bits_out, n, nd, ng);
+        if (e != cudaSuccess) return fail(DYC_ECUDA, "giant-segment kernels: %s", cudaGetErrorString(e));
+        CK(cudaMemcpyAsync(s->h_tnew, s->A.tnew, (size_t)s->ntables * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    // upsize before the inserts where the keys the batch adds would pass the
+    // upper load bound (hash_insert_batch, api.cpp:359-369, per table)
+    bool moved = false;
+    if (s->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE)) {
+        for (uint32_t t = 0; t < s->ntables; ++t) {
+            dyc_table *m = s->tables[t];
+            const uint64_t add = s->h_tnew[t];
+            int guard = 0;
+            while (add && (double)(m->size + add) > m->cfg.upper_load * (double)m->capacity &&
+                   guard++ < 64) {
+                TRY(resize_up_impl(m, st));
+                moved = true;
+            }
+        }
+        if (moved) TRY(set_push_descs(s, st));
+    }
+    TRY(set_run(s, 1, graph, st, [&] { return set_phase_b(s, n, st); }));
+    CK(cudaStreamSynchronize(st));
+    s->gwarm = graph;
+    const Counters g = *s->h_gctr;
+    if (g.spill) return fail(DYC_EOVERFLOW, "internal list overflow (%llu entries)", g.spill);
+    for (uint32_t t = 0; t < s->ntables; ++t) s->tables[t]->size = s->h_tctr[t].size;
+    s->last.inserted = g.inserted;
+    s->last.updated = g.updated;
+    s->last.erased = g.erased;
+    s->last.evict_steps = g.evict_steps;
+    s->last.overflowed = g.overflow;
+    for (dyc_table *m : s->tables) {
+        s->last.resizes_up += m->last.resizes_up;
+        m->last = dyc_op_stats{};
+    }
+    if (g.overflow) {
+        TRY(set_overflow(s, g.overflow, st));
+        moved = true;
+    }
+    // downsize after the batch (hash_delete_batch, api.cpp:494-505, per table)
+    if (s->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE)) {
+        for (dyc_table *m : s->tables) {
+            if ((double)m->size < m->cfg.lower_load * (double)m->capacity &&
+                m->capacity > m->cfg.min_downsize_capacity) {
+                dyc_status r = resize_down_impl(m, st);
+                if (r != DYC_OK && r != DYC_EINVAL) return r;
+                moved = true;
+                s->last.resizes_down += m->last.resizes_down;
+                s->last.resizes_up += m->last.resizes_up;
+                m->last = dyc_op_stats{};
+            }
+        }
+    }
+    if (moved) TRY(set_push_descs(s, st));
+    return DYC_OK;
+}
+
+dyc_status dyc_set_apply_each(dyc_set *s, const uint32_t *d_offsets, const uint32_t *h_offsets,
+                              const uint8_t *d_ops, const void *d_keys, const void *d_vals,
+                              void *d_vals_out, uint32_t *d_bits_out, uint32_t flags,
+                              void *stream) {
+    uint64_t n = 0;
+    if (!set_args_ok(s, d_offsets, h_offsets, d_ops, d_keys, d_vals, &n)) return DYC_EINVAL;
+    if (n == 0) return DYC_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    s->last = dyc_op_stats{};
+    uint64_t maxm = 0;
+    for (uint32_t t = 0; t < s->ntables; ++t)
+        maxm = std::max<uint64_t>(maxm, h_offsets[t + 1] - h_offsets[t]);
+    if (d_bits_out) {
+        const size_t words = (size_t)(maxm / 32 + 1);
+        if (s->bits_tmp_words < words) {
+            if (s->d_bits_tmp) CK(cudaFree(s->d_bits_tmp));
+            s->d_bits_tmp = nullptr;
+            CK(cudaMalloc(&s->d_bits_tmp, words * 4));
+            s->bits_tmp_words = words;
+        }
+        CK(cudaMemsetAsync(d_bits_out, 0, (size_t)((n + 31) / 32) * 4, st));
+    }
+    for (uint32_t t = 0; t < s->ntables; ++t) {
+        const uint64_t o = h_offsets[t], m = h_offsets[t + 1] - o;
+        if (!m) continue;
+        dyc_table *tb = s->tables[t];
+        TRY(dyc_apply(tb, d_ops + o, (const char *)d_keys + o * s->kb,
+                      (const char *)d_vals + o * s->vb,
+                      m, d_vals_out ? (char *)d_vals_out + o * s->vb : nullptr,
+                      d_bits_out ? s->d_bits_tmp : nullptr, flags, st));
+        if (d_bits_out) {
+            k_bits_merge<<<(unsigned)std::min<uint64_t>((m + 255) / 256, 1024), 256, 0, st>>>(
+                d_bits_out, o, s->d_bits_tmp, m);
+            CK(cudaGetLastError());
+        }
+        const dyc_op_stats &l = tb->last;
+        s->last.inserted += l.inserted;
+        s->last.updated += l.updated;
+        s->last.erased += l.erased;
+        s->last.evict_steps += l.evict_steps;
+        s->last.overflowed += l.overflowed;
+        s->last.resizes_up += l.resizes_up;
+        s->last.resizes_down += l.resizes_down;
+    }
+    CK(cudaStreamSynchronize(st));
+    return set_push_descs(s, st);
+}
+
+}  // extern "C"

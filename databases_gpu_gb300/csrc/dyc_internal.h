@@ -47,7 +47,8 @@ struct Scratch {
     uint64_t list_cap;      // entries per list
 };
 
-// Scratch of one mixed batch of at most `cap_ops` ops.
+// Scratch of one mixed batch of at most `cap_ops` ops. The multi-table
+// fields are null for a single table.
 struct ApplyScratch {
     void *cell_key;            // cap_cells keys (4 or 8 bytes), 0 = free
     uint32_t *cell_cnt;        // ops per cell
@@ -60,14 +61,32 @@ struct ApplyScratch {
     uint32_t *pre_hit;         // pre-batch hit bits per distinct key
     void *up_key, *up_val;     // upserts to apply
     void *er_key;              // erases to apply
-    unsigned long long *ctr;   // [0] distinct keys, [1] ops placed, [2] upserts, [3] erases,
-                               // [4] long segments
-    uint32_t *large;           // distinct ids of long segments
+    unsigned long long *ctr;   // see kCtr*
+    uint32_t *mid;             // distinct ids of segments of kShortSeg+1 .. kMidSeg ops
+    uint32_t *giant;           // distinct ids of longer segments
     uint32_t *sort_key, *sort_val, *sort_key2, *sort_val2;  // radix sort buffers
     uint32_t *hist;            // 256 x blocks digit counts
     uint32_t *seg_start;       // start of each distinct key in the sorted order
     uint64_t cap_cells;        // power of two, >= 2 * cap_ops
     uint64_t cap_ops;
+    // multi-table batches
+    uint32_t *cell_tid;        // table of a cell
+    uint32_t *dtid;            // table of a distinct key
+    uint32_t *up_tid, *er_tid; // table of each upsert / erase
+    uint32_t *tnew;            // per table: keys the batch adds
+    uint32_t *tcell_off;       // per table: first cell of its region (ntables + 1)
+    uint32_t ntables;
+};
+
+// ApplyScratch::ctr slots
+enum : int {
+    kCtrDistinct = 0,  // distinct keys
+    kCtrPlaced = 1,    // ops given a segment slot
+    kCtrUp = 2,        // upserts listed
+    kCtrEr = 3,        // erases listed
+    kCtrGiant = 4,     // giant segments
+    kCtrMid = 5,       // mid segments
+    kCtrSlots = 8
 };
 
 // radix-sort elements per block per pass (256 threads x 16)
@@ -113,17 +132,39 @@ template <int KB> struct Ops {
     static cudaError_t collect(const LaunchCtx &L, int sb, const void *sub, uint32_t nb,
                                void *list, unsigned long long *list_count, uint64_t list_cap,
                                unsigned long long *spill);
-    // mixed batches (dyc_apply.cuh): group + compact; scatter + pre-batch
-    // find + replay; the long-segment path
+    // mixed batches (dyc_apply.cuh). One table: apply_group (group +
+    // compact), apply_scatter, find of the distinct keys, apply_replay (short
+    // and mid segments), apply_giant when a key has more than kMidSeg ops.
+    // Many tables (dyc_set.cuh): set_group replaces apply_group and the
+    // set_* probe kernels replace find / erase / place / walk.
     static cudaError_t apply_group(const LaunchCtx &L, const ApplyScratch &A, const void *keys,
                                   uint64_t n);
-    static cudaError_t apply_replay(const LaunchCtx &L, const ApplyScratch &A, const Desc &D,
-                                   int sb, const uint8_t *ops, const void *keys, const void *vals,
-                                   uint32_t vb, void *vals_out, uint32_t *bits_out, uint64_t n,
-                                   uint64_t nd);
-    static cudaError_t apply_long(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
-                                  const void *vals, uint32_t vb, void *vals_out, uint32_t *bits_out,
-                                  uint64_t n, uint64_t nlarge);
+    static cudaError_t apply_scatter(const LaunchCtx &L, const ApplyScratch &A, uint64_t n);
+    static cudaError_t apply_replay(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
+                                   const void *vals, uint32_t vb, void *vals_out,
+                                   uint32_t *bits_out, uint64_t n, uint64_t max_distinct);
+    static cudaError_t apply_giant(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
+                                  const void *vals, uint32_t vb, void *vals_out,
+                                  uint32_t *bits_out, uint64_t n, uint64_t n_distinct,
+                                  uint64_t n_giant);
+    static cudaError_t set_group(const LaunchCtx &L, const ApplyScratch &A, const uint32_t *off,
+                                 const void *keys, uint64_t n);
+    static cudaError_t set_find(const LaunchCtx &L, const Desc *descs, int sb, const void *keys,
+                                const uint32_t *tids, const unsigned long long *n_ptr,
+                                uint64_t max_n, void *vals, uint32_t vb, uint32_t *hits);
+    static cudaError_t set_erase(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
+                                 const void *keys, const uint32_t *tids,
+                                 const unsigned long long *n_ptr, uint64_t max_n, Counters *gctr);
+    static cudaError_t set_place(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
+                                 const void *keys, const void *vals, uint32_t vb,
+                                 const uint32_t *tids, const unsigned long long *n_ptr,
+                                 uint64_t max_n, void *list_a, uint32_t *list_a_tid,
+                                 uint64_t list_cap, Counters *gctr);
+    static cudaError_t set_walk(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
+                                const void *src, const uint32_t *src_tid,
+                                const unsigned long long *src_count, void *dst, uint32_t *dst_tid,
+                                unsigned long long *dst_count, uint64_t dst_cap,
+                                uint32_t max_evict, Counters *gctr, uint64_t max_entries);
     // set the overflow bit of every bucket of a subtable
     static cudaError_t mark_all(const LaunchCtx &L, int sb, void *sub, uint32_t nb);
     static cudaError_t export_all(const LaunchCtx &L, const Desc &D, int sb, void *keys,

@@ -191,8 +191,13 @@ __device__ __forceinline__ ProbeOut<KB> probe(const char *p, typename SlotT<KB>:
 #pragma unroll
             for (int j = 0; j < SPC; ++j) T::from_words(w[qq] + j * WPS, s[j]);
             unsigned mb = 0u, eb = 0u, pb = 0u;
-            uint32_t tq = 0u;
-            if (WANT_PREF) tq = __shfl_sync(kFull, t, src[qq]);
+            uint32_t tq = 0u, dq = d;
+            if (WANT_PREF) {
+                // the bucket's owner: its subtable and (for a bucket of
+                // another table in a multi-table batch) its subtable count
+                tq = __shfl_sync(kFull, t, src[qq]);
+                dq = __shfl_sync(kFull, d, src[qq]);
+            }
 #pragma unroll
             for (int j = 0; j < SPC; ++j) {
                 const int idx = r * SPC + j;
@@ -200,7 +205,7 @@ __device__ __forceinline__ ProbeOut<KB> probe(const char *p, typename SlotT<KB>:
                     if (T::key(s[j]) == kq) mb |= 1u << idx;
                     if (WANT_EMPTY && T::is_empty(s[j])) eb |= 1u << idx;
                     if (WANT_PREF && !T::is_empty(s[j]) &&
-                        pair_of(fold(T::key(s[j])), d).first != tq)
+                        pair_of(fold(T::key(s[j])), dq).first != tq)
                         pb |= 1u << idx;
                 }
             }

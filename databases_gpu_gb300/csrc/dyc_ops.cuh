@@ -7,7 +7,7 @@
 #include <mutex>
 #include <unordered_map>
 
-#include "dyc_apply.cuh"
+#include "dyc_set.cuh"
 #include "dyc_kernels.cuh"
 
 namespace dyc {
@@ -167,32 +167,44 @@ cudaError_t Ops<KB>::apply_group(const LaunchCtx &L, const ApplyScratch &A, cons
 }
 
 template <int KB>
-cudaError_t Ops<KB>::apply_replay(const LaunchCtx &L, const ApplyScratch &A, const Desc &D, int sb,
-                                  const uint8_t *ops, const void *keys, const void *vals,
-                                  uint32_t vb, void *vals_out, uint32_t *bits_out, uint64_t n,
-                                  uint64_t nd) {
+cudaError_t Ops<KB>::apply_scatter(const LaunchCtx &L, const ApplyScratch &A, uint64_t n) {
     if (n == 0) return cudaSuccess;
     auto sc = k_apply_scatter<KB>;
     sc<<<grid_for((const void *)sc, L, n), 256, 0, L.stream>>>(A, n);
-    // state of every distinct key before the batch
-    cudaError_t e = find(L, D, sb, A.dkey, A.pre_val, vb, A.pre_hit, nd);
-    if (e != cudaSuccess) return e;
-    auto r = k_apply_replay<KB>;
-    r<<<grid_for((const void *)r, L, n > nd ? n : nd), 256, 0, L.stream>>>(A, ops, keys, vals, vb,
-                                                                            vals_out, bits_out, n, nd);
     return cudaGetLastError();
 }
 
 template <int KB>
-cudaError_t Ops<KB>::apply_long(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
-                                const void *vals, uint32_t vb, void *vals_out, uint32_t *bits_out,
-                                uint64_t n, uint64_t nlarge) {
-    if (n == 0 || nlarge == 0) return cudaSuccess;
+cudaError_t Ops<KB>::apply_replay(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
+                                  const void *vals, uint32_t vb, void *vals_out,
+                                  uint32_t *bits_out, uint64_t n, uint64_t max_distinct) {
+    if (n == 0) return cudaSuccess;
+    auto r = k_apply_replay<KB>;
+    const uint64_t work = n > max_distinct ? n : max_distinct;
+    r<<<grid_for((const void *)r, L, work), 256, 0, L.stream>>>(A, ops, vals, vb, vals_out,
+                                                                 bits_out, n);
+    auto m = k_apply_replay_mid<KB>;
+    // one block per mid segment; at most n / (kShortSeg + 1) of them
+    m<<<grid_for((const void *)m, L, (n / (kShortSeg + 1) + 1) * 256), 256, 0, L.stream>>>(
+        A, ops, vals, vb, vals_out, bits_out);
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::apply_giant(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
+                                 const void *vals, uint32_t vb, void *vals_out,
+                                 uint32_t *bits_out, uint64_t n, uint64_t n_distinct,
+                                 uint64_t n_giant) {
+    if (n == 0 || n_giant == 0) return cudaSuccess;
     auto si = k_apply_sort_init<KB>;
     si<<<grid_for((const void *)si, L, n), 256, 0, L.stream>>>(A, n);
     const unsigned blocks = (unsigned)((n + kSortTile - 1) / kSortTile);
     uint32_t *k0 = A.sort_key, *v0 = A.sort_val, *k1 = A.sort_key2, *v1 = A.sort_val2;
-    for (int shift = 0; shift < 24; shift += 8) {  // distinct ids fit in 24 bits
+    // digits up to the highest bit of a distinct id (0xffffffff, "no giant
+    // key", sorts after every id on these digits)
+    int bits = 1;
+    while (bits < 32 && (n_distinct >> bits) != 0) ++bits;
+    for (int shift = 0; shift < bits; shift += 8) {
         k_radix_hist<KB><<<blocks, 256, 0, L.stream>>>(k0, n, shift, A.hist);
         k_scan_exclusive<KB><<<1, 1024, 0, L.stream>>>(A.hist, (uint64_t)blocks * 256);
         k_radix_scatter<KB><<<blocks, 256, 0, L.stream>>>(k0, v0, n, shift, A.hist, k1, v1);
@@ -204,9 +216,81 @@ cudaError_t Ops<KB>::apply_long(const LaunchCtx &L, const ApplyScratch &A, const
     }
     auto ss = k_apply_seg_start<KB>;
     ss<<<grid_for((const void *)ss, L, n), 256, 0, L.stream>>>(A, k0, n);
-    auto rl = k_apply_replay_long<KB>;
-    rl<<<grid_for((const void *)rl, L, nlarge * 32), 256, 0, L.stream>>>(A, v0, ops, vals, vb,
-                                                                         vals_out, bits_out, nlarge);
+    auto rg = k_apply_replay_giant<KB>;
+    rg<<<grid_for((const void *)rg, L, n_giant * 32), 256, 0, L.stream>>>(A, v0, ops, vals, vb,
+                                                                          vals_out, bits_out);
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::set_group(const LaunchCtx &L, const ApplyScratch &A, const uint32_t *off,
+                               const void *keys, uint64_t n) {
+    k_set_cells<KB><<<1, 1024, 0, L.stream>>>(A, off);
+    auto cl = k_set_clear<KB>;
+    cl<<<grid_for((const void *)cl, L, A.cap_cells), 256, 0, L.stream>>>(A);
+    if (n) {
+        auto g = k_set_group<KB>;
+        g<<<grid_for((const void *)g, L, n), 256, 0, L.stream>>>(A, off, keys, n);
+        auto c = k_apply_compact<KB>;
+        c<<<grid_for((const void *)c, L, A.cap_cells), 256, 0, L.stream>>>(A);
+    }
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::set_find(const LaunchCtx &L, const Desc *descs, int sb, const void *keys,
+                              const uint32_t *tids, const unsigned long long *n_ptr,
+                              uint64_t max_n, void *vals, uint32_t vb, uint32_t *hits) {
+    if (max_n == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_set_find<KB, SB>;
+        k<<<grid_for((const void *)k, L, max_n), 256, 0, L.stream>>>(descs, keys, tids, n_ptr,
+                                                                      vals, vb, hits);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::set_erase(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
+                               const void *keys, const uint32_t *tids,
+                               const unsigned long long *n_ptr, uint64_t max_n, Counters *gctr) {
+    if (max_n == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_set_erase<KB, SB>;
+        k<<<grid_for((const void *)k, L, max_n), 256, 0, L.stream>>>(descs, tctr, keys, tids,
+                                                                      n_ptr, gctr);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::set_place(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
+                               const void *keys, const void *vals, uint32_t vb,
+                               const uint32_t *tids, const unsigned long long *n_ptr,
+                               uint64_t max_n, void *list_a, uint32_t *list_a_tid,
+                               uint64_t list_cap, Counters *gctr) {
+    if (max_n == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_set_place<KB, SB>;
+        k<<<grid_for((const void *)k, L, max_n), 256, 0, L.stream>>>(
+            descs, tctr, keys, vals, vb, tids, n_ptr, list_a, list_a_tid, list_cap, gctr);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::set_walk(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
+                              const void *src, const uint32_t *src_tid,
+                              const unsigned long long *src_count, void *dst, uint32_t *dst_tid,
+                              unsigned long long *dst_count, uint64_t dst_cap, uint32_t max_evict,
+                              Counters *gctr, uint64_t max_entries) {
+    if (max_entries == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_set_walk<KB, SB>;
+        k<<<grid_for((const void *)k, L, max_entries), 256, 0, L.stream>>>(
+            descs, tctr, src, src_tid, src_count, dst, dst_tid, dst_count, dst_cap, max_evict,
+            gctr, max_entries);
+    });
     return cudaGetLastError();
 }
 

@@ -1,0 +1,292 @@
+// dyc_set.cuh -- probe kernels of a multi-table batch (a table set). They run
+// the find / erase / place / eviction-walk logic of the single-table kernels
+// in dyc_kernels.cuh, but every item carries a table id and reads that
+// table's descriptor from a device array, so one grid-stride launch serves
+// the work of every table in the set. Item counts are read on the device
+// (the counters the mixed-batch kernels fill), so a batch's launch sequence
+// needs no host reads and can be captured as a CUDA graph.
+#pragma once
+
+#include "dyc_apply.cuh"
+
+namespace dyc {
+
+// Per-table size change by `sign` for every lane with pred; one atomic per
+// distinct table in the warp. All 32 lanes must call.
+__device__ __forceinline__ void warp_size_add(Counters *tctr, uint32_t t, bool pred,
+                                              long long sign) {
+    const unsigned peers = __match_any_sync(kFull, pred ? t : 0xffffffffu);
+    if (pred && (__ffs(peers) - 1) == (int)(threadIdx.x & 31))
+        atomicAdd(&tctr[t].size, (unsigned long long)(sign * (long long)__popc(peers)));
+}
+
+// find of keys[i] in table tids[i], i < *n_ptr (k_find per table)
+template <int KB, int SB>
+__global__ void __launch_bounds__(256) k_set_find(const Desc *__restrict__ descs,
+                                                  const void *__restrict__ keys,
+                                                  const uint32_t *__restrict__ tids,
+                                                  const unsigned long long *__restrict__ n_ptr,
+                                                  void *__restrict__ vals, uint32_t vb,
+                                                  uint32_t *__restrict__ hits) {
+    using T = SlotT<KB>;
+    using Gm = Geo<KB, SB>;
+    __shared__ __align__(128) unsigned char s_stage[kWarpsPerBlock][32 * SB];
+    unsigned char *stage = s_stage[threadIdx.x >> 5];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t n = *n_ptr;
+    const uint64_t step = warp_stride();
+    for (uint64_t base = warp_base(); base < n; base += step) {
+        const uint64_t i = base + lane;
+        typename T::K k = 0;
+        uint32_t tb = 0u;
+        if (i < n) {
+            k = load_key<KB>(keys, i);
+            tb = tids[i];
+        }
+        const Desc &D = descs[tb];
+        const bool act = k != 0;
+        const uint32_t hk = fold(k);
+        const Pair p = pair_of(hk, D.d);
+        const char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
+        const KvOut r1 = kv_probe<KB, SB, 1>(p1, k, act, stage);
+        bool hit = act && r1.match >= 0;
+        uint64_t v = hit ? r1.value : 0ull;
+        const bool need2 = act && !hit && (!Gm::kMeta || r1.overflow);
+        if (__any_sync(kFull, need2)) {
+            const char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
+            const KvOut r2 = kv_probe<KB, SB, 1>(p2, k, need2, stage);
+            if (need2 && r2.match >= 0) {
+                hit = true;
+                v = r2.value;
+            }
+        }
+        if (i < n) store_val(vals, vb, i, v);
+        const unsigned m = __ballot_sync(kFull, hit);
+        if (hits != nullptr && lane == 0) hits[base >> 5] = m;
+    }
+}
+
+// erase of unique keys[i] from table tids[i] (k_erase per table, no dedup)
+template <int KB, int SB>
+__global__ void __launch_bounds__(256) k_set_erase(const Desc *__restrict__ descs,
+                                                   Counters *__restrict__ tctr,
+                                                   const void *__restrict__ keys,
+                                                   const uint32_t *__restrict__ tids,
+                                                   const unsigned long long *__restrict__ n_ptr,
+                                                   Counters *gctr) {
+    using T = SlotT<KB>;
+    using Gm = Geo<KB, SB>;
+    __shared__ __align__(128) unsigned char s_stage[kWarpsPerBlock][32 * SB];
+    unsigned char *stage = s_stage[threadIdx.x >> 5];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t n = *n_ptr;
+    const uint64_t step = warp_stride();
+    uint32_t n_del = 0;
+    for (uint64_t base = warp_base(); base < n; base += step) {
+        const uint64_t i = base + lane;
+        typename T::K k = 0;
+        uint32_t tb = 0u;
+        if (i < n) {
+            k = load_key<KB>(keys, i);
+            tb = tids[i];
+        }
+        const Desc &D = descs[tb];
+        const bool act = k != 0;
+        const uint32_t hk = fold(k);
+        const Pair p = pair_of(hk, D.d);
+        char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
+        const KvOut r1 = kv_probe<KB, SB, 2>(p1, k, act, stage);
+        bool erased = false;
+        if (act && r1.match >= 0) {
+            const typename T::S cur = T::make(k, r1.value);
+            const typename T::S old = T::cas(slot_ptr<KB, SB>(p1, r1.match), cur, T::empty());
+            erased = T::same(old, cur);
+        }
+        const bool need2 = act && r1.match < 0 && (!Gm::kMeta || r1.overflow);
+        if (__any_sync(kFull, need2)) {
+            char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
+            const KvOut r2 = kv_probe<KB, SB, 2>(p2, k, need2, stage);
+            if (need2 && r2.match >= 0) {
+                const typename T::S cur = T::make(k, r2.value);
+                const typename T::S old = T::cas(slot_ptr<KB, SB>(p2, r2.match), cur, T::empty());
+                erased = T::same(old, cur);
+            }
+        }
+        warp_size_add(tctr, tb, erased, -1);
+        n_del += erased ? 1u : 0u;
+    }
+    const uint32_t del = __reduce_add_sync(kFull, n_del);
+    if (lane == 0 && del) atomicAdd(&gctr->erased, (unsigned long long)del);
+}
+
+// upsert of unique keys[i] -> vals[i] into table tids[i] (k_place per
+// table); ops left without a slot go to list_a / list_a_tid
+template <int KB, int SB>
+__global__ void __launch_bounds__(256) k_set_place(const Desc *__restrict__ descs,
+                                                   Counters *__restrict__ tctr,
+                                                   const void *__restrict__ keys,
+                                                   const void *__restrict__ vals, uint32_t vb,
+                                                   const uint32_t *__restrict__ tids,
+                                                   const unsigned long long *__restrict__ n_ptr,
+                                                   void *list_a, uint32_t *list_a_tid,
+                                                   uint64_t list_cap, Counters *gctr) {
+    using T = SlotT<KB>;
+    using Sl = typename T::S;
+    using Gm = Geo<KB, SB>;
+    const uint64_t n = *n_ptr;
+    const uint64_t step = warp_stride();
+    uint32_t n_ins = 0, n_upd = 0;
+    for (uint64_t base = warp_base(); base < n; base += step) {
+        const uint64_t i = base + (threadIdx.x & 31);
+        typename T::K k = 0;
+        bool act = false;
+        uint32_t tb = 0u;
+        Sl e = T::empty();
+        if (i < n) {
+            k = load_key<KB>(keys, i);
+            tb = tids[i];
+            act = k != 0;
+            if (act) e = T::make(k, load_val(vals, vb, i));
+        }
+        const Desc &D = descs[tb];
+        const uint32_t hk = fold(k);
+        const Pair p = pair_of(hk, D.d);
+        char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
+        char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
+        const ProbeOut<KB> r1 = probe<KB, SB, 2, true, false>(p1, k, act, p.first, D.d);
+        const bool found1 = act && r1.match >= 0;
+        const bool check2 =
+            act && !found1 && ((!Gm::kMeta || (r1.meta & kOverflowBit)) || r1.empty == 0u);
+        ProbeOut<KB> r2;
+        r2.match = -1;
+        r2.empty = 0u;
+        r2.mslot = T::empty();
+        if (__any_sync(kFull, check2)) r2 = probe<KB, SB, 2, true, false>(p2, k, check2, p.second, D.d);
+        bool pend = false, ins = false;
+        if (found1) {
+            T::exch(slot_ptr<KB, SB>(p1, r1.match), e);
+            ++n_upd;
+        } else if (check2 && r2.match >= 0) {
+            T::exch(slot_ptr<KB, SB>(p2, r2.match), e);
+            ++n_upd;
+        } else if (act) {
+            bool ok = claim_empty<KB, SB>(p1, r1.empty, e);
+            if (!ok && check2 && r2.empty) {
+                mark_overflow<KB, SB>(p1);
+                ok = claim_empty<KB, SB>(p2, r2.empty, e);
+            }
+            if (ok) {
+                ++n_ins;
+                ins = true;
+            } else {
+                pend = true;
+            }
+        }
+        __syncwarp();
+        warp_size_add(tctr, tb, ins, 1);
+        const unsigned long long at = agg_inc(&gctr->pending, pend);
+        if (pend) {
+            if (at < list_cap) {
+                ((Sl *)list_a)[at] = e;
+                list_a_tid[at] = tb;
+            } else {
+                atomicAdd(&gctr->spill, 1ull);
+            }
+        }
+    }
+    agg_add(&gctr->inserted, n_ins);
+    agg_add(&gctr->updated, n_upd);
+}
+
+// eviction walks of src entries (k_walk per table); failures go to dst
+template <int KB, int SB>
+__global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs,
+                                                  Counters *__restrict__ tctr,
+                                                  const void *__restrict__ src,
+                                                  const uint32_t *__restrict__ src_tid,
+                                                  const unsigned long long *src_count, void *dst,
+                                                  uint32_t *dst_tid, unsigned long long *dst_count,
+                                                  uint64_t dst_cap, uint32_t max_evict,
+                                                  Counters *gctr, uint64_t max_entries) {
+    using T = SlotT<KB>;
+    using Sl = typename T::S;
+    uint64_t n = *src_count;
+    if (n > max_entries) n = max_entries;
+    const uint64_t step = warp_stride();
+    uint32_t n_ok = 0, n_steps = 0;
+    const uint32_t max_iter = 2u * max_evict + 8u;
+    for (uint64_t base = warp_base(); base < n; base += step) {
+        const uint64_t i = base + (threadIdx.x & 31);
+        bool live = i < n;
+        Sl e = live ? ((const Sl *)src)[i] : T::empty();
+        const uint32_t tb = live ? src_tid[i] : 0u;
+        const Desc &D = descs[tb];
+        uint32_t hk = 0;
+        Pair pe{0u, 0u};
+        char *fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);
+        uint32_t t = pe.first;
+        char *bp = fb;
+        int mode = 0;  // 0: empties of the first bucket, 1: of the second, 2: walking
+        uint32_t evictions = 0;
+        bool fail = false, ok = false;
+        for (uint32_t it = 0; it < max_iter; ++it) {
+            if (!__any_sync(kFull, live)) break;
+            const ProbeOut<KB> r = probe<KB, SB, 2, true, true>(bp, T::key(e), live, t, D.d);
+            if (!live) continue;
+            bool placed = false;
+            if (r.empty) {
+                if (t != pe.first) mark_overflow<KB, SB>(fb);
+                placed = claim_empty<KB, SB>(bp, r.empty, e);
+            }
+            if (placed) {
+                live = false;
+                ok = true;
+            } else if (mode == 0) {
+                mode = 1;
+                t = pe.second;
+                bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
+            } else if (mode == 1) {
+                mode = 2;
+                t = pe.first;
+                bp = fb;
+            } else if (r.empty) {
+                // every empty slot was taken by another lane: look again
+            } else if (evictions >= max_evict) {
+                live = false;
+                fail = true;
+            } else {
+                const int j = pick_victim<KB, SB>(r.pref, hk + evictions);
+                if (t != pe.first) mark_overflow<KB, SB>(fb);
+                const Sl old = T::exch(slot_ptr<KB, SB>(bp, j), e);
+                ++evictions;
+                ++n_steps;
+                if (T::is_empty(old)) {
+                    live = false;
+                    ok = true;
+                } else {
+                    e = old;  // a resident of the same table
+                    fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);
+                    t = other_of(pe, t);
+                    bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
+                }
+            }
+        }
+        if (live) fail = true;  // iteration bound reached
+        __syncwarp();
+        n_ok += ok ? 1u : 0u;
+        warp_size_add(tctr, tb, ok, 1);
+        const unsigned long long at = agg_inc(dst_count, fail);
+        if (fail) {
+            if (at < dst_cap) {
+                ((Sl *)dst)[at] = e;
+                dst_tid[at] = tb;
+            } else {
+                atomicAdd(&gctr->spill, 1ull);
+            }
+        }
+    }
+    agg_add(&gctr->inserted, n_ok);
+    agg_add(&gctr->evict_steps, n_steps);
+}
+
+}  // namespace dyc

@@ -16,7 +16,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import FLAG_NEW_KEYS, FLAG_NO_RESIZE, FLAG_UNIQUE, check
+from ._lib import FLAG_GRAPH, FLAG_NEW_KEYS, FLAG_NO_RESIZE, FLAG_UNIQUE, check
 
 # test_uilt.h:1-5 of the reference
 UPPER_BOUND = 0.8
@@ -88,8 +88,24 @@ class DyCuckoo:
         self.value_bytes = cfg.value_bytes
         self.device = device
 
+    @classmethod
+    def _member(cls, handle, cfg, owner):
+        """A non-owning handle on a member table of a DyCuckooSet."""
+        t = cls.__new__(cls)
+        t._h = handle
+        t.L = owner.L
+        t.cfg = cfg
+        t.key_bytes = cfg.key_bytes
+        t.value_bytes = cfg.value_bytes
+        t.device = cfg.device
+        t._owner = owner  # keeps the set alive
+        return t
+
     # -- lifetime
     def close(self):
+        if getattr(self, "_owner", None) is not None:
+            self._h = None  # destroyed with its set
+            return
         if getattr(self, "_h", None):
             self.L.dyc_destroy(self._h)
             self._h = None
@@ -273,6 +289,111 @@ class DyCuckoo:
                                     erased_bits.ctypes.data if erased_bits is not None else None,
                                     C.byref(cnt)), "dyc_erase_host")
         return int(cnt.value)
+
+
+class DyCuckooSet:
+    """Many independent DyCuckoo tables served together (dyc_set_*): one
+    launch sequence per mixed batch for the whole set.
+
+    sizes: per-table key counts to size for; num_subtables: optional
+    per-table subtable counts. Other arguments as for DyCuckoo (shared)."""
+
+    def __init__(self, sizes, key_bytes: int = 4, value_bytes: int | None = None,
+                 num_subtables=None, bucket_bytes: int = 128, max_evictions: int = 64,
+                 auto_resize: bool = True, upper_load: float = UPPER_BOUND,
+                 lower_load: float = LOWER_BOUND,
+                 min_downsize_capacity: int = MIN_DOWNSIZE_CAPACITY, device: int = 0,
+                 default_subtables: int = 4):
+        L = _lib.lib()
+        cfg = _lib.DycConfig()
+        L.dyc_config_default(C.byref(cfg))
+        cfg.key_bytes = key_bytes
+        cfg.value_bytes = value_bytes if value_bytes is not None else key_bytes
+        cfg.num_subtables = default_subtables
+        cfg.bucket_bytes = bucket_bytes
+        cfg.max_evictions = max_evictions
+        cfg.auto_resize = 1 if auto_resize else 0
+        cfg.upper_load = upper_load
+        cfg.lower_load = lower_load
+        cfg.min_downsize_capacity = int(min_downsize_capacity)
+        cfg.device = device
+        sz = np.ascontiguousarray(sizes, dtype=np.uint64)
+        ns = None if num_subtables is None else np.ascontiguousarray(num_subtables, np.uint32)
+        h = C.c_void_p()
+        check(L.dyc_set_create(C.byref(cfg), sz.size, sz.ctypes.data,
+                               ns.ctypes.data if ns is not None else None, C.byref(h)),
+              "dyc_set_create")
+        self._h = h
+        self.L = L
+        self.cfg = cfg
+        self.ntables = int(sz.size)
+        self.key_bytes = cfg.key_bytes
+        self.value_bytes = cfg.value_bytes
+        self.device = device
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.L.dyc_set_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def table(self, i: int) -> DyCuckoo:
+        h = C.c_void_p()
+        check(self.L.dyc_set_table(self._h, i, C.byref(h)), "dyc_set_table")
+        cfg = _lib.DycConfig()
+        C.memmove(C.byref(cfg), C.byref(self.cfg), C.sizeof(cfg))
+        return DyCuckoo._member(h, cfg, self)
+
+    def sizes(self):
+        s = np.empty(self.ntables, np.uint64)
+        c = np.empty(self.ntables, np.uint64)
+        check(self.L.dyc_set_sizes(self._h, s.ctypes.data, c.ctypes.data), "dyc_set_sizes")
+        return s, c
+
+    def stats(self) -> dict:
+        st = _lib.DycOpStats()
+        check(self.L.dyc_set_last_stats(self._h, C.byref(st)), "dyc_set_last_stats")
+        return st.as_dict()
+
+    def apply(self, offsets, ops, keys, values, out=None, bits=None, h_offsets=None,
+              each: bool = False, graph: bool = False, no_resize: bool = False, stream=None):
+        """Mixed batch: ops of table t are [offsets[t], offsets[t+1]) of the
+        op / key / value tensors. offsets: uint32 CUDA tensor of ntables+1
+        (h_offsets: its host copy, computed if omitted). each: one dyc_apply
+        per table instead (the per-table launch path). Returns (out, bits)."""
+        torch = _torch()
+        n = keys.numel()
+        if h_offsets is None:
+            h_offsets = offsets.cpu().numpy()
+        h_offsets = np.ascontiguousarray(np.asarray(h_offsets).view(np.uint32)
+                                         if np.asarray(h_offsets).dtype == np.int32
+                                         else np.asarray(h_offsets, dtype=np.uint32))
+        if h_offsets.size != self.ntables + 1 or int(h_offsets[-1]) != n:
+            raise ValueError("offsets must have ntables+1 entries ending at the op count")
+        if out is None:
+            out = torch.empty(n, dtype=torch.int32 if self.value_bytes == 4 else torch.int64,
+                              device=keys.device)
+        if bits is None:
+            bits = torch.empty((n + 31) // 32, dtype=torch.int32, device=keys.device)
+        flags = (FLAG_NO_RESIZE if no_resize else 0) | (FLAG_GRAPH if graph else 0)
+        fn = self.L.dyc_set_apply_each if each else self.L.dyc_set_apply
+        check(fn(self._h, _ptr(offsets, "offsets", 4), h_offsets.ctypes.data,
+                 _ptr(ops, "ops", 1), _ptr(keys, "keys", self.key_bytes),
+                 _ptr(values, "values", self.value_bytes), _ptr(out, "out", self.value_bytes),
+                 _ptr(bits, "bits", 4), flags, _stream_ptr(stream)),
+              "dyc_set_apply_each" if each else "dyc_set_apply")
+        return out, bits
 
 
 def unpack_bits(bits, n: int) -> np.ndarray:

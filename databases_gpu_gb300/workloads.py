@@ -15,6 +15,8 @@ from __future__ import annotations
 
 from dataclasses import dataclass
 
+import numpy as np
+
 _GOLD = 0x9E3779B97F4A7C15
 _C1 = 0xBF58476D1CE4E5B9
 _C2 = 0x94D049BB133111EB
@@ -162,3 +164,92 @@ class ResizeStream:
         self.b += 1
         return StreamBatch(ops.contiguous(), keys.contiguous(), vals, self.hi - self.lo, fnd,
                            d_hit, "grow" if growing else "shrink")
+
+
+_M32 = 0xFFFFFFFF
+
+
+def perm32(x):
+    """A bijection of the 32-bit integers (odd multiplies and xorshifts), on
+    int64 tensors holding values in [0, 2^32)."""
+    x = (x ^ 0x5BD1E995) & _M32
+    x = (x * 0x9E3779B1) & _M32
+    x = x ^ (x >> 16)
+    x = (x * 0x85EBCA6B) & _M32
+    x = x ^ (x >> 13)
+    x = (x * 0xC2B2AE35) & _M32
+    return x ^ (x >> 16)
+
+
+class MultiTableWorkload:
+    """Many independent u32/u32 tables of log-uniform sizes, each receiving a
+    mixed batch of log-uniform size per round.
+
+    Table t's key of index j is perm32((j + t * 0x9E3779B9) mod 2^32) (distinct
+    within a table; 0 is replaced by 2^32 - 1). It starts with indices
+    [0, size_t). A round's ops for table t: `find` share (half on indices in
+    [0, size_t), half on indices from 2^31, never inserted), `insert` share on
+    indices in [0, 2 size_t) (about half update, half add), the rest erases on
+    indices in [0, size_t). Everything is generated on the device.
+    """
+
+    def __init__(self, ntables: int, log2_size=(8, 20), log2_batch=(4, 16),
+                 mix=(0.7, 0.2, 0.1), seed: int = 10327, device="cuda"):
+        import torch
+        self.torch = torch
+        self.device = torch.device(device)
+        self.gen = torch.Generator(device="cpu")
+        self.gen.manual_seed(seed)
+        self.dgen = torch.Generator(device=self.device)
+        self.dgen.manual_seed(seed + 1)
+        self.ntables = ntables
+        u = torch.rand(ntables, generator=self.gen, dtype=torch.float64)
+        self.sizes = torch.round(2.0 ** (log2_size[0] + u * (log2_size[1] - log2_size[0]))).long()
+        u = torch.rand(ntables, generator=self.gen, dtype=torch.float64)
+        self.batch = torch.round(2.0 ** (log2_batch[0] + u * (log2_batch[1] - log2_batch[0]))).long()
+        self.mix = mix
+        off = torch.zeros(ntables + 1, dtype=torch.int64)
+        off[1:] = torch.cumsum(self.batch, 0)
+        self.offsets_host = off.numpy().astype(np.uint32)
+        self.offsets = torch.from_numpy(self.offsets_host.view(np.int32)).to(self.device)
+        self.n_ops = int(off[-1])
+        self._tid = torch.repeat_interleave(torch.arange(ntables, device=self.device),
+                                            self.batch.to(self.device))
+        self._size_dev = self.sizes.to(self.device)
+
+    def key(self, t, j):
+        """Keys of table t (int64 tensors), as int32 tensors (same 32 bits)."""
+        k = perm32((j + t * 0x9E3779B9) & _M32)
+        k = self.torch.where(k == 0, self.torch.full_like(k, _M32), k)
+        return (k - ((k >> 31) << 32)).to(self.torch.int32)
+
+    def preload(self, t: int):
+        """Keys and values table t starts with (int32 CUDA tensors)."""
+        torch = self.torch
+        n = int(self.sizes[t])
+        j = torch.arange(n, dtype=torch.int64, device=self.device)
+        tt = torch.full_like(j, t)
+        vals = (perm32(j ^ (tt << 20)) & 0x7FFFFFFF).to(torch.int32)
+        return self.key(tt, j), vals
+
+    def round(self):
+        """One round: (ops uint8, keys int32, vals int32) over all tables, in
+        table order (ranges given by self.offsets)."""
+        torch = self.torch
+        n = self.n_ops
+        t = self._tid
+        size = self._size_dev[t]
+        u = torch.rand(n, generator=self.dgen, device=self.device)
+        f, i = self.mix[0], self.mix[1]
+        ops = torch.where(u < f, 0, torch.where(u < f + i, 1, 2)).to(torch.uint8)
+        r = torch.rand(n, generator=self.dgen, device=self.device, dtype=torch.float64)
+        hit = torch.rand(n, generator=self.dgen, device=self.device) < 0.5
+        j_present = (r * size).long()
+        j_insert = (r * 2 * size).long()
+        j_miss = (1 << 31) + (r * (1 << 30)).long()
+        j = torch.where(ops == 1, j_insert,
+                        torch.where((ops == 0) & ~hit, j_miss, j_present))
+        keys = self.key(t, j)
+        vals = torch.randint(0, 1 << 31, (n,), generator=self.dgen, device=self.device,
+                             dtype=torch.int64).to(torch.int32)
+        return ops.contiguous(), keys.contiguous(), vals.contiguous()

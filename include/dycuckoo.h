@@ -197,6 +197,57 @@ dyc_status dyc_apply(dyc_table *t, const uint8_t *d_ops, const void *d_keys, con
                      uint64_t n, void *d_vals_out, uint32_t *d_bits_out, uint32_t flags,
                      void *stream);
 
+/* ---- Table sets ----------------------------------------------------------
+ * Many independent tables (each a dyc_table with its own size, subtables and
+ * resizes) whose mixed batches are served together: one launch sequence per
+ * batch for the whole set, each launch a grid-stride pass over a work list
+ * that spans every table, instead of one launch sequence per table. The
+ * reference serves one table per hashAPI object; this extends it to the
+ * many-small-tables case (no reference counterpart).
+ *
+ * A batch is given as per-table op ranges: the ops of table t are indices
+ * [offsets[t], offsets[t+1]) of d_ops / d_keys / d_vals / d_vals_out and
+ * bits of d_bits_out, with offsets[0] = 0 and ntables + 1 entries (a device
+ * copy, read by the kernels, and a host copy, used to size scratch).
+ * Per table the semantics and results are exactly those of dyc_apply on that
+ * table with its range; the resize policy runs per table. */
+typedef struct dyc_set dyc_set;
+
+#define DYC_FLAG_GRAPH 8u /* dyc_set_apply: run the launch sequences as CUDA graphs,
+                             captured on the second call with the same arrays and
+                             op count and replayed after that */
+
+/* ntables tables sharing cfg's key/value width, bucket size, eviction bound
+ * and thresholds; table t is sized for sizes[t] keys (the hashAPI(size)
+ * argument) and has num_subtables[t] subtables (NULL: cfg->num_subtables). */
+dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_t *sizes,
+                          const uint32_t *num_subtables, dyc_set **out);
+dyc_status dyc_set_destroy(dyc_set *s);
+
+/* Member table i. Single-table calls may be made on it between set calls;
+ * it is destroyed with the set. */
+dyc_status dyc_set_table(dyc_set *s, uint32_t i, dyc_table **out);
+
+/* Live keys and slot capacity of every member (host arrays of ntables). */
+dyc_status dyc_set_sizes(dyc_set *s, uint64_t *h_sizes, uint64_t *h_capacities);
+
+/* Mixed batch over the set (see above). Returns when the batch is in the
+ * tables. flags: DYC_FLAG_NO_RESIZE, DYC_FLAG_GRAPH. */
+dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *h_offsets,
+                         const uint8_t *d_ops, const void *d_keys, const void *d_vals,
+                         void *d_vals_out, uint32_t *d_bits_out, uint32_t flags, void *stream);
+
+/* The same batch as one dyc_apply per table, one table after another: the
+ * per-table launch path, for comparison. Same results. */
+dyc_status dyc_set_apply_each(dyc_set *s, const uint32_t *d_offsets, const uint32_t *h_offsets,
+                              const uint8_t *d_ops, const void *d_keys, const void *d_vals,
+                              void *d_vals_out, uint32_t *d_bits_out, uint32_t flags,
+                              void *stream);
+
+/* Counters of the last dyc_set_apply / dyc_set_apply_each, summed over the
+ * tables. */
+dyc_status dyc_set_last_stats(dyc_set *s, dyc_op_stats *out);
+
 /* Erase that allocates nothing. It has no counterpart in the reference.
  *
  * For callers that must not allocate device memory while they run: a host

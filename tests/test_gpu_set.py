@@ -1,0 +1,147 @@
+"""GPU parity of table sets (dyc_set_apply): many tables served by one launch
+sequence per batch.
+
+Every table is compared, op by op and by full contents, with its own oracle
+map after every round; the batched path, the per-table path
+(dyc_set_apply_each) and the graph-replayed path give identical results.
+Cases: tables of very different sizes, tables without ops in a round, small
+tables hit by large batches (segments of up to kMidSeg ops per key and one
+giant segment), key 0, u64 keys, growth through the per-table resize policy.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.helpers import assert_same_contents, to_host
+
+pytestmark = pytest.mark.gpu
+
+
+def _dg():
+    import databases_gpu_gb300 as dg
+    return dg
+
+
+def _check_round(S, maps, w_off, ops, keys, vals, out, bits, label):
+    n = keys.numel()
+    gv = to_host(out, S.value_bytes).astype(np.uint64)
+    gh = _dg().unpack_bits(bits, n)
+    o = ops.cpu().numpy()
+    kb = S.key_bytes
+    k = to_host(keys, kb).astype(np.uint64)
+    v = to_host(vals, S.value_bytes).astype(np.uint64)
+    for t in range(S.ntables):
+        a, b = int(w_off[t]), int(w_off[t + 1])
+        if a == b:
+            continue
+        ov, oh = maps[t].apply(o[a:b], k[a:b], v[a:b])
+        assert np.array_equal(gh[a:b], oh), "%s: table %d hit bits differ" % (label, t)
+        assert np.array_equal(gv[a:b], ov), "%s: table %d values differ" % (label, t)
+    sizes, caps = S.sizes()
+    for t in range(S.ntables):
+        assert int(sizes[t]) == len(maps[t]), "%s: table %d size" % (label, t)
+        assert sizes[t] <= caps[t]
+
+
+def _small_workload(ntables, seed, log2_size=(2, 12), log2_batch=(0, 13)):
+    from databases_gpu_gb300.workloads import MultiTableWorkload
+    return MultiTableWorkload(ntables, log2_size=log2_size, log2_batch=log2_batch, seed=seed)
+
+
+def _preload(S, w, maps):
+    for t in range(S.ntables):
+        k, v = w.preload(t)
+        S.table(t).insert(k, v)
+        maps[t].insert(to_host(k, 4), to_host(v, 4))
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_set_matches_oracle_per_table(graph):
+    w = _small_workload(96, seed=5)
+    S = _dg().DyCuckooSet(w.sizes.numpy(), max_evictions=64)
+    maps = [O.Map() for _ in range(S.ntables)]
+    _preload(S, w, maps)
+    for r in range(4):
+        ops, keys, vals = w.round()
+        out, bits = S.apply(w.offsets, ops, keys, vals, h_offsets=w.offsets_host, graph=graph)
+        _check_round(S, maps, w.offsets_host, ops, keys, vals, out, bits, "round %d" % r)
+    for t in (0, 17, 95):
+        assert_same_contents(S.table(t), maps[t], "table %d contents" % t)
+    S.close()
+
+
+def test_set_batched_equals_per_table_path():
+    w = _small_workload(128, seed=9)
+    A = _dg().DyCuckooSet(w.sizes.numpy())
+    B = _dg().DyCuckooSet(w.sizes.numpy())
+    for t in range(A.ntables):
+        k, v = w.preload(t)
+        A.table(t).insert(k, v)
+        B.table(t).insert(k, v)
+    for r in range(3):
+        ops, keys, vals = w.round()
+        oa, ba = A.apply(w.offsets, ops, keys, vals, h_offsets=w.offsets_host)
+        ob, bb = B.apply(w.offsets, ops, keys, vals, h_offsets=w.offsets_host, each=True)
+        assert bool((oa == ob).all()), "round %d: values differ" % r
+        assert bool((ba == bb).all()), "round %d: bits differ" % r
+        sa, _ = A.sizes()
+        sb, _ = B.sizes()
+        assert np.array_equal(sa, sb)
+    for t in range(0, A.ntables, 7):
+        ka, va = A.table(t).export()
+        kb_, vb_ = B.table(t).export()
+        assert bool((ka == kb_).all()) and bool((va == vb_).all())
+    A.close()
+    B.close()
+
+
+def test_set_long_segments_key_zero_and_empty_tables():
+    """Table 0: a few keys hit thousands of times (mid segments) and one key
+    hit 6000 times (a giant segment); table 1 has no ops; table 2 gets key 0."""
+    import torch
+    rng = np.random.default_rng(4)
+    S = _dg().DyCuckooSet([64, 1000, 5000])
+    maps = [O.Map() for _ in range(3)]
+    hot = rng.integers(1, 1 << 31, 40).astype(np.uint32)
+    k0 = np.concatenate([np.repeat(hot[:1], 6000), hot[rng.integers(1, 40, 20000)]])
+    k0 = k0[rng.permutation(k0.size)]
+    k2 = rng.integers(0, 3, 3000).astype(np.uint32)  # keys 0, 1 and 2
+    keys = np.concatenate([k0, k2])
+    ops = rng.choice(np.array([0, 1, 2], np.uint8), size=keys.size, p=[0.4, 0.4, 0.2])
+    vals = rng.integers(1, 1 << 31, keys.size).astype(np.uint32)
+    off = np.array([0, k0.size, k0.size, keys.size], np.uint32)
+    d = lambda a: torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).cuda()
+    for r in range(2):
+        out, bits = S.apply(d(off), d(ops), d(keys), d(vals + np.uint32(r)), h_offsets=off)
+        _check_round(S, maps, off, d(ops), d(keys), d(vals + np.uint32(r)), out, bits,
+                     "long segments round %d" % r)
+    S.close()
+
+
+def test_set_u64_keys_and_growth():
+    """u64 keys / u64 values; tables start tiny and grow through the per-table
+    upsize policy inside the set call."""
+    import torch
+    rng = np.random.default_rng(8)
+    nt = 40
+    S = _dg().DyCuckooSet([16] * nt, key_bytes=8, value_bytes=8)
+    maps = [O.Map() for _ in range(nt)]
+    for r in range(3):
+        cnt = rng.integers(0, 3000, nt)
+        off = np.zeros(nt + 1, np.uint32)
+        off[1:] = np.cumsum(cnt)
+        n = int(off[-1])
+        keys = rng.integers(1, 1 << 62, n, dtype=np.int64).astype(np.uint64) % np.uint64(5000) + \
+            np.uint64(1 << 40)
+        ops = rng.choice(np.array([0, 1, 2], np.uint8), size=n, p=[0.3, 0.6, 0.1])
+        vals = rng.integers(0, 1 << 62, n, dtype=np.int64).astype(np.uint64)
+        dk = torch.from_numpy(keys.view(np.int64)).cuda()
+        dv = torch.from_numpy(vals.view(np.int64)).cuda()
+        do = torch.from_numpy(ops).cuda()
+        doff = torch.from_numpy(off.view(np.int32)).cuda()
+        out, bits = S.apply(doff, do, dk, dv, h_offsets=off)
+        _check_round(S, maps, off, do, dk, dv, out, bits, "u64 round %d" % r)
+    st = S.stats()
+    sizes, caps = S.sizes()
+    assert caps.max() > 16 * 4  # tables grew
+    S.close()
