@@ -330,6 +330,63 @@ def run_resize_stream(args, dev, torch, dg):
     return res
 
 
+def run_multi_table(args, dev, torch, dg):
+    """4096 independent u32 tables (log-uniform 2^8..2^20 keys), each with a
+    log-uniform 16..2^16-op mixed batch per round (70/20/10, 50% find hits):
+    the batched set path (one launch sequence per round, graph-replayed)
+    against one dyc_apply per table, on twin sets fed the same rounds; every
+    op's result must agree between the two."""
+    from databases_gpu_gb300.workloads import MultiTableWorkload
+    w = MultiTableWorkload(args.mt_tables, seed=10327, device=dev)
+    sets = [dg.DyCuckooSet(w.sizes.numpy(), device=dev.index or 0) for _ in range(2)]
+    for t in range(w.ntables):
+        k, v = w.preload(t)
+        for S in sets:
+            S.table(t).insert(k, v, new_keys=True, unique=True)
+    torch.cuda.synchronize()
+    n = w.n_ops
+    stream = torch.cuda.current_stream()
+    outs = [torch.empty(n, dtype=torch.int32, device=dev) for _ in range(2)]
+    bitss = [torch.empty((n + 31) // 32, dtype=torch.int32, device=dev) for _ in range(2)]
+    lat = {"batched": [], "per_table": []}
+    bad = 0
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    rounds = args.mt_rounds
+    for r in range(rounds + 2):  # two untimed rounds: scratch, graph capture
+        ops, keys, vals = w.round()
+        for which, S in (("batched", sets[0]), ("per_table", sets[1])):
+            i = 0 if which == "batched" else 1
+            torch.cuda.synchronize()
+            e0.record(stream)
+            S.apply(w.offsets, ops, keys, vals, out=outs[i], bits=bitss[i],
+                    h_offsets=w.offsets_host, each=(which == "per_table"),
+                    graph=(which == "batched"), stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if r >= 2:
+                lat[which].append(e0.elapsed_time(e1))
+        bad += int((outs[0] != outs[1]).sum()) + int((bitss[0] != bitss[1]).sum())
+    sa, ca = sets[0].sizes()
+    sb, cb = sets[1].sizes()
+    bad += int((sa != sb).sum())
+    res = {"workload": "batched multi-table: %d u32 tables, sizes log-uniform 2^8..2^20 keys, "
+                       "per-table batches log-uniform 16..2^16 ops (70/20/10 find/insert/erase, "
+                       "50%% find hits), %d ops per round" % (w.ntables, n),
+           "tables": w.ntables, "ops_per_round": n, "rounds": rounds,
+           "keys_total": int(sa.sum()), "capacity_total": int(ca.sum()),
+           "result_mismatches": bad}
+    for which in ("batched", "per_table"):
+        ms = sorted(lat[which])
+        res[which] = {"mops": round(n * len(ms) / (sum(ms) / 1e3) / 1e6, 1),
+                      "round_ms_p50": round(ms[len(ms) // 2], 3), "round_ms_max": round(ms[-1], 3)}
+    res["batched_over_per_table"] = round(res["batched"]["mops"] / res["per_table"]["mops"], 2)
+    res["api"] = "dyc_set_apply (graph replay) vs dyc_set_apply_each (one dyc_apply per table)"
+    for S in sets:
+        S.close()
+    return res
+
+
 def workload_config(args, lf):
     return {
         "workload": "large static table find: u32 keys/values, 4 subtables, 2^%d unique keys "
@@ -358,6 +415,10 @@ def main():
                     help="measure the random 128-byte line ceiling of this GPU and exit")
     ap.add_argument("--skip-stream", action="store_true",
                     help="skip the dynamic resize stream workload")
+    ap.add_argument("--skip-multi", action="store_true",
+                    help="skip the batched multi-table workload")
+    ap.add_argument("--mt-tables", type=int, default=4096)
+    ap.add_argument("--mt-rounds", type=int, default=3)
     ap.add_argument("--stream-batches", type=int, default=512)
     ap.add_argument("--stream-log2-batch", type=int, default=22)
     ap.add_argument("--stream-log2-start", type=int, default=20)
@@ -514,6 +575,8 @@ def main():
     workloads = {}
     if not args.skip_stream and not args.skip_variants:
         workloads["resize_stream"] = run_resize_stream(args, dev, torch, dg)
+    if not args.skip_multi and not args.skip_variants:
+        workloads["multi_table"] = run_multi_table(args, dev, torch, dg)
 
     # ---- e2e: host buffers through the C ABI (dyc_find_host), pinned memory
     q0 = qs_e2e = batch("uniform100")
