@@ -43,6 +43,21 @@ class DycOpStats(C.Structure):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
 
 
+class DycServerConfig(C.Structure):
+    _fields_ = [("hbm_cap_bytes", C.c_uint64), ("max_step_ops", C.c_uint64),
+                ("coalesce", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+
+
+class DycServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "requests", "ops", "steps", "deferred", "rejected", "max_step_ops", "device_bytes")] + \
+        [("busy_seconds", C.c_double)]
+
+    def as_dict(self):
+        return {n: (float if n == "busy_seconds" else int)(getattr(self, n))
+                for n, _ in self._fields_}
+
+
 EXPORTS = [
     "dyc_config_default", "dyc_create", "dyc_destroy", "dyc_insert", "dyc_find", "dyc_erase",
     "dyc_resize_up", "dyc_resize_down", "dyc_size", "dyc_capacity", "dyc_layout",
@@ -50,6 +65,8 @@ EXPORTS = [
     "dyc_erase_host", "dyc_status_string", "dyc_last_error", "dyc_erase_noalloc", "dyc_apply",
     "dyc_set_create", "dyc_set_destroy", "dyc_set_table", "dyc_set_sizes", "dyc_set_apply",
     "dyc_set_apply_each", "dyc_set_last_stats",
+    "dyc_server_config_default", "dyc_server_create", "dyc_server_destroy", "dyc_server_submit",
+    "dyc_server_wait", "dyc_server_stats_get", "dyc_server_set",
 ]
 
 _lock = threading.Lock()
@@ -87,6 +104,14 @@ def _declare(L):
         "dyc_set_apply": (st, [T, vp, vp, vp, vp, vp, vp, vp, u32, vp]),
         "dyc_set_apply_each": (st, [T, vp, vp, vp, vp, vp, vp, vp, u32, vp]),
         "dyc_set_last_stats": (st, [T, C.POINTER(DycOpStats)]),
+        "dyc_server_config_default": (None, [C.POINTER(DycServerConfig)]),
+        "dyc_server_create": (st, [C.POINTER(DycConfig), u32, vp, C.POINTER(DycServerConfig),
+                                   C.POINTER(C.c_void_p)]),
+        "dyc_server_destroy": (st, [T]),
+        "dyc_server_submit": (st, [T, u32, vp, vp, vp, u64, vp, vp, C.POINTER(u64)]),
+        "dyc_server_wait": (st, [T, u64, C.c_int64, C.POINTER(st), C.POINTER(u64)]),
+        "dyc_server_stats_get": (st, [T, C.POINTER(DycServerStats)]),
+        "dyc_server_set": (st, [T, C.POINTER(C.c_void_p)]),
         "dyc_status_string": (C.c_char_p, [st]),
         "dyc_last_error": (C.c_char_p, []),
     }

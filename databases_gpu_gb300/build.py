@@ -17,7 +17,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD_DIR = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libdycuckoo.so")
 
-SOURCES = ["dyc_ops4.cu", "dyc_ops8.cu", "dyc_api.cu"]
+SOURCES = ["dyc_ops4.cu", "dyc_ops8.cu", "dyc_api.cu", "dyc_server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-I", INCLUDE, "-I", CSRC]

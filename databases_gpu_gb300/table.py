@@ -396,6 +396,105 @@ class DyCuckooSet:
         return out, bits
 
 
+class DyCuckooServer:
+    """Request server over per-tenant tables (dyc_server_*): submit mixed-op
+    requests in host memory from any thread, wait for their results.
+
+    sizes: per-tenant key counts to size for; hbm_cap_bytes: admission cap
+    (0: none); coalesce: continuous batching (False: one request per step)."""
+
+    def __init__(self, sizes, key_bytes: int = 8, value_bytes: int = 4,
+                 hbm_cap_bytes: int = 0, max_step_ops: int = 1 << 22, coalesce: bool = True,
+                 bucket_bytes: int = 128, max_evictions: int = 64, auto_resize: bool = True,
+                 upper_load: float = UPPER_BOUND, lower_load: float = LOWER_BOUND,
+                 min_downsize_capacity: int = MIN_DOWNSIZE_CAPACITY, device: int = 0):
+        import threading
+        L = _lib.lib()
+        cfg = _lib.DycConfig()
+        L.dyc_config_default(C.byref(cfg))
+        cfg.key_bytes, cfg.value_bytes = key_bytes, value_bytes
+        cfg.bucket_bytes, cfg.max_evictions = bucket_bytes, max_evictions
+        cfg.auto_resize = 1 if auto_resize else 0
+        cfg.upper_load, cfg.lower_load = upper_load, lower_load
+        cfg.min_downsize_capacity = int(min_downsize_capacity)
+        cfg.device = device
+        sc = _lib.DycServerConfig()
+        L.dyc_server_config_default(C.byref(sc))
+        sc.hbm_cap_bytes = int(hbm_cap_bytes)
+        sc.max_step_ops = int(max_step_ops)
+        sc.coalesce = 1 if coalesce else 0
+        sz = np.ascontiguousarray(sizes, dtype=np.uint64)
+        h = C.c_void_p()
+        check(L.dyc_server_create(C.byref(cfg), sz.size, sz.ctypes.data, C.byref(sc),
+                                  C.byref(h)), "dyc_server_create")
+        self._h, self.L, self.cfg = h, L, cfg
+        self.ntenants = int(sz.size)
+        self.key_bytes, self.value_bytes = key_bytes, value_bytes
+        self._keep = {}  # ticket -> arrays the server reads / writes
+        self._lock = threading.Lock()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.L.dyc_server_destroy(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, tenant: int, ops: np.ndarray, keys: np.ndarray, vals: np.ndarray) -> int:
+        """Queue a request; returns its ticket. Results come from wait()."""
+        ops = np.ascontiguousarray(ops, np.uint8)
+        keys = np.ascontiguousarray(keys)
+        vals = np.ascontiguousarray(vals)
+        n = ops.size
+        if keys.itemsize != self.key_bytes or vals.itemsize != self.value_bytes:
+            raise ValueError("key / value widths do not match the server")
+        out = np.empty(n, np.uint32 if self.value_bytes == 4 else np.uint64)
+        bits = np.empty((n + 31) // 32, np.uint32)
+        t = C.c_uint64()
+        check(self.L.dyc_server_submit(self._h, tenant, ops.ctypes.data, keys.ctypes.data,
+                                       vals.ctypes.data, n, out.ctypes.data, bits.ctypes.data,
+                                       C.byref(t)), "dyc_server_submit")
+        with self._lock:
+            self._keep[t.value] = (ops, keys, vals, out, bits, n)
+        return int(t.value)
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        """(status, values, hit bits as bool array, latency in ns)."""
+        st = C.c_int()
+        lat = C.c_uint64()
+        check(self.L.dyc_server_wait(self._h, ticket, timeout_ms, C.byref(st), C.byref(lat)),
+              "dyc_server_wait")
+        with self._lock:
+            ops, keys, vals, out, bits, n = self._keep.pop(ticket)
+        return int(st.value), out, unpack_bits(bits, n), int(lat.value)
+
+    def stats(self) -> dict:
+        s = _lib.DycServerStats()
+        check(self.L.dyc_server_stats_get(self._h, C.byref(s)), "dyc_server_stats_get")
+        return s.as_dict()
+
+    def table(self, i: int) -> DyCuckoo:
+        """Tenant i's table (use only while nothing is queued or running)."""
+        hs = C.c_void_p()
+        check(self.L.dyc_server_set(self._h, C.byref(hs)), "dyc_server_set")
+        h = C.c_void_p()
+        check(self.L.dyc_set_table(hs, i, C.byref(h)), "dyc_set_table")
+        cfg = _lib.DycConfig()
+        C.memmove(C.byref(cfg), C.byref(self.cfg), C.sizeof(cfg))
+        return DyCuckoo._member(h, cfg, self)
+
+
 def unpack_bits(bits, n: int) -> np.ndarray:
     """Hit / erased bit words (ceil(n/32) uint32) -> bool array of n."""
     if hasattr(bits, "cpu"):

@@ -248,6 +248,73 @@ dyc_status dyc_set_apply_each(dyc_set *s, const uint32_t *d_offsets, const uint3
  * tables. */
 dyc_status dyc_set_last_stats(dyc_set *s, dyc_op_stats *out);
 
+/* ---- Request server --------------------------------------------------------
+ * A serving loop over a table set with one table per tenant (no reference
+ * counterpart: the reference is a library called in batches). Requests --
+ * mixed op batches in host memory for one tenant -- are submitted from any
+ * thread and return a ticket at once. A pipeline of three threads runs
+ * continuous batching: while the device executes one step, the next step is
+ * assembled from every request that has arrived and is admitted (tenants'
+ * ops grouped, copied host->device), and the previous step's results go back
+ * device->host and to their requests. Requests of one tenant take effect in
+ * submission order, ops of a request in index order, so each request's
+ * results are those it gets when run alone after the earlier requests of its
+ * tenant. Admission is first-in first-out against a cap on the device bytes
+ * of tables, scratch and staging, counting each request's possible growth
+ * with resize headroom; a request that cannot fit even on an idle server is
+ * rejected with DYC_ENOMEM. */
+typedef struct dyc_server dyc_server;
+
+typedef struct dyc_server_config {
+    uint64_t hbm_cap_bytes; /* admission cap in device bytes (0: none) */
+    uint64_t max_step_ops;  /* most ops in one step (default 1 << 22); also the
+                               largest request */
+    uint32_t coalesce;      /* 1 (default): continuous batching over the set;
+                               0: one request per step through dyc_apply on its
+                               tenant's table (the per-request path) */
+    uint32_t reserved[7];
+} dyc_server_config;
+
+typedef struct dyc_server_stats {
+    uint64_t requests;      /* completed (including rejected) */
+    uint64_t ops;           /* ops of completed requests */
+    uint64_t steps;         /* device steps run */
+    uint64_t deferred;      /* requests that waited for memory at least once */
+    uint64_t rejected;      /* requests that could never be admitted */
+    uint64_t max_step_ops;  /* largest step */
+    uint64_t device_bytes;  /* tables + scratch + staging, after the last step */
+    double busy_seconds;    /* time the executor spent in device steps */
+} dyc_server_stats;
+
+void dyc_server_config_default(dyc_server_config *c);
+
+/* Tenant tables as dyc_set_create(table_cfg, ntenants, sizes, NULL). */
+dyc_status dyc_server_create(const dyc_config *table_cfg, uint32_t ntenants,
+                             const uint64_t *sizes, const dyc_server_config *cfg,
+                             dyc_server **out);
+
+/* Runs every submitted request, then stops the threads and frees everything. */
+dyc_status dyc_server_destroy(dyc_server *s);
+
+/* Queue a request; the host arrays must stay valid (and outputs unread)
+ * until dyc_server_wait reports it done. h_vals_out (n values) and
+ * h_bits_out (ceil(n/32) words) are optional; results as dyc_apply. */
+dyc_status dyc_server_submit(dyc_server *s, uint32_t tenant, const uint8_t *h_ops,
+                             const void *h_keys, const void *h_vals, uint64_t n,
+                             void *h_vals_out, uint32_t *h_bits_out, uint64_t *ticket);
+
+/* Wait for a request (timeout_ms < 0: no limit). DYC_OK when it completed,
+ * with its own status in *req_status and submit-to-done time in
+ * *latency_ns; DYC_ETIMEOUT when the limit passed first (wait again later).
+ * A ticket can be waited for until it has been reported complete once. */
+dyc_status dyc_server_wait(dyc_server *s, uint64_t ticket, int64_t timeout_ms,
+                           dyc_status *req_status, uint64_t *latency_ns);
+
+dyc_status dyc_server_stats_get(dyc_server *s, dyc_server_stats *out);
+
+/* The tenant tables. Use them only while no request is queued or running. */
+dyc_status dyc_server_set(dyc_server *s, dyc_set **out);
+
 /* Erase that allocates nothing. It has no counterpart in the reference.
  *
  * For callers that must not allocate device memory while they run: a host
