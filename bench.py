@@ -265,6 +265,47 @@ def run_line_probe():
     print(json.dumps(d))
 
 
+def build_serve_load():
+    """The server's load generator (databases_gpu_gb300/csrc/dyc_serve_load.cpp)."""
+    from databases_gpu_gb300 import build as pkg_build
+    lib = pkg_build.build()
+    src = os.path.join(pkg_build.CSRC, "dyc_serve_load.cpp")
+    exe = os.path.join(pkg_build.BUILD_DIR, "dyc_serve_load")
+    os.makedirs(pkg_build.BUILD_DIR, exist_ok=True)
+    if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(src),
+                                                               os.path.getmtime(lib)):
+        subprocess.check_call([pkg_build.nvcc(), "-O3", "-std=c++17", "-I", pkg_build.INCLUDE,
+                               "-o", exe, src, "-L", pkg_build.PKG, "-ldycuckoo",
+                               "-Xlinker", "-rpath=" + pkg_build.PKG])
+    return exe
+
+
+def run_serving(args):
+    """Serving loop: 64 u64/u32 tenants (2^16..2^24 keys), Poisson request
+    arrivals, log-uniform 32..65536-op requests (70/20/10), Zipf(0.9) tenant
+    choice, 120 GB admission cap. Three runs: continuous batching at the
+    offered rate, continuous batching below saturation, and the per-request
+    path (one dyc_apply per request)."""
+    exe = build_serve_load()
+    runs = [("batched", args.serve_rate, args.serve_seconds, 1),
+            ("batched_light", args.serve_rate / 8, args.serve_seconds * 2, 1),
+            ("per_request", args.serve_rate, args.serve_seconds / 10, 0)]
+    res = {"workload": "serving loop: 64 tenants, u64 keys / u32 values, initial 2^16..2^24 keys "
+                       "each; Poisson arrivals; requests log-uniform 32..65536 ops, 70/20/10 "
+                       "find/insert/erase; Zipf(0.9) tenant choice; 120 GB admission cap",
+           "api": "dyc_server_submit / dyc_server_wait (host buffers; latency = completion - "
+                  "scheduled arrival)"}
+    for name, rate, secs, coal in runs:
+        cmd = [exe, "--rate", str(rate), "--seconds", str(secs), "--coalesce", str(coal),
+               "--cap-gb", "120"]
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+        if r.returncode != 0:
+            res[name] = {"error": (r.stderr or r.stdout).strip()[-300:]}
+            continue
+        res[name] = json.loads(r.stdout.strip().splitlines()[-1])
+    return res
+
+
 def unpack_bits_dev(bits, n, torch):
     sh = torch.arange(32, dtype=torch.int32, device=bits.device)
     return ((bits.view(-1, 1) >> sh) & 1).flatten()[:n].bool()
@@ -417,6 +458,9 @@ def main():
                     help="skip the dynamic resize stream workload")
     ap.add_argument("--skip-multi", action="store_true",
                     help="skip the batched multi-table workload")
+    ap.add_argument("--skip-serve", action="store_true", help="skip the serving loop")
+    ap.add_argument("--serve-rate", type=float, default=2e5)
+    ap.add_argument("--serve-seconds", type=float, default=0.25)
     ap.add_argument("--mt-tables", type=int, default=4096)
     ap.add_argument("--mt-rounds", type=int, default=3)
     ap.add_argument("--stream-batches", type=int, default=512)
@@ -577,6 +621,8 @@ def main():
         workloads["resize_stream"] = run_resize_stream(args, dev, torch, dg)
     if not args.skip_multi and not args.skip_variants:
         workloads["multi_table"] = run_multi_table(args, dev, torch, dg)
+    if not args.skip_serve and not args.skip_variants and ws == 1:
+        workloads["serving"] = run_serving(args)
 
     # ---- e2e: host buffers through the C ABI (dyc_find_host), pinned memory
     q0 = qs_e2e = batch("uniform100")
