@@ -26,6 +26,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include <functional>
+
 #include <cuda_runtime.h>
 
 #include "dycuckoo.h"
@@ -33,6 +35,76 @@
 namespace {
 
 using Clock = std::chrono::steady_clock;
+
+// Fixed pool of helper threads for the staging copies: run(n, f) calls f(i)
+// for i in [0, n) on the helpers and the caller, and returns when all are done.
+class CopyPool {
+  public:
+    explicit CopyPool(int helpers) {
+        for (int i = 0; i < helpers; ++i) th_.emplace_back([this] { loop(); });
+    }
+    ~CopyPool() {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+    void run(uint64_t n, const std::function<void(uint64_t)> &f) {
+        if (n == 0) return;
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            job_ = &f;
+            n_ = n;
+            next_ = 0;
+            left_ = n;
+            ++gen_;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> lk(mu_);
+        done_.wait(lk, [&] { return left_ == 0; });
+        job_ = nullptr;
+    }
+
+  private:
+    void work() {
+        for (;;) {
+            uint64_t i;
+            const std::function<void(uint64_t)> *f;
+            {
+                std::lock_guard<std::mutex> g(mu_);
+                if (!job_ || next_ >= n_) return;
+                i = next_++;
+                f = job_;
+            }
+            (*f)(i);
+            std::lock_guard<std::mutex> g(mu_);
+            if (--left_ == 0) done_.notify_all();
+        }
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || (gen_ != seen && job_ && next_ < n_); });
+                if (stop_) return;
+                seen = gen_;
+            }
+            work();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_;
+    const std::function<void(uint64_t)> *job_ = nullptr;
+    uint64_t n_ = 0, next_ = 0, left_ = 0, gen_ = 0;
+    bool stop_ = false;
+};
+
+constexpr int kCopyHelpers = 7;  // per copying stage (assembler, completer)
 
 struct Req {
     uint64_t ticket;
@@ -90,6 +162,7 @@ struct dyc_server {
 
     uint64_t fixed_bytes = 0, table_bytes = 0, pending_growth = 0;
     dyc_server_stats st{};
+    CopyPool asm_pool{kCopyHelpers}, comp_pool{kCopyHelpers};
     std::thread t_asm, t_exec, t_comp;
 };
 
@@ -185,10 +258,13 @@ void assembler(dyc_server *s) {
         for (Req *r : take) {
             r->pos = s->scfg.coalesce ? cnt[r->tenant] : 0;
             if (s->scfg.coalesce) cnt[r->tenant] += r->n;
+        }
+        s->asm_pool.run(take.size(), [&](uint64_t i) {
+            const Req *r = take[i];
             memcpy(sl.h_ops + r->pos, r->ops, r->n);
             memcpy(sl.h_keys + r->pos * s->kb, r->keys, r->n * s->kb);
             memcpy(sl.h_vals + r->pos * s->vb, r->vals, r->n * s->vb);
-        }
+        });
         cudaError_t e = cudaMemcpyAsync(sl.d_ops, sl.h_ops, n, cudaMemcpyHostToDevice, s->up);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(sl.d_keys, sl.h_keys, n * s->kb, cudaMemcpyHostToDevice, s->up);
@@ -274,10 +350,11 @@ void completer(dyc_server *s) {
         if (sl.status != DYC_OK) {
             finish_slot_error(s, sl, sl.status);
         } else {
-            for (Req *r : sl.reqs) {
+            s->comp_pool.run(sl.reqs.size(), [&](uint64_t i) {
+                const Req *r = sl.reqs[i];
                 if (r->out) memcpy(r->out, sl.h_out + r->pos * s->vb, r->n * s->vb);
                 if (r->bits) extract_bits(sl.h_bits, r->pos, r->n, r->bits);
-            }
+            });
         }
         const auto now = Clock::now();
         std::lock_guard<std::mutex> g(s->mu);
