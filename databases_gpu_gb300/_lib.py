@@ -67,6 +67,7 @@ EXPORTS = [
     "dyc_set_apply_each", "dyc_set_last_stats",
     "dyc_server_config_default", "dyc_server_create", "dyc_server_destroy", "dyc_server_submit",
     "dyc_server_wait", "dyc_server_stats_get", "dyc_server_set",
+    "dyc_snapshot_bytes", "dyc_snapshot", "dyc_restore",
 ]
 
 _lock = threading.Lock()
@@ -112,6 +113,9 @@ def _declare(L):
         "dyc_server_wait": (st, [T, u64, C.c_int64, C.POINTER(st), C.POINTER(u64)]),
         "dyc_server_stats_get": (st, [T, C.POINTER(DycServerStats)]),
         "dyc_server_set": (st, [T, C.POINTER(C.c_void_p)]),
+        "dyc_snapshot_bytes": (st, [T, C.POINTER(u64)]),
+        "dyc_snapshot": (st, [T, vp, u64, vp]),
+        "dyc_restore": (st, [vp, u64, C.c_int32, C.POINTER(C.c_void_p)]),
         "dyc_status_string": (C.c_char_p, [st]),
         "dyc_last_error": (C.c_char_p, []),
     }

@@ -383,8 +383,10 @@ const char *dyc_last_error(void) { return g_err.c_str(); }
 namespace {
 // Table creation. ext_d / ext_h: counters owned by a table set (the table
 // then allocates none); sync: wait for the zero-fill before returning.
+// nb_override: bucket count of every subtable (a restored snapshot's layout)
+// instead of the sizing rule.
 dyc_status create_impl(const dyc_config *cfg, Counters *ext_d, Counters *ext_h, bool sync,
-                       dyc_table **out) {
+                       dyc_table **out, const uint32_t *nb_override = nullptr) {
     if (!cfg || !out) return fail(DYC_EINVAL, "null argument");
     *out = nullptr;
     char why[128];
@@ -414,10 +416,11 @@ dyc_status create_impl(const dyc_config *cfg, Counters *ext_d, Counters *ext_h, 
     const uint64_t s0 = cfg->initial_size / per;
     if (s0 >= 0x7FFFFFF0ull) return undo(fail(DYC_EINVAL, "initial_size too large"));
     uint32_t s = next_prime_ref((uint32_t)s0);
-    const uint32_t nb = (s & 1u) ? s + 1u : s;
+    const uint32_t nb_rule = (s & 1u) ? s + 1u : s;
     memset(&t->D, 0, sizeof(t->D));
     t->D.d = cfg->num_subtables;
     for (uint32_t i = 0; i < t->D.d; ++i) {
+        const uint32_t nb = nb_override ? nb_override[i] : nb_rule;
         cudaError_t e = cudaMalloc(&t->D.sub[i], (size_t)nb * t->sb);
         if (e != cudaSuccess) return undo(fail(DYC_ENOMEM, "subtable %u: %s", i, cudaGetErrorString(e)));
         e = cudaMemsetAsync(t->D.sub[i], 0, (size_t)nb * t->sb, 0);
@@ -1448,6 +1451,170 @@ dyc_status dyc_set_apply_each(dyc_set *s, const uint32_t *d_offsets, const uint3
     }
     CK(cudaStreamSynchronize(st));
     return set_push_descs(s, st);
+}
+
+}  // extern "C"
+
+// =============================================================================
+// Snapshot / restore (include/dycuckoo.h dyc_snapshot*, dyc_restore).
+// =============================================================================
+static_assert(sizeof(dyc_snapshot_header) == 256, "snapshot header is 256 bytes");
+
+namespace {
+
+constexpr uint64_t kSnapGold = 0x9E3779B97F4A7C15ull;
+
+__device__ __forceinline__ uint64_t snap_mix(uint64_t x) {
+    x += kSnapGold;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+// sum of snap_mix(w[i] ^ (base + i) * gold) into *sum (mod 2^64, so the
+// order of the additions does not matter)
+__global__ void __launch_bounds__(256) k_snapshot_sum(const uint64_t *__restrict__ w, uint64_t n,
+                                                      uint64_t base,
+                                                      unsigned long long *__restrict__ sum) {
+    uint64_t acc = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        acc += snap_mix(w[i] ^ ((base + i) * kSnapGold));
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(sum, (unsigned long long)acc);
+}
+
+// Checksum of the table's subtables, in subtable order, on `s`.
+dyc_status table_checksum(dyc_table *t, cudaStream_t s, uint64_t *out) {
+    unsigned long long *d = &t->d_ctr->pad[1];
+    CK(cudaMemsetAsync(d, 0, sizeof(unsigned long long), s));
+    uint64_t base = 0;
+    for (uint32_t i = 0; i < t->D.d; ++i) {
+        const uint64_t words = (uint64_t)t->D.nb[i] * t->sb / 8;
+        const unsigned blocks = (unsigned)std::min<uint64_t>((words + 255) / 256, (uint64_t)t->sms * 8);
+        k_snapshot_sum<<<blocks, 256, 0, s>>>((const uint64_t *)t->D.sub[i], words, base, d);
+        CK(cudaGetLastError());
+        base += words;
+    }
+    unsigned long long h = 0;
+    CK(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *out = h;
+    return DYC_OK;
+}
+
+uint64_t snapshot_payload(const dyc_table *t) {
+    uint64_t p = 0;
+    for (uint32_t i = 0; i < t->D.d; ++i) p += (uint64_t)t->D.nb[i] * t->sb;
+    return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+dyc_status dyc_snapshot_bytes(dyc_table *t, uint64_t *bytes) {
+    if (!t || !bytes) return fail(DYC_EINVAL, "null argument");
+    *bytes = sizeof(dyc_snapshot_header) + snapshot_payload(t);
+    return DYC_OK;
+}
+
+dyc_status dyc_snapshot(dyc_table *t, void *h_buf, uint64_t buf_bytes, void *stream) {
+    if (!t || !h_buf) return fail(DYC_EINVAL, "null argument");
+    const uint64_t payload = snapshot_payload(t);
+    if (buf_bytes < sizeof(dyc_snapshot_header) + payload)
+        return fail(DYC_EINVAL, "snapshot buffer of %llu bytes, need %llu",
+                    (unsigned long long)buf_bytes,
+                    (unsigned long long)(sizeof(dyc_snapshot_header) + payload));
+    TRY(set_device(t));
+    cudaStream_t s = (cudaStream_t)stream;
+    dyc_snapshot_header h;
+    memset(&h, 0, sizeof(h));
+    memcpy(h.magic, "DYCSNAP1", 8);
+    h.version = 1;
+    h.header_bytes = sizeof(h);
+    h.key_bytes = t->cfg.key_bytes;
+    h.value_bytes = t->cfg.value_bytes;
+    h.bucket_bytes = t->cfg.bucket_bytes;
+    h.num_subtables = t->D.d;
+    h.max_evictions = t->cfg.max_evictions;
+    h.auto_resize = t->cfg.auto_resize;
+    h.size = t->size;
+    h.capacity = t->capacity;
+    h.upper_load = t->cfg.upper_load;
+    h.lower_load = t->cfg.lower_load;
+    h.min_downsize_capacity = t->cfg.min_downsize_capacity;
+    h.initial_size = t->cfg.initial_size;
+    for (uint32_t i = 0; i < t->D.d; ++i) h.nbuckets[i] = t->D.nb[i];
+    h.payload_bytes = payload;
+    TRY(table_checksum(t, s, &h.checksum));
+    char *dst = (char *)h_buf + sizeof(h);
+    for (uint32_t i = 0; i < t->D.d; ++i) {
+        const uint64_t b = (uint64_t)t->D.nb[i] * t->sb;
+        CK(cudaMemcpyAsync(dst, t->D.sub[i], b, cudaMemcpyDeviceToHost, s));
+        dst += b;
+    }
+    CK(cudaStreamSynchronize(s));
+    memcpy(h_buf, &h, sizeof(h));
+    return DYC_OK;
+}
+
+dyc_status dyc_restore(const void *h_buf, uint64_t buf_bytes, int32_t device, dyc_table **out) {
+    if (!h_buf || !out) return fail(DYC_EINVAL, "null argument");
+    *out = nullptr;
+    dyc_snapshot_header h;
+    if (buf_bytes < sizeof(h)) return fail(DYC_EINVAL, "snapshot shorter than its header");
+    memcpy(&h, h_buf, sizeof(h));
+    if (memcmp(h.magic, "DYCSNAP1", 8) != 0 || h.version != 1 || h.header_bytes != sizeof(h))
+        return fail(DYC_EINVAL, "not a version-1 DyCuckoo snapshot");
+    dyc_config c;
+    dyc_config_default(&c);
+    c.key_bytes = h.key_bytes;
+    c.value_bytes = h.value_bytes;
+    c.bucket_bytes = h.bucket_bytes;
+    c.num_subtables = h.num_subtables;
+    c.max_evictions = h.max_evictions;
+    c.auto_resize = h.auto_resize;
+    c.upper_load = h.upper_load;
+    c.lower_load = h.lower_load;
+    c.min_downsize_capacity = h.min_downsize_capacity;
+    c.initial_size = h.initial_size;
+    c.device = device;
+    char why[128];
+    if (!valid_config(&c, why, sizeof(why))) return fail(DYC_EINVAL, "snapshot header: %s", why);
+    uint64_t payload = 0, slots = 0;
+    const uint64_t per_bucket = c.bucket_bytes / (c.key_bytes == 4 ? 8 : 16) -
+                                (c.bucket_bytes == 128 ? 1 : 0);
+    for (uint32_t i = 0; i < c.num_subtables; ++i) {
+        if (h.nbuckets[i] == 0) return fail(DYC_EINVAL, "snapshot header: empty subtable %u", i);
+        payload += (uint64_t)h.nbuckets[i] * c.bucket_bytes;
+        slots += (uint64_t)h.nbuckets[i] * per_bucket;
+    }
+    if (payload != h.payload_bytes || slots != h.capacity || h.size > slots)
+        return fail(DYC_EINVAL, "snapshot header: inconsistent sizes");
+    if (buf_bytes < sizeof(h) + payload) return fail(DYC_EINVAL, "snapshot payload is truncated");
+    dyc_table *t = nullptr;
+    TRY(create_impl(&c, nullptr, nullptr, true, &t, h.nbuckets));
+    auto undo = [&](dyc_status r) {
+        dyc_destroy(t);
+        return r;
+    };
+    const char *src = (const char *)h_buf + sizeof(h);
+    for (uint32_t i = 0; i < t->D.d; ++i) {
+        const uint64_t b = (uint64_t)t->D.nb[i] * t->sb;
+        cudaError_t e = cudaMemcpy(t->D.sub[i], src, b, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "restore copy: %s", cudaGetErrorString(e)));
+        src += b;
+    }
+    uint64_t sum = 0;
+    dyc_status r = table_checksum(t, 0, &sum);
+    if (r != DYC_OK) return undo(r);
+    if (sum != h.checksum) return undo(fail(DYC_EINVAL, "snapshot checksum mismatch"));
+    t->size = h.size;
+    cudaError_t e = cudaMemcpy(&t->d_ctr->size, &h.size, sizeof(h.size), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "restore size: %s", cudaGetErrorString(e)));
+    *out = t;
+    return DYC_OK;
 }
 
 }  // extern "C"

@@ -269,6 +269,43 @@ class DyCuckoo:
             order = torch.from_numpy(np.argsort(kk, kind="stable")).to(k.device)
         return k[order], v[order]
 
+    # -- snapshot / restore
+    def snapshot(self, stream=None) -> np.ndarray:
+        """The table as a snapshot buffer (header + raw subtables)."""
+        nb = C.c_uint64()
+        check(self.L.dyc_snapshot_bytes(self._h, C.byref(nb)), "dyc_snapshot_bytes")
+        buf = np.empty(nb.value, np.uint8)
+        check(self.L.dyc_snapshot(self._h, buf.ctypes.data, buf.size, _stream_ptr(stream)),
+              "dyc_snapshot")
+        return buf
+
+    @classmethod
+    def restore(cls, buf, device: int = 0) -> "DyCuckoo":
+        """A new table from a snapshot buffer (bytes or uint8 array)."""
+        a = np.frombuffer(buf, np.uint8) if isinstance(buf, (bytes, bytearray)) else \
+            np.ascontiguousarray(buf, np.uint8)
+        L = _lib.lib()
+        h = C.c_void_p()
+        check(L.dyc_restore(a.ctypes.data, a.size, device, C.byref(h)), "dyc_restore")
+        hdr = a[:256].view(np.uint32)
+        t = cls.__new__(cls)
+        cfg = _lib.DycConfig()
+        L.dyc_config_default(C.byref(cfg))
+        cfg.key_bytes, cfg.value_bytes, cfg.bucket_bytes, cfg.num_subtables = \
+            int(hdr[4]), int(hdr[5]), int(hdr[6]), int(hdr[7])
+        cfg.max_evictions, cfg.auto_resize = int(hdr[8]), int(hdr[9])
+        cfg.device = device
+        t._h, t.L, t.cfg = h, L, cfg
+        t.key_bytes, t.value_bytes, t.device = cfg.key_bytes, cfg.value_bytes, device
+        return t
+
+    def save(self, path: str) -> None:
+        self.snapshot().tofile(path)
+
+    @classmethod
+    def load(cls, path: str, device: int = 0) -> "DyCuckoo":
+        return cls.restore(np.fromfile(path, np.uint8), device)
+
     # -- host-buffer forms (reference-facing C ABI with host memory)
     def insert_host(self, keys: np.ndarray, values: np.ndarray, flags: int = 0) -> None:
         keys = np.ascontiguousarray(keys)

@@ -197,6 +197,42 @@ dyc_status dyc_apply(dyc_table *t, const uint8_t *d_ops, const void *d_keys, con
                      uint64_t n, void *d_vals_out, uint32_t *d_bits_out, uint32_t flags,
                      void *stream);
 
+/* ---- Snapshot / restore ----------------------------------------------------
+ * A snapshot is a host buffer: this 256-byte header, then every subtable's
+ * buckets in subtable order, byte for byte as they are in device memory (the
+ * slot layout of dyc_subtable). Restoring gives a table with the same
+ * configuration, subtable sizes and slot positions, so it behaves exactly as
+ * the snapshotted one. The reference has no checkpoint (it writes only
+ * diagnostics, api.cpp:221-242). Little-endian; widths are fixed. */
+typedef struct dyc_snapshot_header {
+    char magic[8];              /* "DYCSNAP1" */
+    uint32_t version;           /* 1 */
+    uint32_t header_bytes;      /* 256 */
+    uint32_t key_bytes, value_bytes, bucket_bytes, num_subtables;
+    uint32_t max_evictions, auto_resize;
+    uint64_t size;              /* live keys */
+    uint64_t capacity;          /* entry slots */
+    double upper_load, lower_load;
+    uint64_t min_downsize_capacity, initial_size;
+    uint32_t nbuckets[6];       /* per subtable; unused entries 0 */
+    uint64_t payload_bytes;     /* sum of nbuckets[i] * bucket_bytes */
+    uint64_t checksum;          /* sum over the payload's 64-bit words w[i] of
+                                   splitmix64(w[i] ^ i * 0x9E3779B97F4A7C15), mod 2^64 */
+    uint8_t reserved[128];
+} dyc_snapshot_header;
+
+/* Bytes dyc_snapshot writes (header + payload). */
+dyc_status dyc_snapshot_bytes(dyc_table *t, uint64_t *bytes);
+
+/* Write the table into h_buf (at least dyc_snapshot_bytes). Waits for work
+ * queued on `stream`, returns when the buffer is complete. */
+dyc_status dyc_snapshot(dyc_table *t, void *h_buf, uint64_t buf_bytes, void *stream);
+
+/* A new table on `device` from a snapshot. DYC_EINVAL (and no table) when
+ * the header is malformed, the buffer is short or the checksum of the
+ * restored subtables does not match. */
+dyc_status dyc_restore(const void *h_buf, uint64_t buf_bytes, int32_t device, dyc_table **out);
+
 /* ---- Table sets ----------------------------------------------------------
  * Many independent tables (each a dyc_table with its own size, subtables and
  * resizes) whose mixed batches are served together: one launch sequence per

@@ -56,8 +56,8 @@ def unique_u32(n: int, seed: int = 10327) -> np.ndarray:
 
 def unique_u64(n: int, seed: int = 10327) -> np.ndarray:
     """n distinct nonzero 64-bit keys (splitmix64 of a seeded counter)."""
-    x = (np.arange(1, n + 1, dtype=np.uint64) + np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15))
-    with np.errstate(over="ignore"):
+    with np.errstate(over="ignore"):  # wrapping 64-bit arithmetic is intended
+        x = (np.arange(1, n + 1, dtype=np.uint64) + np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15))
         x = x * np.uint64(0x9E3779B97F4A7C15)
         x ^= x >> np.uint64(30)
         x *= np.uint64(0xBF58476D1CE4E5B9)

@@ -94,3 +94,57 @@ def test_four_byte_keys_need_four_byte_values():
     cfg.value_bytes = 8
     h = C.c_void_p()
     assert L.dyc_create(C.byref(cfg), C.byref(h)) == _lib.DYC_EINVAL
+
+
+def test_snapshot_header_layout(tmp_path):
+    prog = tmp_path / "snap.c"
+    prog.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "dycuckoo.h"\n'
+        "int main(void){printf(\"%zu %zu %zu %zu %zu\\n\", sizeof(dyc_snapshot_header),"
+        " offsetof(dyc_snapshot_header, size), offsetof(dyc_snapshot_header, nbuckets),"
+        " offsetof(dyc_snapshot_header, payload_bytes), offsetof(dyc_snapshot_header, checksum));"
+        "return 0;}\n")
+    exe = tmp_path / "snap"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(prog), "-o", str(exe)],
+                   check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert got == [256, 40, 88, 112, 120]
+
+
+def _snap_header(**over):
+    import numpy as np
+    h = np.zeros(256, np.uint8)
+    h[:8] = np.frombuffer(b"DYCSNAP1", np.uint8)
+    u32 = h.view(np.uint32)
+    u64 = h.view(np.uint64)
+    f64 = h.view(np.float64)
+    u32[2], u32[3] = 1, 256
+    u32[4:10] = [4, 4, 128, 4, 64, 1]          # widths, bucket, d, bound, auto
+    u64[5], u64[6] = 0, 4 * 2 * 15             # size, capacity
+    f64[7], f64[8] = 0.8, 0.5
+    u64[9], u64[10] = 0, 1024
+    u32[22:28] = [2, 2, 2, 2, 0, 0]            # nbuckets
+    u64[14] = 4 * 2 * 128                      # payload
+    for k, v in over.items():
+        {"u32": u32, "u64": u64}[k[:3]][int(k[4:])] = v
+    return h
+
+
+def test_restore_rejects_malformed_snapshots_before_any_device_call():
+    import numpy as np
+    L = dg.lib()
+    h = C.c_void_p()
+    good = np.concatenate([_snap_header(), np.zeros(1024, np.uint8)])
+    bad = [np.zeros(100, np.uint8),                                   # shorter than a header
+           np.concatenate([_snap_header(u32_2=2), np.zeros(1024, np.uint8)]),   # version
+           np.concatenate([_snap_header(u32_4=3), np.zeros(1024, np.uint8)]),   # key width
+           np.concatenate([_snap_header(u64_14=999), np.zeros(1024, np.uint8)]),  # payload
+           np.concatenate([_snap_header(u64_5=10 ** 6), np.zeros(1024, np.uint8)]),  # size > slots
+           good[:600]]                                                 # truncated payload
+    for i, b in enumerate(bad):
+        assert L.dyc_restore(b.ctypes.data, b.size, 0, C.byref(h)) == _lib.DYC_EINVAL, i
+        assert not h.value
+    wrong_magic = good.copy()
+    wrong_magic[0] = ord("X")
+    assert L.dyc_restore(wrong_magic.ctypes.data, wrong_magic.size, 0, C.byref(h)) == _lib.DYC_EINVAL
