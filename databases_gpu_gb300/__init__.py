@@ -2,6 +2,8 @@
 pauline-ly/databases_gpu), as sm_103a CUDA kernels behind a C ABI
 (include/dycuckoo.h, libdycuckoo.so)."""
 from ._lib import DycError, lib, library_path  # noqa: F401
-from .table import DyCuckoo, DyCuckooServer, DyCuckooSet, hashAPI, unpack_bits  # noqa: F401
+from .table import (DyCuckoo, DyCuckooServer, DyCuckooSet, DyCuckooWide, hashAPI,  # noqa: F401
+                    unpack_bits)
 
-__all__ = ["DyCuckoo", "hashAPI", "unpack_bits", "DycError", "lib", "library_path"]
+__all__ = ["DyCuckoo", "DyCuckooSet", "DyCuckooServer", "DyCuckooWide", "hashAPI", "unpack_bits",
+           "DycError", "lib", "library_path"]

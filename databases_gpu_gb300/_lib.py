@@ -68,6 +68,8 @@ EXPORTS = [
     "dyc_server_config_default", "dyc_server_create", "dyc_server_destroy", "dyc_server_submit",
     "dyc_server_wait", "dyc_server_stats_get", "dyc_server_set",
     "dyc_snapshot_bytes", "dyc_snapshot", "dyc_restore",
+    "dyc_wide_create", "dyc_wide_destroy", "dyc_wide_insert", "dyc_wide_find", "dyc_wide_erase",
+    "dyc_wide_export", "dyc_wide_table", "dyc_wide_last_stats",
 ]
 
 _lock = threading.Lock()
@@ -116,6 +118,14 @@ def _declare(L):
         "dyc_snapshot_bytes": (st, [T, C.POINTER(u64)]),
         "dyc_snapshot": (st, [T, vp, u64, vp]),
         "dyc_restore": (st, [vp, u64, C.c_int32, C.POINTER(C.c_void_p)]),
+        "dyc_wide_create": (st, [C.POINTER(DycConfig), u32, C.POINTER(C.c_void_p)]),
+        "dyc_wide_destroy": (st, [T]),
+        "dyc_wide_insert": (st, [T, vp, vp, u64, u32, vp]),
+        "dyc_wide_find": (st, [T, vp, vp, vp, u64, vp]),
+        "dyc_wide_erase": (st, [T, vp, u64, vp, vp, C.POINTER(u64), u32, vp]),
+        "dyc_wide_export": (st, [T, vp, vp, u64, C.POINTER(u64), vp]),
+        "dyc_wide_table": (st, [T, C.POINTER(C.c_void_p)]),
+        "dyc_wide_last_stats": (st, [T, C.POINTER(DycOpStats)]),
         "dyc_status_string": (C.c_char_p, [st]),
         "dyc_last_error": (C.c_char_p, []),
     }

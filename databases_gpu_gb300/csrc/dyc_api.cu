@@ -1618,3 +1618,321 @@ dyc_status dyc_restore(const void *h_buf, uint64_t buf_bytes, int32_t device, dy
 }
 
 }  // extern "C"
+
+// =============================================================================
+// Wide-value tables (include/dycuckoo.h dyc_wide_*): an ordinary table maps
+// keys to 32-bit handles, values live in a device heap of fixed-size rows.
+// =============================================================================
+#include "dyc_wide.cuh"
+
+using dyc::WideAlloc;
+
+struct dyc_wide {
+    dyc_table *t = nullptr;  // key -> handle
+    uint32_t vbytes = 0, words = 0;
+    uint32_t *heap = nullptr, *stack = nullptr;
+    WideAlloc *d_alloc = nullptr, *h_alloc = nullptr;
+    uint64_t cap = 0, bump = 0, free_top = 0;  // host mirror of the allocator
+    void *scr = nullptr;
+    size_t scr_bytes = 0;
+    uint64_t scr_n = 0;
+    uint32_t *pre_h = nullptr, *bits = nullptr, *new_h = nullptr;
+    void *new_keys = nullptr;
+    unsigned long long *cnt = nullptr;    // [0] new keys, [1] updates (device)
+    unsigned long long *h_cnt = nullptr;  // pinned copy
+    uint32_t *h_cap = nullptr;            // pinned staging of the heap size
+    dyc_op_stats last{};
+};
+
+namespace {
+
+dyc_status wide_ensure_scratch(dyc_wide *w, uint64_t n) {
+    if (w->scr && w->scr_n >= n) return DYC_OK;
+    const uint64_t m = std::max<uint64_t>(n, 1024);
+    auto al = [](uint64_t x) { return (x + 255) & ~(uint64_t)255; };
+    const uint64_t need = al(m * 4) * 2 + al((m / 32 + 1) * 4) + al(m * w->t->kb) + 256;
+    if (w->scr) {
+        CK(cudaDeviceSynchronize());
+        CK(cudaFree(w->scr));
+        w->scr = nullptr;
+    }
+    CK(cudaMalloc(&w->scr, need));
+    char *p = (char *)w->scr;
+    w->pre_h = (uint32_t *)p;
+    p += al(m * 4);
+    w->new_h = (uint32_t *)p;
+    p += al(m * 4);
+    w->bits = (uint32_t *)p;
+    p += al((m / 32 + 1) * 4);
+    w->new_keys = p;
+    p += al(m * w->t->kb);
+    w->cnt = (unsigned long long *)p;
+    w->scr_bytes = need;
+    w->scr_n = m;
+    return DYC_OK;
+}
+
+// Room for n more handles: grow heap and free stack (stream-ordered).
+dyc_status wide_ensure_heap(dyc_wide *w, uint64_t n, cudaStream_t s) {
+    const uint64_t avail = w->cap - w->bump + w->free_top;
+    if (avail >= n) return DYC_OK;
+    uint64_t nc = std::max<uint64_t>(w->cap * 2, w->cap + (n - avail));
+    if (nc > 0xFFFFFFFFull) nc = 0xFFFFFFFFull;
+    if (nc - w->bump + w->free_top < n) return fail(DYC_ENOMEM, "wide table: more than 2^32 values");
+    uint32_t *heap = nullptr, *stack = nullptr;
+    CK(cudaMallocAsync(&heap, nc * w->vbytes, s));
+    CK(cudaMallocAsync(&stack, nc * 4, s));
+    if (w->heap) {
+        if (w->bump)
+            CK(cudaMemcpyAsync(heap, w->heap, w->bump * w->vbytes, cudaMemcpyDeviceToDevice, s));
+        if (w->free_top)
+            CK(cudaMemcpyAsync(stack, w->stack, w->free_top * 4, cudaMemcpyDeviceToDevice, s));
+        CK(cudaFreeAsync(w->heap, s));
+        CK(cudaFreeAsync(w->stack, s));
+    }
+    w->heap = heap;
+    w->stack = stack;
+    w->cap = nc;
+    *w->h_cap = (uint32_t)nc;
+    CK(cudaMemcpyAsync(&w->d_alloc->cap, w->h_cap, 4, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));  // the pinned staging word is reused by the next growth
+    return DYC_OK;
+}
+
+dyc_status wide_read_alloc(dyc_wide *w, cudaStream_t s) {
+    CK(cudaMemcpyAsync(w->h_alloc, w->d_alloc, sizeof(WideAlloc), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    w->bump = w->h_alloc->bump;
+    w->free_top = w->h_alloc->free_top;
+    return DYC_OK;
+}
+
+unsigned wide_grid(dyc_wide *w, uint64_t n) {
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)w->t->sms * 8));
+}
+
+}  // namespace
+
+extern "C" {
+
+dyc_status dyc_wide_create(const dyc_config *cfg, uint32_t value_bytes, dyc_wide **out) {
+    if (!cfg || !out) return fail(DYC_EINVAL, "null argument");
+    *out = nullptr;
+    if (value_bytes == 0 || value_bytes % 4 || value_bytes > 65536)
+        return fail(DYC_EINVAL, "wide values are 4..65536 bytes, a multiple of 4");
+    dyc_config c = *cfg;
+    c.value_bytes = 4;  // the table stores handles
+    dyc_wide *w = new (std::nothrow) dyc_wide();
+    if (!w) return fail(DYC_ENOMEM, "host allocation");
+    w->vbytes = value_bytes;
+    w->words = value_bytes / 4;
+    dyc_status r = create_impl(&c, nullptr, nullptr, true, &w->t);
+    if (r != DYC_OK) {
+        delete w;
+        return r;
+    }
+    cudaError_t e = cudaMalloc(&w->d_alloc, sizeof(WideAlloc));
+    if (e == cudaSuccess) e = cudaMemset(w->d_alloc, 0, sizeof(WideAlloc));
+    if (e == cudaSuccess) e = cudaMallocHost(&w->h_alloc, sizeof(WideAlloc));
+    if (e == cudaSuccess) e = cudaMallocHost(&w->h_cnt, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMallocHost(&w->h_cap, sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        dyc_wide_destroy(w);
+        return fail(DYC_ENOMEM, "wide table setup: %s", cudaGetErrorString(e));
+    }
+    r = wide_ensure_heap(w, std::max<uint64_t>(1024, std::min<uint64_t>(cfg->initial_size, 1ull << 30)), 0);
+    if (r != DYC_OK) {
+        dyc_wide_destroy(w);
+        return r;
+    }
+    *out = w;
+    return DYC_OK;
+}
+
+dyc_status dyc_wide_destroy(dyc_wide *w) {
+    if (!w) return DYC_OK;
+    if (w->t) {
+        cudaSetDevice(w->t->device);
+        cudaDeviceSynchronize();
+    }
+    if (w->heap) cudaFree(w->heap);
+    if (w->stack) cudaFree(w->stack);
+    if (w->d_alloc) cudaFree(w->d_alloc);
+    if (w->h_alloc) cudaFreeHost(w->h_alloc);
+    if (w->h_cnt) cudaFreeHost(w->h_cnt);
+    if (w->h_cap) cudaFreeHost(w->h_cap);
+    if (w->scr) cudaFree(w->scr);
+    if (w->t) dyc_destroy(w->t);
+    delete w;
+    return DYC_OK;
+}
+
+dyc_status dyc_wide_table(dyc_wide *w, dyc_table **out) {
+    if (!w || !out) return fail(DYC_EINVAL, "null argument");
+    *out = w->t;
+    return DYC_OK;
+}
+
+dyc_status dyc_wide_last_stats(dyc_wide *w, dyc_op_stats *out) {
+    if (!w || !out) return fail(DYC_EINVAL, "null argument");
+    *out = w->last;
+    return DYC_OK;
+}
+
+dyc_status dyc_wide_insert(dyc_wide *w, const void *d_keys, const void *d_vals, uint64_t n,
+                           uint32_t flags, void *stream) {
+    if (!w) return fail(DYC_EINVAL, "null table");
+    if (n == 0) return DYC_OK;
+    if (!d_keys || !d_vals) return fail(DYC_EINVAL, "null key or value array");
+    dyc_table *t = w->t;
+    TRY(set_device(t));
+    cudaStream_t s = (cudaStream_t)stream;
+    w->last = dyc_op_stats{};
+    const uint64_t chunk = t->chunk;
+    const uint64_t m0 = std::min(n, chunk);
+    TRY(ensure_scratch(t, m0));
+    TRY(wide_ensure_scratch(w, m0));
+    for (uint64_t off = 0; off < n; off += chunk) {
+        const uint64_t m = std::min(chunk, n - off);
+        const char *k = (const char *)d_keys + off * t->kb;
+        const uint32_t *v = (const uint32_t *)((const char *)d_vals + off * w->vbytes);
+        // current handles of the chunk's keys
+        cudaError_t e = KB_CALL(t, find, ctx(t, s), t->D, t->sb, k, w->pre_h, 4u, w->bits, m);
+        if (e != cudaSuccess) return fail(DYC_ECUDA, "wide find: %s", cudaGetErrorString(e));
+        const bool use_dedup = !(flags & DYC_FLAG_UNIQUE) && m > 1;
+        if (use_dedup) {
+            CK(cudaMemsetAsync(t->S.dedup, 0, (size_t)t->S.dedup_cap * 8, s));
+            if (t->S.dedup_idx) CK(cudaMemsetAsync(t->S.dedup_idx, 0, (size_t)t->S.dedup_cap * 4, s));
+            e = KB_CALL(t, dedup, ctx(t, s), t->S, k, m, dyc::kKeepLast);
+            if (e != cudaSuccess) return fail(DYC_ECUDA, "dedup kernel: %s", cudaGetErrorString(e));
+        }
+        TRY(wide_ensure_heap(w, m, s));
+        CK(cudaMemsetAsync(w->cnt, 0, 2 * sizeof(unsigned long long), s));
+        const unsigned grid = wide_grid(w, m);
+        if (t->kb == 4)
+            dyc::k_wide_stage<4><<<grid, 256, 0, s>>>(t->S, use_dedup ? 1 : 0, k, v, w->words, m,
+                                                      w->pre_h, w->bits, w->heap, w->stack,
+                                                      w->d_alloc, w->new_keys, w->new_h, w->cnt,
+                                                      w->cnt + 1);
+        else
+            dyc::k_wide_stage<8><<<grid, 256, 0, s>>>(t->S, use_dedup ? 1 : 0, k, v, w->words, m,
+                                                      w->pre_h, w->bits, w->heap, w->stack,
+                                                      w->d_alloc, w->new_keys, w->new_h, w->cnt,
+                                                      w->cnt + 1);
+        dyc::k_wide_commit<<<1, 1, 0, s>>>(w->d_alloc);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(w->h_cnt, w->cnt, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        TRY(wide_read_alloc(w, s));
+        const uint64_t fresh = w->h_cnt[0];
+        w->last.updated += w->h_cnt[1];
+        if (fresh) {
+            if (t->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE)) {
+                int guard = 0;
+                while ((double)(t->size + fresh) > t->cfg.upper_load * (double)t->capacity &&
+                       guard++ < 64)
+                    TRY(resize_up_impl(t, s));
+            }
+            t->last = dyc_op_stats{};
+            TRY(insert_chunk(t, w->new_keys, w->new_h, fresh, DYC_FLAG_UNIQUE | DYC_FLAG_NEW_KEYS, s));
+            w->last.inserted += t->last.inserted;
+            w->last.evict_steps += t->last.evict_steps;
+            w->last.overflowed += t->last.overflowed;
+            w->last.resizes_up += t->last.resizes_up;
+        }
+    }
+    return DYC_OK;
+}
+
+dyc_status dyc_wide_find(dyc_wide *w, const void *d_keys, void *d_vals_out, uint32_t *d_hit_bits,
+                         uint64_t n, void *stream) {
+    if (!w) return fail(DYC_EINVAL, "null table");
+    if (n == 0) return DYC_OK;
+    if (!d_keys || !d_vals_out) return fail(DYC_EINVAL, "null key or value array");
+    dyc_table *t = w->t;
+    TRY(set_device(t));
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint64_t chunk = t->chunk;
+    TRY(wide_ensure_scratch(w, std::min(n, chunk)));
+    for (uint64_t off = 0; off < n; off += chunk) {
+        const uint64_t m = std::min(chunk, n - off);
+        uint32_t *bits = d_hit_bits ? d_hit_bits + off / 32 : w->bits;
+        cudaError_t e = KB_CALL(t, find, ctx(t, s), t->D, t->sb, (const char *)d_keys + off * t->kb,
+                                w->pre_h, 4u, bits, m);
+        if (e != cudaSuccess) return fail(DYC_ECUDA, "wide find: %s", cudaGetErrorString(e));
+        dyc::k_wide_gather<<<wide_grid(w, m), 256, 0, s>>>(
+            w->pre_h, bits, m, w->heap, w->words,
+            (uint32_t *)((char *)d_vals_out + off * w->vbytes));
+        CK(cudaGetLastError());
+    }
+    return DYC_OK;
+}
+
+dyc_status dyc_wide_erase(dyc_wide *w, const void *d_keys, uint64_t n, void *d_vals_out,
+                          uint32_t *d_erased_bits, uint64_t *h_erased_count, uint32_t flags,
+                          void *stream) {
+    if (!w) return fail(DYC_EINVAL, "null table");
+    if (h_erased_count) *h_erased_count = 0;
+    if (n == 0) return DYC_OK;
+    if (!d_keys) return fail(DYC_EINVAL, "null key array");
+    dyc_table *t = w->t;
+    TRY(set_device(t));
+    cudaStream_t s = (cudaStream_t)stream;
+    w->last = dyc_op_stats{};
+    const uint64_t chunk = t->chunk;
+    TRY(wide_ensure_scratch(w, std::min(n, chunk)));
+    uint64_t total = 0;
+    for (uint64_t off = 0; off < n; off += chunk) {
+        const uint64_t m = std::min(chunk, n - off);
+        const char *k = (const char *)d_keys + off * t->kb;
+        // handles before the erase
+        cudaError_t e = KB_CALL(t, find, ctx(t, s), t->D, t->sb, k, w->pre_h, 4u, w->bits, m);
+        if (e != cudaSuccess) return fail(DYC_ECUDA, "wide find: %s", cudaGetErrorString(e));
+        uint32_t *eb = d_erased_bits ? d_erased_bits + off / 32 : w->bits;
+        uint64_t cnt = 0;
+        // no downsize inside: the erased bits and handles are read below
+        TRY(dyc_erase(t, k, m, eb, &cnt, flags | DYC_FLAG_NO_RESIZE, s));
+        total += cnt;
+        dyc::k_wide_free<<<wide_grid(w, m), 256, 0, s>>>(
+            w->pre_h, eb, m, w->heap, w->words,
+            d_vals_out ? (uint32_t *)((char *)d_vals_out + off * w->vbytes) : nullptr, w->stack,
+            w->d_alloc);
+        dyc::k_wide_commit_free<<<1, 1, 0, s>>>(w->d_alloc);
+        CK(cudaGetLastError());
+        TRY(wide_read_alloc(w, s));
+    }
+    w->last.erased = total;
+    if (h_erased_count) *h_erased_count = total;
+    // downsize after the batch (api.cpp:494-505); handles move with their keys
+    if (t->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE) &&
+        (double)t->size < t->cfg.lower_load * (double)t->capacity &&
+        t->capacity > t->cfg.min_downsize_capacity) {
+        t->last = dyc_op_stats{};
+        dyc_status st = resize_down_impl(t, s);
+        if (st != DYC_OK && st != DYC_EINVAL) return st;
+        w->last.resizes_down += t->last.resizes_down;
+        w->last.resizes_up += t->last.resizes_up;
+    }
+    return DYC_OK;
+}
+
+dyc_status dyc_wide_export(dyc_wide *w, void *d_keys_out, void *d_vals_out, uint64_t capacity,
+                           uint64_t *n_out, void *stream) {
+    if (!w) return fail(DYC_EINVAL, "null table");
+    dyc_table *t = w->t;
+    cudaStream_t s = (cudaStream_t)stream;
+    TRY(set_device(t));
+    TRY(wide_ensure_scratch(w, std::max<uint64_t>(capacity, 1)));
+    uint64_t got = 0;
+    TRY(dyc_export(t, d_keys_out, w->pre_h, capacity, &got, stream));
+    if (n_out) *n_out = got;
+    const uint64_t m = std::min(got, capacity);
+    if (m && d_vals_out) {
+        dyc::k_wide_gather<<<wide_grid(w, m), 256, 0, s>>>(w->pre_h, nullptr, m, w->heap, w->words,
+                                                           (uint32_t *)d_vals_out);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(s));
+    }
+    return DYC_OK;
+}
+
+}  // extern "C"

@@ -98,7 +98,7 @@ class DyCuckoo:
         t.key_bytes = cfg.key_bytes
         t.value_bytes = cfg.value_bytes
         t.device = cfg.device
-        t._owner = owner  # keeps the set alive
+        t._owner = owner  # keeps the owner (set, server, wide table) alive
         return t
 
     # -- lifetime
@@ -431,6 +431,110 @@ class DyCuckooSet:
                  _ptr(bits, "bits", 4), flags, _stream_ptr(stream)),
               "dyc_set_apply_each" if each else "dyc_set_apply")
         return out, bits
+
+
+class DyCuckooWide:
+    """Table with values of value_bytes (a multiple of 4) per key (dyc_wide_*).
+    Keys: CUDA tensor of int32/int64; values: CUDA tensor of n * value_bytes
+    bytes, e.g. shape (n, value_bytes // 4) int32."""
+
+    def __init__(self, size: int, value_bytes: int, key_bytes: int = 4, num_subtables: int = 4,
+                 bucket_bytes: int = 128, max_evictions: int = 64, auto_resize: bool = True,
+                 upper_load: float = UPPER_BOUND, lower_load: float = LOWER_BOUND,
+                 min_downsize_capacity: int = MIN_DOWNSIZE_CAPACITY, device: int = 0):
+        L = _lib.lib()
+        cfg = _lib.DycConfig()
+        L.dyc_config_default(C.byref(cfg))
+        cfg.key_bytes, cfg.value_bytes = key_bytes, 4
+        cfg.num_subtables, cfg.bucket_bytes = num_subtables, bucket_bytes
+        cfg.max_evictions, cfg.auto_resize = max_evictions, 1 if auto_resize else 0
+        cfg.initial_size = int(size)
+        cfg.upper_load, cfg.lower_load = upper_load, lower_load
+        cfg.min_downsize_capacity = int(min_downsize_capacity)
+        cfg.device = device
+        h = C.c_void_p()
+        check(L.dyc_wide_create(C.byref(cfg), value_bytes, C.byref(h)), "dyc_wide_create")
+        self._h, self.L, self.cfg = h, L, cfg
+        self.key_bytes, self.value_bytes, self.device = key_bytes, value_bytes, device
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.L.dyc_wide_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _vals(self, v, n, what):
+        if v.numel() * v.element_size() != n * self.value_bytes:
+            raise ValueError("%s must hold %d bytes per key" % (what, self.value_bytes))
+        return _ptr(v, what)
+
+    def insert(self, keys, values, unique: bool = False, no_resize: bool = False, stream=None):
+        n = keys.numel()
+        flags = (FLAG_UNIQUE if unique else 0) | (FLAG_NO_RESIZE if no_resize else 0)
+        check(self.L.dyc_wide_insert(self._h, _ptr(keys, "keys", self.key_bytes),
+                                     self._vals(values, n, "values"), n, flags,
+                                     _stream_ptr(stream)), "dyc_wide_insert")
+        return self.stats()
+
+    def find(self, keys, stream=None):
+        torch = _torch()
+        n = keys.numel()
+        out = torch.empty((n, self.value_bytes // 4), dtype=torch.int32, device=keys.device)
+        bits = torch.empty((n + 31) // 32, dtype=torch.int32, device=keys.device)
+        check(self.L.dyc_wide_find(self._h, _ptr(keys, "keys", self.key_bytes), _ptr(out, "out"),
+                                   _ptr(bits, "bits", 4), n, _stream_ptr(stream)), "dyc_wide_find")
+        return out, bits
+
+    def erase(self, keys, no_resize: bool = False, stream=None):
+        """(count removed, removed values (zeros where nothing was removed), erased bits)"""
+        torch = _torch()
+        n = keys.numel()
+        out = torch.empty((n, self.value_bytes // 4), dtype=torch.int32, device=keys.device)
+        bits = torch.empty((n + 31) // 32, dtype=torch.int32, device=keys.device)
+        cnt = C.c_uint64()
+        check(self.L.dyc_wide_erase(self._h, _ptr(keys, "keys", self.key_bytes), n,
+                                    _ptr(out, "out"), _ptr(bits, "bits", 4), C.byref(cnt),
+                                    FLAG_NO_RESIZE if no_resize else 0, _stream_ptr(stream)),
+              "dyc_wide_erase")
+        return int(cnt.value), out, bits
+
+    def table(self) -> DyCuckoo:
+        h = C.c_void_p()
+        check(self.L.dyc_wide_table(self._h, C.byref(h)), "dyc_wide_table")
+        cfg = _lib.DycConfig()
+        C.memmove(C.byref(cfg), C.byref(self.cfg), C.sizeof(cfg))
+        return DyCuckoo._member(h, cfg, self)
+
+    @property
+    def size(self) -> int:
+        return self.table().size
+
+    def stats(self) -> dict:
+        st = _lib.DycOpStats()
+        check(self.L.dyc_wide_last_stats(self._h, C.byref(st)), "dyc_wide_last_stats")
+        return st.as_dict()
+
+    def export(self, stream=None):
+        """(keys, values (n, value_bytes // 4) int32) of every live entry, sorted by key."""
+        torch = _torch()
+        n = self.size
+        cap = max(n, 1)
+        dev = "cuda:%d" % self.device
+        k = torch.empty(cap, dtype=torch.int32 if self.key_bytes == 4 else torch.int64, device=dev)
+        v = torch.empty((cap, self.value_bytes // 4), dtype=torch.int32, device=dev)
+        got = C.c_uint64()
+        check(self.L.dyc_wide_export(self._h, _ptr(k, "keys"), _ptr(v, "vals"), cap,
+                                     C.byref(got), _stream_ptr(stream)), "dyc_wide_export")
+        m = int(got.value)
+        k, v = k[:m], v[:m]
+        kk = k.cpu().numpy().view(np.uint32 if self.key_bytes == 4 else np.uint64)
+        order = torch.from_numpy(np.argsort(kk, kind="stable")).to(k.device)
+        return k[order], v[order]
 
 
 class DyCuckooServer:

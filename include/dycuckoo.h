@@ -197,6 +197,43 @@ dyc_status dyc_apply(dyc_table *t, const uint8_t *d_ops, const void *d_keys, con
                      uint64_t n, void *d_vals_out, uint32_t *d_bits_out, uint32_t flags,
                      void *stream);
 
+/* ---- Wide values -----------------------------------------------------------
+ * Tables whose values are value_bytes long (any multiple of 4 up to 65536),
+ * the counterpart of the reference's lock-based variant for values wider
+ * than a slot (GPU/warp: key[]/value[] buckets, cuckoo.h:15-18, bucket locks
+ * cuckoo.cu:95-101, delete returning the value :353-359). Here the cuckoo
+ * table maps each key to a 32-bit handle, a row of a device value heap; a
+ * batch is deduplicated before it touches the table, so every key has one
+ * writer and no lock is needed, and evictions and resizes move the (key,
+ * handle) slot, never the value. A find costs one more random access (the
+ * heap row). Semantics are those of the plain table: upsert, last insert of
+ * a key in a batch wins, first erase removes; erase hands back the removed
+ * values. Arrays of values are dense, value_bytes per key. */
+typedef struct dyc_wide dyc_wide;
+
+/* cfg as for dyc_create (its value_bytes is ignored: the table holds
+ * handles); the heap starts with room for cfg->initial_size values and
+ * doubles when needed. */
+dyc_status dyc_wide_create(const dyc_config *cfg, uint32_t value_bytes, dyc_wide **out);
+dyc_status dyc_wide_destroy(dyc_wide *w);
+/* Returns after the batch is in the table. */
+dyc_status dyc_wide_insert(dyc_wide *w, const void *d_keys, const void *d_vals, uint64_t n,
+                           uint32_t flags, void *stream);
+/* Values of hits, zeros for misses; d_hit_bits optional. Asynchronous. */
+dyc_status dyc_wide_find(dyc_wide *w, const void *d_keys, void *d_vals_out, uint32_t *d_hit_bits,
+                         uint64_t n, void *stream);
+/* d_vals_out (optional): the removed value for each op that removed its key,
+ * zeros for the others. Returns after the erase is complete. */
+dyc_status dyc_wide_erase(dyc_wide *w, const void *d_keys, uint64_t n, void *d_vals_out,
+                          uint32_t *d_erased_bits, uint64_t *h_erased_count, uint32_t flags,
+                          void *stream);
+/* Every live (key, value), at most `capacity`; *n_out = live entries. */
+dyc_status dyc_wide_export(dyc_wide *w, void *d_keys_out, void *d_vals_out, uint64_t capacity,
+                           uint64_t *n_out, void *stream);
+/* The key -> handle table (for its size, capacity and layout). */
+dyc_status dyc_wide_table(dyc_wide *w, dyc_table **out);
+dyc_status dyc_wide_last_stats(dyc_wide *w, dyc_op_stats *out);
+
 /* ---- Snapshot / restore ----------------------------------------------------
  * A snapshot is a host buffer: this 256-byte header, then every subtable's
  * buckets in subtable order, byte for byte as they are in device memory (the
