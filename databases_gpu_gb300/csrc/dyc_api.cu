@@ -759,15 +759,16 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
     const uint64_t blocks = (ops + dyc::kSortTile - 1) / dyc::kSortTile;
     const bool multi = ntables > 0;
     const size_t K = (size_t)kb, V = (size_t)vb;
+    const size_t CB = kb == 4 ? 8 : 16;  // cell bytes
     const size_t sizes[] = {
-        cells * K, cells * 4, cells * 4,              // cell_key, cell_cnt, cell_did
-        ops * 4, ops * K, ops * 4, ops * 4, ops * 4,  // op_cell, dkey, dcnt, doff, dfill
+        cells * CB,                                   // cells
+        ops * 4, ops * K, ops * 4, ops * 8,           // op_cell, dkey, dcnt, dseg
         ops * 4, ops * V, (ops / 32 + 1) * 4,         // seg, pre_val, pre_hit
         ops * K, ops * V, ops * K,                    // up_key, up_val, er_key
-        dyc::kCtrSlots * 8, ops * 4, ops * 4,         // ctr, mid, giant
+        dyc::kCtrSlots * 8, ops * 4, ops * 4, ops * 4,  // ctr, wseg, mid, giant
         ops * 4, ops * 4, ops * 4, ops * 4,           // sort buffers
         blocks * 256 * 4, ops * 4,                    // hist, seg_start
-        multi ? cells * 4 : 0, multi ? ops * 4 : 0,   // cell_tid, dtid
+        multi ? ops * 4 : 0,                          // dtid
         multi ? ops * 4 : 0, multi ? ops * 4 : 0,     // up_tid, er_tid
         multi ? (size_t)ntables * 4 : 0,              // tnew
         multi ? ((size_t)ntables + 1) * 4 : 0};       // tcell_off
@@ -790,14 +791,11 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
         return (void *)r;
     };
     dyc::ApplyScratch A{};
-    A.cell_key = carve();
-    A.cell_cnt = (uint32_t *)carve();
-    A.cell_did = (uint32_t *)carve();
+    A.cells = carve();
     A.op_cell = (uint32_t *)carve();
     A.dkey = carve();
     A.dcnt = (uint32_t *)carve();
-    A.doff = (uint32_t *)carve();
-    A.dfill = (uint32_t *)carve();
+    A.dseg = (unsigned long long *)carve();
     A.seg = (uint32_t *)carve();
     A.pre_val = carve();
     A.pre_hit = (uint32_t *)carve();
@@ -805,6 +803,7 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
     A.up_val = carve();
     A.er_key = carve();
     A.ctr = (unsigned long long *)carve();
+    A.wseg = (uint32_t *)carve();
     A.mid = (uint32_t *)carve();
     A.giant = (uint32_t *)carve();
     A.sort_key = (uint32_t *)carve();
@@ -813,7 +812,6 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
     A.sort_val2 = (uint32_t *)carve();
     A.hist = (uint32_t *)carve();
     A.seg_start = (uint32_t *)carve();
-    A.cell_tid = (uint32_t *)carve();
     A.dtid = (uint32_t *)carve();
     A.up_tid = (uint32_t *)carve();
     A.er_tid = (uint32_t *)carve();
@@ -828,11 +826,10 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
 
 // Mixed-batch scratch of a single table for `n` ops per chunk (grow only).
 dyc_status ensure_apply(dyc_table *t, uint64_t n) {
-    const uint64_t ops = n < 128 ? 128 : n;  // cap_cells >= 256: whole blocks
+    const uint64_t ops = n < 128 ? 128 : n;
     if (t->apply_buf && t->A.cap_ops >= ops) return DYC_OK;
     if (!t->h_actr) CK(cudaMallocHost(&t->h_actr, dyc::kCtrSlots * sizeof(unsigned long long)));
-    return carve_apply(t->kb, t->vb, ops, next_pow2(2 * ops), 0, &t->apply_buf, &t->apply_bytes,
-                       &t->A);
+    return carve_apply(t->kb, t->vb, ops, 2 * ops, 0, &t->apply_buf, &t->apply_bytes, &t->A);
 }
 
 dyc_status read_apply_counters(dyc_table *t, cudaStream_t s) {
@@ -848,8 +845,7 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     const dyc::ApplyScratch &A = t->A;
     const LaunchCtx L = ctx(t, s);
     const uint32_t vb = (uint32_t)t->vb;
-    CK(cudaMemsetAsync(A.cell_key, 0, (size_t)A.cap_cells * t->kb, s));
-    CK(cudaMemsetAsync(A.cell_cnt, 0, (size_t)A.cap_cells * 4, s));
+    CK(cudaMemsetAsync(A.cells, 0, (size_t)(2 * n) * (t->kb == 4 ? 8 : 16), s));  // 2n cells used
     CK(cudaMemsetAsync(A.ctr, 0, dyc::kCtrSlots * sizeof(unsigned long long), s));
     if (bits_out) CK(cudaMemsetAsync(bits_out, 0, (size_t)((n + 31) / 32) * 4, s));
     cudaError_t e = KB_CALL(t, apply_group, L, A, keys, n);
@@ -1066,7 +1062,7 @@ dyc_status set_ensure_scratch(dyc_set *s, uint64_t n) {
     const uint64_t ops = n < 128 ? 128 : n;
     if (s->abuf && s->A.cap_ops >= ops) return DYC_OK;
     set_drop_graphs(s);
-    TRY(carve_apply(s->kb, s->vb, ops, 4 * ops, s->ntables, &s->abuf, &s->abytes, &s->A));
+    TRY(carve_apply(s->kb, s->vb, ops, 2 * ops, s->ntables, &s->abuf, &s->abytes, &s->A));
     const size_t slot = s->kb == 4 ? 8 : 16;
     const size_t lb = ((ops * slot + 255) & ~(size_t)255) * 2 + ((ops * 4 + 255) & ~(size_t)255) * 2;
     if (s->lbuf) {

@@ -6,19 +6,20 @@
 //
 // Steps (stream-ordered kernels):
 //   group   : each op claims its key's cell in an open-addressing scratch
-//             table and counts the cell (atomics in L2); for a batch over
-//             many tables every table has its own region of cells
-//   compact : each used cell gets a distinct-key id, a segment of the op
-//             index array and the key itself
+//             table, a {key, count} word updated by one atomic for a new key;
+//             for a batch over many tables every table has its own region of
+//             twice its ops in cells
+//   compact : each used cell gets a distinct-key id (written over its count),
+//             a segment of the op index array and the key itself
 //   scatter : op indices land in their key's segment (in no order)
 //   (the table's own find kernel reads the pre-batch state of every
 //    distinct key)
-//   replay  : one thread per distinct key sorts a short segment (at most
-//             kShortSeg ops) by op index and replays it, writing every op's
-//             result and the key's final state; keys whose state changed are
-//             listed as erases or upserts. Mid segments (up to kMidSeg ops)
-//             are sorted in shared memory by one block and replayed by a
-//             warp; giant ones go through a stable radix sort of the batch.
+//   replay  : one thread per distinct key replays a segment of at most
+//             kShortSeg ops after sorting it in registers; longer segments are
+//             sorted in shared memory and replayed by a warp (up to kWarpSeg
+//             ops) or by one block (up to kMidSeg), giant ones after a stable
+//             radix sort of the batch. Every op's result is written; keys
+//             whose state changed are listed as erases or upserts.
 //   (the table's erase and insert kernels apply the lists)
 // Only the lists touch the table, each key at most once, so the usual
 // insert/erase phases keep their guarantees. Counts the kernels need are read
@@ -31,47 +32,80 @@ namespace dyc {
 
 enum : uint8_t { kOpFind = 0, kOpInsert = 1, kOpErase = 2 };
 
-constexpr uint32_t kShortSeg = 64;   // segments replayed by one thread
+constexpr uint32_t kShortSeg = 8;    // segments replayed by one thread
+constexpr uint32_t kWarpSeg = 256;   // segments sorted and replayed by one warp
 constexpr uint32_t kMidSeg = 4096;   // segments sorted in shared memory by one block
 constexpr uint32_t kNoCell = 0xffffffffu;
 
-__device__ __forceinline__ uint64_t cell_hash(uint64_t k) {
+// Cells: 4-byte keys {key (low word), count (high word)} in one 64-bit word;
+// 8-byte keys {key, count, pad} in 16 bytes. After compaction the count
+// field holds the distinct-key id.
+template <int KB> __host__ __device__ constexpr int cell_bytes() { return KB == 4 ? 8 : 16; }
+
+__device__ __forceinline__ uint32_t cell_hash(uint64_t k) {
     return mix32(fold(k) ^ (uint32_t)(k >> 32));
 }
 
 template <int KB>
-__device__ __forceinline__ uint32_t claim_cell(typename SlotT<KB>::K *ck, uint64_t base,
-                                               uint64_t mask, typename SlotT<KB>::K k) {
-    using K = typename SlotT<KB>::K;
-    uint64_t h = cell_hash((uint64_t)k) & mask;
-    for (uint64_t probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
-        K old;
-        if (KB == 4) old = (K)atomicCAS((unsigned *)&ck[base + h], 0u, (unsigned)k);
-        else old = (K)atomicCAS((unsigned long long *)&ck[base + h], 0ull, (unsigned long long)k);
-        if (old == 0 || old == k) return (uint32_t)(base + h);
-    }
-    return kNoCell;  // unreachable: a region has at least twice as many cells as ops
+__device__ __forceinline__ typename SlotT<KB>::K cell_key(const void *cells, uint64_t c) {
+    if constexpr (KB == 4) return (uint32_t)((const unsigned long long *)cells)[c];
+    else return *(const unsigned long long *)((const char *)cells + c * 16);
+}
+template <int KB> __device__ __forceinline__ uint32_t *cell_word(void *cells, uint64_t c) {
+    if constexpr (KB == 4) return (uint32_t *)cells + 2 * c + 1;
+    else return (uint32_t *)((char *)cells + c * 16 + 8);
 }
 
+// Claim (or join) key k's cell in region [base, base + size): fastrange
+// start, linear probing. One 64-bit CAS claims a new 4-byte key with count 1.
+// (L2 atomic throughput bounds the grouping kernels; keeping several first
+// probes of a thread in flight measured slower.)
+template <int KB>
+__device__ __forceinline__ uint32_t claim_cell(void *cells, uint64_t base, uint64_t size,
+                                               typename SlotT<KB>::K k) {
+    uint64_t idx = ((uint64_t)cell_hash((uint64_t)k) * size) >> 32;
+    for (uint64_t probe = 0; probe < size; ++probe) {
+        const uint64_t c = base + idx;
+        if constexpr (KB == 4) {
+            unsigned long long *p = (unsigned long long *)cells + c;
+            const unsigned long long old =
+                atomicCAS(p, 0ull, (unsigned long long)k | (1ull << 32));
+            if (old == 0ull) return (uint32_t)c;
+            if ((uint32_t)old == k) {
+                atomicAdd(p, 1ull << 32);
+                return (uint32_t)c;
+            }
+        } else {
+            unsigned long long *p = (unsigned long long *)((char *)cells + c * 16);
+            const unsigned long long old = atomicCAS(p, 0ull, (unsigned long long)k);
+            if (old == 0ull || old == k) {
+                atomicAdd((unsigned *)(p + 1), 1u);
+                return (uint32_t)c;
+            }
+        }
+        idx = idx + 1 == size ? 0 : idx + 1;
+    }
+    return kNoCell;  // unreachable: a region has twice as many cells as ops
+}
+
+// One table: cells [0, 2n).
 template <int KB>
 __global__ void __launch_bounds__(256) k_apply_group(const __grid_constant__ ApplyScratch A,
                                                      const void *__restrict__ keys, uint64_t n) {
     using K = typename SlotT<KB>::K;
-    K *ck = (K *)A.cell_key;
+    const uint64_t size = 2 * n;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const K k = load_key<KB>(keys, i);
-        const uint32_t cell = k == 0 ? kNoCell : claim_cell<KB>(ck, 0, A.cap_cells - 1, k);
-        A.op_cell[i] = cell;  // key 0: a miss / rejected op, no cell
-        if (cell != kNoCell) atomicAdd(&A.cell_cnt[cell], 1u);
+        A.op_cell[i] = k == 0 ? kNoCell : claim_cell<KB>(A.cells, 0, size, k);  // key 0: no cell
     }
 }
 
-// Many tables: ops of table t are [off[t], off[t+1]); its cells are
-// [tcell_off[t], tcell_off[t+1]), a power of two at least twice its ops.
+// Largest t < ntables with off[t] <= i (for cell offsets: the table owning
+// cell i, since a table without cells shares its offset with the next one).
 __device__ __forceinline__ uint32_t table_of(const uint32_t *__restrict__ off, uint32_t ntables,
                                              uint32_t i) {
-    uint32_t lo = 0, hi = ntables;  // largest t with off[t] <= i
+    uint32_t lo = 0, hi = ntables;
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
         if (__ldg(off + mid) <= i) lo = mid;
@@ -80,31 +114,35 @@ __device__ __forceinline__ uint32_t table_of(const uint32_t *__restrict__ off, u
     return lo;
 }
 
+// Many tables: ops of table t are [off[t], off[t+1]); its cells are
+// [tcell_off[t], tcell_off[t+1]), twice its ops.
 template <int KB>
 __global__ void __launch_bounds__(256) k_set_group(const __grid_constant__ ApplyScratch A,
                                                    const uint32_t *__restrict__ off,
                                                    const void *__restrict__ keys, uint64_t n) {
     using K = typename SlotT<KB>::K;
-    K *ck = (K *)A.cell_key;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    // warp-uniform loop: a warp's 32 consecutive ops mostly belong to one
+    // table, found by one search when the first and last lane's tables agree
+    for (uint64_t base = warp_base(); base < n; base += warp_stride()) {
+        const uint64_t i = base + (threadIdx.x & 31);
+        const uint64_t last = base + 31 < n ? base + 31 : n - 1;
+        const uint32_t t0 = table_of(off, A.ntables, (uint32_t)base);
+        const bool one = t0 == A.ntables - 1 || __ldg(off + t0 + 1) > (uint32_t)last;
+        if (i >= n) continue;
         const K k = load_key<KB>(keys, i);
         uint32_t cell = kNoCell;
         if (k != 0) {
-            const uint32_t t = table_of(off, A.ntables, (uint32_t)i);
+            const uint32_t t = one ? t0 : table_of(off, A.ntables, (uint32_t)i);
             const uint32_t c0 = A.tcell_off[t], c1 = A.tcell_off[t + 1];
-            cell = claim_cell<KB>(ck, c0, (uint64_t)(c1 - c0) - 1, k);
-            A.cell_tid[cell] = t;
+            cell = claim_cell<KB>(A.cells, c0, c1 - c0, k);
         }
         A.op_cell[i] = cell;
-        if (cell != kNoCell) atomicAdd(&A.cell_cnt[cell], 1u);
     }
 }
 
-// Cell regions: next_pow2(2 * ops of table t) cells each (none for a table
-// without ops); exclusive scan into tcell_off, total in tcell_off[ntables].
-// One block of 1024 threads. (A template only so that each key width's
-// translation unit has its own copy.)
+// Cell regions: 2 * (ops of table t) cells each; exclusive scan into
+// tcell_off, total in tcell_off[ntables]. One block of 1024 threads. (A
+// template only so that each key width's translation unit has its own copy.)
 template <int KB>
 __global__ void __launch_bounds__(1024) k_set_cells(const __grid_constant__ ApplyScratch A,
                                                     const uint32_t *__restrict__ off) {
@@ -112,15 +150,8 @@ __global__ void __launch_bounds__(1024) k_set_cells(const __grid_constant__ Appl
     const uint32_t m = A.ntables;
     const uint32_t per = (m + 1023) / 1024;
     const uint32_t lo = per * threadIdx.x, hi = lo + per < m ? lo + per : m;
-    auto cells = [&](uint32_t t) {
-        const uint32_t c = off[t + 1] - off[t];
-        if (!c) return 0u;
-        uint32_t p = 2;
-        while (p < 2 * c) p <<= 1;
-        return p;
-    };
     uint32_t sum = 0u;
-    for (uint32_t t = lo; t < hi; ++t) sum += cells(t);
+    for (uint32_t t = lo; t < hi; ++t) sum += 2u * (off[t + 1] - off[t]);
     part[threadIdx.x] = sum;
     __syncthreads();
     for (int o = 1; o < 1024; o <<= 1) {
@@ -132,7 +163,7 @@ __global__ void __launch_bounds__(1024) k_set_cells(const __grid_constant__ Appl
     uint32_t run = part[threadIdx.x] - sum;
     for (uint32_t t = lo; t < hi; ++t) {
         A.tcell_off[t] = run;
-        run += cells(t);
+        run += 2u * (off[t + 1] - off[t]);
     }
     if (threadIdx.x == 1023) A.tcell_off[m] = part[1023];
 }
@@ -140,48 +171,56 @@ __global__ void __launch_bounds__(1024) k_set_cells(const __grid_constant__ Appl
 // Zero the cells in use (tcell_off[ntables] of them) and the per-table counts.
 template <int KB>
 __global__ void __launch_bounds__(256) k_set_clear(const __grid_constant__ ApplyScratch A) {
-    using K = typename SlotT<KB>::K;
-    const uint64_t nc = A.tcell_off[A.ntables];
+    const uint64_t words = (uint64_t)A.tcell_off[A.ntables] * (cell_bytes<KB>() / 8);
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += stride) {
-        ((K *)A.cell_key)[c] = 0;
-        A.cell_cnt[c] = 0u;
-    }
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < words; c += stride)
+        ((unsigned long long *)A.cells)[c] = 0ull;
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < A.ntables; t += stride)
         A.tnew[t] = 0u;
 }
 
-// Block-wide allocation from a shared counter: thread gets base + the sum of
-// x over the threads before it in the block; one atomic per block (the same
-// address taken once per warp serialised these kernels). Every thread of the
-// block must call it at the same point.
-__device__ __forceinline__ uint32_t block_alloc(unsigned long long *ctr, uint32_t x) {
-    __shared__ uint32_t wsum[32];
-    __shared__ unsigned long long bbase;
+// Block-wide exclusive allocation of F counters at once: x packs F fields of
+// B bits (no field's block total may exceed B bits); one scan, one atomic per
+// nonzero field total, out[f] = that counter's base + the field's sum over
+// the threads before this one. Every thread of the block must call it at the
+// same point.
+template <int F, int B>
+__device__ __forceinline__ void block_alloc(unsigned long long *ctr, const int (&slot)[F],
+                                            unsigned long long x, uint32_t (&out)[F]) {
+    __shared__ unsigned long long wsum[32];
+    __shared__ unsigned long long bbase[F];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    uint32_t incl = x;
+    const unsigned long long mask = B == 64 ? ~0ull : ((1ull << B) - 1ull);
+    unsigned long long incl = x;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(kFull, incl, o);
+        const unsigned long long y = __shfl_up_sync(kFull, incl, o);
         if (lane >= o) incl += y;
     }
     if (lane == 31) wsum[w] = incl;
     __syncthreads();
     if (w == 0) {
-        const uint32_t v = lane < nw ? wsum[lane] : 0u;
-        uint32_t vi = v;
+        const unsigned long long v = lane < nw ? wsum[lane] : 0ull;
+        unsigned long long vi = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(kFull, vi, o);
+            const unsigned long long y = __shfl_up_sync(kFull, vi, o);
             if (lane >= o) vi += y;
         }
         if (lane < nw) wsum[lane] = vi - v;
-        if (lane == 31) bbase = vi ? atomicAdd(ctr, (unsigned long long)vi) : 0ull;
+        if (lane == 31) {
+#pragma unroll
+            for (int f = 0; f < F; ++f) {
+                const unsigned long long tot = (vi >> (f * B)) & mask;
+                bbase[f] = tot ? atomicAdd(&ctr[slot[f]], tot) : 0ull;
+            }
+        }
     }
     __syncthreads();
-    const uint32_t r = (uint32_t)bbase + wsum[w] + incl - x;
+    const unsigned long long ex = wsum[w] + incl - x;
+#pragma unroll
+    for (int f = 0; f < F; ++f) out[f] = (uint32_t)(bbase[f] + ((ex >> (f * B)) & mask));
     __syncthreads();  // wsum / bbase are reused by the next call
-    return r;
 }
 
 // Add 1 to cnt[t] for every lane with pred, one atomic per distinct t in the
@@ -192,27 +231,72 @@ __device__ __forceinline__ void warp_count_by(uint32_t *cnt, uint32_t t, bool pr
     if (pred && (__ffs(peers) - 1) == lane) atomicAdd(&cnt[t], (uint32_t)__popc(peers));
 }
 
-// Compaction of the cells in use: cap_cells for one table, tcell_off[ntables]
-// for many. Whole blocks step through the cells so every thread reaches each
-// block_alloc.
+// Compaction of the cells in use: nc for one table, tcell_off[ntables] for
+// many (nc = 0). A block takes a tile of 256 * kCompactRun cells; in step k
+// its threads read cells k * 256 + threadIdx.x of the tile (coalesced), so
+// ids and segment offsets come out in cell order from per-(step, warp)
+// ballots and one shared-memory scan per tile.
+constexpr int kCompactRun = 4;
+
 template <int KB>
-__global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ ApplyScratch A) {
-    using K = typename SlotT<KB>::K;
-    const K *ck = (const K *)A.cell_key;
-    const uint64_t nc = A.tcell_off ? (uint64_t)A.tcell_off[A.ntables] : A.cap_cells;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t c0 = (uint64_t)blockIdx.x * blockDim.x; c0 < nc; c0 += stride) {
-        const uint64_t c = c0 + threadIdx.x;
-        const uint32_t cnt = c < nc ? A.cell_cnt[c] : 0u;
-        const uint32_t d = block_alloc(&A.ctr[kCtrDistinct], cnt ? 1u : 0u);
-        const uint32_t off = block_alloc(&A.ctr[kCtrPlaced], cnt);
-        if (!cnt) continue;
-        A.cell_did[c] = d;
-        ((K *)A.dkey)[d] = ck[c];
-        A.dcnt[d] = cnt;
-        A.doff[d] = off;
-        A.dfill[d] = 0u;
-        if (A.dtid) A.dtid[d] = A.cell_tid[c];
+__global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ ApplyScratch A,
+                                                       uint64_t nc) {
+    __shared__ unsigned long long part[kCompactRun * kWarpsPerBlock];  // ops << 32 | keys
+    __shared__ unsigned long long base_keys, base_ops;
+    if (A.tcell_off) nc = A.tcell_off[A.ntables];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint64_t tile = (uint64_t)blockDim.x * kCompactRun;
+    const uint64_t stride = (uint64_t)gridDim.x * tile;
+    for (uint64_t c0 = (uint64_t)blockIdx.x * tile; c0 < nc; c0 += stride) {
+        uint32_t cnt[kCompactRun], ex_ops[kCompactRun], ex_keys[kCompactRun];
+#pragma unroll
+        for (int k = 0; k < kCompactRun; ++k) {
+            const uint64_t c = c0 + (uint64_t)k * blockDim.x + threadIdx.x;
+            cnt[k] = c < nc ? *cell_word<KB>(A.cells, c) : 0u;
+            const unsigned used = __ballot_sync(kFull, cnt[k] != 0u);
+            ex_keys[k] = __popc(used & ((1u << lane) - 1u));
+            uint32_t incl = cnt[k];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += y;
+            }
+            ex_ops[k] = incl - cnt[k];
+            if (lane == 31)
+                part[k * kWarpsPerBlock + w] = ((unsigned long long)incl << 32) | __popc(used);
+        }
+        __syncthreads();
+        if (w == 0) {  // exclusive scan of the 32 (step, warp) totals, one per lane
+            static_assert(kCompactRun * kWarpsPerBlock == 32, "one total per lane");
+            const unsigned long long a0 = part[lane];
+            unsigned long long incl = a0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long y = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += y;
+            }
+            part[lane] = incl - a0;
+            if (lane == 31) {
+                const unsigned long long nk = incl & 0xffffffffull, no = incl >> 32;
+                base_keys = nk ? atomicAdd(&A.ctr[kCtrDistinct], nk) : 0ull;
+                base_ops = no ? atomicAdd(&A.ctr[kCtrPlaced], no) : 0ull;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kCompactRun; ++k) {
+            if (!cnt[k]) continue;
+            const unsigned long long pk = part[k * kWarpsPerBlock + w];
+            const uint32_t d = (uint32_t)base_keys + (uint32_t)pk + ex_keys[k];
+            const uint32_t off = (uint32_t)base_ops + (uint32_t)(pk >> 32) + ex_ops[k];
+            const uint64_t c = c0 + (uint64_t)k * blockDim.x + threadIdx.x;
+            *cell_word<KB>(A.cells, c) = d;  // the count becomes the distinct id
+            ((typename SlotT<KB>::K *)A.dkey)[d] = cell_key<KB>(A.cells, c);
+            A.dcnt[d] = cnt[k];
+            A.dseg[d] = (unsigned long long)off << 32;
+            if (A.dtid) A.dtid[d] = table_of(A.tcell_off, A.ntables, (uint32_t)c);
+        }
+        __syncthreads();  // part / bases are reused by the next tile
     }
 }
 
@@ -223,10 +307,14 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const uint32_t cell = A.op_cell[i];
         if (cell == kNoCell) continue;
-        const uint32_t d = A.cell_did[cell];
-        const uint32_t pos = A.doff[d] + atomicAdd(&A.dfill[d], 1u);
-        A.seg[pos] = (uint32_t)i;
+        const uint32_t d = *cell_word<KB>(A.cells, cell);
+        const unsigned long long o = atomicAdd(&A.dseg[d], 1ull);
+        A.seg[(uint32_t)(o >> 32) + (uint32_t)o] = (uint32_t)i;
     }
+}
+
+__device__ __forceinline__ uint32_t seg_off(const ApplyScratch &A, uint32_t d) {
+    return (uint32_t)(A.dseg[d] >> 32);
 }
 
 // State after one op (an insert stores inval, an erase removes, any other
@@ -242,7 +330,8 @@ __device__ __forceinline__ void replay_op(uint8_t op, uint64_t inval, bool &pres
     }
 }
 
-// Final state of distinct key d, recorded by one thread (mid / giant paths).
+// Final state of distinct key d, recorded by one thread (warp, mid and giant
+// paths).
 template <int KB>
 __device__ __forceinline__ void record_final_one(const ApplyScratch &A, uint32_t d, bool present,
                                                  uint64_t value, bool pre_present,
@@ -321,38 +410,46 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
     // key-0 ops (no cell): miss, output 0
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
         if (A.op_cell[i] == kNoCell && vals_out) store_val(vals_out, vb, i, 0ull);
+    const int slots[4] = {kCtrUp, kCtrEr, kCtrWarp, kCtrMid};
     // whole blocks step through the distinct keys so every thread reaches
-    // the block_alloc calls
+    // the block_alloc call
     for (uint64_t d0 = (uint64_t)blockIdx.x * blockDim.x; d0 < nd; d0 += stride) {
         const uint64_t d = d0 + threadIdx.x;
-        bool up = false, er = false, md = false, gi = false, fresh = false;
+        bool up = false, er = false, wp = false, md = false, gi = false, fresh = false;
         K k = 0;
         uint64_t value = 0ull;
         uint32_t tid = 0u;
         if (d < nd) {
-            const uint32_t cnt = A.dcnt[d], off = A.doff[d];
+            const uint32_t cnt = A.dcnt[d];
             if (cnt > kMidSeg) {
                 gi = true;
-            } else if (cnt > kShortSeg) {
+            } else if (cnt > kWarpSeg) {
                 md = true;
+            } else if (cnt > kShortSeg) {
+                wp = true;
             } else {
-                uint32_t *s = A.seg + off;
-                // insertion sort of the segment by op index (segments are short)
-                for (uint32_t a = 1; a < cnt; ++a) {
-                    const uint32_t x = s[a];
-                    uint32_t b = a;
-                    while (b > 0 && s[b - 1] > x) {
-                        s[b] = s[b - 1];
-                        --b;
+                uint32_t s[kShortSeg];
+                const uint32_t off = seg_off(A, (uint32_t)d);
+#pragma unroll
+                for (uint32_t a = 0; a < kShortSeg; ++a) s[a] = a < cnt ? A.seg[off + a] : 0xffffffffu;
+                // odd-even transposition network in registers (padding sorts last)
+#pragma unroll
+                for (uint32_t r = 0; r < kShortSeg; ++r) {
+#pragma unroll
+                    for (uint32_t a = r & 1u; a + 1 < kShortSeg; a += 2) {
+                        const uint32_t lo = min(s[a], s[a + 1]), hi = max(s[a], s[a + 1]);
+                        s[a] = lo;
+                        s[a + 1] = hi;
                     }
-                    s[b] = x;
                 }
                 k = ((const K *)A.dkey)[d];
                 const bool pre_present = (A.pre_hit[d >> 5] >> (d & 31)) & 1u;
                 const uint64_t pre_value = load_val(A.pre_val, vb, d);
                 bool present = pre_present;
                 value = pre_value;
-                for (uint32_t a = 0; a < cnt; ++a) {
+#pragma unroll
+                for (uint32_t a = 0; a < kShortSeg; ++a) {
+                    if (a >= cnt) break;
                     const uint32_t i = s[a];
                     const uint8_t op = ops[i];
                     // every op reports the state just before it
@@ -366,29 +463,118 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
                 if (A.dtid) tid = A.dtid[d];
             }
         }
-        const uint32_t u = block_alloc(&A.ctr[kCtrUp], up ? 1u : 0u);
-        const uint32_t e = block_alloc(&A.ctr[kCtrEr], er ? 1u : 0u);
-        const uint32_t m = block_alloc(&A.ctr[kCtrMid], md ? 1u : 0u);
-        const uint32_t g = block_alloc(&A.ctr[kCtrGiant], gi ? 1u : 0u);
+        uint32_t got[4];
+        block_alloc<4, 16>(A.ctr, slots,
+                           (unsigned long long)up | ((unsigned long long)er << 16) |
+                               ((unsigned long long)wp << 32) | ((unsigned long long)md << 48),
+                           got);
+        const unsigned long long gpos = agg_inc(&A.ctr[kCtrGiant], gi);  // rare
         if (A.tnew) warp_count_by(A.tnew, tid, fresh);
         if (up) {
-            ((K *)A.up_key)[u] = k;
-            if (vb == 4) ((uint32_t *)A.up_val)[u] = (uint32_t)value;
-            else ((unsigned long long *)A.up_val)[u] = value;
-            if (A.up_tid) A.up_tid[u] = tid;
+            ((K *)A.up_key)[got[0]] = k;
+            if (vb == 4) ((uint32_t *)A.up_val)[got[0]] = (uint32_t)value;
+            else ((unsigned long long *)A.up_val)[got[0]] = value;
+            if (A.up_tid) A.up_tid[got[0]] = tid;
         } else if (er) {
-            ((K *)A.er_key)[e] = k;
-            if (A.er_tid) A.er_tid[e] = tid;
+            ((K *)A.er_key)[got[1]] = k;
+            if (A.er_tid) A.er_tid[got[1]] = tid;
+        } else if (wp) {
+            A.wseg[got[2]] = (uint32_t)d;
         } else if (md) {
-            A.mid[m] = (uint32_t)d;
+            A.mid[got[3]] = (uint32_t)d;
         } else if (gi) {
-            A.giant[g] = (uint32_t)d;
+            A.giant[gpos] = (uint32_t)d;
         }
     }
 }
 
-// Mid segments: one block per segment sorts its op indices in shared memory
-// (bitonic network over the next power of two), then warp 0 replays them.
+// Ascending bitonic sort of s[0..P) (P a power of two) by the threads
+// [t0, t0 + nt) of the caller's group; sync() separates the stages.
+template <class Sync>
+__device__ __forceinline__ void bitonic_sort(uint32_t *s, uint32_t P, uint32_t t0, uint32_t nt,
+                                             Sync sync) {
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t t = t0; t < P; t += nt) {
+                const uint32_t u = t ^ j;
+                if (u > t) {
+                    const uint32_t a = s[t], b = s[u];
+                    if ((a > b) == ((t & k) == 0)) {
+                        s[t] = b;
+                        s[u] = a;
+                    }
+                }
+            }
+            sync();
+        }
+    }
+}
+
+// Warp segments (kShortSeg < ops <= kWarpSeg): one warp per segment sorts
+// it in its own shared memory and replays it. A warp takes 32 segments in a
+// row and keeps segment j's final state in lane j, so the erase / upsert
+// lists get one warp-aggregated allocation per 32 segments (one global
+// counter bumped per segment serialised this kernel).
+template <int KB>
+__global__ void __launch_bounds__(256) k_apply_replay_warp(const __grid_constant__ ApplyScratch A,
+                                                           const uint8_t *__restrict__ ops,
+                                                           const void *__restrict__ vals,
+                                                           uint32_t vb, void *__restrict__ vals_out,
+                                                           uint32_t *__restrict__ bits_out) {
+    using K = typename SlotT<KB>::K;
+    __shared__ uint32_t s_all[kWarpsPerBlock][kWarpSeg];
+    uint32_t *s = s_all[threadIdx.x >> 5];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t nw = A.ctr[kCtrWarp];
+    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (uint64_t x0 = gw * 32; x0 < nw; x0 += warps * 32) {
+        uint32_t rd = 0;
+        bool rvalid = false, rpresent = false, rpre = false;
+        uint64_t rvalue = 0ull, rpre_value = 0ull;
+        for (uint32_t j = 0; j < 32 && x0 + j < nw; ++j) {
+            const uint32_t d = A.wseg[x0 + j];
+            const uint32_t cnt = A.dcnt[d], off = seg_off(A, d);  // kShortSeg < cnt <= kWarpSeg
+            uint32_t P = 32;
+            while (P < cnt) P <<= 1;
+            for (uint32_t q = lane; q < P; q += 32) s[q] = q < cnt ? A.seg[off + q] : 0xffffffffu;
+            __syncwarp();
+            bitonic_sort(s, P, lane, 32, [] { __syncwarp(); });
+            const bool pre_present = (A.pre_hit[d >> 5] >> (d & 31)) & 1u;
+            const uint64_t pre_value = load_val(A.pre_val, vb, d);
+            bool present = pre_present;
+            uint64_t value = pre_value;
+            warp_replay(s, cnt, present, value, ops, vals, vb, vals_out, bits_out);
+            if (lane == j) {
+                rd = d;
+                rvalid = true;
+                rpresent = present;
+                rvalue = value;
+                rpre = pre_present;
+                rpre_value = pre_value;
+            }
+            __syncwarp();  // s is reused by the next segment
+        }
+        const bool up = rvalid && rpresent && (!rpre || rvalue != rpre_value);
+        const bool er = rvalid && !rpresent && rpre;
+        const uint32_t tid = (rvalid && A.dtid) ? A.dtid[rd] : 0u;
+        const uint32_t u = (uint32_t)agg_inc(&A.ctr[kCtrUp], up);
+        const uint32_t e = (uint32_t)agg_inc(&A.ctr[kCtrEr], er);
+        if (A.tnew) warp_count_by(A.tnew, tid, up && !rpre);
+        if (up) {
+            ((K *)A.up_key)[u] = ((const K *)A.dkey)[rd];
+            if (vb == 4) ((uint32_t *)A.up_val)[u] = (uint32_t)rvalue;
+            else ((unsigned long long *)A.up_val)[u] = rvalue;
+            if (A.up_tid) A.up_tid[u] = tid;
+        } else if (er) {
+            ((K *)A.er_key)[e] = ((const K *)A.dkey)[rd];
+            if (A.er_tid) A.er_tid[e] = tid;
+        }
+    }
+}
+
+// Mid segments (kWarpSeg < ops <= kMidSeg): one block per segment sorts its
+// op indices in shared memory, then warp 0 replays them.
 template <int KB>
 __global__ void __launch_bounds__(256) k_apply_replay_mid(const __grid_constant__ ApplyScratch A,
                                                           const uint8_t *__restrict__ ops,
@@ -399,27 +585,13 @@ __global__ void __launch_bounds__(256) k_apply_replay_mid(const __grid_constant_
     const uint64_t nmid = A.ctr[kCtrMid];
     for (uint64_t x = blockIdx.x; x < nmid; x += gridDim.x) {
         const uint32_t d = A.mid[x];
-        const uint32_t cnt = A.dcnt[d], off = A.doff[d];  // kShortSeg < cnt <= kMidSeg
-        uint32_t P = 2u * kShortSeg;
+        const uint32_t cnt = A.dcnt[d], off = seg_off(A, d);
+        uint32_t P = 2u * kWarpSeg;
         while (P < cnt) P <<= 1;
         for (uint32_t j = threadIdx.x; j < P; j += blockDim.x)
             s[j] = j < cnt ? A.seg[off + j] : 0xffffffffu;
         __syncthreads();
-        for (uint32_t k = 2; k <= P; k <<= 1) {
-            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-                for (uint32_t t = threadIdx.x; t < P; t += blockDim.x) {
-                    const uint32_t u = t ^ j;
-                    if (u > t) {
-                        const uint32_t a = s[t], b = s[u];
-                        if ((a > b) == ((t & k) == 0)) {
-                            s[t] = b;
-                            s[u] = a;
-                        }
-                    }
-                }
-                __syncthreads();
-            }
-        }
+        bitonic_sort(s, P, threadIdx.x, blockDim.x, [] { __syncthreads(); });
         if (threadIdx.x < 32) {
             const bool pre_present = (A.pre_hit[d >> 5] >> (d & 31)) & 1u;
             const uint64_t pre_value = load_val(A.pre_val, vb, d);
@@ -447,7 +619,7 @@ __global__ void __launch_bounds__(256) k_apply_sort_init(const __grid_constant__
         const uint32_t cell = A.op_cell[i];
         uint32_t key = 0xffffffffu;
         if (cell != kNoCell) {
-            const uint32_t d = A.cell_did[cell];
+            const uint32_t d = *cell_word<KB>(A.cells, cell);
             if (A.dcnt[d] > kMidSeg) key = d;
         }
         A.sort_key[i] = key;

@@ -50,27 +50,29 @@ struct Scratch {
 // Scratch of one mixed batch of at most `cap_ops` ops. The multi-table
 // fields are null for a single table.
 struct ApplyScratch {
-    void *cell_key;            // cap_cells keys (4 or 8 bytes), 0 = free
-    uint32_t *cell_cnt;        // ops per cell
-    uint32_t *cell_did;        // distinct id of a cell
+    // cap_cells cells: 4-byte keys {key, count} in 8 bytes, 8-byte keys
+    // {key, count, pad} in 16; key 0 = free. After compaction the count field
+    // holds the cell's distinct-key id.
+    void *cells;
     uint32_t *op_cell;         // cell of each op
     void *dkey;                // distinct keys
-    uint32_t *dcnt, *doff, *dfill;  // per distinct key: ops, segment start, fill cursor
+    uint32_t *dcnt;            // per distinct key: ops
+    unsigned long long *dseg;  // per distinct key: segment start << 32 | fill cursor
     uint32_t *seg;             // op indices grouped by key
     void *pre_val;             // pre-batch value per distinct key
     uint32_t *pre_hit;         // pre-batch hit bits per distinct key
     void *up_key, *up_val;     // upserts to apply
     void *er_key;              // erases to apply
     unsigned long long *ctr;   // see kCtr*
-    uint32_t *mid;             // distinct ids of segments of kShortSeg+1 .. kMidSeg ops
+    uint32_t *wseg;            // distinct ids of segments replayed by a warp
+    uint32_t *mid;             // distinct ids of segments replayed by a block
     uint32_t *giant;           // distinct ids of longer segments
     uint32_t *sort_key, *sort_val, *sort_key2, *sort_val2;  // radix sort buffers
     uint32_t *hist;            // 256 x blocks digit counts
     uint32_t *seg_start;       // start of each distinct key in the sorted order
-    uint64_t cap_cells;        // power of two, >= 2 * cap_ops
+    uint64_t cap_cells;        // >= 2 * cap_ops
     uint64_t cap_ops;
     // multi-table batches
-    uint32_t *cell_tid;        // table of a cell
     uint32_t *dtid;            // table of a distinct key
     uint32_t *up_tid, *er_tid; // table of each upsert / erase
     uint32_t *tnew;            // per table: keys the batch adds
@@ -86,6 +88,7 @@ enum : int {
     kCtrEr = 3,        // erases listed
     kCtrGiant = 4,     // giant segments
     kCtrMid = 5,       // mid segments
+    kCtrWarp = 6,      // warp segments
     kCtrSlots = 8
 };
 

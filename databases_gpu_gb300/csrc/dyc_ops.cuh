@@ -162,7 +162,7 @@ cudaError_t Ops<KB>::apply_group(const LaunchCtx &L, const ApplyScratch &A, cons
     auto g = k_apply_group<KB>;
     g<<<grid_for((const void *)g, L, n), 256, 0, L.stream>>>(A, keys, n);
     auto c = k_apply_compact<KB>;
-    c<<<grid_for((const void *)c, L, A.cap_cells), 256, 0, L.stream>>>(A);
+    c<<<grid_for((const void *)c, L, 2 * n), 256, 0, L.stream>>>(A, 2 * n);
     return cudaGetLastError();
 }
 
@@ -183,9 +183,13 @@ cudaError_t Ops<KB>::apply_replay(const LaunchCtx &L, const ApplyScratch &A, con
     const uint64_t work = n > max_distinct ? n : max_distinct;
     r<<<grid_for((const void *)r, L, work), 256, 0, L.stream>>>(A, ops, vals, vb, vals_out,
                                                                  bits_out, n);
+    auto w = k_apply_replay_warp<KB>;
+    // one warp per 32 warp segments; at most n / (kShortSeg + 1) segments
+    w<<<grid_for((const void *)w, L, n / (kShortSeg + 1) + 32), 256, 0, L.stream>>>(
+        A, ops, vals, vb, vals_out, bits_out);
     auto m = k_apply_replay_mid<KB>;
-    // one block per mid segment; at most n / (kShortSeg + 1) of them
-    m<<<grid_for((const void *)m, L, (n / (kShortSeg + 1) + 1) * 256), 256, 0, L.stream>>>(
+    // one block per mid segment; at most n / (kWarpSeg + 1) of them
+    m<<<grid_for((const void *)m, L, (n / (kWarpSeg + 1) + 1) * 256), 256, 0, L.stream>>>(
         A, ops, vals, vb, vals_out, bits_out);
     return cudaGetLastError();
 }
@@ -232,7 +236,7 @@ cudaError_t Ops<KB>::set_group(const LaunchCtx &L, const ApplyScratch &A, const 
         auto g = k_set_group<KB>;
         g<<<grid_for((const void *)g, L, n), 256, 0, L.stream>>>(A, off, keys, n);
         auto c = k_apply_compact<KB>;
-        c<<<grid_for((const void *)c, L, A.cap_cells), 256, 0, L.stream>>>(A);
+        c<<<grid_for((const void *)c, L, 2 * n), 256, 0, L.stream>>>(A, 0);
     }
     return cudaGetLastError();
 }
