@@ -425,7 +425,56 @@ def run_multi_table(args, dev, torch, dg):
     res["api"] = "dyc_set_apply (graph replay) vs dyc_set_apply_each (one dyc_apply per table)"
     for S in sets:
         S.close()
+    if not args.skip_tune:
+        res["tuned"] = run_tuned_set(args, w, dev, torch, dg)
     return res
+
+
+def run_tuned_set(args, w, dev, torch, dg):
+    """The same workload on a set configured by the tuner: per size class the
+    bucket size, subtable count and eviction bound that ran the class's own
+    mixed batches fastest, then the blocks-per-SM cap with the fastest round."""
+    from databases_gpu_gb300 import tune
+    sizes, batches = w.sizes.numpy(), w.batch.numpy()
+    t0 = time.perf_counter()
+    results = tune.tune_classes(sizes, batches, device=dev.index or 0)
+    sb, dsub, ev = tune.plan_set(sizes, batches, results)
+    T = dg.DyCuckooSet(sizes, bucket_bytes=sb, num_subtables=dsub, device=dev.index or 0)
+    T.configure(0, ev)
+    for t in range(w.ntables):
+        k, v = w.preload(t)
+        T.table(t).insert(k, v, new_keys=True, unique=True)
+    n = w.n_ops
+    out = torch.empty(n, dtype=torch.int32, device=dev)
+    bits = torch.empty((n + 31) // 32, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def run_round(cap, graph=False):
+        T.configure(cap, None)
+        ops, keys, vals = w.round()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        T.apply(w.offsets, ops, keys, vals, out=out, bits=bits, h_offsets=w.offsets_host,
+                graph=graph, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    run_round(0)  # scratch
+    cap = tune.tune_launch(run_round)
+    tune_s = time.perf_counter() - t0
+    T.configure(cap, None)
+    for _ in range(2):  # graph capture
+        run_round(cap, graph=True)
+    ms = sorted(run_round(cap, graph=True) for _ in range(args.mt_rounds))
+    T.close()
+    return {"mops": round(n * len(ms) / (sum(ms) / 1e3) / 1e6, 1),
+            "round_ms_p50": round(ms[len(ms) // 2], 3), "bucket_bytes": int(sb),
+            "blocks_per_sm": int(cap), "tune_seconds": round(tune_s, 1),
+            "classes": {int(c): {"batch": r.batch, **r.best, "class_mops": r.mops}
+                        for c, r in results.items()}}
 
 
 def workload_config(args, lf):
@@ -462,6 +511,7 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=2e5)
     ap.add_argument("--serve-seconds", type=float, default=0.25)
     ap.add_argument("--mt-tables", type=int, default=4096)
+    ap.add_argument("--skip-tune", action="store_true", help="skip the tuned multi-table set")
     ap.add_argument("--mt-rounds", type=int, default=3)
     ap.add_argument("--stream-batches", type=int, default=512)
     ap.add_argument("--stream-log2-batch", type=int, default=22)

@@ -64,7 +64,7 @@ EXPORTS = [
     "dyc_subtable", "dyc_export", "dyc_last_stats", "dyc_insert_host", "dyc_find_host",
     "dyc_erase_host", "dyc_status_string", "dyc_last_error", "dyc_erase_noalloc", "dyc_apply",
     "dyc_set_create", "dyc_set_destroy", "dyc_set_table", "dyc_set_sizes", "dyc_set_apply",
-    "dyc_set_apply_each", "dyc_set_last_stats",
+    "dyc_set_apply_each", "dyc_set_last_stats", "dyc_set_configure",
     "dyc_server_config_default", "dyc_server_create", "dyc_server_destroy", "dyc_server_submit",
     "dyc_server_wait", "dyc_server_stats_get", "dyc_server_set",
     "dyc_snapshot_bytes", "dyc_snapshot", "dyc_restore",
@@ -107,6 +107,7 @@ def _declare(L):
         "dyc_set_apply": (st, [T, vp, vp, vp, vp, vp, vp, vp, u32, vp]),
         "dyc_set_apply_each": (st, [T, vp, vp, vp, vp, vp, vp, vp, u32, vp]),
         "dyc_set_last_stats": (st, [T, C.POINTER(DycOpStats)]),
+        "dyc_set_configure": (st, [T, u32, vp]),
         "dyc_server_config_default": (None, [C.POINTER(DycServerConfig)]),
         "dyc_server_create": (st, [C.POINTER(DycConfig), u32, vp, C.POINTER(DycServerConfig),
                                    C.POINTER(C.c_void_p)]),

@@ -419,6 +419,7 @@ dyc_status create_impl(const dyc_config *cfg, Counters *ext_d, Counters *ext_h, 
     const uint32_t nb_rule = (s & 1u) ? s + 1u : s;
     memset(&t->D, 0, sizeof(t->D));
     t->D.d = cfg->num_subtables;
+    t->D.max_evict = cfg->max_evictions;
     for (uint32_t i = 0; i < t->D.d; ++i) {
         const uint32_t nb = nb_override ? nb_override[i] : nb_rule;
         cudaError_t e = cudaMalloc(&t->D.sub[i], (size_t)nb * t->sb);
@@ -1028,6 +1029,8 @@ struct dyc_set {
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     std::vector<uintptr_t> gkey;
     bool gwarm = false;
+    uint32_t blocks_per_sm = 0;  // launch cap of the set kernels (0: as many as fit)
+    uint32_t max_evict_all = 0;  // largest member eviction bound
     dyc_op_stats last{};
 };
 
@@ -1088,7 +1091,7 @@ dyc_status set_ensure_scratch(dyc_set *s, uint64_t n) {
 dyc_status set_phase_a(dyc_set *s, const uint32_t *d_off, const uint8_t *ops, const void *keys,
                        const void *vals, void *out, uint32_t *bits, uint64_t n, cudaStream_t st) {
     const dyc::ApplyScratch &A = s->A;
-    const LaunchCtx L{s->sms, st};
+    const LaunchCtx L{s->sms, st, (int)s->blocks_per_sm};
     const uint32_t vb = (uint32_t)s->vb;
     CK(cudaMemsetAsync(A.ctr, 0, dyc::kCtrSlots * sizeof(unsigned long long), st));
     if (bits) CK(cudaMemsetAsync(bits, 0, (size_t)((n + 31) / 32) * 4, st));
@@ -1108,7 +1111,7 @@ dyc_status set_phase_a(dyc_set *s, const uint32_t *d_off, const uint8_t *ops, co
 // Phase B: erase list, upsert list, eviction walks; counters to the host.
 dyc_status set_phase_b(dyc_set *s, uint64_t n, cudaStream_t st) {
     const dyc::ApplyScratch &A = s->A;
-    const LaunchCtx L{s->sms, st};
+    const LaunchCtx L{s->sms, st, (int)s->blocks_per_sm};
     CK(cudaMemsetAsync(s->d_gctr, 0, sizeof(Counters), st));
     cudaError_t e = SET_KB_CALL(s, set_erase, L, s->d_desc, s->d_tctr, s->sb, A.er_key, A.er_tid,
                                 &A.ctr[dyc::kCtrEr], n, s->d_gctr);
@@ -1119,7 +1122,7 @@ dyc_status set_phase_b(dyc_set *s, uint64_t n, cudaStream_t st) {
     if (e == cudaSuccess)
         e = SET_KB_CALL(s, set_walk, L, s->d_desc, s->d_tctr, s->sb, s->list_a, s->tid_a,
                         &s->d_gctr->pending, s->list_b, s->tid_b, &s->d_gctr->overflow,
-                        s->list_cap, s->cfg.max_evictions, s->d_gctr, s->list_cap);
+                        s->list_cap, s->max_evict_all, s->d_gctr, s->list_cap);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "set phase B kernels: %s", cudaGetErrorString(e));
     CK(cudaMemcpyAsync(s->h_gctr, s->d_gctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(s->h_tctr, s->d_tctr, sizeof(Counters) * s->ntables,
@@ -1258,6 +1261,7 @@ dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_
     }
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "set setup: %s", cudaGetErrorString(e)));
+    s->max_evict_all = cfg->max_evictions;
     dyc_status r = set_push_descs(s, 0);
     if (r != DYC_OK) return undo(r);
     *out = s;
@@ -1283,6 +1287,27 @@ dyc_status dyc_set_destroy(dyc_set *s) {
     if (s->lbuf) cudaFree(s->lbuf);
     if (s->d_bits_tmp) cudaFree(s->d_bits_tmp);
     delete s;
+    return DYC_OK;
+}
+
+dyc_status dyc_set_configure(dyc_set *s, uint32_t blocks_per_sm, const uint32_t *max_evictions) {
+    if (!s) return fail(DYC_EINVAL, "null set");
+    if (blocks_per_sm > 64) return fail(DYC_EINVAL, "blocks_per_sm must be 0..64");
+    if (max_evictions)
+        for (uint32_t t = 0; t < s->ntables; ++t)
+            if (max_evictions[t] < 1 || max_evictions[t] > 100000)
+                return fail(DYC_EINVAL, "max_evictions[%u] must be 1..100000", t);
+    set_drop_graphs(s);
+    s->blocks_per_sm = blocks_per_sm;
+    if (max_evictions) {
+        s->max_evict_all = 0;
+        for (uint32_t t = 0; t < s->ntables; ++t) {
+            s->tables[t]->cfg.max_evictions = max_evictions[t];
+            s->tables[t]->D.max_evict = max_evictions[t];
+            s->max_evict_all = std::max(s->max_evict_all, max_evictions[t]);
+        }
+        TRY(set_push_descs(s, 0));
+    }
     return DYC_OK;
 }
 
@@ -1342,7 +1367,7 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
     CK(cudaStreamSynchronize(st));
     const uint64_t nd = s->h_actr[dyc::kCtrDistinct], ng = s->h_actr[dyc::kCtrGiant];
     if (ng) {
-        cudaError_t e = SET_KB_CALL(s, apply_giant, LaunchCtx{s->sms, st}, s->A, d_ops, d_vals,
+        cudaError_t e = SET_KB_CALL(s, apply_giant, LaunchCtx{s->sms, st, (int)s->blocks_per_sm}, s->A, d_ops, d_vals,
                                     (uint32_t)s->vb, d_vals_out, d_bits_out, n, nd, ng);
         if (e != cudaSuccess) return fail(DYC_ECUDA, "giant-segment kernels: %s", cudaGetErrorString(e));
         CK(cudaMemcpyAsync(s->h_tnew, s->A.tnew, (size_t)s->ntables * 4, cudaMemcpyDeviceToHost, st));

@@ -22,6 +22,7 @@ struct Desc {
     uint64_t magic[kMaxSub];  // fastmod reciprocals of nb[]
     uint32_t nb[kMaxSub];     // buckets per subtable
     uint32_t d;               // subtable count
+    uint32_t max_evict;       // eviction bound of this table (read by the set kernels)
 };
 
 // Per-table device counters (one 128-byte block). `size` persists; the rest
@@ -100,6 +101,7 @@ constexpr int kSortTile = 4096;
 struct LaunchCtx {
     int sms;
     cudaStream_t stream;
+    int max_blocks_per_sm = 0;  // 0: as many as fit (else a cap, chosen by a tuner)
 };
 
 // Kernel launchers, one set per key width; `sb` = bucket bytes (32/64/128).

@@ -32,6 +32,7 @@ inline int grid_for(const void *kernel, const LaunchCtx &L, uint64_t work, int b
             per_sm = it->second;
         }
     }
+    if (L.max_blocks_per_sm > 0 && L.max_blocks_per_sm < per_sm) per_sm = L.max_blocks_per_sm;
     const uint64_t need = (work + block - 1) / block;
     const uint64_t wave = (uint64_t)per_sm * (uint64_t)(L.sms > 0 ? L.sms : 1);
     uint64_t g = need < wave ? need : wave;

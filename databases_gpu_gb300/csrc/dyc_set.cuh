@@ -198,7 +198,9 @@ __global__ void __launch_bounds__(256) k_set_place(const Desc *__restrict__ desc
     agg_add(&gctr->updated, n_upd);
 }
 
-// eviction walks of src entries (k_walk per table); failures go to dst
+// eviction walks of src entries (k_walk per table, each with its own
+// eviction bound; max_evict is the largest, which bounds the loop); failures
+// go to dst
 template <int KB, int SB>
 __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs,
                                                   Counters *__restrict__ tctr,
@@ -251,7 +253,7 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
                 bp = fb;
             } else if (r.empty) {
                 // every empty slot was taken by another lane: look again
-            } else if (evictions >= max_evict) {
+            } else if (evictions >= D.max_evict) {  // this table's bound
                 live = false;
                 fail = true;
             } else {

@@ -385,6 +385,15 @@ class DyCuckooSet:
     def __exit__(self, *exc):
         self.close()
 
+    def configure(self, blocks_per_sm: int = 0, max_evictions=None) -> None:
+        """Launch cap of the set kernels and per-table eviction bounds."""
+        ev = None if max_evictions is None else np.ascontiguousarray(max_evictions, np.uint32)
+        if ev is not None and ev.size != self.ntables:
+            raise ValueError("one eviction bound per table")
+        check(self.L.dyc_set_configure(self._h, int(blocks_per_sm),
+                                       ev.ctypes.data if ev is not None else None),
+              "dyc_set_configure")
+
     def table(self, i: int) -> DyCuckoo:
         h = C.c_void_p()
         check(self.L.dyc_set_table(self._h, i, C.byref(h)), "dyc_set_table")

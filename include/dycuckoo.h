@@ -297,6 +297,12 @@ dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_
                           const uint32_t *num_subtables, dyc_set **out);
 dyc_status dyc_set_destroy(dyc_set *s);
 
+/* Launch and table parameters, typically chosen by a tuner per table-size
+ * class (databases_gpu_gb300/tune.py): blocks_per_sm caps the resident
+ * blocks per SM of the set's launches (0: as many as fit); max_evictions
+ * (NULL: unchanged) gives every member its own eviction bound. */
+dyc_status dyc_set_configure(dyc_set *s, uint32_t blocks_per_sm, const uint32_t *max_evictions);
+
 /* Member table i. Single-table calls may be made on it between set calls;
  * it is destroyed with the set. */
 dyc_status dyc_set_table(dyc_set *s, uint32_t i, dyc_table **out);

@@ -55,10 +55,18 @@ def _preload(S, w, maps):
         maps[t].insert(to_host(k, 4), to_host(v, 4))
 
 
-@pytest.mark.parametrize("graph", [False, True])
-def test_set_matches_oracle_per_table(graph):
+@pytest.mark.parametrize("graph,tuned", [(False, False), (True, False), (False, True)])
+def test_set_matches_oracle_per_table(graph, tuned):
+    """tuned: per-table subtable counts and eviction bounds (2..4, 1..256, as
+    a tuner may pick), 64-byte buckets and a launch cap of 2 blocks per SM."""
     w = _small_workload(96, seed=5)
-    S = _dg().DyCuckooSet(w.sizes.numpy(), max_evictions=64)
+    if tuned:
+        rng = np.random.default_rng(2)
+        S = _dg().DyCuckooSet(w.sizes.numpy(), bucket_bytes=64,
+                              num_subtables=rng.integers(2, 5, 96))
+        S.configure(2, rng.choice(np.array([1, 16, 256], np.uint32), 96))
+    else:
+        S = _dg().DyCuckooSet(w.sizes.numpy(), max_evictions=64)
     maps = [O.Map() for _ in range(S.ntables)]
     _preload(S, w, maps)
     for r in range(4):
@@ -145,3 +153,15 @@ def test_set_u64_keys_and_growth():
     sizes, caps = S.sizes()
     assert caps.max() > 16 * 4  # tables grew
     S.close()
+
+
+def test_tuner_picks_a_measured_candidate():
+    from databases_gpu_gb300 import tune
+    space = {"bucket_bytes": (64, 128), "num_subtables": (2, 4), "max_evictions": (16, 64)}
+    r = tune.tune_class(10, 512, space, rounds=2)
+    assert len(r.candidates) == 8
+    assert r.best in [{k: c[k] for k in ("bucket_bytes", "num_subtables", "max_evictions")}
+                      for c in r.candidates]
+    assert r.mops > 0 and set(r.by_bucket) == {64, 128}
+    sb, d, ev = tune.plan_set([1000, 1100], [500, 600], {9: r, 10: r})
+    assert sb in (64, 128) and list(d) == [r.by_bucket[sb][0]["num_subtables"]] * 2
