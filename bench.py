@@ -265,6 +265,38 @@ def run_line_probe():
     print(json.dumps(d))
 
 
+def run_set_profile(args):
+    """One table set (the multi-table workload with args.mt_tables tables),
+    args.mt_rounds rounds of dyc_set_apply without graphs, each timed with
+    CUDA events: the command the set-path ncu captures run under."""
+    import torch
+
+    import databases_gpu_gb300 as dg
+    from databases_gpu_gb300.workloads import MultiTableWorkload
+    w = MultiTableWorkload(args.mt_tables, seed=10327, device="cuda")
+    S = dg.DyCuckooSet(w.sizes.numpy())
+    for t in range(w.ntables):
+        k, v = w.preload(t)
+        S.table(t).insert(k, v, new_keys=True, unique=True)
+    n = w.n_ops
+    out = torch.empty(n, dtype=torch.int32, device="cuda")
+    bits = torch.empty((n + 31) // 32, dtype=torch.int32, device="cuda")
+    s = torch.cuda.current_stream()
+    for r in range(args.mt_rounds):
+        ops, keys, vals = w.round()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(s)
+        S.apply(w.offsets, ops, keys, vals, out=out, bits=bits, h_offsets=w.offsets_host, stream=s)
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        print(json.dumps({"round": r, "ms": round(ms, 3), "ops": n,
+                          "mops": round(n / ms / 1e3, 1), "tables": w.ntables}))
+    S.close()
+
+
 def build_serve_load():
     """The server's load generator (databases_gpu_gb300/csrc/dyc_serve_load.cpp)."""
     from databases_gpu_gb300 import build as pkg_build
@@ -503,6 +535,8 @@ def main():
     ap.add_argument("--skip-variants", action="store_true")
     ap.add_argument("--line-probe", action="store_true",
                     help="measure the random 128-byte line ceiling of this GPU and exit")
+    ap.add_argument("--set-profile", action="store_true",
+                    help="run --mt-rounds untimed-graph rounds of the multi-table set and exit")
     ap.add_argument("--skip-stream", action="store_true",
                     help="skip the dynamic resize stream workload")
     ap.add_argument("--skip-multi", action="store_true",
@@ -523,6 +557,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.line_probe:
         return run_line_probe()
+    if args.set_profile:
+        return run_set_profile(args)
     if args.impl == "reference":
         return run_reference(args)
 
