@@ -700,6 +700,39 @@ def main():
                  stream=stream)
         torch.cuda.synchronize()
         assert t.size == N
+        # ---- resize: double the subtable the reference would pick, then
+        # halve it back (even bucket count: bucket j merges with j + nb/2);
+        # algorithmic bytes: upsize reads S and writes 2S, downsize reads 2S
+        # and writes S (S = the subtable before the upsize)
+        nb0 = t.layout()
+        times = []
+        for rep in range(2):  # the first pair maps the pool's memory, the second reuses it
+            e0.record(stream)
+            t.resize_up(stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            up_ms = e0.elapsed_time(e1)
+            grown = [i for i, (a, b) in enumerate(zip(nb0, t.layout())) if a != b][0]
+            e0.record(stream)
+            t.resize_down(stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append((up_ms, e0.elapsed_time(e1)))
+            assert t.layout() == nb0 and t.size == N
+        S = nb0[grown] * args.bucket_bytes
+        peak_gbs = load_peaks()[0]
+        (up_cold, down_cold), (up_ms, down_ms) = times
+        ops["resize"] = {"subtable_bytes": S,
+                         "upsize_ms": round(up_ms, 3),
+                         "upsize_gbs": round(3 * S / (up_ms / 1e3) / 1e9, 1),
+                         "upsize_frac": round(3 * S / (up_ms / 1e3) / 1e9 / peak_gbs, 3),
+                         "downsize_ms": round(down_ms, 3),
+                         "downsize_gbs": round(3 * S / (down_ms / 1e3) / 1e9, 1),
+                         "downsize_frac": round(3 * S / (down_ms / 1e3) / 1e9 / peak_gbs, 3),
+                         "first_pair_ms": [round(up_cold, 3), round(down_cold, 3)],
+                         "note": "events around dyc_resize_up / dyc_resize_down (allocation, "
+                                 "kernel, host counter read, stream-ordered free), second "
+                                 "up/down pair; first_pair_ms includes mapping pool memory"}
 
     # ---- dynamic resize stream (its own u64 table; the find table is kept)
     workloads = {}

@@ -4,6 +4,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "dycuckoo.h"
@@ -75,6 +76,49 @@ uint64_t next_pow2(uint64_t x) {
     return p;
 }
 
+// Library-owned stream-ordered memory pool per device for everything a
+// resize allocates and frees (subtables, entry lists, value heaps). The
+// default pool hands freed memory back to the driver at every
+// synchronisation, so each resize mapped fresh physical memory (a 1.27 GB
+// upsize spent most of its 4.4 ms there); this pool keeps up to a quarter of
+// the device's memory cached for the next resize, and is trimmed when the
+// last table on the device is destroyed.
+std::mutex g_pool_mu;
+constexpr int kPoolDevices = 256;
+cudaMemPool_t g_pool[kPoolDevices];
+int g_pool_tables[kPoolDevices];
+
+cudaError_t lib_pool(int device, cudaMemPool_t *out) {
+    if (device < 0 || device >= kPoolDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> g(g_pool_mu);
+    if (!g_pool[device]) {
+        cudaMemPoolProps props;
+        memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        cudaMemPool_t p = nullptr;
+        cudaError_t e = cudaMemPoolCreate(&p, &props);
+        if (e != cudaSuccess) return e;
+        size_t free_b = 0, total_b = 0;
+        e = cudaMemGetInfo(&free_b, &total_b);
+        if (e != cudaSuccess) return e;
+        uint64_t keep = total_b / 4;
+        e = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+        if (e != cudaSuccess) return e;
+        g_pool[device] = p;
+    }
+    *out = g_pool[device];
+    return cudaSuccess;
+}
+
+void pool_table_count(int device, int delta) {
+    if (device < 0 || device >= kPoolDevices) return;
+    std::lock_guard<std::mutex> g(g_pool_mu);
+    g_pool_tables[device] += delta;
+    if (g_pool_tables[device] == 0 && g_pool[device]) cudaMemPoolTrimTo(g_pool[device], 0);
+}
+
 constexpr uint64_t kChunkDefault = 1ull << 22;  // ops per insert/erase pass
 constexpr int kMaxOverflowRounds = 24;
 
@@ -88,6 +132,7 @@ struct dyc_table {
     Counters *d_ctr = nullptr;
     Counters *h_ctr = nullptr;
     bool owns_ctr = true;  // false for a member of a table set (the set's arrays)
+    bool counted = false;  // counted among the live tables of its device's pool
     // scratch for one chunk
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
@@ -120,6 +165,14 @@ dyc_status set_device(dyc_table *t) {
 }
 
 LaunchCtx ctx(dyc_table *t, void *stream) { return LaunchCtx{t->sms, (cudaStream_t)stream}; }
+
+// Stream-ordered allocation from the library pool of the table's device.
+cudaError_t pool_alloc(int device, void **p, size_t bytes, cudaStream_t s) {
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = lib_pool(device, &pool);
+    if (e != cudaSuccess) return e;
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
 
 // dispatch on key width
 #define KB_CALL(t, fn, ...) ((t)->kb == 4 ? Ops<4>::fn(__VA_ARGS__) : Ops<8>::fn(__VA_ARGS__))
@@ -178,7 +231,7 @@ dyc_status resize_up_impl(dyc_table *t, cudaStream_t s) {
     if ((uint64_t)onb * 2 > 0xFFFFFFFFull) return fail(DYC_EINVAL, "subtable %u too large", ti);
     const uint32_t nnb = onb * 2;
     void *nw = nullptr;
-    CK(cudaMallocAsync(&nw, (size_t)nnb * t->sb, s));
+    CK(pool_alloc(t->device, &nw, (size_t)nnb * t->sb, s));
     void *old = t->D.sub[ti];
     cudaError_t e = KB_CALL(t, resize_up, ctx(t, s), t->sb, ti, old, onb, nw);
     if (e != cudaSuccess) {
@@ -295,9 +348,9 @@ dyc_status resize_down_impl(dyc_table *t, cudaStream_t s) {
     const uint32_t nnb = even ? onb / 2 : (onb + 1) / 2;
     const uint64_t list_cap = even ? (uint64_t)nnb * t->slots : (uint64_t)onb * t->slots;
     void *nw = nullptr, *la = nullptr, *lb = nullptr;
-    CK(cudaMallocAsync(&nw, (size_t)nnb * t->sb, s));
-    CK(cudaMallocAsync(&la, (size_t)list_cap * t->slot_bytes, s));
-    CK(cudaMallocAsync(&lb, (size_t)list_cap * t->slot_bytes, s));
+    CK(pool_alloc(t->device, &nw, (size_t)nnb * t->sb, s));
+    CK(pool_alloc(t->device, &la, (size_t)list_cap * t->slot_bytes, s));
+    CK(pool_alloc(t->device, &lb, (size_t)list_cap * t->slot_bytes, s));
     TRY(reset_call_counters(t, s));
     void *old = t->D.sub[ti];
     cudaError_t e;
@@ -443,6 +496,8 @@ dyc_status create_impl(const dyc_config *cfg, Counters *ext_d, Counters *ext_h, 
     }
     if (e == cudaSuccess && sync) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "table setup: %s", cudaGetErrorString(e)));
+    t->counted = true;
+    pool_table_count(t->device, 1);
     *out = t;
     return DYC_OK;
 }
@@ -471,6 +526,7 @@ dyc_status dyc_destroy(dyc_table *t) {
         if (t->pipe_buf[i]) cudaFree(t->pipe_buf[i]);
         if (t->pipe_stream[i]) cudaStreamDestroy(t->pipe_stream[i]);
     }
+    if (t->counted) pool_table_count(t->device, -1);
     delete t;
     return DYC_OK;
 }
@@ -1701,8 +1757,8 @@ dyc_status wide_ensure_heap(dyc_wide *w, uint64_t n, cudaStream_t s) {
     if (nc > 0xFFFFFFFFull) nc = 0xFFFFFFFFull;
     if (nc - w->bump + w->free_top < n) return fail(DYC_ENOMEM, "wide table: more than 2^32 values");
     uint32_t *heap = nullptr, *stack = nullptr;
-    CK(cudaMallocAsync(&heap, nc * w->vbytes, s));
-    CK(cudaMallocAsync(&stack, nc * 4, s));
+    CK(pool_alloc(w->t->device, (void **)&heap, nc * w->vbytes, s));
+    CK(pool_alloc(w->t->device, (void **)&stack, nc * 4, s));
     if (w->heap) {
         if (w->bump)
             CK(cudaMemcpyAsync(heap, w->heap, w->bump * w->vbytes, cudaMemcpyDeviceToDevice, s));
