@@ -219,6 +219,9 @@ dyc_status read_counters(dyc_table *t, cudaStream_t s) {
     if (t->h_ctr->spill)
         return fail(DYC_EOVERFLOW, "internal list overflow (%llu entries)",
                     (unsigned long long)t->h_ctr->spill);
+    if (t->h_ctr->timeouts)
+        return fail(DYC_ETIMEOUT, "%llu bounded device wait(s) gave up",
+                    (unsigned long long)t->h_ctr->timeouts);
     t->size = t->h_ctr->size;
     return DYC_OK;
 }
@@ -356,7 +359,7 @@ dyc_status resize_down_impl(dyc_table *t, cudaStream_t s) {
     cudaError_t e;
     if (even) {
         e = KB_CALL(t, resize_down, ctx(t, s), t->sb, old, onb, nw, la, &t->d_ctr->pending,
-                    list_cap, &t->d_ctr->spill);
+                    list_cap, &t->d_ctr->spill, &t->d_ctr->timeouts);
     } else {
         CK(cudaMemsetAsync(nw, 0, (size_t)nnb * t->sb, s));
         e = KB_CALL(t, collect, ctx(t, s), t->sb, old, onb, la, &t->d_ctr->pending, list_cap,

@@ -32,7 +32,9 @@ struct Counters {
     unsigned long long inserted, updated, erased, rejected, superseded;
     unsigned long long pending, overflow, evict_steps;
     unsigned long long spill;  // pending entries a list could not hold (must stay 0)
-    unsigned long long pad[6];
+    unsigned long long pad[2];      // scratch words of dyc_export and dyc_snapshot
+    unsigned long long timeouts;    // bounded device waits that gave up (must stay 0)
+    unsigned long long pad2[3];
 };
 static_assert(sizeof(Counters) == 128, "Counters is one 128-byte block");
 
@@ -132,7 +134,7 @@ template <int KB> struct Ops {
     static cudaError_t resize_down(const LaunchCtx &L, int sb, const void *old_sub,
                                    uint32_t old_nb, void *new_sub, void *list,
                                    unsigned long long *list_count, uint64_t list_cap,
-                                   unsigned long long *spill);
+                                   unsigned long long *spill, unsigned long long *timeouts);
     // every live slot of one subtable to list (general rehash)
     static cudaError_t collect(const LaunchCtx &L, int sb, const void *sub, uint32_t nb,
                                void *list, unsigned long long *list_count, uint64_t list_cap,

@@ -771,49 +771,192 @@ __global__ void __launch_bounds__(256) k_resize_up(uint32_t t, const char *__res
 }
 
 // ----------------------------------------------------------------------------
-// downsize of an even subtable: new bucket j = old buckets j and j+nb/2
-// merged, metadata OR-ed; entries that do not fit are listed for eviction
-// walks (cuckoo_resize_down, cuckoo.cu:638-728, drops the ones its walks
-// cannot place). Thread per new bucket.
+// Bulk-copy helpers (cp.async.bulk through an mbarrier) for streaming a
+// subtable through shared memory. Waits are bounded: a wait that gives up
+// is counted in *timeouts and the caller stops using the buffer.
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes,
+                                          uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void bulk_store(void *dst, uint32_t src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// true when phase `parity` of the barrier completed within the bound
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    constexpr uint32_t kMaxTries = 1u << 22;  // far beyond any copy's completion
+    for (uint32_t i = 0; i < kMaxTries; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
+            "selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 // ----------------------------------------------------------------------------
+// even downsize: new bucket j = old bucket j merged with old bucket j + nb/2
+// (both halves of old bucket j's upsize image); entries that do not fit go to
+// the list for eviction walks (cuckoo_resize_down, cuckoo.cu:638-728, whose
+// residuals are dropped; here they are placed again). Tiles of kMergeTile
+// buckets stream through shared memory by bulk copies: two loads (the tile
+// of each half) completing on an mbarrier, a merge by one thread per bucket
+// in place, one bulk store of the merged tile. The metadata words are OR-ed.
+// ----------------------------------------------------------------------------
+constexpr int kMergeTile = 128;  // buckets per tile = threads per block
+
 template <int KB, int SB>
-__global__ void __launch_bounds__(256) k_resize_down(const char *__restrict__ old_sub,
-                                                     uint32_t new_nb, char *__restrict__ new_sub,
-                                                     void *list, unsigned long long *list_count,
-                                                     uint64_t list_cap,
-                                                     unsigned long long *spill) {
+__global__ void __launch_bounds__(kMergeTile) k_resize_down(const char *__restrict__ old_sub,
+                                                            uint32_t new_nb,
+                                                            char *__restrict__ new_sub,
+                                                            void *list,
+                                                            unsigned long long *list_count,
+                                                            uint64_t list_cap,
+                                                            unsigned long long *spill,
+                                                            unsigned long long *timeouts) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
     using Gm = Geo<KB, SB>;
-    constexpr int B = Gm::kSlots;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < new_nb; j += stride) {
-        Bucket<KB, SB> a, c;
-        a.template load<0>(old_sub + j * SB);
-        c.template load<0>(old_sub + (j + new_nb) * SB);
-        unsigned freem = a.empty_mask();
+    constexpr int B = Gm::kSlots, TOT = Gm::kTotal, W = T::kBytes / 4;
+    __shared__ __align__(128) unsigned char sa[kMergeTile * SB];
+    __shared__ __align__(128) unsigned char sc[kMergeTile * SB];
+    __shared__ __align__(8) unsigned long long bar_storage;
+    __shared__ int failed;
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&bar_storage);
+    const uint32_t sa_addr = (uint32_t)__cvta_generic_to_shared(sa);
+    const uint32_t sc_addr = (uint32_t)__cvta_generic_to_shared(sc);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        failed = 0;
+    }
+    __syncthreads();
+    uint32_t parity = 0;
+    const uint64_t tiles = ((uint64_t)new_nb + kMergeTile - 1) / kMergeTile;
+    for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const uint64_t j0 = tile * kMergeTile;
+        const uint32_t cnt = (uint32_t)((uint64_t)new_nb - j0 < kMergeTile ? new_nb - j0 : kMergeTile);
+        const uint32_t bytes = cnt * SB;
+        if (tid == 0) {
+            // the previous tile's store has read sa; generic accesses before
+            // the barrier are ordered before the async proxy's writes
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(bar, 2 * bytes);
+            bulk_load(sa_addr, old_sub + j0 * SB, bytes, bar);
+            bulk_load(sc_addr, old_sub + (j0 + new_nb) * SB, bytes, bar);
+        }
+        const bool ok = mbar_wait(bar, parity);
+        parity ^= 1u;
+        if (!ok) {
+            if (tid == 0) atomicAdd(timeouts, 1ull);
+            failed = 1;
+        }
+        __syncthreads();
+        if (failed) break;
+        // merge: a group of G = SB/32 lanes per bucket, 32 bytes (SPC slots)
+        // per lane, 32/G buckets per warp step (contiguous shared reads); the
+        // second half's entries move into the first half's empty slots by
+        // shuffles, SPC rounds of one slot per lane
+        {
+            constexpr int G = Gm::kG, SPC = Gm::kSPC, BPS = 32 / G;
+            const int lane = tid & 31, g = lane / G, r = lane % G;
+            const unsigned entry_mask = (B == 32) ? kFull : ((1u << B) - 1u);
+            for (uint32_t b0 = (uint32_t)(tid >> 5) * BPS; b0 < cnt; b0 += 4 * BPS) {
+                const uint32_t bk = b0 + g;
+                const bool valid = bk < cnt;
+                Sl a[SPC], c[SPC];
+                unsigned my_a = 0u, my_c = 0u;
 #pragma unroll
-        for (int q = 0; q < B; ++q) {
-            if (T::is_empty(c.s[q])) continue;
-            if (freem) {
-                const int pos = __ffs(freem) - 1;
-                freem &= freem - 1;
+                for (int j = 0; j < SPC; ++j) {
+                    if (valid) {
+                        T::from_words((const uint32_t *)(sa + bk * SB + r * 32) + j * W, a[j]);
+                        T::from_words((const uint32_t *)(sc + bk * SB + r * 32) + j * W, c[j]);
+                    } else {
+                        a[j] = T::empty();
+                        c[j] = T::empty();
+                    }
+                    if (!T::is_empty(a[j])) my_a |= 1u << (r * SPC + j);
+                    if (!T::is_empty(c[j])) my_c |= 1u << (r * SPC + j);
+                }
+                const unsigned occ_a = group_or<G>(my_a) & entry_mask;
+                const unsigned cocc = group_or<G>(my_c) & entry_mask;
+                const unsigned freem = ~occ_a & entry_mask;
+                const int nfree = __popc(freem), nc = __popc(cocc);
+                // which c slot (lane of the group, slot in the lane) each of my
+                // empty slots takes
+                int src_lane[SPC], src_j[SPC];
 #pragma unroll
-                for (int r = 0; r < B; ++r)
-                    if (r == pos) a.s[r] = c.s[q];
-            } else {
-                const unsigned long long at = atomicAdd(list_count, 1ull);
-                if (at < list_cap) ((Sl *)list)[at] = c.s[q];
-                else atomicAdd(spill, 1ull);
+                for (int j = 0; j < SPC; ++j) {
+                    const int idx = r * SPC + j;
+                    src_lane[j] = -1;
+                    src_j[j] = 0;
+                    if (idx < B && ((freem >> idx) & 1u)) {
+                        const int rank = __popc(freem & ((1u << idx) - 1u));
+                        if (rank < nc) {
+                            const int si = nth_set(cocc, rank);
+                            src_lane[j] = g * G + si / SPC;
+                            src_j[j] = si % SPC;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int jj = 0; jj < SPC; ++jj) {
+#pragma unroll
+                    for (int j = 0; j < SPC; ++j) {
+                        const Sl v = shfl_slot(c[jj], src_lane[j] < 0 ? lane : src_lane[j]);
+                        if (src_lane[j] >= 0 && src_j[j] == jj) a[j] = v;
+                    }
+                }
+                // c entries beyond the free slots go to the list
+#pragma unroll
+                for (int j = 0; j < SPC; ++j) {
+                    const int idx = r * SPC + j;
+                    if (valid && idx < B && ((cocc >> idx) & 1u) &&
+                        __popc(cocc & ((1u << idx) - 1u)) >= nfree) {
+                        const unsigned long long at = atomicAdd(list_count, 1ull);
+                        if (at < list_cap) ((Sl *)list)[at] = c[j];
+                        else atomicAdd(spill, 1ull);
+                    }
+                }
+                if (Gm::kMeta && r == G - 1) {  // metadata word: last slot of the bucket
+                    uint32_t ma[4], mc[4];
+                    T::to_words(a[SPC - 1], ma);
+                    T::to_words(c[SPC - 1], mc);
+                    uint32_t mw[4] = {ma[0] | mc[0], ma[1] | mc[1], 0u, 0u};
+                    T::from_words(mw, a[SPC - 1]);
+                }
+                if (valid) {
+#pragma unroll
+                    for (int j = 0; j < SPC; ++j)
+                        T::to_words(a[j], (uint32_t *)(sa + bk * SB + r * 32) + j * W);
+                }
             }
         }
-        if (Gm::kMeta) {
-            const unsigned long long m = a.meta() | c.meta();
-            uint32_t mw[4] = {(uint32_t)m, (uint32_t)(m >> 32), 0u, 0u};
-            T::from_words(mw, a.s[Gm::kTotal - 1]);
-        }
-        a.store(new_sub + j * SB);
+        // the merged tile (written by generic stores) goes out by the async proxy
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) bulk_store(new_sub + j0 * SB, sa_addr, bytes);
     }
+    if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    if (failed && tid == 0) mbar_wait(bar, parity ^ 1u);  // copies of the failed tile, bounded
 }
 
 // every live slot of one subtable into a list (odd-size downsize)
