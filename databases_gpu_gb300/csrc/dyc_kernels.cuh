@@ -262,6 +262,7 @@ struct KvOut {
     int match;
     uint64_t value;
     bool overflow;
+    unsigned empty;  // empty entry slots (probe_staged with WANT_EMPTY)
 };
 
 constexpr int kBlockThreads = 256;
@@ -302,7 +303,7 @@ __device__ __forceinline__ void stage_rounds(const char *p, unsigned am, unsigne
     __syncwarp();  // other lanes' copies are visible after the warp barrier
 }
 
-template <int KB, int SB>
+template <int KB, int SB, bool WANT_EMPTY = false>
 __device__ __forceinline__ KvOut probe_staged(const char *p, typename SlotT<KB>::K key, bool act,
                                               unsigned char *stage) {
     using T = SlotT<KB>;
@@ -312,7 +313,7 @@ __device__ __forceinline__ KvOut probe_staged(const char *p, typename SlotT<KB>:
     __syncwarp();  // the previous use of the stage is finished in every lane
     if (am == kFull) stage_rounds<SB, true>(p, am, stage);
     else if (am) stage_rounds<SB, false>(p, am, stage);
-    KvOut out{-1, 0ull, false};
+    KvOut out{-1, 0ull, false, 0u};
     if (!act) return out;
     const int lane = threadIdx.x & 31;
     const uint32_t base = (uint32_t)__cvta_generic_to_shared(stage);
@@ -332,6 +333,7 @@ __device__ __forceinline__ KvOut probe_staged(const char *p, typename SlotT<KB>:
                     out.match = idx;
                     out.value = T::val(sl);
                 }
+                if (WANT_EMPTY && T::is_empty(sl)) out.empty |= 1u << idx;
             } else if (Gm::kMeta && idx == Gm::kTotal - 1) {
                 out.overflow = (v[j * (T::kBytes / 4)] & 1u) != 0u;
             }
@@ -355,6 +357,26 @@ __device__ __forceinline__ KvOut kv_probe(const char *p, typename SlotT<KB>::K k
         o.match = r.match;
         o.value = SlotT<KB>::val(r.mslot);
         o.overflow = false;
+        o.empty = 0u;
+        return o;
+    }
+}
+
+// Probe used by insert placement: matching slot, empty entry slots and the
+// overflow bit, through the shared-memory stage for 64- and 128-byte buckets
+// (a coherent L2 snapshot: cp.async.cg), the register probe for 32-byte ones.
+template <int KB, int SB>
+__device__ __forceinline__ KvOut place_probe(const char *p, typename SlotT<KB>::K key, bool act,
+                                             uint32_t t, uint32_t d, unsigned char *stage) {
+    if constexpr (SB >= 64) {
+        return probe_staged<KB, SB, true>(p, key, act, stage);
+    } else {
+        const ProbeOut<KB> r = probe<KB, SB, 2, true, false>(p, key, act, t, d);
+        KvOut o;
+        o.match = r.match;
+        o.value = 0ull;
+        o.overflow = (r.meta & kOverflowBit) != 0ull;
+        o.empty = r.empty;
         return o;
     }
 }
@@ -494,6 +516,8 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
     using T = SlotT<KB>;
     using Sl = typename T::S;
     using Gm = Geo<KB, SB>;
+    __shared__ __align__(128) unsigned char s_stage[SB >= 64 ? kWarpsPerBlock : 1][32 * SB];
+    unsigned char *stage = s_stage[SB >= 64 ? (threadIdx.x >> 5) : 0];
     const uint64_t step = warp_stride();
     uint32_t n_ins = 0, n_upd = 0, n_rej = 0, n_sup = 0;
     for (uint64_t base = warp_base(); base < n; base += step) {
@@ -516,18 +540,14 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
         const Pair p = pair_of(hk, D.d);
         char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
         char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-        const ProbeOut<KB> r1 = probe<KB, SB, 2, true, false>(p1, k, act, p.first, D.d);
+        const KvOut r1 = place_probe<KB, SB>(p1, k, act, p.first, D.d, stage);
         const bool found1 = act && r1.match >= 0;
         // the second bucket is needed to look for the key (upsert, unless the
         // first bucket's overflow bit rules it out) or for an empty slot
         const bool check2 =
-            act && !found1 &&
-            ((!new_keys && (!Gm::kMeta || (r1.meta & kOverflowBit))) || r1.empty == 0u);
-        ProbeOut<KB> r2;
-        r2.match = -1;
-        r2.empty = 0u;
-        r2.mslot = T::empty();
-        if (__any_sync(kFull, check2)) r2 = probe<KB, SB, 2, true, false>(p2, k, check2, p.second, D.d);
+            act && !found1 && ((!new_keys && (!Gm::kMeta || r1.overflow)) || r1.empty == 0u);
+        KvOut r2{-1, 0ull, false, 0u};
+        if (__any_sync(kFull, check2)) r2 = place_probe<KB, SB>(p2, k, check2, p.second, D.d, stage);
         bool pend = false;
         if (found1) {
             T::exch(slot_ptr<KB, SB>(p1, r1.match), e);

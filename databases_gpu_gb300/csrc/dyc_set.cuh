@@ -133,6 +133,8 @@ __global__ void __launch_bounds__(256) k_set_place(const Desc *__restrict__ desc
     using T = SlotT<KB>;
     using Sl = typename T::S;
     using Gm = Geo<KB, SB>;
+    __shared__ __align__(128) unsigned char s_stage[SB >= 64 ? kWarpsPerBlock : 1][32 * SB];
+    unsigned char *stage = s_stage[SB >= 64 ? (threadIdx.x >> 5) : 0];
     const uint64_t n = *n_ptr;
     const uint64_t step = warp_stride();
     uint32_t n_ins = 0, n_upd = 0;
@@ -153,15 +155,12 @@ __global__ void __launch_bounds__(256) k_set_place(const Desc *__restrict__ desc
         const Pair p = pair_of(hk, D.d);
         char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
         char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-        const ProbeOut<KB> r1 = probe<KB, SB, 2, true, false>(p1, k, act, p.first, D.d);
+        const KvOut r1 = place_probe<KB, SB>(p1, k, act, p.first, D.d, stage);
         const bool found1 = act && r1.match >= 0;
         const bool check2 =
-            act && !found1 && ((!Gm::kMeta || (r1.meta & kOverflowBit)) || r1.empty == 0u);
-        ProbeOut<KB> r2;
-        r2.match = -1;
-        r2.empty = 0u;
-        r2.mslot = T::empty();
-        if (__any_sync(kFull, check2)) r2 = probe<KB, SB, 2, true, false>(p2, k, check2, p.second, D.d);
+            act && !found1 && ((!Gm::kMeta || r1.overflow) || r1.empty == 0u);
+        KvOut r2{-1, 0ull, false, 0u};
+        if (__any_sync(kFull, check2)) r2 = place_probe<KB, SB>(p2, k, check2, p.second, D.d, stage);
         bool pend = false, ins = false;
         if (found1) {
             T::exch(slot_ptr<KB, SB>(p1, r1.match), e);
