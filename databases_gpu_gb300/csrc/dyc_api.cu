@@ -365,7 +365,7 @@ dyc_status resize_down_impl(dyc_table *t, cudaStream_t s) {
         e = KB_CALL(t, collect, ctx(t, s), t->sb, old, onb, la, &t->d_ctr->pending, list_cap,
                     &t->d_ctr->spill);
         // keys of other subtables may have had their first-probe bucket here:
-        // start every new bucket with its overflow bit set
+        // start every new bucket with all fingerprint bits set
         if (e == cudaSuccess) e = KB_CALL(t, mark_all, ctx(t, s), t->sb, nw, nnb);
     }
     if (e != cudaSuccess) return fail(DYC_ECUDA, "downsize kernel: %s", cudaGetErrorString(e));
@@ -1611,7 +1611,7 @@ dyc_status dyc_snapshot(dyc_table *t, void *h_buf, uint64_t buf_bytes, void *str
     dyc_snapshot_header h;
     memset(&h, 0, sizeof(h));
     memcpy(h.magic, "DYCSNAP1", 8);
-    h.version = 1;
+    h.version = 2;
     h.header_bytes = sizeof(h);
     h.key_bytes = t->cfg.key_bytes;
     h.value_bytes = t->cfg.value_bytes;
@@ -1645,8 +1645,8 @@ dyc_status dyc_restore(const void *h_buf, uint64_t buf_bytes, int32_t device, dy
     dyc_snapshot_header h;
     if (buf_bytes < sizeof(h)) return fail(DYC_EINVAL, "snapshot shorter than its header");
     memcpy(&h, h_buf, sizeof(h));
-    if (memcmp(h.magic, "DYCSNAP1", 8) != 0 || h.version != 1 || h.header_bytes != sizeof(h))
-        return fail(DYC_EINVAL, "not a version-1 DyCuckoo snapshot");
+    if (memcmp(h.magic, "DYCSNAP1", 8) != 0 || h.version != 2 || h.header_bytes != sizeof(h))
+        return fail(DYC_EINVAL, "not a version-2 DyCuckoo snapshot");
     dyc_config c;
     dyc_config_default(&c);
     c.key_bytes = h.key_bytes;

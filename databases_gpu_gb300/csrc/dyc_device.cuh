@@ -260,14 +260,21 @@ __device__ __forceinline__ void ld_ca(const void *p, uint32_t (&w)[8]) {
 // of the group reads chunk r), so a warp instruction fetches 32/kG whole
 // buckets and every DRAM line it touches is used in full.
 //
-// A 128-byte bucket keeps its last slot as a metadata word; bit 0 (the
-// overflow bit) is set once any key whose first-probe bucket this is has been
-// stored in its second bucket. While it is clear, a key missing from this
-// bucket is missing from the table, and a find or erase stops after one
-// probe. Bits are only ever set (erase leaves them), so a set bit is a hint
-// that costs one extra probe, never a wrong answer.
+// A 128-byte bucket keeps its last slot as a metadata word of displacement
+// fingerprints: bit fp(k) of its low 64 bits is set once a key k whose
+// first-probe bucket this is has been stored in its second bucket, with fp(k)
+// the top 6 bits of fold(k) * 0x9E3779B1 (bits the bucket index does not
+// use). While k's bit is clear, k missing from this bucket is missing from the
+// table, so a find or erase stops after one probe; a single "something was
+// displaced" bit, set in most buckets at load factor 0.9, sent nearly every
+// miss to a second line. Bits are only ever set (erase leaves them, a full
+// rehash sets all), so a set bit is a hint that costs one extra probe, never a
+// wrong answer.
 // ----------------------------------------------------------------------------
-constexpr unsigned long long kOverflowBit = 1ull;
+__host__ __device__ __forceinline__ unsigned long long fp_bit(uint32_t hk) {
+    return 1ull << ((hk * 0x9E3779B1u) >> 26);
+}
+constexpr unsigned long long kAllFingerprints = ~0ull;
 
 template <int KB, int SB> struct Geo {
     using T = SlotT<KB>;

@@ -172,7 +172,7 @@ template <int KB> struct Ops {
                                 const unsigned long long *src_count, void *dst, uint32_t *dst_tid,
                                 unsigned long long *dst_count, uint64_t dst_cap,
                                 uint32_t max_evict, Counters *gctr, uint64_t max_entries);
-    // set the overflow bit of every bucket of a subtable
+    // set every fingerprint bit of every bucket of a subtable
     static cudaError_t mark_all(const LaunchCtx &L, int sb, void *sub, uint32_t nb);
     static cudaError_t export_all(const LaunchCtx &L, const Desc &D, int sb, void *keys,
                                   void *vals, uint32_t vb, uint64_t cap,

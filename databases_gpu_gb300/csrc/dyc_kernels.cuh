@@ -75,10 +75,11 @@ __device__ __forceinline__ char *first_bucket(const Desc &D, typename SlotT<KB>:
     return bucket_ptr<KB, SB>(D, pr.first, bucket_index(D, pr.first, hk));
 }
 
-// Mark the entry's first-probe bucket before storing it anywhere else.
+// Set the entry's fingerprint in its first-probe bucket before storing it
+// anywhere else (hk = fold(key)).
 template <int KB, int SB>
-__device__ __forceinline__ void mark_overflow(char *first) {
-    if (Geo<KB, SB>::kMeta) atomicOr(meta_ptr<KB, SB>(first), kOverflowBit);
+__device__ __forceinline__ void mark_overflow(char *first, uint32_t hk) {
+    if (Geo<KB, SB>::kMeta) atomicOr(meta_ptr<KB, SB>(first), fp_bit(hk));
 }
 
 // ----------------------------------------------------------------------------
@@ -335,7 +336,9 @@ __device__ __forceinline__ KvOut probe_staged(const char *p, typename SlotT<KB>:
                 }
                 if (WANT_EMPTY && T::is_empty(sl)) out.empty |= 1u << idx;
             } else if (Gm::kMeta && idx == Gm::kTotal - 1) {
-                out.overflow = (v[j * (T::kBytes / 4)] & 1u) != 0u;
+                const unsigned long long meta = (unsigned long long)v[j * (T::kBytes / 4)] |
+                                                ((unsigned long long)v[j * (T::kBytes / 4) + 1] << 32);
+                out.overflow = (meta & fp_bit(fold(key))) != 0ull;  // key's fingerprint
             }
         }
     }
@@ -375,7 +378,7 @@ __device__ __forceinline__ KvOut place_probe(const char *p, typename SlotT<KB>::
         KvOut o;
         o.match = r.match;
         o.value = 0ull;
-        o.overflow = (r.meta & kOverflowBit) != 0ull;
+        o.overflow = (r.meta & fp_bit(fold(key))) != 0ull;
         o.empty = r.empty;
         return o;
     }
@@ -558,7 +561,7 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
         } else if (act) {
             bool ok = claim_empty<KB, SB>(p1, r1.empty, e);
             if (!ok && check2 && r2.empty) {
-                mark_overflow<KB, SB>(p1);
+                mark_overflow<KB, SB>(p1, hk);
                 ok = claim_empty<KB, SB>(p2, r2.empty, e);
             }
             if (ok) ++n_ins;
@@ -630,7 +633,7 @@ __global__ void __launch_bounds__(256) k_walk(const __grid_constant__ Desc D,
             if (!live) continue;
             bool placed = false;
             if (r.empty) {
-                if (t != pe.first) mark_overflow<KB, SB>(fb);
+                if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
                 placed = claim_empty<KB, SB>(bp, r.empty, e);
             }
             if (placed) {
@@ -651,7 +654,7 @@ __global__ void __launch_bounds__(256) k_walk(const __grid_constant__ Desc D,
                 fail = true;
             } else {
                 const int j = pick_victim<KB, SB>(r.pref, hk + evictions);
-                if (t != pe.first) mark_overflow<KB, SB>(fb);
+                if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
                 const Sl old = T::exch(slot_ptr<KB, SB>(bp, j), e);
                 ++evictions;
                 ++n_steps;
@@ -1010,7 +1013,7 @@ template <int KB, int SB>
 __global__ void __launch_bounds__(256) k_mark_all(char *__restrict__ sub, uint32_t nb) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nb; j += stride)
-        if (Geo<KB, SB>::kMeta) *meta_ptr<KB, SB>(sub + j * SB) = kOverflowBit;
+        if (Geo<KB, SB>::kMeta) *meta_ptr<KB, SB>(sub + j * SB) = kAllFingerprints;
 }
 
 // every live (key, value) of one subtable

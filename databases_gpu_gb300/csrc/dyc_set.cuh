@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(256) k_set_place(const Desc *__restrict__ desc
         } else if (act) {
             bool ok = claim_empty<KB, SB>(p1, r1.empty, e);
             if (!ok && check2 && r2.empty) {
-                mark_overflow<KB, SB>(p1);
+                mark_overflow<KB, SB>(p1, hk);
                 ok = claim_empty<KB, SB>(p2, r2.empty, e);
             }
             if (ok) {
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
             if (!live) continue;
             bool placed = false;
             if (r.empty) {
-                if (t != pe.first) mark_overflow<KB, SB>(fb);
+                if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
                 placed = claim_empty<KB, SB>(bp, r.empty, e);
             }
             if (placed) {
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
                 fail = true;
             } else {
                 const int j = pick_victim<KB, SB>(r.pref, hk + evictions);
-                if (t != pe.first) mark_overflow<KB, SB>(fb);
+                if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
                 const Sl old = T::exch(slot_ptr<KB, SB>(bp, j), e);
                 ++evictions;
                 ++n_steps;

@@ -149,8 +149,9 @@ dyc_status dyc_layout(dyc_table *t, uint32_t *nbuckets_out, uint32_t *num_subtab
  * table.table[i], cuckoo.h:42). Slots are bucket_bytes/slot_bytes per
  * bucket; a 4-byte-key slot is key | value << 32, an 8-byte-key slot is
  * {key, value} (16 bytes). In 128-byte buckets the last slot is a metadata
- * word, not an entry (bit 0: some key whose first-probe bucket this is lives
- * in its second bucket). */
+ * word, not an entry: bit f of its low 64 bits is set once some key k whose
+ * first-probe bucket this is, with f = (fold(k) * 0x9E3779B1 mod 2^32) >> 26,
+ * was stored in its second bucket (fold(k) = k for 4-byte keys). */
 dyc_status dyc_subtable(dyc_table *t, uint32_t i, void **d_ptr, uint64_t *bytes);
 
 /* Every live (key, value) into d_keys_out / d_vals_out (no order), at most
@@ -243,7 +244,7 @@ dyc_status dyc_wide_last_stats(dyc_wide *w, dyc_op_stats *out);
  * diagnostics, api.cpp:221-242). Little-endian; widths are fixed. */
 typedef struct dyc_snapshot_header {
     char magic[8];              /* "DYCSNAP1" */
-    uint32_t version;           /* 1 */
+    uint32_t version;           /* 2 (metadata words hold displacement fingerprints) */
     uint32_t header_bytes;      /* 256 */
     uint32_t key_bytes, value_bytes, bucket_bytes, num_subtables;
     uint32_t max_evictions, auto_resize;
@@ -266,7 +267,7 @@ dyc_status dyc_snapshot_bytes(dyc_table *t, uint64_t *bytes);
 dyc_status dyc_snapshot(dyc_table *t, void *h_buf, uint64_t buf_bytes, void *stream);
 
 /* A new table on `device` from a snapshot. DYC_EINVAL (and no table) when
- * the header is malformed, the buffer is short or the checksum of the
+ * the header is malformed (or of another version), the buffer is short or the checksum of the
  * restored subtables does not match. */
 dyc_status dyc_restore(const void *h_buf, uint64_t buf_bytes, int32_t device, dyc_table **out);
 

@@ -119,7 +119,7 @@ def _snap_header(**over):
     u32 = h.view(np.uint32)
     u64 = h.view(np.uint64)
     f64 = h.view(np.float64)
-    u32[2], u32[3] = 1, 256
+    u32[2], u32[3] = 2, 256
     u32[4:10] = [4, 4, 128, 4, 64, 1]          # widths, bucket, d, bound, auto
     u64[5], u64[6] = 0, 4 * 2 * 15             # size, capacity
     f64[7], f64[8] = 0.8, 0.5
@@ -137,7 +137,7 @@ def test_restore_rejects_malformed_snapshots_before_any_device_call():
     h = C.c_void_p()
     good = np.concatenate([_snap_header(), np.zeros(1024, np.uint8)])
     bad = [np.zeros(100, np.uint8),                                   # shorter than a header
-           np.concatenate([_snap_header(u32_2=2), np.zeros(1024, np.uint8)]),   # version
+           np.concatenate([_snap_header(u32_2=1), np.zeros(1024, np.uint8)]),   # version
            np.concatenate([_snap_header(u32_4=3), np.zeros(1024, np.uint8)]),   # key width
            np.concatenate([_snap_header(u64_14=999), np.zeros(1024, np.uint8)]),  # payload
            np.concatenate([_snap_header(u64_5=10 ** 6), np.zeros(1024, np.uint8)]),  # size > slots

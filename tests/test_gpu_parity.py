@@ -176,9 +176,17 @@ def test_first_probe_serves_most_hits(bucket_bytes, floor):
     t.close()
 
 
+def _fp_bit(keys: np.ndarray) -> np.ndarray:
+    """Displacement fingerprint bit of 4-byte keys: 1 << ((k * 0x9E3779B1 mod
+    2^32) >> 26)."""
+    with np.errstate(over="ignore"):
+        f = (keys.astype(np.uint32) * np.uint32(0x9E3779B1)) >> np.uint32(26)
+    return np.uint64(1) << f.astype(np.uint64)
+
+
 def _check_overflow_bits(t, d=4):
-    """Every key stored in its second bucket has the overflow bit set on its
-    first-probe bucket (128-byte buckets)."""
+    """Every key stored in its second bucket has its fingerprint bit set in
+    the metadata word of its first-probe bucket (128-byte buckets)."""
     nb = t.layout()
     metas = [t.subtable(s, with_meta=True)[:, -1] for s in range(d)]
     bad = 0
@@ -194,7 +202,7 @@ def _check_overflow_bits(t, d=4):
         for ft in range(d):
             sel = second & (first_t == ft)
             if sel.any():
-                bits = metas[ft][first_b[sel]] & np.uint64(1)
+                bits = metas[ft][first_b[sel]] & _fp_bit(rk[sel])
                 bad += int((bits == 0).sum())
     return bad
 
