@@ -232,7 +232,7 @@ def run_reference(args):
     value = args.steps * sample / total / 1e6
     line = {
         "metric": "find Mops/s", "impl": "reference", "value": round(value, 2), "unit": "Mops/s",
-        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": workload_config(args, lf=None),
