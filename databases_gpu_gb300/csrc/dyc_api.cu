@@ -816,7 +816,6 @@ namespace {
 // arrays.
 dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t ntables,
                        void **buf, size_t *buf_bytes, dyc::ApplyScratch *out) {
-    const uint64_t blocks = (ops + dyc::kSortTile - 1) / dyc::kSortTile;
     const bool multi = ntables > 0;
     const size_t K = (size_t)kb, V = (size_t)vb;
     const size_t CB = kb == 4 ? 8 : 16;  // cell bytes
@@ -825,9 +824,8 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
         ops * 4, ops * K, ops * 4, ops * 8,           // op_cell, dkey, dcnt, dseg
         ops * 4, ops * V, (ops / 32 + 1) * 4,         // seg, pre_val, pre_hit
         ops * K, ops * V, ops * K,                    // up_key, up_val, er_key
-        dyc::kCtrSlots * 8, ops * 4, ops * 4, ops * 4,  // ctr, wseg, mid, giant
-        ops * 4, ops * 4, ops * 4, ops * 4,           // sort buffers
-        blocks * 256 * 4, ops * 4,                    // hist, seg_start
+        dyc::kCtrSlots * 8, ops * 4, ops * 4,         // ctr, wseg, mid
+        ops * 4,                                      // sort_tmp
         multi ? ops * 4 : 0,                          // dtid
         multi ? ops * 4 : 0, multi ? ops * 4 : 0,     // up_tid, er_tid
         multi ? (size_t)ntables * 4 : 0,              // tnew
@@ -865,13 +863,7 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
     A.ctr = (unsigned long long *)carve();
     A.wseg = (uint32_t *)carve();
     A.mid = (uint32_t *)carve();
-    A.giant = (uint32_t *)carve();
-    A.sort_key = (uint32_t *)carve();
-    A.sort_val = (uint32_t *)carve();
-    A.sort_key2 = (uint32_t *)carve();
-    A.sort_val2 = (uint32_t *)carve();
-    A.hist = (uint32_t *)carve();
-    A.seg_start = (uint32_t *)carve();
+    A.sort_tmp = (uint32_t *)carve();
     A.dtid = (uint32_t *)carve();
     A.up_tid = (uint32_t *)carve();
     A.er_tid = (uint32_t *)carve();
@@ -918,13 +910,6 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     if (e == cudaSuccess) e = KB_CALL(t, apply_replay, L, A, ops, vals, vb, vals_out, bits_out, n, nd);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "apply replay kernels: %s", cudaGetErrorString(e));
     TRY(read_apply_counters(t, s));
-    if (t->h_actr[dyc::kCtrGiant]) {
-        e = KB_CALL(t, apply_giant, L, A, ops, vals, vb, vals_out, bits_out, n, nd,
-                    t->h_actr[dyc::kCtrGiant]);
-        if (e != cudaSuccess)
-            return fail(DYC_ECUDA, "apply giant-segment kernels: %s", cudaGetErrorString(e));
-        TRY(read_apply_counters(t, s));
-    }
     const uint64_t nu = t->h_actr[dyc::kCtrUp], ne = t->h_actr[dyc::kCtrEr];
     if (ne) TRY(erase_chunk(t, A.er_key, ne, nullptr, DYC_FLAG_UNIQUE, s));
     if (nu) {
@@ -1424,14 +1409,6 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
         return set_phase_a(s, d_offsets, d_ops, d_keys, d_vals, d_vals_out, d_bits_out, n, st);
     }));
     CK(cudaStreamSynchronize(st));
-    const uint64_t nd = s->h_actr[dyc::kCtrDistinct], ng = s->h_actr[dyc::kCtrGiant];
-    if (ng) {
-        cudaError_t e = SET_KB_CALL(s, apply_giant, LaunchCtx{s->sms, st, (int)s->blocks_per_sm}, s->A, d_ops, d_vals,
-                                    (uint32_t)s->vb, d_vals_out, d_bits_out, n, nd, ng);
-        if (e != cudaSuccess) return fail(DYC_ECUDA, "giant-segment kernels: %s", cudaGetErrorString(e));
-        CK(cudaMemcpyAsync(s->h_tnew, s->A.tnew, (size_t)s->ntables * 4, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-    }
     // upsize before the inserts where the keys the batch adds would pass the
     // upper load bound (hash_insert_batch, api.cpp:359-369, per table)
     bool moved = false;

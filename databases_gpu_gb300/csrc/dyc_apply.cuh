@@ -16,10 +16,10 @@
 //    distinct key)
 //   replay  : one thread per distinct key replays a segment of at most
 //             kShortSeg ops after sorting it in registers; longer segments are
-//             sorted in shared memory and replayed by a warp (up to kWarpSeg
-//             ops) or by one block (up to kMidSeg), giant ones after a stable
-//             radix sort of the batch. Every op's result is written; keys
-//             whose state changed are listed as erases or upserts.
+//             sorted and replayed by a warp (up to kWarpSeg ops) or by one
+//             block (any length: shared-memory sort, merged in global memory
+//             beyond kMidSeg). Every op's result is written; keys whose state
+//             changed are listed as erases or upserts.
 //   (the table's erase and insert kernels apply the lists)
 // Only the lists touch the table, each key at most once, so the usual
 // insert/erase phases keep their guarantees. Counts the kernels need are read
@@ -34,7 +34,7 @@ enum : uint8_t { kOpFind = 0, kOpInsert = 1, kOpErase = 2 };
 
 constexpr uint32_t kShortSeg = 8;    // segments replayed by one thread
 constexpr uint32_t kWarpSeg = 256;   // segments sorted and replayed by one warp
-constexpr uint32_t kMidSeg = 4096;   // segments sorted in shared memory by one block
+constexpr uint32_t kMidSeg = 4096;   // longest segment sorted in shared memory alone
 constexpr uint32_t kNoCell = 0xffffffffu;
 
 // Cells: 4-byte keys {key (low word), count (high word)} in one 64-bit word;
@@ -330,7 +330,7 @@ __device__ __forceinline__ void replay_op(uint8_t op, uint64_t inval, bool &pres
     }
 }
 
-// Final state of distinct key d, recorded by one thread (warp, mid and giant
+// Final state of distinct key d, recorded by one thread (warp and block
 // paths).
 template <int KB>
 __device__ __forceinline__ void record_final_one(const ApplyScratch &A, uint32_t d, bool present,
@@ -415,15 +415,13 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
     // the block_alloc call
     for (uint64_t d0 = (uint64_t)blockIdx.x * blockDim.x; d0 < nd; d0 += stride) {
         const uint64_t d = d0 + threadIdx.x;
-        bool up = false, er = false, wp = false, md = false, gi = false, fresh = false;
+        bool up = false, er = false, wp = false, md = false, fresh = false;
         K k = 0;
         uint64_t value = 0ull;
         uint32_t tid = 0u;
         if (d < nd) {
             const uint32_t cnt = A.dcnt[d];
-            if (cnt > kMidSeg) {
-                gi = true;
-            } else if (cnt > kWarpSeg) {
+            if (cnt > kWarpSeg) {
                 md = true;
             } else if (cnt > kShortSeg) {
                 wp = true;
@@ -468,7 +466,6 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
                            (unsigned long long)up | ((unsigned long long)er << 16) |
                                ((unsigned long long)wp << 32) | ((unsigned long long)md << 48),
                            got);
-        const unsigned long long gpos = agg_inc(&A.ctr[kCtrGiant], gi);  // rare
         if (A.tnew) warp_count_by(A.tnew, tid, fresh);
         if (up) {
             ((K *)A.up_key)[got[0]] = k;
@@ -482,8 +479,6 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
             A.wseg[got[2]] = (uint32_t)d;
         } else if (md) {
             A.mid[got[3]] = (uint32_t)d;
-        } else if (gi) {
-            A.giant[gpos] = (uint32_t)d;
         }
     }
 }
@@ -573,8 +568,12 @@ __global__ void __launch_bounds__(256) k_apply_replay_warp(const __grid_constant
     }
 }
 
-// Mid segments (kWarpSeg < ops <= kMidSeg): one block per segment sorts its
-// op indices in shared memory, then warp 0 replays them.
+// Block segments (more than kWarpSeg ops on one key): one block per segment.
+// Up to kMidSeg ops are sorted in shared memory; a longer segment is sorted
+// in kMidSeg chunks in shared memory and then merged in global memory, run
+// widths doubling, each element placed by its rank in the other run (op
+// indices are distinct, so ranks are exact), ping-ponging with the scratch
+// copy at the same offsets. Warp 0 replays the sorted segment.
 template <int KB>
 __global__ void __launch_bounds__(256) k_apply_replay_mid(const __grid_constant__ ApplyScratch A,
                                                           const uint8_t *__restrict__ ops,
@@ -583,160 +582,60 @@ __global__ void __launch_bounds__(256) k_apply_replay_mid(const __grid_constant_
                                                           uint32_t *__restrict__ bits_out) {
     __shared__ uint32_t s[kMidSeg];
     const uint64_t nmid = A.ctr[kCtrMid];
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
     for (uint64_t x = blockIdx.x; x < nmid; x += gridDim.x) {
         const uint32_t d = A.mid[x];
-        const uint32_t cnt = A.dcnt[d], off = seg_off(A, d);
-        uint32_t P = 2u * kWarpSeg;
-        while (P < cnt) P <<= 1;
-        for (uint32_t j = threadIdx.x; j < P; j += blockDim.x)
-            s[j] = j < cnt ? A.seg[off + j] : 0xffffffffu;
-        __syncthreads();
-        bitonic_sort(s, P, threadIdx.x, blockDim.x, [] { __syncthreads(); });
-        if (threadIdx.x < 32) {
+        const uint32_t cnt = A.dcnt[d], off = seg_off(A, d);  // cnt > kWarpSeg
+        const uint32_t *sorted = s;
+        if (cnt <= kMidSeg) {
+            uint32_t P = 2u * kWarpSeg;
+            while (P < cnt) P <<= 1;
+            for (uint32_t j = tid; j < P; j += nt) s[j] = j < cnt ? A.seg[off + j] : 0xffffffffu;
+            __syncthreads();
+            bitonic_sort(s, P, tid, nt, [] { __syncthreads(); });
+        } else {
+            uint32_t *src = A.seg + off, *dst = A.sort_tmp + off;
+            for (uint32_t c0 = 0; c0 < cnt; c0 += kMidSeg) {  // sorted chunks, in place
+                const uint32_t m = cnt - c0 < kMidSeg ? cnt - c0 : kMidSeg;
+                for (uint32_t j = tid; j < kMidSeg; j += nt) s[j] = j < m ? src[c0 + j] : 0xffffffffu;
+                __syncthreads();
+                bitonic_sort(s, kMidSeg, tid, nt, [] { __syncthreads(); });
+                for (uint32_t j = tid; j < m; j += nt) src[c0 + j] = s[j];
+                __syncthreads();
+            }
+            for (uint32_t w = kMidSeg; w < cnt; w *= 2) {  // merge runs of w into runs of 2w
+                for (uint32_t i = tid; i < cnt; i += nt) {
+                    const uint32_t r0 = i / (2 * w) * (2 * w);
+                    const uint32_t mid = r0 + w < cnt ? r0 + w : cnt;
+                    const uint32_t end = r0 + 2 * w < cnt ? r0 + 2 * w : cnt;
+                    const uint32_t v = src[i];
+                    // rank of v in the other run (elements smaller than v)
+                    uint32_t lo = i < mid ? mid : r0, hi = i < mid ? end : mid;
+                    const uint32_t base = lo;
+                    while (lo < hi) {
+                        const uint32_t m = (lo + hi) >> 1;
+                        if (src[m] < v) lo = m + 1;
+                        else hi = m;
+                    }
+                    const uint32_t own = i < mid ? i - r0 : i - mid;
+                    dst[r0 + own + (lo - base)] = v;
+                }
+                __syncthreads();
+                uint32_t *t = src;
+                src = dst;
+                dst = t;
+            }
+            sorted = src;
+        }
+        if (tid < 32) {
             const bool pre_present = (A.pre_hit[d >> 5] >> (d & 31)) & 1u;
             const uint64_t pre_value = load_val(A.pre_val, vb, d);
             bool present = pre_present;
             uint64_t value = pre_value;
-            warp_replay(s, cnt, present, value, ops, vals, vb, vals_out, bits_out);
-            if (threadIdx.x == 0)
-                record_final_one<KB>(A, d, present, value, pre_present, pre_value, vb);
+            warp_replay(sorted, cnt, present, value, ops, vals, vb, vals_out, bits_out);
+            if (tid == 0) record_final_one<KB>(A, d, present, value, pre_present, pre_value, vb);
         }
-        __syncthreads();  // s is reused by the next segment
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Giant segments (more than kMidSeg ops on one key). A stable LSD radix sort
-// of (distinct id, op index) pairs by distinct id -- the input is in
-// op-index order, so stability keeps every segment in op-index order; ops of
-// other keys sort last -- and one warp per giant segment replays it.
-// ---------------------------------------------------------------------------
-template <int KB>
-__global__ void __launch_bounds__(256) k_apply_sort_init(const __grid_constant__ ApplyScratch A,
-                                                         uint64_t n) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint32_t cell = A.op_cell[i];
-        uint32_t key = 0xffffffffu;
-        if (cell != kNoCell) {
-            const uint32_t d = *cell_word<KB>(A.cells, cell);
-            if (A.dcnt[d] > kMidSeg) key = d;
-        }
-        A.sort_key[i] = key;
-        A.sort_val[i] = (uint32_t)i;
-    }
-}
-
-template <int KB>
-__global__ void __launch_bounds__(256) k_radix_hist(const uint32_t *__restrict__ key, uint64_t n,
-                                                    int shift, uint32_t *__restrict__ hist) {
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0u;
-    __syncthreads();
-    const uint64_t base = (uint64_t)blockIdx.x * kSortTile;
-    for (int j = 0; j < kSortTile / 256; ++j) {
-        const uint64_t i = base + (uint64_t)j * 256 + threadIdx.x;
-        if (i < n) atomicAdd(&h[(key[i] >> shift) & 255u], 1u);
-    }
-    __syncthreads();
-    hist[(uint64_t)threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
-}
-
-// exclusive scan of m counts in place, one block of 1024 threads
-template <int KB>
-__global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t *__restrict__ v, uint64_t m) {
-    __shared__ uint32_t part[1024];
-    const uint64_t per = (m + 1023) / 1024;
-    const uint64_t lo = per * threadIdx.x, hi = lo + per < m ? lo + per : m;
-    uint32_t sum = 0u;
-    for (uint64_t i = lo; i < hi; ++i) sum += v[i];
-    part[threadIdx.x] = sum;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const uint32_t x = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += x;
-        __syncthreads();
-    }
-    uint32_t run = part[threadIdx.x] - sum;  // exclusive prefix of this thread's range
-    for (uint64_t i = lo; i < hi; ++i) {
-        const uint32_t c = v[i];
-        v[i] = run;
-        run += c;
-    }
-}
-
-// stable scatter: rounds of 256 elements in order; ranks among equal digits
-// come from match_any within a warp and per-warp digit counts across warps
-template <int KB>
-__global__ void __launch_bounds__(256) k_radix_scatter(const uint32_t *__restrict__ key,
-                                                       const uint32_t *__restrict__ val, uint64_t n,
-                                                       int shift, const uint32_t *__restrict__ hist,
-                                                       uint32_t *__restrict__ okey,
-                                                       uint32_t *__restrict__ oval) {
-    __shared__ uint32_t run[256];
-    __shared__ uint32_t wcnt[8][256];
-    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    run[tid] = hist[(uint64_t)tid * gridDim.x + blockIdx.x];
-    const uint64_t base = (uint64_t)blockIdx.x * kSortTile;
-    for (int j = 0; j < kSortTile / 256; ++j) {
-        for (int q = 0; q < 8; ++q) wcnt[q][tid] = 0u;
-        __syncthreads();
-        const uint64_t i = base + (uint64_t)j * 256 + tid;
-        const bool valid = i < n;
-        const uint32_t k = valid ? key[i] : 0u;
-        const uint32_t dg = valid ? (k >> shift) & 255u : 256u + (uint32_t)lane;  // invalid: unique
-        const unsigned peers = __match_any_sync(kFull, dg);
-        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-        if (valid && rank == 0) wcnt[w][dg] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            uint32_t before = 0u;
-            for (int q = 0; q < w; ++q) before += wcnt[q][dg];
-            const uint32_t pos = run[dg] + before + rank;
-            okey[pos] = k;
-            oval[pos] = val[i];
-        }
-        __syncthreads();
-        uint32_t tot = 0u;
-        for (int q = 0; q < 8; ++q) tot += wcnt[q][tid];
-        run[tid] += tot;
-        __syncthreads();
-    }
-}
-
-template <int KB>
-__global__ void __launch_bounds__(256) k_apply_seg_start(const __grid_constant__ ApplyScratch A,
-                                                         const uint32_t *__restrict__ skey,
-                                                         uint64_t n) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
-        const uint32_t d = skey[p];
-        if (d != 0xffffffffu && (p == 0 || skey[p - 1] != d)) A.seg_start[d] = (uint32_t)p;
-    }
-}
-
-template <int KB>
-__global__ void __launch_bounds__(256) k_apply_replay_giant(const __grid_constant__ ApplyScratch A,
-                                                            const uint32_t *__restrict__ sval,
-                                                            const uint8_t *__restrict__ ops,
-                                                            const void *__restrict__ vals,
-                                                            uint32_t vb,
-                                                            void *__restrict__ vals_out,
-                                                            uint32_t *__restrict__ bits_out) {
-    const uint64_t ngiant = A.ctr[kCtrGiant];
-    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t x = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; x < ngiant;
-         x += warps) {
-        const uint32_t d = A.giant[x];
-        const bool pre_present = (A.pre_hit[d >> 5] >> (d & 31)) & 1u;
-        const uint64_t pre_value = load_val(A.pre_val, vb, d);
-        bool present = pre_present;
-        uint64_t value = pre_value;
-        warp_replay(sval + A.seg_start[d], A.dcnt[d], present, value, ops, vals, vb, vals_out,
-                    bits_out);
-        if ((threadIdx.x & 31) == 0)
-            record_final_one<KB>(A, d, present, value, pre_present, pre_value, vb);
+        __syncthreads();  // s and the scratch run are reused by the next segment
     }
 }
 

@@ -69,10 +69,7 @@ struct ApplyScratch {
     unsigned long long *ctr;   // see kCtr*
     uint32_t *wseg;            // distinct ids of segments replayed by a warp
     uint32_t *mid;             // distinct ids of segments replayed by a block
-    uint32_t *giant;           // distinct ids of longer segments
-    uint32_t *sort_key, *sort_val, *sort_key2, *sort_val2;  // radix sort buffers
-    uint32_t *hist;            // 256 x blocks digit counts
-    uint32_t *seg_start;       // start of each distinct key in the sorted order
+    uint32_t *sort_tmp;        // merge scratch of long segments (same offsets as seg)
     uint64_t cap_cells;        // >= 2 * cap_ops
     uint64_t cap_ops;
     // multi-table batches
@@ -89,14 +86,11 @@ enum : int {
     kCtrPlaced = 1,    // ops given a segment slot
     kCtrUp = 2,        // upserts listed
     kCtrEr = 3,        // erases listed
-    kCtrGiant = 4,     // giant segments
-    kCtrMid = 5,       // mid segments
-    kCtrWarp = 6,      // warp segments
+    kCtrMid = 4,       // block segments
+    kCtrWarp = 5,      // warp segments
     kCtrSlots = 8
 };
 
-// radix-sort elements per block per pass (256 threads x 16)
-constexpr int kSortTile = 4096;
 
 
 // Launch parameters picked once per kernel from the occupancy calculator.
@@ -140,8 +134,7 @@ template <int KB> struct Ops {
                                void *list, unsigned long long *list_count, uint64_t list_cap,
                                unsigned long long *spill);
     // mixed batches (dyc_apply.cuh). One table: apply_group (group +
-    // compact), apply_scatter, find of the distinct keys, apply_replay (short
-    // and mid segments), apply_giant when a key has more than kMidSeg ops.
+    // compact), apply_scatter, find of the distinct keys, apply_replay.
     // Many tables (dyc_set.cuh): set_group replaces apply_group and the
     // set_* probe kernels replace find / erase / place / walk.
     static cudaError_t apply_group(const LaunchCtx &L, const ApplyScratch &A, const void *keys,
@@ -150,10 +143,6 @@ template <int KB> struct Ops {
     static cudaError_t apply_replay(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
                                    const void *vals, uint32_t vb, void *vals_out,
                                    uint32_t *bits_out, uint64_t n, uint64_t max_distinct);
-    static cudaError_t apply_giant(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
-                                  const void *vals, uint32_t vb, void *vals_out,
-                                  uint32_t *bits_out, uint64_t n, uint64_t n_distinct,
-                                  uint64_t n_giant);
     static cudaError_t set_group(const LaunchCtx &L, const ApplyScratch &A, const uint32_t *off,
                                  const void *keys, uint64_t n);
     static cudaError_t set_find(const LaunchCtx &L, const Desc *descs, int sb, const void *keys,

@@ -197,38 +197,6 @@ cudaError_t Ops<KB>::apply_replay(const LaunchCtx &L, const ApplyScratch &A, con
 }
 
 template <int KB>
-cudaError_t Ops<KB>::apply_giant(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
-                                 const void *vals, uint32_t vb, void *vals_out,
-                                 uint32_t *bits_out, uint64_t n, uint64_t n_distinct,
-                                 uint64_t n_giant) {
-    if (n == 0 || n_giant == 0) return cudaSuccess;
-    auto si = k_apply_sort_init<KB>;
-    si<<<grid_for((const void *)si, L, n), 256, 0, L.stream>>>(A, n);
-    const unsigned blocks = (unsigned)((n + kSortTile - 1) / kSortTile);
-    uint32_t *k0 = A.sort_key, *v0 = A.sort_val, *k1 = A.sort_key2, *v1 = A.sort_val2;
-    // digits up to the highest bit of a distinct id (0xffffffff, "no giant
-    // key", sorts after every id on these digits)
-    int bits = 1;
-    while (bits < 32 && (n_distinct >> bits) != 0) ++bits;
-    for (int shift = 0; shift < bits; shift += 8) {
-        k_radix_hist<KB><<<blocks, 256, 0, L.stream>>>(k0, n, shift, A.hist);
-        k_scan_exclusive<KB><<<1, 1024, 0, L.stream>>>(A.hist, (uint64_t)blocks * 256);
-        k_radix_scatter<KB><<<blocks, 256, 0, L.stream>>>(k0, v0, n, shift, A.hist, k1, v1);
-        uint32_t *tk = k0, *tv = v0;
-        k0 = k1;
-        v0 = v1;
-        k1 = tk;
-        v1 = tv;
-    }
-    auto ss = k_apply_seg_start<KB>;
-    ss<<<grid_for((const void *)ss, L, n), 256, 0, L.stream>>>(A, k0, n);
-    auto rg = k_apply_replay_giant<KB>;
-    rg<<<grid_for((const void *)rg, L, n_giant * 32), 256, 0, L.stream>>>(A, v0, ops, vals, vb,
-                                                                          vals_out, bits_out);
-    return cudaGetLastError();
-}
-
-template <int KB>
 cudaError_t Ops<KB>::set_group(const LaunchCtx &L, const ApplyScratch &A, const uint32_t *off,
                                const void *keys, uint64_t n) {
     k_set_cells<KB><<<1, 1024, 0, L.stream>>>(A, off);
