@@ -37,7 +37,7 @@ class DycConfig(C.Structure):
 class DycOpStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "inserted", "updated", "erased", "rejected", "superseded", "evict_steps",
-        "overflowed", "resizes_up", "resizes_down")]
+        "overflowed", "resizes_up", "resizes_down", "split_phases")]
 
     def as_dict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
@@ -51,11 +51,14 @@ class DycServerConfig(C.Structure):
 class DycServerStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "requests", "ops", "steps", "deferred", "rejected", "max_step_ops", "device_bytes")] + \
-        [("busy_seconds", C.c_double)]
+        [("busy_seconds", C.c_double), ("resizes_up", C.c_uint64), ("resizes_down", C.c_uint64),
+         ("resize_step_seconds", C.c_double), ("assemble_seconds", C.c_double),
+         ("exec_idle_seconds", C.c_double), ("upload_late_steps", C.c_uint64),
+         ("split_steps", C.c_uint64)]
 
     def as_dict(self):
-        return {n: (float if n == "busy_seconds" else int)(getattr(self, n))
-                for n, _ in self._fields_}
+        return {n: (float if t is C.c_double else int)(getattr(self, n))
+                for n, t in self._fields_}
 
 
 EXPORTS = [

@@ -1047,6 +1047,7 @@ extern "C" dyc_status dyc_erase_noalloc(dyc_table *t, const void *d_keys, uint64
 // dyc_tables whose counters live in one set-owned array, so resizes,
 // overflow handling and single-table calls reuse the code above.
 // =============================================================================
+#include <algorithm>
 #include <vector>
 
 struct dyc_set {
@@ -1065,14 +1066,23 @@ struct dyc_set {
     void *list_a = nullptr, *list_b = nullptr;
     uint32_t *tid_a = nullptr, *tid_b = nullptr;
     uint64_t list_cap = 0;
-    unsigned long long *h_actr = nullptr;  // pinned copy of A.ctr
     uint32_t *h_tnew = nullptr;            // pinned copy of A.tnew
     uint32_t *d_bits_tmp = nullptr;        // dyc_set_apply_each: one table's result bits
     size_t bits_tmp_words = 0;
-    // CUDA graphs of the two launch sequences, for the last call shape
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-    std::vector<uintptr_t> gkey;
-    bool gwarm = false;
+    // CUDA graphs of the launch sequences (phase A, phase B, both), one entry
+    // per buffer set: the kernels read the op count on the device and size
+    // their grids by the scratch capacity, so one graph serves any batch size
+    struct Graph {
+        std::vector<uintptr_t> key;
+        cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
+        bool warm = false;
+        uint64_t used = 0;
+    };
+    std::vector<Graph> graphs;
+    uint64_t graph_clock = 0;
+    cudaStream_t cap_stream = nullptr;  // capture stream (the caller's may be the legacy one)
+    cudaStream_t side = nullptr;        // replays that run beside the main sequence
+    cudaEvent_t fork = nullptr, join = nullptr;
     uint32_t blocks_per_sm = 0;  // launch cap of the set kernels (0: as many as fit)
     uint32_t max_evict_all = 0;  // largest member eviction bound
     dyc_op_stats last{};
@@ -1080,14 +1090,44 @@ struct dyc_set {
 
 namespace {
 
-void set_drop_graphs(dyc_set *s) {
-    for (auto &g : s->gexec)
-        if (g) {
-            cudaGraphExecDestroy(g);
-            g = nullptr;
+constexpr size_t kSetGraphs = 4;  // cached buffer sets (a server uses one per staging slot)
+
+void set_drop_graph(dyc_set::Graph &g) {
+    for (auto &x : g.exec)
+        if (x) {
+            cudaGraphExecDestroy(x);
+            x = nullptr;
         }
-    s->gkey.clear();
-    s->gwarm = false;
+    g.warm = false;
+}
+
+void set_drop_graphs(dyc_set *s) {
+    for (auto &g : s->graphs) set_drop_graph(g);
+    s->graphs.clear();
+}
+
+// The cache entry for this buffer set (least recently used one replaced).
+dyc_set::Graph *set_graph_for(dyc_set *s, std::vector<uintptr_t> &&key) {
+    ++s->graph_clock;
+    for (auto &g : s->graphs)
+        if (g.key == key) {
+            g.used = s->graph_clock;
+            return &g;
+        }
+    if (s->graphs.size() < kSetGraphs) {
+        s->graphs.emplace_back();
+    } else {
+        auto lru = std::min_element(s->graphs.begin(), s->graphs.end(),
+                                    [](const dyc_set::Graph &a, const dyc_set::Graph &b) {
+                                        return a.used < b.used;
+                                    });
+        set_drop_graph(*lru);
+        std::swap(*lru, s->graphs.back());
+    }
+    dyc_set::Graph &g = s->graphs.back();
+    g.key = std::move(key);
+    g.used = s->graph_clock;
+    return &g;
 }
 
 dyc_status set_push_descs(dyc_set *s, cudaStream_t st) {
@@ -1132,23 +1172,26 @@ dyc_status set_ensure_scratch(dyc_set *s, uint64_t n) {
 #define SET_KB_CALL(s, fn, ...) ((s)->kb == 4 ? Ops<4>::fn(__VA_ARGS__) : Ops<8>::fn(__VA_ARGS__))
 
 // Phase A: group, scatter, pre-batch find, replay; counters to the host.
+// Every kernel reads the op count from d_off[ntables] on the device; n (the
+// scratch capacity under a graph) only sizes the grids.
 dyc_status set_phase_a(dyc_set *s, const uint32_t *d_off, const uint8_t *ops, const void *keys,
-                       const void *vals, void *out, uint32_t *bits, uint64_t n, cudaStream_t st) {
+                       const void *vals, void *out, uint32_t *bits, uint64_t n, bool new_counts,
+                       cudaStream_t st) {
     const dyc::ApplyScratch &A = s->A;
-    const LaunchCtx L{s->sms, st, (int)s->blocks_per_sm};
+    const LaunchCtx L{s->sms, st, (int)s->blocks_per_sm, s->side, s->fork, s->join};
     const uint32_t vb = (uint32_t)s->vb;
-    CK(cudaMemsetAsync(A.ctr, 0, dyc::kCtrSlots * sizeof(unsigned long long), st));
-    if (bits) CK(cudaMemsetAsync(bits, 0, (size_t)((n + 31) / 32) * 4, st));
-    cudaError_t e = SET_KB_CALL(s, set_group, L, A, d_off, keys, n);
-    if (e == cudaSuccess) e = SET_KB_CALL(s, apply_scatter, L, A, n);
+    const uint32_t *d_n = d_off + s->ntables;
+    // also zeroes phase B's counters (nothing between the phases uses them)
+    cudaError_t e = SET_KB_CALL(s, set_group, L, A, d_off, keys, n, bits, s->d_gctr);
+    if (e == cudaSuccess) e = SET_KB_CALL(s, apply_scatter, L, A, n, d_n);
     if (e == cudaSuccess)
         e = SET_KB_CALL(s, set_find, L, s->d_desc, s->sb, A.dkey, A.dtid, &A.ctr[dyc::kCtrDistinct],
                         n, A.pre_val, vb, A.pre_hit);
-    if (e == cudaSuccess) e = SET_KB_CALL(s, apply_replay, L, A, ops, vals, vb, out, bits, n, n);
+    if (e == cudaSuccess)
+        e = SET_KB_CALL(s, apply_replay, L, A, ops, vals, vb, out, bits, n, n, d_n);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "set phase A kernels: %s", cudaGetErrorString(e));
-    CK(cudaMemcpyAsync(s->h_actr, A.ctr, dyc::kCtrSlots * sizeof(unsigned long long),
-                       cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(s->h_tnew, A.tnew, (size_t)s->ntables * 4, cudaMemcpyDeviceToHost, st));
+    if (new_counts)  // keys each table gains, for the upsize decision
+        CK(cudaMemcpyAsync(s->h_tnew, A.tnew, (size_t)s->ntables * 4, cudaMemcpyDeviceToHost, st));
     return DYC_OK;
 }
 
@@ -1156,13 +1199,10 @@ dyc_status set_phase_a(dyc_set *s, const uint32_t *d_off, const uint8_t *ops, co
 dyc_status set_phase_b(dyc_set *s, uint64_t n, cudaStream_t st) {
     const dyc::ApplyScratch &A = s->A;
     const LaunchCtx L{s->sms, st, (int)s->blocks_per_sm};
-    CK(cudaMemsetAsync(s->d_gctr, 0, sizeof(Counters), st));
-    cudaError_t e = SET_KB_CALL(s, set_erase, L, s->d_desc, s->d_tctr, s->sb, A.er_key, A.er_tid,
-                                &A.ctr[dyc::kCtrEr], n, s->d_gctr);
-    if (e == cudaSuccess)
-        e = SET_KB_CALL(s, set_place, L, s->d_desc, s->d_tctr, s->sb, A.up_key, A.up_val,
-                        (uint32_t)s->vb, A.up_tid, &A.ctr[dyc::kCtrUp], n, s->list_a, s->tid_a,
-                        s->list_cap, s->d_gctr);
+    cudaError_t e = SET_KB_CALL(s, set_mutate, L, s->d_desc, s->d_tctr, s->sb, A.er_key,
+                                A.er_tid, &A.ctr[dyc::kCtrEr], A.up_key, A.up_val,
+                                (uint32_t)s->vb, A.up_tid, &A.ctr[dyc::kCtrUp], n, s->list_a,
+                                s->tid_a, s->list_cap, s->d_gctr);
     if (e == cudaSuccess)
         e = SET_KB_CALL(s, set_walk, L, s->d_desc, s->d_tctr, s->sb, s->list_a, s->tid_a,
                         &s->d_gctr->pending, s->list_b, s->tid_b, &s->d_gctr->overflow,
@@ -1174,33 +1214,40 @@ dyc_status set_phase_b(dyc_set *s, uint64_t n, cudaStream_t st) {
     return DYC_OK;
 }
 
-// Run a phase directly, or through its captured graph when `graph` (captured
-// on the second call with the same shape, after one direct run has warmed the
-// launch-configuration caches).
+// Run a launch sequence issue(stream) directly on st, or through its
+// captured graph in entry g (captured on the second call with the same
+// buffers, after one direct run has warmed the launch-configuration caches).
+// Capture runs on the set's own stream, since the legacy default stream
+// cannot be captured; the graph is then launched on st.
 template <class F>
-dyc_status set_run(dyc_set *s, int which, bool graph, cudaStream_t st, F &&issue) {
-    if (!graph || !s->gwarm) return issue();
-    if (!s->gexec[which]) {
-        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        dyc_status r = issue();
-        cudaGraph_t g = nullptr;
-        cudaError_t e = cudaStreamEndCapture(st, &g);
+dyc_status set_run(dyc_set *s, dyc_set::Graph *g, int which, cudaStream_t st, F &&issue) {
+    if (!g || !g->warm) return issue(st);
+    if (!g->exec[which]) {
+        if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
+        const cudaStream_t cs = s->cap_stream;
+        CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        dyc_status r = issue(cs);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(cs, &graph);
         if (r != DYC_OK) {
-            if (g) cudaGraphDestroy(g);
+            if (graph) cudaGraphDestroy(graph);
             return r;
         }
         if (e != cudaSuccess) return fail(DYC_ECUDA, "stream capture: %s", cudaGetErrorString(e));
-        e = cudaGraphInstantiate(&s->gexec[which], g, 0);
-        cudaGraphDestroy(g);
+        e = cudaGraphInstantiate(&g->exec[which], graph, 0);
+        cudaGraphDestroy(graph);
         if (e != cudaSuccess) return fail(DYC_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
     }
-    CK(cudaGraphLaunch(s->gexec[which], st));
+    CK(cudaGraphLaunch(g->exec[which], st));
     return DYC_OK;
 }
 
 // Entries whose eviction walks reached the bound: place them per table after
 // an upsize of that table (never dropped).
-dyc_status set_overflow(dyc_set *s, uint64_t cnt, cudaStream_t st) {
+// Tables with grew[t] set were upsized by the policy after the batch: their
+// entries are placed without the extra upsize an overflow otherwise takes.
+dyc_status set_overflow(dyc_set *s, uint64_t cnt, const std::vector<uint8_t> &grew,
+                        cudaStream_t st) {
     const size_t slot = s->kb == 4 ? 8 : 16;
     std::vector<unsigned char> ent(cnt * slot);
     std::vector<uint32_t> tid(cnt);
@@ -1226,9 +1273,9 @@ dyc_status set_overflow(dyc_set *s, uint64_t cnt, cudaStream_t st) {
         CK(cudaMemcpyAsync(dv, hv.data(), c * s->vb, cudaMemcpyHostToDevice, st));
         TRY(ensure_scratch(m, c));
         int guard = 0;
-        do {
+        if (grew.empty() || !grew[t]) TRY(resize_up_impl(m, st));
+        while ((double)(m->size + c) > m->cfg.upper_load * (double)m->capacity && ++guard < 64)
             TRY(resize_up_impl(m, st));
-        } while ((double)(m->size + c) > m->cfg.upper_load * (double)m->capacity && ++guard < 64);
         TRY(insert_chunk(m, dk, dv, c, DYC_FLAG_UNIQUE | DYC_FLAG_NEW_KEYS, st));
         CK(cudaStreamSynchronize(st));  // hk / hv and the io buffer are reused
         s->last.resizes_up += m->last.resizes_up;
@@ -1291,8 +1338,10 @@ dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_desc, sizeof(Desc) * ntables);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_gctr, sizeof(Counters));
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_gctr, sizeof(Counters));
-    if (e == cudaSuccess) e = cudaMallocHost(&s->h_actr, dyc::kCtrSlots * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_tnew, sizeof(uint32_t) * ntables);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming);
     if (e != cudaSuccess) return undo(fail(DYC_ENOMEM, "set setup: %s", cudaGetErrorString(e)));
     memset(s->h_tctr, 0, sizeof(Counters) * ntables);
     s->tables.assign(ntables, nullptr);
@@ -1317,6 +1366,10 @@ dyc_status dyc_set_destroy(dyc_set *s) {
     cudaSetDevice(s->device);
     cudaDeviceSynchronize();
     set_drop_graphs(s);
+    if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+    if (s->side) cudaStreamDestroy(s->side);
+    if (s->fork) cudaEventDestroy(s->fork);
+    if (s->join) cudaEventDestroy(s->join);
     for (dyc_table *t : s->tables)
         if (t) dyc_destroy(t);
     if (s->d_tctr) cudaFree(s->d_tctr);
@@ -1325,7 +1378,6 @@ dyc_status dyc_set_destroy(dyc_set *s) {
     if (s->h_desc) cudaFreeHost(s->h_desc);
     if (s->d_gctr) cudaFree(s->d_gctr);
     if (s->h_gctr) cudaFreeHost(s->h_gctr);
-    if (s->h_actr) cudaFreeHost(s->h_actr);
     if (s->h_tnew) cudaFreeHost(s->h_tnew);
     if (s->abuf) cudaFree(s->abuf);
     if (s->lbuf) cudaFree(s->lbuf);
@@ -1382,7 +1434,8 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
     uint64_t n = 0;
     if (!set_args_ok(s, d_offsets, h_offsets, d_ops, d_keys, d_vals, &n)) return DYC_EINVAL;
     if (n == 0) return DYC_OK;
-    if (n >= 0xFFFFFFFFull) return fail(DYC_EINVAL, "a set batch takes fewer than 2^32 ops");
+    // cells are indexed by 32 bits and a batch uses twice its ops of them
+    if (n >= 0x80000000ull) return fail(DYC_EINVAL, "a set batch takes fewer than 2^31 ops");
     cudaStream_t st = (cudaStream_t)stream;
     {
         int cur = -1;
@@ -1395,24 +1448,32 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
     // them: the kernels must see the current subtables
     TRY(set_refresh_descs(s, st));
     TRY(set_ensure_scratch(s, n));
-    const bool graph = (flags & DYC_FLAG_GRAPH) != 0;
-    if (graph) {
-        const std::vector<uintptr_t> key = {(uintptr_t)d_offsets, (uintptr_t)d_ops,
-                                            (uintptr_t)d_keys,    (uintptr_t)d_vals,
-                                            (uintptr_t)d_vals_out, (uintptr_t)d_bits_out, n};
-        if (key != s->gkey) {
-            set_drop_graphs(s);
-            s->gkey = key;
+    dyc_set::Graph *gr = nullptr;
+    if (flags & DYC_FLAG_GRAPH)
+        gr = set_graph_for(s, {(uintptr_t)d_offsets, (uintptr_t)d_ops, (uintptr_t)d_keys,
+                              (uintptr_t)d_vals, (uintptr_t)d_vals_out, (uintptr_t)d_bits_out});
+    // under a graph the grids are sized by the scratch capacity, not by n
+    const uint64_t ng = gr ? s->A.cap_ops : n;
+    const bool resize = s->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE);
+    // The upsize policy (hash_insert_batch, api.cpp:359-369, per table): while
+    // size + the keys the batch adds > upper bound x capacity, upsize. The
+    // keys added are known on the device after phase A. Where even a batch
+    // of nothing but new keys stays within a table's slots, the batch runs
+    // both phases back to back and the policy is applied after it with the
+    // same sizes and counts, so capacities end as if it had run before the
+    // inserts (entries a fuller table could not place go through the
+    // overflow path). Otherwise the host reads the counts between the phases
+    // and upsizes first.
+    bool deferred = true;
+    if (resize)
+        for (uint32_t t = 0; t < s->ntables && deferred; ++t) {
+            const dyc_table *m = s->tables[t];
+            const uint64_t cnt = h_offsets[t + 1] - h_offsets[t];
+            deferred = m->size + cnt <= m->capacity;
         }
-    }
-    TRY(set_run(s, 0, graph, st, [&] {
-        return set_phase_a(s, d_offsets, d_ops, d_keys, d_vals, d_vals_out, d_bits_out, n, st);
-    }));
-    CK(cudaStreamSynchronize(st));
-    // upsize before the inserts where the keys the batch adds would pass the
-    // upper load bound (hash_insert_batch, api.cpp:359-369, per table)
     bool moved = false;
-    if (s->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE)) {
+    std::vector<uint8_t> grew;
+    auto upsize_policy = [&]() -> dyc_status {
         for (uint32_t t = 0; t < s->ntables; ++t) {
             dyc_table *m = s->tables[t];
             const uint64_t add = s->h_tnew[t];
@@ -1421,13 +1482,33 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
                    guard++ < 64) {
                 TRY(resize_up_impl(m, st));
                 moved = true;
+                if (grew.empty()) grew.assign(s->ntables, 0);
+                grew[t] = 1;
             }
         }
+        return DYC_OK;
+    };
+    if (deferred) {
+        TRY(set_run(s, gr, 2, st, [&](cudaStream_t cs) {
+            TRY(set_phase_a(s, d_offsets, d_ops, d_keys, d_vals, d_vals_out, d_bits_out, ng,
+                            resize, cs));
+            return set_phase_b(s, ng, cs);
+        }));
+        CK(cudaStreamSynchronize(st));
+        if (resize) TRY(upsize_policy());  // m->size is still the size before the batch
+    } else {
+        s->last.split_phases = 1;
+        TRY(set_run(s, gr, 0, st, [&](cudaStream_t cs) {
+            return set_phase_a(s, d_offsets, d_ops, d_keys, d_vals, d_vals_out, d_bits_out, ng,
+                               true, cs);
+        }));
+        CK(cudaStreamSynchronize(st));
+        TRY(upsize_policy());
         if (moved) TRY(set_push_descs(s, st));
+        TRY(set_run(s, gr, 1, st, [&](cudaStream_t cs) { return set_phase_b(s, ng, cs); }));
+        CK(cudaStreamSynchronize(st));
     }
-    TRY(set_run(s, 1, graph, st, [&] { return set_phase_b(s, n, st); }));
-    CK(cudaStreamSynchronize(st));
-    s->gwarm = graph;
+    if (gr) gr->warm = true;
     const Counters g = *s->h_gctr;
     if (g.spill) return fail(DYC_EOVERFLOW, "internal list overflow (%llu entries)", g.spill);
     for (uint32_t t = 0; t < s->ntables; ++t) s->tables[t]->size = s->h_tctr[t].size;
@@ -1441,7 +1522,7 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
         m->last = dyc_op_stats{};
     }
     if (g.overflow) {
-        TRY(set_overflow(s, g.overflow, st));
+        TRY(set_overflow(s, g.overflow, grew, st));
         moved = true;
     }
     // downsize after the batch (hash_delete_batch, api.cpp:494-505, per table)

@@ -119,8 +119,9 @@ __device__ __forceinline__ uint32_t table_of(const uint32_t *__restrict__ off, u
 template <int KB>
 __global__ void __launch_bounds__(256) k_set_group(const __grid_constant__ ApplyScratch A,
                                                    const uint32_t *__restrict__ off,
-                                                   const void *__restrict__ keys, uint64_t n) {
+                                                   const void *__restrict__ keys) {
     using K = typename SlotT<KB>::K;
+    const uint64_t n = off[A.ntables];  // the op count, read on the device
     // warp-uniform loop: a warp's 32 consecutive ops mostly belong to one
     // table, found by one search when the first and last lane's tables agree
     for (uint64_t base = warp_base(); base < n; base += warp_stride()) {
@@ -140,43 +141,30 @@ __global__ void __launch_bounds__(256) k_set_group(const __grid_constant__ Apply
     }
 }
 
-// Cell regions: 2 * (ops of table t) cells each; exclusive scan into
-// tcell_off, total in tcell_off[ntables]. One block of 1024 threads. (A
-// template only so that each key width's translation unit has its own copy.)
+// Start of a set batch of off[ntables] ops, in one launch: zero the batch
+// counters, the probe phase's counters (gctr, gctr_words words) and the
+// result bits; cell regions of twice each table's ops, so table t's region
+// starts at tcell_off[t] = 2 * off[t]; zero the cells in use and the
+// per-table new-key counts.
 template <int KB>
-__global__ void __launch_bounds__(1024) k_set_cells(const __grid_constant__ ApplyScratch A,
-                                                    const uint32_t *__restrict__ off) {
-    __shared__ uint32_t part[1024];
-    const uint32_t m = A.ntables;
-    const uint32_t per = (m + 1023) / 1024;
-    const uint32_t lo = per * threadIdx.x, hi = lo + per < m ? lo + per : m;
-    uint32_t sum = 0u;
-    for (uint32_t t = lo; t < hi; ++t) sum += 2u * (off[t + 1] - off[t]);
-    part[threadIdx.x] = sum;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const uint32_t x = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += x;
-        __syncthreads();
-    }
-    uint32_t run = part[threadIdx.x] - sum;
-    for (uint32_t t = lo; t < hi; ++t) {
-        A.tcell_off[t] = run;
-        run += 2u * (off[t + 1] - off[t]);
-    }
-    if (threadIdx.x == 1023) A.tcell_off[m] = part[1023];
-}
-
-// Zero the cells in use (tcell_off[ntables] of them) and the per-table counts.
-template <int KB>
-__global__ void __launch_bounds__(256) k_set_clear(const __grid_constant__ ApplyScratch A) {
-    const uint64_t words = (uint64_t)A.tcell_off[A.ntables] * (cell_bytes<KB>() / 8);
+__global__ void __launch_bounds__(256) k_set_prep(const __grid_constant__ ApplyScratch A,
+                                                  const uint32_t *__restrict__ off,
+                                                  uint32_t *__restrict__ bits,
+                                                  unsigned long long *__restrict__ gctr,
+                                                  uint32_t gctr_words) {
+    const uint64_t n = off[A.ntables];
+    const uint64_t id = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < words; c += stride)
-        ((unsigned long long *)A.cells)[c] = 0ull;
-    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < A.ntables; t += stride)
-        A.tnew[t] = 0u;
+    if (id < (uint64_t)kCtrSlots) A.ctr[id] = 0ull;
+    if (gctr != nullptr && id < gctr_words) gctr[id] = 0ull;
+    for (uint64_t t = id; t <= A.ntables; t += stride) {
+        A.tcell_off[t] = 2u * off[t];
+        if (t < A.ntables) A.tnew[t] = 0u;
+    }
+    const uint64_t words = 2 * n * (cell_bytes<KB>() / 8);
+    for (uint64_t c = id; c < words; c += stride) ((unsigned long long *)A.cells)[c] = 0ull;
+    if (bits != nullptr)
+        for (uint64_t w = id; w < (n + 31) / 32; w += stride) bits[w] = 0u;
 }
 
 // Block-wide exclusive allocation of F counters at once: x packs F fields of
@@ -300,9 +288,12 @@ __global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ A
     }
 }
 
+// n_ptr (many tables: offsets[ntables]) gives the op count on the device
+// instead of n, so that a captured launch serves batches of any size.
 template <int KB>
 __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ ApplyScratch A,
-                                                       uint64_t n) {
+                                                       uint64_t n, const uint32_t *n_ptr) {
+    if (n_ptr) n = *n_ptr;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const uint32_t cell = A.op_cell[i];
@@ -403,8 +394,10 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
                                                       const uint8_t *__restrict__ ops,
                                                       const void *__restrict__ vals, uint32_t vb,
                                                       void *__restrict__ vals_out,
-                                                      uint32_t *__restrict__ bits_out, uint64_t n) {
+                                                      uint32_t *__restrict__ bits_out, uint64_t n,
+                                                      const uint32_t *n_ptr) {
     using K = typename SlotT<KB>::K;
+    if (n_ptr) n = *n_ptr;
     const uint64_t nd = A.ctr[kCtrDistinct];
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     // key-0 ops (no cell): miss, output 0

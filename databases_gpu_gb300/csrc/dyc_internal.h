@@ -98,6 +98,10 @@ struct LaunchCtx {
     int sms;
     cudaStream_t stream;
     int max_blocks_per_sm = 0;  // 0: as many as fit (else a cap, chosen by a tuner)
+    // optional second stream for launches independent of the main sequence:
+    // forked after `fork` is recorded on `stream`, joined back through `join`
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 // Kernel launchers, one set per key width; `sb` = bucket bytes (32/64/128).
@@ -135,27 +139,30 @@ template <int KB> struct Ops {
                                unsigned long long *spill);
     // mixed batches (dyc_apply.cuh). One table: apply_group (group +
     // compact), apply_scatter, find of the distinct keys, apply_replay.
-    // Many tables (dyc_set.cuh): set_group replaces apply_group and the
-    // set_* probe kernels replace find / erase / place / walk.
+    // Many tables (dyc_set.cuh): set_group replaces apply_group, and
+    // set_find / set_mutate / set_walk replace find / erase + place / walk.
     static cudaError_t apply_group(const LaunchCtx &L, const ApplyScratch &A, const void *keys,
                                   uint64_t n);
-    static cudaError_t apply_scatter(const LaunchCtx &L, const ApplyScratch &A, uint64_t n);
+    // n_ptr (many tables): the op count on the device; n then only sizes grids
+    static cudaError_t apply_scatter(const LaunchCtx &L, const ApplyScratch &A, uint64_t n,
+                                     const uint32_t *n_ptr = nullptr);
     static cudaError_t apply_replay(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
                                    const void *vals, uint32_t vb, void *vals_out,
-                                   uint32_t *bits_out, uint64_t n, uint64_t max_distinct);
+                                   uint32_t *bits_out, uint64_t n, uint64_t max_distinct,
+                                   const uint32_t *n_ptr = nullptr);
+    // prep (counters, gctr, result bits, cell regions) + grouping + compaction
     static cudaError_t set_group(const LaunchCtx &L, const ApplyScratch &A, const uint32_t *off,
-                                 const void *keys, uint64_t n);
+                                 const void *keys, uint64_t n, uint32_t *bits, Counters *gctr);
     static cudaError_t set_find(const LaunchCtx &L, const Desc *descs, int sb, const void *keys,
                                 const uint32_t *tids, const unsigned long long *n_ptr,
                                 uint64_t max_n, void *vals, uint32_t vb, uint32_t *hits);
-    static cudaError_t set_erase(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
-                                 const void *keys, const uint32_t *tids,
-                                 const unsigned long long *n_ptr, uint64_t max_n, Counters *gctr);
-    static cudaError_t set_place(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
-                                 const void *keys, const void *vals, uint32_t vb,
-                                 const uint32_t *tids, const unsigned long long *n_ptr,
-                                 uint64_t max_n, void *list_a, uint32_t *list_a_tid,
-                                 uint64_t list_cap, Counters *gctr);
+    // erases and upserts of a set batch in one launch (max_n: both lists' bound)
+    static cudaError_t set_mutate(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
+                                  const void *er_keys, const uint32_t *er_tids,
+                                  const unsigned long long *ne_ptr, const void *up_keys,
+                                  const void *up_vals, uint32_t vb, const uint32_t *up_tids,
+                                  const unsigned long long *nu_ptr, uint64_t max_n, void *list_a,
+                                  uint32_t *list_a_tid, uint64_t list_cap, Counters *gctr);
     static cudaError_t set_walk(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
                                 const void *src, const uint32_t *src_tid,
                                 const unsigned long long *src_count, void *dst, uint32_t *dst_tid,

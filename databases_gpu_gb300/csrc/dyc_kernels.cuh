@@ -37,6 +37,20 @@ __device__ __forceinline__ uint64_t warp_stride() {
     return ((uint64_t)gridDim.x * blockDim.x) & ~31ull;
 }
 
+// Entries a warp takes per pass of an eviction-walk kernel. A walk step
+// costs one dependent memory round trip per probe round (RO buckets), and a
+// short list leaves most of the grid idle, so short lists are spread over
+// every warp, down to one round (RO entries) per warp; long lists fill all
+// 32 lanes.
+template <int RO>
+__device__ __forceinline__ uint32_t walk_share(uint64_t n) {
+    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t per = (n + warps - 1) / warps;
+    if (per <= (uint64_t)RO) return RO;
+    if (per >= 32) return 32;
+    return (uint32_t)((per + RO - 1) / RO * RO);
+}
+
 template <int KB, int SB>
 __device__ __forceinline__ typename SlotT<KB>::S *slot_ptr(char *bucket, int j) {
     return reinterpret_cast<typename SlotT<KB>::S *>(bucket + j * SlotT<KB>::kBytes);
@@ -612,12 +626,15 @@ __global__ void __launch_bounds__(256) k_walk(const __grid_constant__ Desc D,
     using Sl = typename T::S;
     uint64_t n = *src_count;
     if (n > max_entries) n = max_entries;
-    const uint64_t step = warp_stride();
+    const uint32_t per = walk_share<Geo<KB, SB>::kRoundOps>(n);
+    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t wid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31;
     uint32_t n_ok = 0, n_steps = 0;
     const uint32_t max_iter = 2u * max_evict + 8u;
-    for (uint64_t base = warp_base(); base < n; base += step) {
-        const uint64_t i = base + (threadIdx.x & 31);
-        bool live = i < n;
+    for (uint64_t base = wid * per; base < n; base += warps * per) {
+        const uint64_t i = base + lane;
+        bool live = lane < per && i < n;
         Sl e = live ? ((const Sl *)src)[i] : T::empty();
         uint32_t hk = 0;
         Pair pe{0u, 0u};

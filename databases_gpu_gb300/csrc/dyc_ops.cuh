@@ -169,42 +169,58 @@ cudaError_t Ops<KB>::apply_group(const LaunchCtx &L, const ApplyScratch &A, cons
 }
 
 template <int KB>
-cudaError_t Ops<KB>::apply_scatter(const LaunchCtx &L, const ApplyScratch &A, uint64_t n) {
+cudaError_t Ops<KB>::apply_scatter(const LaunchCtx &L, const ApplyScratch &A, uint64_t n,
+                                   const uint32_t *n_ptr) {
     if (n == 0) return cudaSuccess;
     auto sc = k_apply_scatter<KB>;
-    sc<<<grid_for((const void *)sc, L, n), 256, 0, L.stream>>>(A, n);
+    sc<<<grid_for((const void *)sc, L, n), 256, 0, L.stream>>>(A, n, n_ptr);
     return cudaGetLastError();
 }
 
 template <int KB>
 cudaError_t Ops<KB>::apply_replay(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
                                   const void *vals, uint32_t vb, void *vals_out,
-                                  uint32_t *bits_out, uint64_t n, uint64_t max_distinct) {
+                                  uint32_t *bits_out, uint64_t n, uint64_t max_distinct,
+                                  const uint32_t *n_ptr) {
     if (n == 0) return cudaSuccess;
     auto r = k_apply_replay<KB>;
     const uint64_t work = n > max_distinct ? n : max_distinct;
     r<<<grid_for((const void *)r, L, work), 256, 0, L.stream>>>(A, ops, vals, vb, vals_out,
-                                                                 bits_out, n);
+                                                                 bits_out, n, n_ptr);
+    // the segment classes are disjoint: with a side stream the warp and
+    // block replays run beside the thread replay
+    const bool forked = L.side != nullptr;
+    cudaStream_t s2 = forked ? L.side : L.stream;
+    if (forked) {
+        cudaError_t e = cudaEventRecord(L.fork, L.stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(L.side, L.fork, 0);
+        if (e != cudaSuccess) return e;
+    }
     auto w = k_apply_replay_warp<KB>;
     // one warp per 32 warp segments; at most n / (kShortSeg + 1) segments
-    w<<<grid_for((const void *)w, L, n / (kShortSeg + 1) + 32), 256, 0, L.stream>>>(
+    w<<<grid_for((const void *)w, L, n / (kShortSeg + 1) + 32), 256, 0, s2>>>(
         A, ops, vals, vb, vals_out, bits_out);
     auto m = k_apply_replay_mid<KB>;
     // one block per mid segment; at most n / (kWarpSeg + 1) of them
-    m<<<grid_for((const void *)m, L, (n / (kWarpSeg + 1) + 1) * 256), 256, 0, L.stream>>>(
+    m<<<grid_for((const void *)m, L, (n / (kWarpSeg + 1) + 1) * 256), 256, 0, s2>>>(
         A, ops, vals, vb, vals_out, bits_out);
+    if (forked) {
+        cudaError_t e = cudaEventRecord(L.join, L.side);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(L.stream, L.join, 0);
+        if (e != cudaSuccess) return e;
+    }
     return cudaGetLastError();
 }
 
 template <int KB>
 cudaError_t Ops<KB>::set_group(const LaunchCtx &L, const ApplyScratch &A, const uint32_t *off,
-                               const void *keys, uint64_t n) {
-    k_set_cells<KB><<<1, 1024, 0, L.stream>>>(A, off);
-    auto cl = k_set_clear<KB>;
-    cl<<<grid_for((const void *)cl, L, A.cap_cells), 256, 0, L.stream>>>(A);
-    if (n) {
+                               const void *keys, uint64_t n, uint32_t *bits, Counters *gctr) {
+    auto pr = k_set_prep<KB>;
+    pr<<<grid_for((const void *)pr, L, 2 * n * (cell_bytes<KB>() / 8) + 1), 256, 0, L.stream>>>(
+        A, off, bits, (unsigned long long *)gctr, (uint32_t)(sizeof(Counters) / 8));
+    if (n) {  // n sizes the grids; the kernels read the op count from off[ntables]
         auto g = k_set_group<KB>;
-        g<<<grid_for((const void *)g, L, n), 256, 0, L.stream>>>(A, off, keys, n);
+        g<<<grid_for((const void *)g, L, n), 256, 0, L.stream>>>(A, off, keys);
         auto c = k_apply_compact<KB>;
         c<<<grid_for((const void *)c, L, 2 * n), 256, 0, L.stream>>>(A, 0);
     }
@@ -225,29 +241,18 @@ cudaError_t Ops<KB>::set_find(const LaunchCtx &L, const Desc *descs, int sb, con
 }
 
 template <int KB>
-cudaError_t Ops<KB>::set_erase(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
-                               const void *keys, const uint32_t *tids,
-                               const unsigned long long *n_ptr, uint64_t max_n, Counters *gctr) {
+cudaError_t Ops<KB>::set_mutate(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
+                                const void *er_keys, const uint32_t *er_tids,
+                                const unsigned long long *ne_ptr, const void *up_keys,
+                                const void *up_vals, uint32_t vb, const uint32_t *up_tids,
+                                const unsigned long long *nu_ptr, uint64_t max_n, void *list_a,
+                                uint32_t *list_a_tid, uint64_t list_cap, Counters *gctr) {
     if (max_n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
-        auto k = k_set_erase<KB, SB>;
-        k<<<grid_for((const void *)k, L, max_n), 256, 0, L.stream>>>(descs, tctr, keys, tids,
-                                                                      n_ptr, gctr);
-    });
-    return cudaGetLastError();
-}
-
-template <int KB>
-cudaError_t Ops<KB>::set_place(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
-                               const void *keys, const void *vals, uint32_t vb,
-                               const uint32_t *tids, const unsigned long long *n_ptr,
-                               uint64_t max_n, void *list_a, uint32_t *list_a_tid,
-                               uint64_t list_cap, Counters *gctr) {
-    if (max_n == 0) return cudaSuccess;
-    DYC_SB_DISPATCH(sb, {
-        auto k = k_set_place<KB, SB>;
-        k<<<grid_for((const void *)k, L, max_n), 256, 0, L.stream>>>(
-            descs, tctr, keys, vals, vb, tids, n_ptr, list_a, list_a_tid, list_cap, gctr);
+        auto k = k_set_mutate<KB, SB>;
+        k<<<grid_for((const void *)k, L, max_n + 32), 256, 0, L.stream>>>(
+            descs, tctr, er_keys, er_tids, ne_ptr, up_keys, up_vals, vb, up_tids, nu_ptr, list_a,
+            list_a_tid, list_cap, gctr);
     });
     return cudaGetLastError();
 }

@@ -202,14 +202,20 @@ int main(int argc, char **argv) {
            "\"max_ms\": %.3f, \"submit_late_max_ms\": %.3f, \"steps\": %llu, "
            "\"max_step_ops\": %llu, \"deferred\": %llu, \"rejected\": %llu, \"failures\": %d, "
            "\"executor_busy_frac\": %.3f, \"device_bytes\": %llu, \"tenants\": %d, "
-           "\"keys_preloaded\": %llu, \"setup_s\": %.2f, \"coalesce\": %d, \"wall_s\": %.3f}\n",
+           "\"keys_preloaded\": %llu, \"setup_s\": %.2f, \"coalesce\": %d, \"wall_s\": %.3f, "
+           "\"resizes_up\": %llu, \"resizes_down\": %llu, \"resize_step_busy_frac\": %.3f, "
+           "\"assemble_frac\": %.3f, \"exec_idle_frac\": %.3f, \"upload_late_steps\": %llu, "
+           "\"split_steps\": %llu}\n",
            (unsigned long long)N, (unsigned long long)total_ops, rate, at[N - 1],
            total_ops / at[N - 1] / 1e6, total_ops / last_done / 1e6, pct(0.5), pct(0.99),
            sl[N - 1] * 1e3, late_max * 1e3, (unsigned long long)st.steps,
            (unsigned long long)st.max_step_ops, (unsigned long long)st.deferred,
            (unsigned long long)st.rejected, failures.load(), st.busy_seconds / last_done,
            (unsigned long long)st.device_bytes, tenants, (unsigned long long)total_keys, setup_s,
-           coalesce, wall);
+           coalesce, wall, (unsigned long long)st.resizes_up, (unsigned long long)st.resizes_down,
+           st.busy_seconds > 0 ? st.resize_step_seconds / st.busy_seconds : 0.0,
+           st.assemble_seconds / last_done, st.exec_idle_seconds / last_done,
+           (unsigned long long)st.upload_late_steps, (unsigned long long)st.split_steps);
     dyc_server_destroy(srv);
     return failures.load() ? 2 : 0;
 }

@@ -245,6 +245,7 @@ void assembler(dyc_server *s) {
         s->free_slots.pop_front();
         s->in_flight++;
         lk.unlock();
+        const auto ta = Clock::now();
 
         Slot &sl = s->slot[b];
         sl.reqs = take;
@@ -275,7 +276,9 @@ void assembler(dyc_server *s) {
                                 cudaMemcpyHostToDevice, s->up);
         if (e == cudaSuccess) e = cudaEventRecord(sl.up, s->up);
         if (e != cudaSuccess) sl.status = DYC_ECUDA;
+        const double asm_s = std::chrono::duration<double>(Clock::now() - ta).count();
         lk.lock();
+        s->st.assemble_seconds += asm_s;
         s->to_exec.push_back(b);
         s->cv.notify_all();
     }
@@ -288,6 +291,7 @@ void executor(dyc_server *s) {
     cudaSetDevice(s->device);
     for (;;) {
         int b;
+        const auto tw = Clock::now();
         {
             std::unique_lock<std::mutex> lk(s->mu);
             s->cv.wait(lk, [&] { return !s->to_exec.empty() || s->asm_done; });
@@ -297,11 +301,14 @@ void executor(dyc_server *s) {
         }
         Slot &sl = s->slot[b];
         const auto t0 = Clock::now();
+        const double idle = std::chrono::duration<double>(t0 - tw).count();
+        const bool late = cudaEventQuery(sl.up) == cudaErrorNotReady;
         dyc_status r = sl.status;
         if (r == DYC_OK && cudaStreamWaitEvent(s->exec, sl.up, 0) != cudaSuccess) r = DYC_ECUDA;
         if (r == DYC_OK && s->scfg.coalesce) {
+            // each staging slot's buffers get their own captured launch graph
             r = dyc_set_apply(s->set, sl.d_off, sl.h_off, sl.d_ops, sl.d_keys, sl.d_vals,
-                              sl.d_out, sl.d_bits, 0, s->exec);
+                              sl.d_out, sl.d_bits, DYC_FLAG_GRAPH, s->exec);
         } else if (r == DYC_OK) {
             Req *q = sl.reqs[0];
             r = dyc_apply(s->members[q->tenant], sl.d_ops, sl.d_keys, sl.d_vals, q->n, sl.d_out,
@@ -309,6 +316,11 @@ void executor(dyc_server *s) {
         }
         if (r == DYC_OK && cudaStreamSynchronize(s->exec) != cudaSuccess) r = DYC_ECUDA;
         const double busy = std::chrono::duration<double>(Clock::now() - t0).count();
+        dyc_op_stats os{};
+        if (r == DYC_OK) {
+            if (s->scfg.coalesce) dyc_set_last_stats(s->set, &os);
+            else dyc_last_stats(s->members[sl.reqs[0]->tenant], &os);
+        }
         const uint64_t tb = r == DYC_OK ? table_device_bytes(s) : 0;
         if (r == DYC_OK) {
             cudaError_t e = cudaMemcpyAsync(sl.h_out, sl.d_out, sl.n * s->vb,
@@ -324,6 +336,12 @@ void executor(dyc_server *s) {
         if (r == DYC_OK) s->table_bytes = tb;
         s->st.steps++;
         s->st.busy_seconds += busy;
+        if (s->st.steps > 1) s->st.exec_idle_seconds += idle;  // not the wait for the first
+        s->st.upload_late_steps += late ? 1 : 0;
+        s->st.split_steps += os.split_phases;
+        s->st.resizes_up += os.resizes_up;
+        s->st.resizes_down += os.resizes_down;
+        if (os.resizes_up || os.resizes_down) s->st.resize_step_seconds += busy;
         s->st.max_step_ops = std::max(s->st.max_step_ops, sl.n);
         s->to_complete.push_back(b);
         s->cv.notify_all();

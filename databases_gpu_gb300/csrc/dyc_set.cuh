@@ -66,133 +66,148 @@ __global__ void __launch_bounds__(256) k_set_find(const Desc *__restrict__ descs
     }
 }
 
-// erase of unique keys[i] from table tids[i] (k_erase per table, no dedup)
+// erase of unique keys[i] from table tids[i], i in [base, base + 32) and
+// below n (k_erase per table, no dedup). Warp-collective; returns whether
+// this lane erased its key.
 template <int KB, int SB>
-__global__ void __launch_bounds__(256) k_set_erase(const Desc *__restrict__ descs,
-                                                   Counters *__restrict__ tctr,
-                                                   const void *__restrict__ keys,
-                                                   const uint32_t *__restrict__ tids,
-                                                   const unsigned long long *__restrict__ n_ptr,
-                                                   Counters *gctr) {
+__device__ __forceinline__ bool set_erase_warp(const Desc *__restrict__ descs,
+                                               Counters *__restrict__ tctr,
+                                               const void *__restrict__ keys,
+                                               const uint32_t *__restrict__ tids, uint64_t n,
+                                               uint64_t base, unsigned char *stage) {
     using T = SlotT<KB>;
     using Gm = Geo<KB, SB>;
-    __shared__ __align__(128) unsigned char s_stage[kWarpsPerBlock][32 * SB];
-    unsigned char *stage = s_stage[threadIdx.x >> 5];
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t n = *n_ptr;
-    const uint64_t step = warp_stride();
-    uint32_t n_del = 0;
-    for (uint64_t base = warp_base(); base < n; base += step) {
-        const uint64_t i = base + lane;
-        typename T::K k = 0;
-        uint32_t tb = 0u;
-        if (i < n) {
-            k = load_key<KB>(keys, i);
-            tb = tids[i];
-        }
-        const Desc &D = descs[tb];
-        const bool act = k != 0;
-        const uint32_t hk = fold(k);
-        const Pair p = pair_of(hk, D.d);
-        char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
-        const KvOut r1 = kv_probe<KB, SB, 2>(p1, k, act, stage);
-        bool erased = false;
-        if (act && r1.match >= 0) {
-            const typename T::S cur = T::make(k, r1.value);
-            const typename T::S old = T::cas(slot_ptr<KB, SB>(p1, r1.match), cur, T::empty());
+    const uint64_t i = base + (threadIdx.x & 31);
+    typename T::K k = 0;
+    uint32_t tb = 0u;
+    if (i < n) {
+        k = load_key<KB>(keys, i);
+        tb = tids[i];
+    }
+    const Desc &D = descs[tb];
+    const bool act = k != 0;
+    const uint32_t hk = fold(k);
+    const Pair p = pair_of(hk, D.d);
+    char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
+    const KvOut r1 = kv_probe<KB, SB, 2>(p1, k, act, stage);
+    bool erased = false;
+    if (act && r1.match >= 0) {
+        const typename T::S cur = T::make(k, r1.value);
+        const typename T::S old = T::cas(slot_ptr<KB, SB>(p1, r1.match), cur, T::empty());
+        erased = T::same(old, cur);
+    }
+    const bool need2 = act && r1.match < 0 && (!Gm::kMeta || r1.overflow);
+    if (__any_sync(kFull, need2)) {
+        char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
+        const KvOut r2 = kv_probe<KB, SB, 2>(p2, k, need2, stage);
+        if (need2 && r2.match >= 0) {
+            const typename T::S cur = T::make(k, r2.value);
+            const typename T::S old = T::cas(slot_ptr<KB, SB>(p2, r2.match), cur, T::empty());
             erased = T::same(old, cur);
         }
-        const bool need2 = act && r1.match < 0 && (!Gm::kMeta || r1.overflow);
-        if (__any_sync(kFull, need2)) {
-            char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-            const KvOut r2 = kv_probe<KB, SB, 2>(p2, k, need2, stage);
-            if (need2 && r2.match >= 0) {
-                const typename T::S cur = T::make(k, r2.value);
-                const typename T::S old = T::cas(slot_ptr<KB, SB>(p2, r2.match), cur, T::empty());
-                erased = T::same(old, cur);
-            }
-        }
-        warp_size_add(tctr, tb, erased, -1);
-        n_del += erased ? 1u : 0u;
     }
-    const uint32_t del = __reduce_add_sync(kFull, n_del);
-    if (lane == 0 && del) atomicAdd(&gctr->erased, (unsigned long long)del);
+    warp_size_add(tctr, tb, erased, -1);
+    return erased;
 }
 
-// upsert of unique keys[i] -> vals[i] into table tids[i] (k_place per
-// table); ops left without a slot go to list_a / list_a_tid
+// upsert of unique keys[i] -> vals[i] into table tids[i], i in [base,
+// base + 32) and below n (k_place per table); ops left without a slot go to
+// list_a / list_a_tid. Warp-collective; adds to n_ins / n_upd.
 template <int KB, int SB>
-__global__ void __launch_bounds__(256) k_set_place(const Desc *__restrict__ descs,
-                                                   Counters *__restrict__ tctr,
-                                                   const void *__restrict__ keys,
-                                                   const void *__restrict__ vals, uint32_t vb,
-                                                   const uint32_t *__restrict__ tids,
-                                                   const unsigned long long *__restrict__ n_ptr,
-                                                   void *list_a, uint32_t *list_a_tid,
-                                                   uint64_t list_cap, Counters *gctr) {
+__device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs,
+                                               Counters *__restrict__ tctr,
+                                               const void *__restrict__ keys,
+                                               const void *__restrict__ vals, uint32_t vb,
+                                               const uint32_t *__restrict__ tids, uint64_t n,
+                                               uint64_t base, void *list_a, uint32_t *list_a_tid,
+                                               uint64_t list_cap, Counters *gctr,
+                                               unsigned char *stage, uint32_t &n_ins,
+                                               uint32_t &n_upd) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
     using Gm = Geo<KB, SB>;
-    __shared__ __align__(128) unsigned char s_stage[SB >= 64 ? kWarpsPerBlock : 1][32 * SB];
-    unsigned char *stage = s_stage[SB >= 64 ? (threadIdx.x >> 5) : 0];
-    const uint64_t n = *n_ptr;
-    const uint64_t step = warp_stride();
-    uint32_t n_ins = 0, n_upd = 0;
-    for (uint64_t base = warp_base(); base < n; base += step) {
-        const uint64_t i = base + (threadIdx.x & 31);
-        typename T::K k = 0;
-        bool act = false;
-        uint32_t tb = 0u;
-        Sl e = T::empty();
-        if (i < n) {
-            k = load_key<KB>(keys, i);
-            tb = tids[i];
-            act = k != 0;
-            if (act) e = T::make(k, load_val(vals, vb, i));
+    const uint64_t i = base + (threadIdx.x & 31);
+    typename T::K k = 0;
+    bool act = false;
+    uint32_t tb = 0u;
+    Sl e = T::empty();
+    if (i < n) {
+        k = load_key<KB>(keys, i);
+        tb = tids[i];
+        act = k != 0;
+        if (act) e = T::make(k, load_val(vals, vb, i));
+    }
+    const Desc &D = descs[tb];
+    const uint32_t hk = fold(k);
+    const Pair p = pair_of(hk, D.d);
+    char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
+    char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
+    const KvOut r1 = place_probe<KB, SB>(p1, k, act, p.first, D.d, stage);
+    const bool found1 = act && r1.match >= 0;
+    const bool check2 = act && !found1 && ((!Gm::kMeta || r1.overflow) || r1.empty == 0u);
+    KvOut r2{-1, 0ull, false, 0u};
+    if (__any_sync(kFull, check2)) r2 = place_probe<KB, SB>(p2, k, check2, p.second, D.d, stage);
+    bool pend = false, ins = false;
+    if (found1) {
+        T::exch(slot_ptr<KB, SB>(p1, r1.match), e);
+        ++n_upd;
+    } else if (check2 && r2.match >= 0) {
+        T::exch(slot_ptr<KB, SB>(p2, r2.match), e);
+        ++n_upd;
+    } else if (act) {
+        bool ok = claim_empty<KB, SB>(p1, r1.empty, e);
+        if (!ok && check2 && r2.empty) {
+            mark_overflow<KB, SB>(p1, hk);
+            ok = claim_empty<KB, SB>(p2, r2.empty, e);
         }
-        const Desc &D = descs[tb];
-        const uint32_t hk = fold(k);
-        const Pair p = pair_of(hk, D.d);
-        char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
-        char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-        const KvOut r1 = place_probe<KB, SB>(p1, k, act, p.first, D.d, stage);
-        const bool found1 = act && r1.match >= 0;
-        const bool check2 =
-            act && !found1 && ((!Gm::kMeta || r1.overflow) || r1.empty == 0u);
-        KvOut r2{-1, 0ull, false, 0u};
-        if (__any_sync(kFull, check2)) r2 = place_probe<KB, SB>(p2, k, check2, p.second, D.d, stage);
-        bool pend = false, ins = false;
-        if (found1) {
-            T::exch(slot_ptr<KB, SB>(p1, r1.match), e);
-            ++n_upd;
-        } else if (check2 && r2.match >= 0) {
-            T::exch(slot_ptr<KB, SB>(p2, r2.match), e);
-            ++n_upd;
-        } else if (act) {
-            bool ok = claim_empty<KB, SB>(p1, r1.empty, e);
-            if (!ok && check2 && r2.empty) {
-                mark_overflow<KB, SB>(p1, hk);
-                ok = claim_empty<KB, SB>(p2, r2.empty, e);
-            }
-            if (ok) {
-                ++n_ins;
-                ins = true;
-            } else {
-                pend = true;
-            }
-        }
-        __syncwarp();
-        warp_size_add(tctr, tb, ins, 1);
-        const unsigned long long at = agg_inc(&gctr->pending, pend);
-        if (pend) {
-            if (at < list_cap) {
-                ((Sl *)list_a)[at] = e;
-                list_a_tid[at] = tb;
-            } else {
-                atomicAdd(&gctr->spill, 1ull);
-            }
+        if (ok) {
+            ++n_ins;
+            ins = true;
+        } else {
+            pend = true;
         }
     }
+    __syncwarp();
+    warp_size_add(tctr, tb, ins, 1);
+    const unsigned long long at = agg_inc(&gctr->pending, pend);
+    if (pend) {
+        if (at < list_cap) {
+            ((Sl *)list_a)[at] = e;
+            list_a_tid[at] = tb;
+        } else {
+            atomicAdd(&gctr->spill, 1ull);
+        }
+    }
+}
+
+// The batch's erases (er_keys, *ne_ptr of them) and upserts (up_keys,
+// *nu_ptr) in one grid-stride pass: warp items [0, ceil32(ne)) erase, the
+// rest upsert. The keys of the two lists are distinct, so the two kinds may
+// run concurrently (an upsert only claims empty slots or rewrites its own
+// key; an erase only empties its own key's slot).
+template <int KB, int SB>
+__global__ void __launch_bounds__(256) k_set_mutate(
+    const Desc *__restrict__ descs, Counters *__restrict__ tctr, const void *__restrict__ er_keys,
+    const uint32_t *__restrict__ er_tids, const unsigned long long *__restrict__ ne_ptr,
+    const void *__restrict__ up_keys, const void *__restrict__ up_vals, uint32_t vb,
+    const uint32_t *__restrict__ up_tids, const unsigned long long *__restrict__ nu_ptr,
+    void *list_a, uint32_t *list_a_tid, uint64_t list_cap, Counters *gctr) {
+    __shared__ __align__(128) unsigned char s_stage[kWarpsPerBlock][32 * SB];
+    unsigned char *stage = s_stage[threadIdx.x >> 5];
+    const uint64_t ne = *ne_ptr, nu = *nu_ptr;
+    const uint64_t ne32 = (ne + 31) & ~(uint64_t)31;
+    const uint64_t step = warp_stride();
+    uint32_t n_del = 0, n_ins = 0, n_upd = 0;
+    for (uint64_t base = warp_base(); base < ne32 + nu; base += step) {
+        if (base < ne32) {  // warp-uniform: base is a multiple of 32
+            n_del += set_erase_warp<KB, SB>(descs, tctr, er_keys, er_tids, ne, base, stage) ? 1u
+                                                                                           : 0u;
+        } else {
+            set_place_warp<KB, SB>(descs, tctr, up_keys, up_vals, vb, up_tids, nu, base - ne32,
+                                   list_a, list_a_tid, list_cap, gctr, stage, n_ins, n_upd);
+        }
+    }
+    agg_add(&gctr->erased, n_del);
     agg_add(&gctr->inserted, n_ins);
     agg_add(&gctr->updated, n_upd);
 }
@@ -213,12 +228,15 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
     using Sl = typename T::S;
     uint64_t n = *src_count;
     if (n > max_entries) n = max_entries;
-    const uint64_t step = warp_stride();
+    const uint32_t per = walk_share<Geo<KB, SB>::kRoundOps>(n);
+    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t wid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31;
     uint32_t n_ok = 0, n_steps = 0;
     const uint32_t max_iter = 2u * max_evict + 8u;
-    for (uint64_t base = warp_base(); base < n; base += step) {
-        const uint64_t i = base + (threadIdx.x & 31);
-        bool live = i < n;
+    for (uint64_t base = wid * per; base < n; base += warps * per) {
+        const uint64_t i = base + lane;
+        bool live = lane < per && i < n;
         Sl e = live ? ((const Sl *)src)[i] : T::empty();
         const uint32_t tb = live ? src_tid[i] : 0u;
         const Desc &D = descs[tb];
@@ -227,7 +245,11 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
         char *fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);
         uint32_t t = pe.first;
         char *bp = fb;
-        int mode = 0;  // 0: empties of the first bucket, 1: of the second, 2: walking
+        // 0: empties of the first bucket, 1: of the second, 2: walking. The
+        // entries come from the upsert pass, which found both buckets full:
+        // the walk starts at the first bucket (still taking an empty slot
+        // there if one has appeared since).
+        int mode = 2;
         uint32_t evictions = 0;
         bool fail = false, ok = false;
         for (uint32_t it = 0; it < max_iter; ++it) {

@@ -92,6 +92,8 @@ typedef struct dyc_op_stats {
     uint64_t overflowed;  /* chains that reached the bound and were re-placed */
     uint64_t resizes_up;
     uint64_t resizes_down;
+    uint64_t split_phases; /* dyc_set_apply: 1 when the host read the batch's new-key
+                              counts between its phases (a table could have filled) */
 } dyc_op_stats;
 
 /* Defaults: 4-byte keys and values, d = 4, 128-byte buckets, bound 64,
@@ -284,12 +286,15 @@ dyc_status dyc_restore(const void *h_buf, uint64_t buf_bytes, int32_t device, dy
  * bits of d_bits_out, with offsets[0] = 0 and ntables + 1 entries (a device
  * copy, read by the kernels, and a host copy, used to size scratch).
  * Per table the semantics and results are exactly those of dyc_apply on that
- * table with its range; the resize policy runs per table. */
+ * table with its range; the resize policy runs per table. A batch holds
+ * fewer than 2^31 ops. */
 typedef struct dyc_set dyc_set;
 
 #define DYC_FLAG_GRAPH 8u /* dyc_set_apply: run the launch sequences as CUDA graphs,
-                             captured on the second call with the same arrays and
-                             op count and replayed after that */
+                             captured on the second call with the same arrays
+                             and replayed after that, whatever the op count (the
+                             kernels read it from the device offsets); up to
+                             four array sets are kept */
 
 /* ntables tables sharing cfg's key/value width, bucket size, eviction bound
  * and thresholds; table t is sized for sizes[t] keys (the hashAPI(size)
@@ -364,6 +369,13 @@ typedef struct dyc_server_stats {
     uint64_t max_step_ops;  /* largest step */
     uint64_t device_bytes;  /* tables + scratch + staging, after the last step */
     double busy_seconds;    /* time the executor spent in device steps */
+    uint64_t resizes_up;    /* table upsizes inside steps */
+    uint64_t resizes_down;  /* table downsizes inside steps */
+    double resize_step_seconds; /* executor time of the steps that resized a table */
+    double assemble_seconds;    /* assembler time from taking requests to queuing the step */
+    double exec_idle_seconds;   /* executor time waiting for an assembled step */
+    uint64_t upload_late_steps; /* steps whose upload was still running when picked up */
+    uint64_t split_steps;       /* steps with split_phases set */
 } dyc_server_stats;
 
 void dyc_server_config_default(dyc_server_config *c);

@@ -165,3 +165,95 @@ def test_tuner_picks_a_measured_candidate():
     assert r.mops > 0 and set(r.by_bucket) == {64, 128}
     sb, d, ev = tune.plan_set([1000, 1100], [500, 600], {9: r, 10: r})
     assert sb in (64, 128) and list(d) == [r.by_bucket[sb][0]["num_subtables"]] * 2
+
+
+def test_set_graph_reuses_buffers_across_batch_sizes():
+    """Fixed staging buffers (as a request server holds them), a different op
+    count every round: the captured graphs read the count on the device, so
+    each round replays the same graph. Rounds that cannot grow a table run
+    both phases back to back; the growing rounds (small tables, many inserts)
+    take the path with an upsize between the phases, also under the graph."""
+    import torch
+    rng = np.random.default_rng(13)
+    nt = 48
+    S = _dg().DyCuckooSet(rng.integers(64, 4096, nt).tolist())
+    maps = [O.Map() for _ in range(nt)]
+    cap = nt * 2500
+    b_ops = torch.empty(cap, dtype=torch.uint8, device="cuda")
+    b_keys = torch.empty(cap, dtype=torch.int32, device="cuda")
+    b_vals = torch.empty(cap, dtype=torch.int32, device="cuda")
+    b_out = torch.empty(cap, dtype=torch.int32, device="cuda")
+    b_bits = torch.empty(cap // 32 + 1, dtype=torch.int32, device="cuda")
+    b_off = torch.empty(nt + 1, dtype=torch.int32, device="cuda")
+    for r in range(8):
+        grow = r in (2, 5)
+        cnt = rng.integers(0, 2500 if grow else 600, nt)
+        off = np.zeros(nt + 1, np.uint32)
+        off[1:] = np.cumsum(cnt)
+        n = int(off[-1])
+        p = [0.1, 0.85, 0.05] if grow else [0.6, 0.2, 0.2]
+        ops = rng.choice(np.array([0, 1, 2], np.uint8), size=n, p=p)
+        keys = rng.integers(1, 1 << 20, n).astype(np.uint32)
+        vals = rng.integers(0, 1 << 31, n).astype(np.uint32)
+        b_ops[:n].copy_(torch.from_numpy(ops))
+        b_keys[:n].copy_(torch.from_numpy(keys.view(np.int32)))
+        b_vals[:n].copy_(torch.from_numpy(vals.view(np.int32)))
+        b_off.copy_(torch.from_numpy(off.view(np.int32)))
+        nw = (n + 31) // 32
+        out, bits = S.apply(b_off, b_ops[:n], b_keys[:n], b_vals[:n], out=b_out[:n],
+                            bits=b_bits[:nw], h_offsets=off, graph=True)
+        _check_round(S, maps, off, b_ops[:n], b_keys[:n], b_vals[:n], out, bits,
+                     "graph round %d (n=%d)" % (r, n))
+    for t in (0, 21, nt - 1):
+        assert_same_contents(S.table(t), maps[t], "table %d contents" % t)
+    S.close()
+
+
+def test_set_deferred_upsize_matches_per_table_path():
+    """Tables preloaded to 75 % of their slots (below the 0.8 upper bound),
+    then a batch of new keys worth 20 % more: the batch fits the slots, so
+    the set runs it without a host
+    round trip and applies the upsize policy afterwards (entries the fuller
+    tables could not place take the overflow path). Results, sizes,
+    capacities and contents equal those of one dyc_apply per table, which
+    upsizes before inserting."""
+    import torch
+    rng = np.random.default_rng(21)
+    nt = 8
+    A = _dg().DyCuckooSet([3000] * nt)
+    B = _dg().DyCuckooSet([3000] * nt)
+    _, caps = A.sizes()
+    maps = [O.Map() for _ in range(nt)]
+    for t in range(nt):
+        m = int(0.75 * int(caps[t]))
+        k = (np.arange(m, dtype=np.uint64) * 2654435761 % (1 << 31) + 1).astype(np.uint32)
+        k = np.unique(k)
+        v = rng.integers(0, 1 << 31, k.size).astype(np.uint32)
+        dk = torch.from_numpy(k.view(np.int32)).cuda()
+        dv = torch.from_numpy(v.view(np.int32)).cuda()
+        A.table(t).insert(dk, dv)
+        B.table(t).insert(dk, dv)
+        maps[t].insert(k, v)
+    assert np.array_equal(A.sizes()[1], caps)  # no upsize while preloading
+    cnt = (0.2 * caps.astype(np.float64)).astype(np.int64)
+    off = np.zeros(nt + 1, np.uint32)
+    off[1:] = np.cumsum(cnt)
+    n = int(off[-1])
+    keys = rng.integers((1 << 31) + 1, (1 << 32) - 1, n, dtype=np.uint64).astype(np.uint32)
+    ops = np.ones(n, np.uint8)
+    vals = rng.integers(0, 1 << 31, n).astype(np.uint32)
+    d = lambda a: torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).cuda()
+    oa, ba = A.apply(d(off), d(ops), d(keys), d(vals), h_offsets=off)
+    sa = A.stats()
+    ob, bb = B.apply(d(off), d(ops), d(keys), d(vals), h_offsets=off, each=True)
+    _check_round(A, maps, off, d(ops), d(keys), d(vals), oa, ba, "deferred upsize")
+    assert bool((oa == ob).all()) and bool((ba == bb).all())
+    sza, capa = A.sizes()
+    szb, capb = B.sizes()
+    assert np.array_equal(sza, szb)
+    assert np.array_equal(capa, capb), (capa, capb)
+    assert sa["resizes_up"] >= nt
+    for t in range(nt):
+        assert_same_contents(A.table(t), maps[t], "table %d contents" % t)
+    A.close()
+    B.close()
