@@ -37,20 +37,6 @@ __device__ __forceinline__ uint64_t warp_stride() {
     return ((uint64_t)gridDim.x * blockDim.x) & ~31ull;
 }
 
-// Entries a warp takes per pass of an eviction-walk kernel. A walk step
-// costs one dependent memory round trip per probe round (RO buckets), and a
-// short list leaves most of the grid idle, so short lists are spread over
-// every warp, down to one round (RO entries) per warp; long lists fill all
-// 32 lanes.
-template <int RO>
-__device__ __forceinline__ uint32_t walk_share(uint64_t n) {
-    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const uint64_t per = (n + warps - 1) / warps;
-    if (per <= (uint64_t)RO) return RO;
-    if (per >= 32) return 32;
-    return (uint32_t)((per + RO - 1) / RO * RO);
-}
-
 template <int KB, int SB>
 __device__ __forceinline__ typename SlotT<KB>::S *slot_ptr(char *bucket, int j) {
     return reinterpret_cast<typename SlotT<KB>::S *>(bucket + j * SlotT<KB>::kBytes);
@@ -608,12 +594,157 @@ __device__ __forceinline__ int pick_victim(unsigned pref, uint32_t rot) {
     return (int)((__ffs(rotated) - 1 + rot) % (uint32_t)B);
 }
 
+
 // ----------------------------------------------------------------------------
-// insert phase 3: eviction walks (warp_insert, cuckoo.cu:365-432). Each
-// entry of `src` first tries the empty slots of its first-probe bucket, then
-// of its second, then walks: exchange into the current bucket, carry the
-// resident to the other bucket of its own pair. An entry whose walk reaches
-// max_evict exchanges goes to `dst` for the host to place after an upsize.
+// Eviction walk with one-level lookahead, one entry per warp. A plain walk
+// exchanges the entry into its full bucket and carries the resident to that
+// resident's other bucket, which is full again with the probability of the
+// load factor, so the longest of a batch's chains (a dozen steps of
+// dependent memory round trips at load 0.8) sets the walk kernel's time.
+// Here the warp reads the full bucket, then the other buckets of all its
+// residents at once (group g of kG lanes reads resident g's, kRoundOps per
+// round), and evicts a resident whose other bucket has an empty slot: that
+// resident is placed by the next atomic, and a chain rarely needs a second
+// level. Without such a resident it evicts as the plain walk does (a
+// resident in its second bucket first). The same atomics as the plain walk
+// keep concurrent walks safe: an exchange hands the warp whatever was in the
+// slot, a claim succeeds only on a slot still empty, and the lookahead only
+// guides the choice.
+// Returns whether the carried entry was placed, the exchanges made and, if
+// not placed, the entry carried at the end (the caller re-places it).
+// Walk kernels switch to cooperative probing of 32 entries per warp when the
+// list holds more than this many entries per warp of the grid.
+constexpr int kCoopWalk = 4;
+
+template <int KB> struct WalkOut {
+    bool ok;
+    uint32_t steps;
+    typename SlotT<KB>::S left;
+};
+
+template <int KB, int SB>
+__device__ __forceinline__ WalkOut<KB> walk_lookahead(const Desc &D, typename SlotT<KB>::S e,
+                                                      uint32_t max_evict) {
+    using T = SlotT<KB>;
+    using Sl = typename T::S;
+    using K = typename T::K;
+    using Gm = Geo<KB, SB>;
+    constexpr int G = Gm::kG, RO = Gm::kRoundOps, NS = Gm::kSlots;
+    constexpr int LR = (NS + RO - 1) / RO;  // lookahead rounds
+    const int lane = threadIdx.x & 31, g = lane / G, r = lane % G;
+    uint32_t hk;
+    Pair pe;
+    char *fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);
+    uint32_t t = pe.first;
+    char *bp = fb;
+    uint32_t steps = 0;
+    for (uint32_t level = 0; level <= max_evict; ++level) {
+        Bucket<KB, SB> B;
+        B.template load<2>(bp);  // every lane: the same lines, one request
+        const unsigned em = B.empty_mask();
+        if (em) {
+            bool ok = false;
+            if (lane == 0) {
+                if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
+                ok = claim_empty<KB, SB>(bp, em, e);
+            }
+            if (__shfl_sync(kFull, ok, 0)) return {true, steps, T::empty()};
+            continue;  // the slots were taken meanwhile: read again
+        }
+        if (level == max_evict) break;
+        // lookahead: resident j = q * RO + g's other bucket, chunk r per lane
+        unsigned cand = 0u, pref = 0u;
+        char *alt[LR];
+        unsigned alt_em[LR];
+#pragma unroll
+        for (int q = 0; q < LR; ++q) {
+            const int j = q * RO + g;
+            K kj = 0;
+#pragma unroll
+            for (int x = 0; x < NS; ++x)
+                if (x == j) kj = T::key(B.s[x]);
+            const uint32_t hj = fold(kj);
+            const Pair pj = pair_of(hj, D.d);
+            const uint32_t tj = other_of(pj, t);
+            alt[q] = bucket_ptr<KB, SB>(D, tj, bucket_index(D, tj, hj));
+            unsigned m = 0u;
+            if (j < NS) {
+                uint32_t w[8];
+                ld_cg(alt[q] + r * 32, w);
+                constexpr int SPC = Gm::kSPC, WPS = T::kBytes / 4;
+#pragma unroll
+                for (int x = 0; x < SPC; ++x) {
+                    Sl sx;
+                    T::from_words(w + x * WPS, sx);
+                    const int idx = r * SPC + x;
+                    if (idx < NS && T::is_empty(sx)) m |= 1u << idx;
+                }
+            }
+#pragma unroll
+            for (int o = 1; o < G; o <<= 1) m |= __shfl_xor_sync(kFull, m, o);
+            alt_em[q] = m;
+            const unsigned have = __ballot_sync(kFull, r == 0 && j < NS && m != 0u);
+            const unsigned second = __ballot_sync(kFull, r == 0 && j < NS && pj.first != t);
+#pragma unroll
+            for (int x = 0; x < RO; ++x) {
+                if (q * RO + x >= NS) break;
+                cand |= ((have >> (x * G)) & 1u) << (q * RO + x);
+                pref |= ((second >> (x * G)) & 1u) << (q * RO + x);
+            }
+        }
+        const int j = pick_victim<KB, SB>(cand ? cand : pref, hk + level);
+        const int src = (j % RO) * G;
+        char *aj = nullptr;
+        unsigned aem = 0u;
+#pragma unroll
+        for (int q = 0; q < LR; ++q) {
+            char *a = (char *)shfl64((unsigned long long)alt[q], src);
+            const unsigned am = __shfl_sync(kFull, alt_em[q], src);
+            if (q == j / RO) {
+                aj = a;
+                aem = am;
+            }
+        }
+        K kj = 0;
+#pragma unroll
+        for (int x = 0; x < NS; ++x)
+            if (x == j) kj = T::key(B.s[x]);
+        // exchange the carried entry into slot j
+        Sl old = T::empty();
+        if (lane == 0) {
+            if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
+            old = T::exch(slot_ptr<KB, SB>(bp, j), e);
+        }
+        old = shfl_slot(old, 0);
+        ++steps;
+        if (T::is_empty(old)) return {true, steps, T::empty()};
+        // carry the resident to its other bucket
+        e = old;
+        const uint32_t from = t;
+        fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);
+        t = other_of(pe, from);
+        bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
+        if (((cand >> j) & 1u) && T::key(old) == kj) {  // bp == aj: its empty slots are known
+            bool ok = false;
+            if (lane == 0) {
+                if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
+                ok = claim_empty<KB, SB>(aj, aem, e);
+            }
+            if (__shfl_sync(kFull, ok, 0)) return {true, steps, T::empty()};
+        }
+    }
+    return {false, steps, e};
+}
+
+// ----------------------------------------------------------------------------
+// insert phase 3: eviction walks (warp_insert, cuckoo.cu:365-432). The
+// reference walks one entry per thread: exchange into the current bucket,
+// carry the resident to the other bucket of its own pair. Here each entry of
+// `src` is walked by a whole warp with one-level lookahead (walk_lookahead):
+// the first-probe bucket's empty slots first, then an exchange that
+// preferably evicts a resident whose other bucket has room. An entry whose
+// walk reaches max_evict exchanges goes to `dst` for the host to place after
+// an upsize.
 // ----------------------------------------------------------------------------
 template <int KB, int SB>
 __global__ void __launch_bounds__(256) k_walk(const __grid_constant__ Desc D,
@@ -624,81 +755,109 @@ __global__ void __launch_bounds__(256) k_walk(const __grid_constant__ Desc D,
                                               uint64_t max_entries) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
+    __shared__ unsigned long long s_sum[2];
+    if (threadIdx.x < 2) s_sum[threadIdx.x] = 0ull;
+    __syncthreads();
     uint64_t n = *src_count;
     if (n > max_entries) n = max_entries;
-    const uint32_t per = walk_share<Geo<KB, SB>::kRoundOps>(n);
     const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const uint64_t wid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31;
+    const bool lead = lane == 0;
     uint32_t n_ok = 0, n_steps = 0;
-    const uint32_t max_iter = 2u * max_evict + 8u;
-    for (uint64_t base = wid * per; base < n; base += warps * per) {
-        const uint64_t i = base + lane;
-        bool live = lane < per && i < n;
-        Sl e = live ? ((const Sl *)src)[i] : T::empty();
-        uint32_t hk = 0;
-        Pair pe{0u, 0u};
-        char *fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);  // first bucket of e
-        uint32_t t = pe.first;
-        char *bp = fb;
-        int mode = 0;  // 0: empties of the first bucket, 1: of the second, 2: walking
-        uint32_t evictions = 0;
-        bool fail = false;
-        for (uint32_t it = 0; it < max_iter; ++it) {
-            if (!__any_sync(kFull, live)) break;
-            const ProbeOut<KB> r = probe<KB, SB, 2, true, true>(bp, T::key(e), live, t, D.d);
-            if (!live) continue;
-            bool placed = false;
-            if (r.empty) {
-                if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
-                placed = claim_empty<KB, SB>(bp, r.empty, e);
-            }
-            if (placed) {
-                live = false;
-                ++n_ok;
-            } else if (mode == 0) {
-                mode = 1;
-                t = pe.second;
-                bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
-            } else if (mode == 1) {
-                mode = 2;
-                t = pe.first;
-                bp = fb;
-            } else if (r.empty) {
-                // every empty slot was taken by another lane: look again
-            } else if (evictions >= max_evict) {
-                live = false;
-                fail = true;
-            } else {
-                const int j = pick_victim<KB, SB>(r.pref, hk + evictions);
-                if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
-                const Sl old = T::exch(slot_ptr<KB, SB>(bp, j), e);
-                ++evictions;
-                ++n_steps;
-                if (T::is_empty(old)) {
+    if (n > (uint64_t)kCoopWalk * warps) {
+        // long list: 32 entries per warp, probed cooperatively (throughput)
+        const uint32_t max_iter = 2u * max_evict + 8u;
+        for (uint64_t base = wid * 32; base < n; base += warps * 32) {
+            const uint64_t i = base + lane;
+            bool live = i < n;
+            Sl e = live ? ((const Sl *)src)[i] : T::empty();
+            uint32_t hk = 0;
+            Pair pe{0u, 0u};
+            char *fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);  // first bucket of e
+            uint32_t t = pe.first;
+            char *bp = fb;
+            int mode = 0;  // 0: empties of the first bucket, 1: of the second, 2: walking
+            uint32_t evictions = 0;
+            bool fail = false;
+            for (uint32_t it = 0; it < max_iter; ++it) {
+                if (!__any_sync(kFull, live)) break;
+                const ProbeOut<KB> r = probe<KB, SB, 2, true, true>(bp, T::key(e), live, t, D.d);
+                if (!live) continue;
+                bool placed = false;
+                if (r.empty) {
+                    if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
+                    placed = claim_empty<KB, SB>(bp, r.empty, e);
+                }
+                if (placed) {
                     live = false;
                     ++n_ok;
-                } else {
-                    e = old;
-                    fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);
-                    t = other_of(pe, t);
+                } else if (mode == 0) {
+                    mode = 1;
+                    t = pe.second;
                     bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
+                } else if (mode == 1) {
+                    mode = 2;
+                    t = pe.first;
+                    bp = fb;
+                } else if (r.empty) {
+                    // every empty slot was taken by another lane: look again
+                } else if (evictions >= max_evict) {
+                    live = false;
+                    fail = true;
+                } else {
+                    const int j = pick_victim<KB, SB>(r.pref, hk + evictions);
+                    if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
+                    const Sl old = T::exch(slot_ptr<KB, SB>(bp, j), e);
+                    ++evictions;
+                    ++n_steps;
+                    if (T::is_empty(old)) {
+                        live = false;
+                        ++n_ok;
+                    } else {
+                        e = old;
+                        fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);
+                        t = other_of(pe, t);
+                        bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
+                    }
                 }
             }
+            if (live) fail = true;  // iteration bound reached
+            __syncwarp();
+            const unsigned long long at = agg_inc(dst_count, fail);
+            if (fail) {
+                if (at < dst_cap) ((Sl *)dst)[at] = e;
+                else atomicAdd(&ctr->spill, 1ull);
+            }
         }
-        if (live) fail = true;  // iteration bound reached
-        __syncwarp();
-        const unsigned long long at = agg_inc(dst_count, fail);
-        if (fail) {
-            if (at < dst_cap) ((Sl *)dst)[at] = e;
-            else atomicAdd(&ctr->spill, 1ull);
+    } else {
+        for (uint64_t i = wid; i < n; i += warps) {
+            const WalkOut<KB> w = walk_lookahead<KB, SB>(D, ((const Sl *)src)[i], max_evict);
+            if (!lead) continue;
+            n_steps += w.steps;
+            if (w.ok) {
+                ++n_ok;
+            } else {
+                const unsigned long long at = atomicAdd(dst_count, 1ull);
+                if (at < dst_cap) ((Sl *)dst)[at] = w.left;
+                else atomicAdd(&ctr->spill, 1ull);
+            }
         }
     }
-    if (count_new) {
-        agg_add(&ctr->inserted, n_ok);
-        agg_add(&ctr->size, n_ok);
+    n_ok = __reduce_add_sync(kFull, n_ok);
+    n_steps = __reduce_add_sync(kFull, n_steps);
+    if (lead && (n_ok | n_steps)) {
+        atomicAdd(&s_sum[0], (unsigned long long)n_ok);
+        atomicAdd(&s_sum[1], (unsigned long long)n_steps);
     }
-    agg_add(&ctr->evict_steps, n_steps);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (count_new && s_sum[0]) {
+            atomicAdd(&ctr->inserted, s_sum[0]);
+            atomicAdd(&ctr->size, s_sum[0]);
+        }
+        if (s_sum[1]) atomicAdd(&ctr->evict_steps, s_sum[1]);
+    }
 }
 
 // ----------------------------------------------------------------------------

@@ -213,8 +213,8 @@ __global__ void __launch_bounds__(256) k_set_mutate(
 }
 
 // eviction walks of src entries (k_walk per table, each with its own
-// eviction bound; max_evict is the largest, which bounds the loop); failures
-// go to dst
+// eviction bound; max_evict, the largest, bounds the cooperative loop);
+// failures go to dst
 template <int KB, int SB>
 __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs,
                                                   Counters *__restrict__ tctr,
@@ -226,90 +226,126 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
                                                   Counters *gctr, uint64_t max_entries) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
+    __shared__ unsigned long long s_sum[2];
+    if (threadIdx.x < 2) s_sum[threadIdx.x] = 0ull;
+    __syncthreads();
     uint64_t n = *src_count;
     if (n > max_entries) n = max_entries;
-    const uint32_t per = walk_share<Geo<KB, SB>::kRoundOps>(n);
     const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const uint64_t wid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31;
+    const bool lead = lane == 0;
     uint32_t n_ok = 0, n_steps = 0;
-    const uint32_t max_iter = 2u * max_evict + 8u;
-    for (uint64_t base = wid * per; base < n; base += warps * per) {
-        const uint64_t i = base + lane;
-        bool live = lane < per && i < n;
-        Sl e = live ? ((const Sl *)src)[i] : T::empty();
-        const uint32_t tb = live ? src_tid[i] : 0u;
-        const Desc &D = descs[tb];
-        uint32_t hk = 0;
-        Pair pe{0u, 0u};
-        char *fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);
-        uint32_t t = pe.first;
-        char *bp = fb;
-        // 0: empties of the first bucket, 1: of the second, 2: walking. The
-        // entries come from the upsert pass, which found both buckets full:
-        // the walk starts at the first bucket (still taking an empty slot
-        // there if one has appeared since).
-        int mode = 2;
-        uint32_t evictions = 0;
-        bool fail = false, ok = false;
-        for (uint32_t it = 0; it < max_iter; ++it) {
-            if (!__any_sync(kFull, live)) break;
-            const ProbeOut<KB> r = probe<KB, SB, 2, true, true>(bp, T::key(e), live, t, D.d);
-            if (!live) continue;
-            bool placed = false;
-            if (r.empty) {
-                if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
-                placed = claim_empty<KB, SB>(bp, r.empty, e);
-            }
-            if (placed) {
-                live = false;
-                ok = true;
-            } else if (mode == 0) {
-                mode = 1;
-                t = pe.second;
-                bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
-            } else if (mode == 1) {
-                mode = 2;
-                t = pe.first;
-                bp = fb;
-            } else if (r.empty) {
-                // every empty slot was taken by another lane: look again
-            } else if (evictions >= D.max_evict) {  // this table's bound
-                live = false;
-                fail = true;
-            } else {
-                const int j = pick_victim<KB, SB>(r.pref, hk + evictions);
-                if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
-                const Sl old = T::exch(slot_ptr<KB, SB>(bp, j), e);
-                ++evictions;
-                ++n_steps;
-                if (T::is_empty(old)) {
+    if (n > (uint64_t)kCoopWalk * warps) {
+        // long list: 32 entries per warp, probed cooperatively (throughput)
+        const uint32_t max_iter = 2u * max_evict + 8u;
+        for (uint64_t base = wid * 32; base < n; base += warps * 32) {
+            const uint64_t i = base + lane;
+            bool live = i < n;
+            Sl e = live ? ((const Sl *)src)[i] : T::empty();
+            const uint32_t tb = live ? src_tid[i] : 0u;
+            const Desc &D = descs[tb];
+            uint32_t hk = 0;
+            Pair pe{0u, 0u};
+            char *fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);
+            uint32_t t = pe.first;
+            char *bp = fb;
+            // 0: empties of the first bucket, 1: of the second, 2: walking. The
+            // entries come from the upsert pass, which found both buckets full:
+            // the walk starts at the first bucket (still taking an empty slot
+            // there if one has appeared since).
+            int mode = 2;
+            uint32_t evictions = 0;
+            bool fail = false, ok = false;
+            for (uint32_t it = 0; it < max_iter; ++it) {
+                if (!__any_sync(kFull, live)) break;
+                const ProbeOut<KB> r = probe<KB, SB, 2, true, true>(bp, T::key(e), live, t, D.d);
+                if (!live) continue;
+                bool placed = false;
+                if (r.empty) {
+                    if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
+                    placed = claim_empty<KB, SB>(bp, r.empty, e);
+                }
+                if (placed) {
                     live = false;
                     ok = true;
-                } else {
-                    e = old;  // a resident of the same table
-                    fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);
-                    t = other_of(pe, t);
+                } else if (mode == 0) {
+                    mode = 1;
+                    t = pe.second;
                     bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
+                } else if (mode == 1) {
+                    mode = 2;
+                    t = pe.first;
+                    bp = fb;
+                } else if (r.empty) {
+                    // every empty slot was taken by another lane: look again
+                } else if (evictions >= D.max_evict) {  // this table's bound
+                    live = false;
+                    fail = true;
+                } else {
+                    const int j = pick_victim<KB, SB>(r.pref, hk + evictions);
+                    if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
+                    const Sl old = T::exch(slot_ptr<KB, SB>(bp, j), e);
+                    ++evictions;
+                    ++n_steps;
+                    if (T::is_empty(old)) {
+                        live = false;
+                        ok = true;
+                    } else {
+                        e = old;  // a resident of the same table
+                        fb = first_bucket<KB, SB>(D, T::key(e), pe, hk);
+                        t = other_of(pe, t);
+                        bp = bucket_ptr<KB, SB>(D, t, bucket_index(D, t, hk));
+                    }
+                }
+            }
+            if (live) fail = true;  // iteration bound reached
+            __syncwarp();
+            n_ok += ok ? 1u : 0u;
+            warp_size_add(tctr, tb, ok, 1);
+            const unsigned long long at = agg_inc(dst_count, fail);
+            if (fail) {
+                if (at < dst_cap) {
+                    ((Sl *)dst)[at] = e;
+                    dst_tid[at] = tb;
+                } else {
+                    atomicAdd(&gctr->spill, 1ull);
                 }
             }
         }
-        if (live) fail = true;  // iteration bound reached
-        __syncwarp();
-        n_ok += ok ? 1u : 0u;
-        warp_size_add(tctr, tb, ok, 1);
-        const unsigned long long at = agg_inc(dst_count, fail);
-        if (fail) {
-            if (at < dst_cap) {
-                ((Sl *)dst)[at] = e;
-                dst_tid[at] = tb;
+    } else {
+        for (uint64_t i = wid; i < n; i += warps) {
+            const Sl e = ((const Sl *)src)[i];
+            const uint32_t tb = src_tid[i];
+            const Desc &D = descs[tb];
+            const WalkOut<KB> w = walk_lookahead<KB, SB>(D, e, D.max_evict);
+            if (!lead) continue;
+            n_steps += w.steps;
+            if (w.ok) {
+                ++n_ok;
+                atomicAdd(&tctr[tb].size, 1ull);
             } else {
-                atomicAdd(&gctr->spill, 1ull);
+                const unsigned long long at = atomicAdd(dst_count, 1ull);
+                if (at < dst_cap) {
+                    ((Sl *)dst)[at] = w.left;
+                    dst_tid[at] = tb;
+                } else {
+                    atomicAdd(&gctr->spill, 1ull);
+                }
             }
         }
     }
-    agg_add(&gctr->inserted, n_ok);
-    agg_add(&gctr->evict_steps, n_steps);
+    n_ok = __reduce_add_sync(kFull, n_ok);
+    n_steps = __reduce_add_sync(kFull, n_steps);
+    if (lead && (n_ok | n_steps)) {
+        atomicAdd(&s_sum[0], (unsigned long long)n_ok);
+        atomicAdd(&s_sum[1], (unsigned long long)n_steps);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_sum[0]) atomicAdd(&gctr->inserted, s_sum[0]);
+        if (s_sum[1]) atomicAdd(&gctr->evict_steps, s_sum[1]);
+    }
 }
 
 }  // namespace dyc
