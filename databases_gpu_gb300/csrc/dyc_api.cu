@@ -143,6 +143,8 @@ struct dyc_table {
     size_t apply_bytes = 0;
     dyc::ApplyScratch A{};
     unsigned long long *h_actr = nullptr;  // pinned copy of A.ctr
+    Desc *d_desc = nullptr;  // device copy of D for the mixed-batch probe kernels
+    Desc *h_desc = nullptr;  // its pinned mirror (the last pushed state)
     // host-form staging
     cudaStream_t io_stream = nullptr;
     void *d_io = nullptr;
@@ -523,6 +525,8 @@ dyc_status dyc_destroy(dyc_table *t) {
     if (t->scratch) cudaFree(t->scratch);
     if (t->apply_buf) cudaFree(t->apply_buf);
     if (t->h_actr) cudaFreeHost(t->h_actr);
+    if (t->d_desc) cudaFree(t->d_desc);
+    if (t->h_desc) cudaFreeHost(t->h_desc);
     if (t->d_io) cudaFree(t->d_io);
     if (t->io_stream) cudaStreamDestroy(t->io_stream);
     for (int i = 0; i < 3; ++i) {
@@ -828,7 +832,8 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
         ops * 4,                                      // sort_tmp
         multi ? ops * 4 : 0,                          // dtid
         multi ? ops * 4 : 0, multi ? ops * 4 : 0,     // up_tid, er_tid
-        multi ? (size_t)ntables * 4 : 0,              // tnew
+        multi ? (size_t)ntables * 4 : 0,              // tup
+        multi ? (size_t)ntables * 4 : 0,              // ter
         multi ? ((size_t)ntables + 1) * 4 : 0};       // tcell_off
     size_t need = 0;
     for (size_t b : sizes) need += (b + 255) & ~(size_t)255;
@@ -867,7 +872,8 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
     A.dtid = (uint32_t *)carve();
     A.up_tid = (uint32_t *)carve();
     A.er_tid = (uint32_t *)carve();
-    A.tnew = (uint32_t *)carve();
+    A.tup = (uint32_t *)carve();
+    A.ter = (uint32_t *)carve();
     A.tcell_off = (uint32_t *)carve();
     A.ntables = ntables;
     A.cap_cells = cells;
@@ -879,9 +885,24 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
 // Mixed-batch scratch of a single table for `n` ops per chunk (grow only).
 dyc_status ensure_apply(dyc_table *t, uint64_t n) {
     const uint64_t ops = n < 128 ? 128 : n;
+    if (!t->d_desc) {
+        CK(cudaMalloc(&t->d_desc, sizeof(Desc)));
+        CK(cudaMallocHost(&t->h_desc, sizeof(Desc)));
+        memset(t->h_desc, 0, sizeof(Desc));  // differs from any live D: the first push copies
+    }
     if (t->apply_buf && t->A.cap_ops >= ops) return DYC_OK;
     if (!t->h_actr) CK(cudaMallocHost(&t->h_actr, dyc::kCtrSlots * sizeof(unsigned long long)));
     return carve_apply(t->kb, t->vb, ops, 2 * ops, 0, &t->apply_buf, &t->apply_bytes, &t->A);
+}
+
+// Copy D to the device if it changed since the last push. The pinned mirror
+// is rewritten only after the previous copy has run: every mixed-batch chunk
+// ends with a host read of the stream, and a push inside a chunk follows one.
+dyc_status push_desc(dyc_table *t, cudaStream_t s) {
+    if (memcmp(t->h_desc, &t->D, sizeof(Desc)) == 0) return DYC_OK;
+    *t->h_desc = t->D;
+    CK(cudaMemcpyAsync(t->d_desc, t->h_desc, sizeof(Desc), cudaMemcpyHostToDevice, s));
+    return DYC_OK;
 }
 
 dyc_status read_apply_counters(dyc_table *t, cudaStream_t s) {
@@ -891,35 +912,80 @@ dyc_status read_apply_counters(dyc_table *t, cudaStream_t s) {
     return DYC_OK;
 }
 
+// A chunk of n mixed ops: grouping, scatter and replay (dyc_apply.cuh), then
+// the table-set probe kernels (dyc_set.cuh) with this table's one-entry
+// descriptor array: the find of the distinct keys, one pass for the erases
+// and upserts, the eviction walks. Every kernel reads its item count on the
+// device, so the host reads the counters once, at the end. The upsize
+// policy (api.cpp:359-369: the size after the batch's erases plus its
+// inserts above upper bound x capacity) needs the batch's upsert and erase
+// counts: where even n inserts fit the table's slots it is applied after the
+// batch with the same counts, so the capacity ends as if it had run first
+// (entries the fuller table could not place take the overflow path);
+// otherwise the host reads the counts after the replay and upsizes first.
 dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const void *vals,
                        uint64_t n, void *vals_out, uint32_t *bits_out, uint32_t flags,
                        cudaStream_t s) {
     const dyc::ApplyScratch &A = t->A;
     const LaunchCtx L = ctx(t, s);
     const uint32_t vb = (uint32_t)t->vb;
+    const bool resize = t->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE);
+    const bool deferred = !resize || t->size + n <= t->capacity;
+    const uint64_t size0 = t->size;
+    bool grew = false;
+    auto upsize_policy = [&]() -> dyc_status {
+        const uint64_t nu = t->h_actr[dyc::kCtrUp], ne = t->h_actr[dyc::kCtrEr];
+        int guard = 0;
+        while (resize && nu &&
+               (double)size0 - (double)ne + (double)nu > t->cfg.upper_load * (double)t->capacity &&
+               guard++ < 64) {
+            TRY(resize_up_impl(t, s));
+            grew = true;
+        }
+        return DYC_OK;
+    };
+    TRY(push_desc(t, s));
+    TRY(reset_call_counters(t, s));
     CK(cudaMemsetAsync(A.cells, 0, (size_t)(2 * n) * (t->kb == 4 ? 8 : 16), s));  // 2n cells used
     CK(cudaMemsetAsync(A.ctr, 0, dyc::kCtrSlots * sizeof(unsigned long long), s));
     if (bits_out) CK(cudaMemsetAsync(bits_out, 0, (size_t)((n + 31) / 32) * 4, s));
     cudaError_t e = KB_CALL(t, apply_group, L, A, keys, n);
-    if (e != cudaSuccess) return fail(DYC_ECUDA, "apply group kernels: %s", cudaGetErrorString(e));
-    TRY(read_apply_counters(t, s));
-    const uint64_t nd = t->h_actr[dyc::kCtrDistinct];
-    e = KB_CALL(t, apply_scatter, L, A, n);
+    if (e == cudaSuccess) e = KB_CALL(t, apply_scatter, L, A, n);
     // state of every distinct key before the batch
-    if (e == cudaSuccess) e = KB_CALL(t, find, L, t->D, t->sb, A.dkey, A.pre_val, vb, A.pre_hit, nd);
-    if (e == cudaSuccess) e = KB_CALL(t, apply_replay, L, A, ops, vals, vb, vals_out, bits_out, n, nd);
-    if (e != cudaSuccess) return fail(DYC_ECUDA, "apply replay kernels: %s", cudaGetErrorString(e));
-    TRY(read_apply_counters(t, s));
-    const uint64_t nu = t->h_actr[dyc::kCtrUp], ne = t->h_actr[dyc::kCtrEr];
-    if (ne) TRY(erase_chunk(t, A.er_key, ne, nullptr, DYC_FLAG_UNIQUE, s));
-    if (nu) {
-        if (t->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE)) {
-            int guard = 0;
-            while ((double)(t->size + nu) > t->cfg.upper_load * (double)t->capacity &&
-                   guard++ < 64)
-                TRY(resize_up_impl(t, s));
-        }
-        TRY(insert_chunk(t, A.up_key, A.up_val, nu, DYC_FLAG_UNIQUE, s));
+    if (e == cudaSuccess)
+        e = KB_CALL(t, set_find, L, t->d_desc, t->sb, A.dkey, nullptr, &A.ctr[dyc::kCtrDistinct],
+                    n, A.pre_val, vb, A.pre_hit);
+    if (e == cudaSuccess) e = KB_CALL(t, apply_replay, L, A, ops, vals, vb, vals_out, bits_out, n, n);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "apply kernels: %s", cudaGetErrorString(e));
+    if (!deferred) {
+        TRY(read_apply_counters(t, s));
+        TRY(upsize_policy());
+        if (grew) TRY(push_desc(t, s));
+    }
+    e = KB_CALL(t, set_mutate, L, t->d_desc, t->d_ctr, t->sb, A.er_key, nullptr,
+                &A.ctr[dyc::kCtrEr], A.up_key, A.up_val, vb, nullptr, &A.ctr[dyc::kCtrUp], n,
+                t->S.list_a, nullptr, t->S.list_cap, t->d_ctr);
+    if (e == cudaSuccess)
+        e = KB_CALL(t, set_walk, L, t->d_desc, t->d_ctr, t->sb, t->S.list_a, nullptr,
+                    &t->d_ctr->pending, t->S.list_b, nullptr, &t->d_ctr->overflow,
+                    t->S.list_cap, t->cfg.max_evictions, t->d_ctr, t->S.list_cap);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "apply probe kernels: %s", cudaGetErrorString(e));
+    CK(cudaMemcpyAsync(t->h_actr, A.ctr, dyc::kCtrSlots * sizeof(unsigned long long),
+                       cudaMemcpyDeviceToHost, s));
+    TRY(read_counters(t, s));
+    if (deferred) TRY(upsize_policy());
+    const Counters c = *t->h_ctr;
+    dyc_op_stats &St = t->last;
+    St.inserted += c.inserted;
+    St.updated += c.updated;
+    St.erased += c.erased;
+    St.evict_steps += c.evict_steps;
+    St.overflowed += c.overflow;
+    if (c.overflow) {
+        TRY(drain(t, s, t->S.list_b, &t->d_ctr->overflow, t->S.list_a, &t->d_ctr->pending,
+                  t->S.list_cap, true, !grew));
+        St.inserted += t->h_ctr->inserted - c.inserted;
+        St.evict_steps += t->h_ctr->evict_steps - c.evict_steps;
     }
     return DYC_OK;
 }
@@ -1066,7 +1132,7 @@ struct dyc_set {
     void *list_a = nullptr, *list_b = nullptr;
     uint32_t *tid_a = nullptr, *tid_b = nullptr;
     uint64_t list_cap = 0;
-    uint32_t *h_tnew = nullptr;            // pinned copy of A.tnew
+    uint32_t *h_tup = nullptr, *h_ter = nullptr;  // pinned copies of A.tup / A.ter
     uint32_t *d_bits_tmp = nullptr;        // dyc_set_apply_each: one table's result bits
     size_t bits_tmp_words = 0;
     // CUDA graphs of the launch sequences (phase A, phase B, both), one entry
@@ -1190,8 +1256,11 @@ dyc_status set_phase_a(dyc_set *s, const uint32_t *d_off, const uint8_t *ops, co
     if (e == cudaSuccess)
         e = SET_KB_CALL(s, apply_replay, L, A, ops, vals, vb, out, bits, n, n, d_n);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "set phase A kernels: %s", cudaGetErrorString(e));
-    if (new_counts)  // keys each table gains, for the upsize decision
-        CK(cudaMemcpyAsync(s->h_tnew, A.tnew, (size_t)s->ntables * 4, cudaMemcpyDeviceToHost, st));
+    if (new_counts)  // each table's upserts, for the upsize decision
+    {
+        CK(cudaMemcpyAsync(s->h_tup, A.tup, (size_t)s->ntables * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(s->h_ter, A.ter, (size_t)s->ntables * 4, cudaMemcpyDeviceToHost, st));
+    }
     return DYC_OK;
 }
 
@@ -1338,7 +1407,8 @@ dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_desc, sizeof(Desc) * ntables);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_gctr, sizeof(Counters));
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_gctr, sizeof(Counters));
-    if (e == cudaSuccess) e = cudaMallocHost(&s->h_tnew, sizeof(uint32_t) * ntables);
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_tup, sizeof(uint32_t) * ntables);
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_ter, sizeof(uint32_t) * ntables);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming);
@@ -1378,7 +1448,8 @@ dyc_status dyc_set_destroy(dyc_set *s) {
     if (s->h_desc) cudaFreeHost(s->h_desc);
     if (s->d_gctr) cudaFree(s->d_gctr);
     if (s->h_gctr) cudaFreeHost(s->h_gctr);
-    if (s->h_tnew) cudaFreeHost(s->h_tnew);
+    if (s->h_tup) cudaFreeHost(s->h_tup);
+    if (s->h_ter) cudaFreeHost(s->h_ter);
     if (s->abuf) cudaFree(s->abuf);
     if (s->lbuf) cudaFree(s->lbuf);
     if (s->d_bits_tmp) cudaFree(s->d_bits_tmp);
@@ -1456,11 +1527,13 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
     const uint64_t ng = gr ? s->A.cap_ops : n;
     const bool resize = s->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE);
     // The upsize policy (hash_insert_batch, api.cpp:359-369, per table): while
-    // size + the keys the batch adds > upper bound x capacity, upsize. The
-    // keys added are known on the device after phase A. Where even a batch
-    // of nothing but new keys stays within a table's slots, the batch runs
-    // both phases back to back and the policy is applied after it with the
-    // same sizes and counts, so capacities end as if it had run before the
+    // size + the batch's inserts > upper bound x capacity, upsize, where the
+    // inserts are the table's upserts after the batch is reduced per key and
+    // the size is the one after the table's erases (as in dyc_apply), both
+    // known on the device after phase A. Where even a batch of
+    // nothing but new keys stays within a table's slots, the batch runs both
+    // phases back to back and the policy is applied after it with the same
+    // sizes and counts, so capacities end as if it had run before the
     // inserts (entries a fuller table could not place go through the
     // overflow path). Otherwise the host reads the counts between the phases
     // and upsizes first.
@@ -1476,9 +1549,11 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
     auto upsize_policy = [&]() -> dyc_status {
         for (uint32_t t = 0; t < s->ntables; ++t) {
             dyc_table *m = s->tables[t];
-            const uint64_t add = s->h_tnew[t];
+            const uint64_t add = s->h_tup[t];
+            // the size the inserts meet: the table's erases go first, as in dyc_apply
+            const double base = (double)m->size - (double)s->h_ter[t];
             int guard = 0;
-            while (add && (double)(m->size + add) > m->cfg.upper_load * (double)m->capacity &&
+            while (add && base + (double)add > m->cfg.upper_load * (double)m->capacity &&
                    guard++ < 64) {
                 TRY(resize_up_impl(m, st));
                 moved = true;

@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) k_set_prep(const __grid_constant__ ApplyS
     if (gctr != nullptr && id < gctr_words) gctr[id] = 0ull;
     for (uint64_t t = id; t <= A.ntables; t += stride) {
         A.tcell_off[t] = 2u * off[t];
-        if (t < A.ntables) A.tnew[t] = 0u;
+        if (t < A.ntables) A.tup[t] = A.ter[t] = 0u;
     }
     const uint64_t words = 2 * n * (cell_bytes<KB>() / 8);
     for (uint64_t c = id; c < words; c += stride) ((unsigned long long *)A.cells)[c] = 0ull;
@@ -336,12 +336,15 @@ __device__ __forceinline__ void record_final_one(const ApplyScratch &A, uint32_t
         else ((unsigned long long *)A.up_val)[u] = value;
         if (A.dtid) {
             A.up_tid[u] = A.dtid[d];
-            if (!pre_present) atomicAdd(&A.tnew[A.dtid[d]], 1u);
+            atomicAdd(&A.tup[A.dtid[d]], 1u);
         }
     } else if (!present && pre_present) {
         const uint32_t e = (uint32_t)atomicAdd(&A.ctr[kCtrEr], 1ull);
         ((K *)A.er_key)[e] = k;
-        if (A.dtid) A.er_tid[e] = A.dtid[d];
+        if (A.dtid) {
+            A.er_tid[e] = A.dtid[d];
+            atomicAdd(&A.ter[A.dtid[d]], 1u);
+        }
     }
 }
 
@@ -408,7 +411,7 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
     // the block_alloc call
     for (uint64_t d0 = (uint64_t)blockIdx.x * blockDim.x; d0 < nd; d0 += stride) {
         const uint64_t d = d0 + threadIdx.x;
-        bool up = false, er = false, wp = false, md = false, fresh = false;
+        bool up = false, er = false, wp = false, md = false;
         K k = 0;
         uint64_t value = 0ull;
         uint32_t tid = 0u;
@@ -450,7 +453,6 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
                 }
                 up = present && (!pre_present || value != pre_value);
                 er = !present && pre_present;
-                fresh = up && !pre_present;
                 if (A.dtid) tid = A.dtid[d];
             }
         }
@@ -459,7 +461,10 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
                            (unsigned long long)up | ((unsigned long long)er << 16) |
                                ((unsigned long long)wp << 32) | ((unsigned long long)md << 48),
                            got);
-        if (A.tnew) warp_count_by(A.tnew, tid, fresh);
+        if (A.tup) {
+            warp_count_by(A.tup, tid, up);
+            warp_count_by(A.ter, tid, er);
+        }
         if (up) {
             ((K *)A.up_key)[got[0]] = k;
             if (vb == 4) ((uint32_t *)A.up_val)[got[0]] = (uint32_t)value;
@@ -548,7 +553,10 @@ __global__ void __launch_bounds__(256) k_apply_replay_warp(const __grid_constant
         const uint32_t tid = (rvalid && A.dtid) ? A.dtid[rd] : 0u;
         const uint32_t u = (uint32_t)agg_inc(&A.ctr[kCtrUp], up);
         const uint32_t e = (uint32_t)agg_inc(&A.ctr[kCtrEr], er);
-        if (A.tnew) warp_count_by(A.tnew, tid, up && !rpre);
+        if (A.tup) {
+            warp_count_by(A.tup, tid, up);
+            warp_count_by(A.ter, tid, er);
+        }
         if (up) {
             ((K *)A.up_key)[u] = ((const K *)A.dkey)[rd];
             if (vb == 4) ((uint32_t *)A.up_val)[u] = (uint32_t)rvalue;

@@ -75,7 +75,8 @@ struct ApplyScratch {
     // multi-table batches
     uint32_t *dtid;            // table of a distinct key
     uint32_t *up_tid, *er_tid; // table of each upsert / erase
-    uint32_t *tnew;            // per table: keys the batch adds
+    uint32_t *tup;             // per table: upserts listed (the upsize policy's insert batch)
+    uint32_t *ter;             // per table: erases listed (keys present before the batch)
     uint32_t *tcell_off;       // per table: first cell of its region (ntables + 1)
     uint32_t ntables;
 };

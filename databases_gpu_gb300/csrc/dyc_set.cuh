@@ -4,7 +4,9 @@
 // table's descriptor from a device array, so one grid-stride launch serves
 // the work of every table in the set. Item counts are read on the device
 // (the counters the mixed-batch kernels fill), so a batch's launch sequence
-// needs no host reads and can be captured as a CUDA graph.
+// needs no host reads and can be captured as a CUDA graph. A null table-id
+// array means table 0 for every item: a single table's mixed batch runs
+// through the same kernels with a one-entry descriptor array.
 #pragma once
 
 #include "dyc_apply.cuh"
@@ -41,7 +43,7 @@ __global__ void __launch_bounds__(256) k_set_find(const Desc *__restrict__ descs
         uint32_t tb = 0u;
         if (i < n) {
             k = load_key<KB>(keys, i);
-            tb = tids[i];
+            tb = tids ? tids[i] : 0u;
         }
         const Desc &D = descs[tb];
         const bool act = k != 0;
@@ -82,7 +84,7 @@ __device__ __forceinline__ bool set_erase_warp(const Desc *__restrict__ descs,
     uint32_t tb = 0u;
     if (i < n) {
         k = load_key<KB>(keys, i);
-        tb = tids[i];
+        tb = tids ? tids[i] : 0u;
     }
     const Desc &D = descs[tb];
     const bool act = k != 0;
@@ -133,7 +135,7 @@ __device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs,
     Sl e = T::empty();
     if (i < n) {
         k = load_key<KB>(keys, i);
-        tb = tids[i];
+        tb = tids ? tids[i] : 0u;
         act = k != 0;
         if (act) e = T::make(k, load_val(vals, vb, i));
     }
@@ -173,7 +175,7 @@ __device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs,
     if (pend) {
         if (at < list_cap) {
             ((Sl *)list_a)[at] = e;
-            list_a_tid[at] = tb;
+            if (list_a_tid) list_a_tid[at] = tb;
         } else {
             atomicAdd(&gctr->spill, 1ull);
         }
@@ -243,7 +245,7 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
             const uint64_t i = base + lane;
             bool live = i < n;
             Sl e = live ? ((const Sl *)src)[i] : T::empty();
-            const uint32_t tb = live ? src_tid[i] : 0u;
+            const uint32_t tb = (live && src_tid) ? src_tid[i] : 0u;
             const Desc &D = descs[tb];
             uint32_t hk = 0;
             Pair pe{0u, 0u};
@@ -307,7 +309,7 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
             if (fail) {
                 if (at < dst_cap) {
                     ((Sl *)dst)[at] = e;
-                    dst_tid[at] = tb;
+                    if (dst_tid) dst_tid[at] = tb;
                 } else {
                     atomicAdd(&gctr->spill, 1ull);
                 }
@@ -316,7 +318,7 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
     } else {
         for (uint64_t i = wid; i < n; i += warps) {
             const Sl e = ((const Sl *)src)[i];
-            const uint32_t tb = src_tid[i];
+            const uint32_t tb = src_tid ? src_tid[i] : 0u;
             const Desc &D = descs[tb];
             const WalkOut<KB> w = walk_lookahead<KB, SB>(D, e, D.max_evict);
             if (!lead) continue;
@@ -328,7 +330,7 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
                 const unsigned long long at = atomicAdd(dst_count, 1ull);
                 if (at < dst_cap) {
                     ((Sl *)dst)[at] = w.left;
-                    dst_tid[at] = tb;
+                    if (dst_tid) dst_tid[at] = tb;
                 } else {
                     atomicAdd(&gctr->spill, 1ull);
                 }

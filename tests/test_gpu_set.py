@@ -209,10 +209,13 @@ def test_set_graph_reuses_buffers_across_batch_sizes():
     S.close()
 
 
-def test_set_deferred_upsize_matches_per_table_path():
-    """Tables preloaded to 75 % of their slots (below the 0.8 upper bound),
-    then a batch of new keys worth 20 % more: the batch fits the slots, so
-    the set runs it without a host
+@pytest.mark.parametrize("kind", ["new_keys", "half_updates"])
+def test_set_deferred_upsize_matches_per_table_path(kind):
+    """new_keys: tables preloaded to 75 % of their slots (below the 0.8 upper
+    bound), then a batch of new keys worth 20 % more. half_updates: preloaded
+    to 70 %, a batch worth 16 % of which half update present keys, so only
+    counting every insert (as the reference's policy does) passes the bound.
+    Either batch fits the slots, so the set runs it without a host
     round trip and applies the upsize policy afterwards (entries the fuller
     tables could not place take the overflow path). Results, sizes,
     capacities and contents equal those of one dyc_apply per table, which
@@ -224,8 +227,11 @@ def test_set_deferred_upsize_matches_per_table_path():
     B = _dg().DyCuckooSet([3000] * nt)
     _, caps = A.sizes()
     maps = [O.Map() for _ in range(nt)]
+    pre = 0.75 if kind == "new_keys" else 0.70
+    share = 0.2 if kind == "new_keys" else 0.16
+    preloaded = []
     for t in range(nt):
-        m = int(0.75 * int(caps[t]))
+        m = int(pre * int(caps[t]))
         k = (np.arange(m, dtype=np.uint64) * 2654435761 % (1 << 31) + 1).astype(np.uint32)
         k = np.unique(k)
         v = rng.integers(0, 1 << 31, k.size).astype(np.uint32)
@@ -234,12 +240,17 @@ def test_set_deferred_upsize_matches_per_table_path():
         A.table(t).insert(dk, dv)
         B.table(t).insert(dk, dv)
         maps[t].insert(k, v)
+        preloaded.append(k)
     assert np.array_equal(A.sizes()[1], caps)  # no upsize while preloading
-    cnt = (0.2 * caps.astype(np.float64)).astype(np.int64)
+    cnt = (share * caps.astype(np.float64)).astype(np.int64)
     off = np.zeros(nt + 1, np.uint32)
     off[1:] = np.cumsum(cnt)
     n = int(off[-1])
     keys = rng.integers((1 << 31) + 1, (1 << 32) - 1, n, dtype=np.uint64).astype(np.uint32)
+    if kind == "half_updates":
+        for t in range(nt):
+            a, h = int(off[t]), int(cnt[t]) // 2
+            keys[a:a + h] = rng.choice(preloaded[t], h, replace=False)
     ops = np.ones(n, np.uint8)
     vals = rng.integers(0, 1 << 31, n).astype(np.uint32)
     d = lambda a: torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).cuda()
