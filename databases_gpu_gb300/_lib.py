@@ -45,7 +45,8 @@ class DycOpStats(C.Structure):
 
 class DycServerConfig(C.Structure):
     _fields_ = [("hbm_cap_bytes", C.c_uint64), ("max_step_ops", C.c_uint64),
-                ("coalesce", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+                ("coalesce", C.c_uint32), ("pad0", C.c_uint32),
+                ("pool_reserve_bytes", C.c_uint64), ("reserved", C.c_uint32 * 4)]
 
 
 class DycServerStats(C.Structure):
@@ -66,6 +67,7 @@ EXPORTS = [
     "dyc_resize_up", "dyc_resize_down", "dyc_size", "dyc_capacity", "dyc_layout",
     "dyc_subtable", "dyc_export", "dyc_last_stats", "dyc_insert_host", "dyc_find_host",
     "dyc_erase_host", "dyc_status_string", "dyc_last_error", "dyc_erase_noalloc", "dyc_apply",
+    "dyc_pool_reserve",
     "dyc_set_create", "dyc_set_destroy", "dyc_set_table", "dyc_set_sizes", "dyc_set_apply",
     "dyc_set_apply_each", "dyc_set_last_stats", "dyc_set_configure",
     "dyc_server_config_default", "dyc_server_create", "dyc_server_destroy", "dyc_server_submit",
@@ -87,6 +89,7 @@ def _declare(L):
         "dyc_config_default": (None, [C.POINTER(DycConfig)]),
         "dyc_create": (st, [C.POINTER(DycConfig), C.POINTER(C.c_void_p)]),
         "dyc_destroy": (st, [T]),
+        "dyc_pool_reserve": (st, [C.c_int32, u64]),
         "dyc_insert": (st, [T, vp, vp, u64, u32, vp]),
         "dyc_find": (st, [T, vp, vp, vp, u64, vp]),
         "dyc_erase": (st, [T, vp, u64, vp, C.POINTER(u64), u32, vp]),

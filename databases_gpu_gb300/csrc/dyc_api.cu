@@ -538,6 +538,32 @@ dyc_status dyc_destroy(dyc_table *t) {
     return DYC_OK;
 }
 
+dyc_status dyc_pool_reserve(int32_t device, uint64_t bytes) {
+    if (bytes == 0) return DYC_OK;
+    int cur = -1;
+    CK(cudaGetDevice(&cur));
+    if (cur != device) CK(cudaSetDevice(device));
+    cudaMemPool_t pool = nullptr;
+    CK(lib_pool(device, &pool));
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const uint64_t keep = total_b / 4;  // the pool's release threshold
+    if (bytes > keep) bytes = keep;
+    cudaStream_t s = nullptr;
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    void *p = nullptr;
+    cudaError_t e = cudaMallocFromPoolAsync(&p, (size_t)bytes, pool, s);
+    if (e == cudaSuccess) e = cudaFreeAsync(p, s);
+    const cudaError_t e2 = cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    if (cur != device) cudaSetDevice(cur);
+    if (e == cudaErrorMemoryAllocation) return fail(DYC_ENOMEM, "pool reserve of %llu bytes",
+                                                    (unsigned long long)bytes);
+    if (e != cudaSuccess || e2 != cudaSuccess)
+        return fail(DYC_ECUDA, "pool reserve: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+    return DYC_OK;
+}
+
 dyc_status dyc_insert(dyc_table *t, const void *d_keys, const void *d_vals, uint64_t n,
                       uint32_t flags, void *stream) {
     if (!t) return fail(DYC_EINVAL, "null table");

@@ -57,7 +57,8 @@ template <int KB> __device__ __forceinline__ uint32_t *cell_word(void *cells, ui
 }
 
 // Claim (or join) key k's cell in region [base, base + size): fastrange
-// start, linear probing. One 64-bit CAS claims a new 4-byte key with count 1.
+// start, linear probing. One CAS (64-bit for 4-byte keys, 128-bit for
+// 8-byte keys) claims a new key with count 1.
 // (L2 atomic throughput bounds the grouping kernels; keeping several first
 // probes of a thread in flight measured slower.)
 template <int KB>
@@ -76,10 +77,12 @@ __device__ __forceinline__ uint32_t claim_cell(void *cells, uint64_t base, uint6
                 return (uint32_t)c;
             }
         } else {
-            unsigned long long *p = (unsigned long long *)((char *)cells + c * 16);
-            const unsigned long long old = atomicCAS(p, 0ull, (unsigned long long)k);
-            if (old == 0ull || old == k) {
-                atomicAdd((unsigned *)(p + 1), 1u);
+            // one 128-bit CAS claims a new key with count 1; a repeat adds 1
+            u128 *p = (u128 *)((char *)cells + c * 16);
+            const u128 old = SlotT<8>::cas(p, u128{0ull, 0ull}, u128{(unsigned long long)k, 1ull});
+            if (old.lo == 0ull) return (uint32_t)c;
+            if (old.lo == k) {
+                atomicAdd((unsigned *)&p->hi, 1u);
                 return (uint32_t)c;
             }
         }

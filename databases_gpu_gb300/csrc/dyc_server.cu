@@ -9,10 +9,9 @@
 //               issues the host->device copies (upload stream)
 //   executor  : runs the slot's step on the device (dyc_set_apply, or
 //               dyc_apply per request without coalescing) once its upload is
-//               done, then issues the device->host copy of the results
-//               (download stream)
-//   completer : waits for the download, hands every request its values and
-//               bits, frees the slot
+//               done
+//   completer : copies the step's results device->host (download stream),
+//               hands every request its values and bits, frees the slot
 // so one step's uploads and the previous step's downloads overlap the
 // current step's kernels. Only this file's public calls touch the set.
 #include <algorithm>
@@ -322,16 +321,7 @@ void executor(dyc_server *s) {
             else dyc_last_stats(s->members[sl.reqs[0]->tenant], &os);
         }
         const uint64_t tb = r == DYC_OK ? table_device_bytes(s) : 0;
-        if (r == DYC_OK) {
-            cudaError_t e = cudaMemcpyAsync(sl.h_out, sl.d_out, sl.n * s->vb,
-                                            cudaMemcpyDeviceToHost, s->down);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(sl.h_bits, sl.d_bits, (sl.n + 31) / 32 * 4,
-                                    cudaMemcpyDeviceToHost, s->down);
-            if (e == cudaSuccess) e = cudaEventRecord(sl.down, s->down);
-            if (e != cudaSuccess) r = DYC_ECUDA;
-        }
-        sl.status = r;
+        sl.status = r;  // the completer downloads the results (the step has finished)
         std::lock_guard<std::mutex> g(s->mu);
         if (r == DYC_OK) s->table_bytes = tb;
         s->st.steps++;
@@ -363,8 +353,16 @@ void completer(dyc_server *s) {
             s->to_complete.pop_front();
         }
         Slot &sl = s->slot[b];
-        if (sl.status == DYC_OK && cudaEventSynchronize(sl.down) != cudaSuccess)
-            sl.status = DYC_ECUDA;
+        if (sl.status == DYC_OK) {
+            cudaError_t e = cudaMemcpyAsync(sl.h_out, sl.d_out, sl.n * s->vb,
+                                            cudaMemcpyDeviceToHost, s->down);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(sl.h_bits, sl.d_bits, (sl.n + 31) / 32 * 4,
+                                    cudaMemcpyDeviceToHost, s->down);
+            if (e == cudaSuccess) e = cudaEventRecord(sl.down, s->down);
+            if (e == cudaSuccess) e = cudaEventSynchronize(sl.down);
+            if (e != cudaSuccess) sl.status = DYC_ECUDA;
+        }
         if (sl.status != DYC_OK) {
             finish_slot_error(s, sl, sl.status);
         } else {
@@ -418,6 +416,7 @@ void dyc_server_config_default(dyc_server_config *c) {
     memset(c, 0, sizeof(*c));
     c->max_step_ops = 1ull << 22;
     c->coalesce = 1;
+    c->pool_reserve_bytes = DYC_POOL_RESERVE_AUTO;
 }
 
 dyc_status dyc_server_create(const dyc_config *table_cfg, uint32_t ntenants,
@@ -491,6 +490,23 @@ dyc_status dyc_server_create(const dyc_config *table_cfg, uint32_t ntenants,
     // step size) count against the cap from the start
     s->fixed_bytes = kSlots * bytes + m * 160;
     s->table_bytes = table_device_bytes(s);
+    // growth headroom mapped into the allocation pool now rather than by the
+    // first resizes inside steps
+    uint64_t reserve = s->scfg.pool_reserve_bytes;
+    if (reserve == DYC_POOL_RESERVE_AUTO) {
+        reserve = 2 * s->table_bytes;
+        const uint64_t used = s->fixed_bytes + s->table_bytes;
+        if (s->scfg.hbm_cap_bytes)
+            reserve = std::min<uint64_t>(
+                reserve, s->scfg.hbm_cap_bytes > used ? s->scfg.hbm_cap_bytes - used : 0);
+    }
+    if (reserve) {
+        r = dyc_pool_reserve(s->device, reserve);
+        if (r != DYC_OK && r != DYC_ENOMEM) {  // a reserve that does not fit is only skipped
+            free_server(s);
+            return r;
+        }
+    }
     s->t_comp = std::thread(completer, s);
     s->t_exec = std::thread(executor, s);
     s->t_asm = std::thread(assembler, s);

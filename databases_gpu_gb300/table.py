@@ -645,6 +645,13 @@ class DyCuckooServer:
         return DyCuckoo._member(h, cfg, self)
 
 
+def pool_reserve(nbytes: int, device: int = 0) -> None:
+    """Map nbytes of device memory into the library's allocation pool now
+    (dyc_pool_reserve), so later resizes on `device` reuse it."""
+    L = _lib.lib()
+    check(L.dyc_pool_reserve(device, int(nbytes)), "dyc_pool_reserve")
+
+
 def unpack_bits(bits, n: int) -> np.ndarray:
     """Hit / erased bit words (ceil(n/32) uint32) -> bool array of n."""
     if hasattr(bits, "cpu"):

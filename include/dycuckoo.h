@@ -102,11 +102,22 @@ void dyc_config_default(dyc_config *cfg);
 
 /* Replaces hashAPI::hashAPI(size) (GPU/dyhash/api.cpp:26-91): subtables of
  * nextPrime(size / (d * slots)) buckets, rounded up to even (api.cpp:46-56);
- * no memory pool, no __constant__ descriptor, any number of live tables. */
+ * no __constant__ descriptor, any number of live tables. Subtables and
+ * resize buffers come from a stream-ordered allocation pool the library
+ * keeps per device (in place of the reference's CNMeM pool), which holds
+ * freed memory up to a quarter of the device and returns it when the
+ * device's last table is destroyed. */
 dyc_status dyc_create(const dyc_config *cfg, dyc_table **out);
 
 /* Replaces hashAPI::~hashAPI (api.cpp:93-109). */
 dyc_status dyc_destroy(dyc_table *t);
+
+/* Map `bytes` of device memory into the library pool of `device` now
+ * (allocate and free), so that later resizes reuse it instead of mapping
+ * new memory, which costs about 3 ms per GB on a GB300. The pool keeps at
+ * most a quarter of the device's memory. Call it after creating a table on
+ * the device (the pool is emptied when the device's last table goes). */
+dyc_status dyc_pool_reserve(int32_t device, uint64_t bytes);
 
 /* Replaces gpu_lp_insert / cuckoo_insert (GPU/dyhash/cuckoo.cu:858-877,
  * :324-432) and the resize-before-insert check of hashAPI::hash_insert_batch
@@ -357,8 +368,15 @@ typedef struct dyc_server_config {
     uint32_t coalesce;      /* 1 (default): continuous batching over the set;
                                0: one request per step through dyc_apply on its
                                tenant's table (the per-request path) */
-    uint32_t reserved[7];
+    uint32_t pad0;
+    uint64_t pool_reserve_bytes; /* dyc_pool_reserve at creation, so tenant growth
+                                    does not map memory inside steps; default
+                                    DYC_POOL_RESERVE_AUTO: twice the tables' bytes
+                                    at creation, within hbm_cap_bytes; 0: none */
+    uint32_t reserved[4];
 } dyc_server_config;
+
+#define DYC_POOL_RESERVE_AUTO (~(uint64_t)0)
 
 typedef struct dyc_server_stats {
     uint64_t requests;      /* completed (including rejected) */

@@ -281,6 +281,24 @@ def test_downsize_into_full_subtables_never_drops():
     t.close()
 
 
+def test_pool_reserve_then_resizes_keep_everything():
+    """dyc_pool_reserve maps memory into the allocation pool; the resizes that
+    follow take their buffers from it and keep every key."""
+    n = 200_000
+    keys = unique_u32(n, seed=31)
+    t = _dg().DyCuckoo(n, auto_resize=False)
+    _dg().pool_reserve(256 << 20)
+    m = O.Map()
+    t.insert(to_dev(keys), to_dev(keys ^ np.uint32(0x5A5A)))
+    m.insert(keys, keys ^ np.uint32(0x5A5A))
+    for _ in range(3):
+        t.resize_up()
+    t.resize_down()
+    assert_same_contents(t, m, "resizes after a pool reserve")
+    find_and_compare(t, m, keys, "after resizes")
+    t.close()
+
+
 def test_eviction_overflow_upsizes_and_keeps_everything():
     n = 50_000
     keys = unique_u32(n, seed=8)
