@@ -297,6 +297,77 @@ def run_set_profile(args):
     S.close()
 
 
+def run_serve_profile(args):
+    """Serving steps without the server's threads: 64 u64/u32 tenant tables
+    (2^16..2^24 keys, preloaded), then args.serve_steps steps of about
+    args.serve_step_ops ops each, made of log-uniform 32..65536-op requests on
+    Zipf(0.9) tenants (70 % find on j < 2^17, 20 % insert on j < 2^25, 10 %
+    erase on j < 2^17), applied from fixed staging buffers through
+    dyc_set_apply with graph replay, as the server's executor does. Each step
+    is timed on the host around the call (which returns after its host read).
+    The command the serving-step ncu captures run under."""
+    import torch
+
+    import databases_gpu_gb300 as dg
+    from databases_gpu_gb300.workloads import splitmix64
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(10327)
+    nt = 64
+    sizes = np.round(2.0 ** (16 + 8 * rng.random(nt))).astype(np.int64)
+    S = dg.DyCuckooSet(sizes.tolist(), key_bytes=8, value_bytes=4)
+    for t in range(nt):
+        k = splitmix64(torch.arange(int(sizes[t]), device=dev, dtype=torch.int64), 1)
+        v = torch.randint(0, 1 << 30, (int(sizes[t]),), device=dev, dtype=torch.int32)
+        S.table(t).insert(k, v, unique=True, new_keys=True)
+    zipf = np.arange(1, nt + 1) ** -0.9
+    zipf /= zipf.sum()
+    cap = 1 << 22
+    b_ops = torch.empty(cap, dtype=torch.uint8, device=dev)
+    b_keys = torch.empty(cap, dtype=torch.int64, device=dev)
+    b_vals = torch.empty(cap, dtype=torch.int32, device=dev)
+    b_out = torch.empty(cap, dtype=torch.int32, device=dev)
+    b_bits = torch.empty(cap // 32 + 1, dtype=torch.int32, device=dev)
+    b_off = torch.empty(nt + 1, dtype=torch.int32, device=dev)
+    st = torch.cuda.Stream(dev)
+    target = min(args.serve_step_ops, cap - (1 << 16))
+    rows = []
+    for step in range(args.serve_steps):
+        cnt = np.zeros(nt, np.int64)
+        n = 0
+        while n < target:
+            r = int(round(2.0 ** (5 + 11 * rng.random())))
+            cnt[rng.choice(nt, p=zipf)] += r
+            n += r
+        off = np.zeros(nt + 1, np.uint32)
+        off[1:] = np.cumsum(cnt)
+        u = torch.rand(n, device=dev)
+        ops = torch.where(u < 0.7, 0, torch.where(u < 0.9, 1, 2)).to(torch.uint8)
+        j = torch.where(ops == 1, torch.randint(0, 1 << 25, (n,), device=dev),
+                        torch.randint(0, 1 << 17, (n,), device=dev))
+        b_ops[:n].copy_(ops)
+        b_keys[:n].copy_(splitmix64(j, 1))
+        b_vals[:n].copy_(torch.randint(0, 1 << 30, (n,), device=dev, dtype=torch.int32))
+        b_off.copy_(torch.from_numpy(off.view(np.int32)))
+        torch.cuda.synchronize()
+        nw = (n + 31) // 32
+        t0 = time.perf_counter()
+        S.apply(b_off, b_ops[:n], b_keys[:n], b_vals[:n], out=b_out[:n], bits=b_bits[:nw],
+                h_offsets=off, graph=True, stream=st)
+        ms = (time.perf_counter() - t0) * 1e3
+        stt = S.stats()
+        rows.append((ms, n, stt["resizes_up"] + stt["resizes_down"], stt["split_phases"]))
+    a = np.array([r[0] for r in rows[3:]])
+    rz = np.array([r[2] for r in rows[3:]])
+    plain = a[rz == 0] if (rz == 0).any() else a
+    print(json.dumps({"steps": len(rows), "ops_per_step": target,
+                      "step_ms_median": round(float(np.median(a)), 4),
+                      "no_resize_step_ms_median": round(float(np.median(plain)), 4),
+                      "resize_steps": int((rz > 0).sum()),
+                      "split_steps": int(sum(r[3] for r in rows)),
+                      "no_resize_mops": round(target / float(np.median(plain)) / 1e3, 1)}))
+    S.close()
+
+
 def build_serve_load():
     """The server's load generator (databases_gpu_gb300/csrc/dyc_serve_load.cpp)."""
     from databases_gpu_gb300 import build as pkg_build
@@ -542,6 +613,10 @@ def main():
     ap.add_argument("--skip-multi", action="store_true",
                     help="skip the batched multi-table workload")
     ap.add_argument("--skip-serve", action="store_true", help="skip the serving loop")
+    ap.add_argument("--serve-profile", action="store_true",
+                    help="only serving-like set steps (the serving-step profiling command)")
+    ap.add_argument("--serve-steps", type=int, default=300)
+    ap.add_argument("--serve-step-ops", type=int, default=363000)
     ap.add_argument("--serve-rate", type=float, default=2e5)
     ap.add_argument("--serve-seconds", type=float, default=0.25)
     ap.add_argument("--mt-tables", type=int, default=4096)
@@ -559,6 +634,8 @@ def main():
         return run_line_probe()
     if args.set_profile:
         return run_set_profile(args)
+    if args.serve_profile:
+        return run_serve_profile(args)
     if args.impl == "reference":
         return run_reference(args)
 
