@@ -292,8 +292,11 @@ def run_set_profile(args):
         e1.record(s)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
+        st = S.stats()
         print(json.dumps({"round": r, "ms": round(ms, 3), "ops": n,
-                          "mops": round(n / ms / 1e3, 1), "tables": w.ntables}))
+                          "mops": round(n / ms / 1e3, 1), "tables": w.ntables,
+                          "resizes_up": st["resizes_up"], "resizes_down": st["resizes_down"],
+                          "split_phases": st["split_phases"]}))
     S.close()
 
 
@@ -493,6 +496,7 @@ def run_multi_table(args, dev, torch, dg):
     outs = [torch.empty(n, dtype=torch.int32, device=dev) for _ in range(2)]
     bitss = [torch.empty((n + 31) // 32, dtype=torch.int32, device=dev) for _ in range(2)]
     lat = {"batched": [], "per_table": []}
+    resized = {"up": 0, "down": 0, "split": 0}
     bad = 0
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -510,6 +514,11 @@ def run_multi_table(args, dev, torch, dg):
             torch.cuda.synchronize()
             if r >= 2:
                 lat[which].append(e0.elapsed_time(e1))
+                if which == "batched":
+                    st = S.stats()
+                    resized["up"] += st["resizes_up"]
+                    resized["down"] += st["resizes_down"]
+                    resized["split"] += st["split_phases"]
         bad += int((outs[0] != outs[1]).sum()) + int((bitss[0] != bitss[1]).sum())
     sa, ca = sets[0].sizes()
     sb, cb = sets[1].sizes()
@@ -524,6 +533,9 @@ def run_multi_table(args, dev, torch, dg):
         ms = sorted(lat[which])
         res[which] = {"mops": round(n * len(ms) / (sum(ms) / 1e3) / 1e6, 1),
                       "round_ms_p50": round(ms[len(ms) // 2], 3), "round_ms_max": round(ms[-1], 3)}
+    res["batched"]["upsizes_per_round"] = round(resized["up"] / rounds, 1)
+    res["batched"]["downsizes_per_round"] = round(resized["down"] / rounds, 1)
+    res["batched"]["split_rounds"] = resized["split"]
     res["batched_over_per_table"] = round(res["batched"]["mops"] / res["per_table"]["mops"], 2)
     res["api"] = "dyc_set_apply (graph replay) vs dyc_set_apply_each (one dyc_apply per table)"
     for S in sets:

@@ -851,7 +851,7 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
     const size_t CB = kb == 4 ? 8 : 16;  // cell bytes
     const size_t sizes[] = {
         cells * CB,                                   // cells
-        ops * 4, ops * K, ops * 4, ops * 8,           // op_cell, dkey, dcnt, dseg
+        ops * 4, ops * 4, ops * K, ops * 4, ops * 8,  // op_cell, op_rank, dkey, dcnt, dseg
         ops * 4, ops * V, (ops / 32 + 1) * 4,         // seg, pre_val, pre_hit
         ops * K, ops * V, ops * K,                    // up_key, up_val, er_key
         dyc::kCtrSlots * 8, ops * 4, ops * 4,         // ctr, wseg, mid
@@ -882,6 +882,7 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
     dyc::ApplyScratch A{};
     A.cells = carve();
     A.op_cell = (uint32_t *)carve();
+    A.op_rank = (uint32_t *)carve();
     A.dkey = carve();
     A.dcnt = (uint32_t *)carve();
     A.dseg = (unsigned long long *)carve();

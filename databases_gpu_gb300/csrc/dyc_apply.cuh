@@ -58,12 +58,14 @@ template <int KB> __device__ __forceinline__ uint32_t *cell_word(void *cells, ui
 
 // Claim (or join) key k's cell in region [base, base + size): fastrange
 // start, linear probing. One CAS (64-bit for 4-byte keys, 128-bit for
-// 8-byte keys) claims a new key with count 1.
-// (L2 atomic throughput bounds the grouping kernels; keeping several first
-// probes of a thread in flight measured slower.)
+// 8-byte keys) claims a new key with count 1; a repeat adds 1 to the count.
+// `rank` gets the count before this op (0 for the op that claimed the cell):
+// a distinct place for the op inside its key's segment, so the scatter pass
+// needs no atomics. (L2 atomic throughput bounds the grouping kernels;
+// keeping several first probes of a thread in flight measured slower.)
 template <int KB>
 __device__ __forceinline__ uint32_t claim_cell(void *cells, uint64_t base, uint64_t size,
-                                               typename SlotT<KB>::K k) {
+                                               typename SlotT<KB>::K k, uint32_t &rank) {
     uint64_t idx = ((uint64_t)cell_hash((uint64_t)k) * size) >> 32;
     for (uint64_t probe = 0; probe < size; ++probe) {
         const uint64_t c = base + idx;
@@ -71,18 +73,23 @@ __device__ __forceinline__ uint32_t claim_cell(void *cells, uint64_t base, uint6
             unsigned long long *p = (unsigned long long *)cells + c;
             const unsigned long long old =
                 atomicCAS(p, 0ull, (unsigned long long)k | (1ull << 32));
-            if (old == 0ull) return (uint32_t)c;
+            if (old == 0ull) {
+                rank = 0u;
+                return (uint32_t)c;
+            }
             if ((uint32_t)old == k) {
-                atomicAdd(p, 1ull << 32);
+                rank = (uint32_t)(atomicAdd(p, 1ull << 32) >> 32);
                 return (uint32_t)c;
             }
         } else {
-            // one 128-bit CAS claims a new key with count 1; a repeat adds 1
             u128 *p = (u128 *)((char *)cells + c * 16);
             const u128 old = SlotT<8>::cas(p, u128{0ull, 0ull}, u128{(unsigned long long)k, 1ull});
-            if (old.lo == 0ull) return (uint32_t)c;
+            if (old.lo == 0ull) {
+                rank = 0u;
+                return (uint32_t)c;
+            }
             if (old.lo == k) {
-                atomicAdd((unsigned *)&p->hi, 1u);
+                rank = atomicAdd((unsigned *)&p->hi, 1u);
                 return (uint32_t)c;
             }
         }
@@ -100,7 +107,9 @@ __global__ void __launch_bounds__(256) k_apply_group(const __grid_constant__ App
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const K k = load_key<KB>(keys, i);
-        A.op_cell[i] = k == 0 ? kNoCell : claim_cell<KB>(A.cells, 0, size, k);  // key 0: no cell
+        uint32_t rank = 0u;
+        A.op_cell[i] = k == 0 ? kNoCell : claim_cell<KB>(A.cells, 0, size, k, rank);  // key 0: none
+        A.op_rank[i] = rank;
     }
 }
 
@@ -134,13 +143,14 @@ __global__ void __launch_bounds__(256) k_set_group(const __grid_constant__ Apply
         const bool one = t0 == A.ntables - 1 || __ldg(off + t0 + 1) > (uint32_t)last;
         if (i >= n) continue;
         const K k = load_key<KB>(keys, i);
-        uint32_t cell = kNoCell;
+        uint32_t cell = kNoCell, rank = 0u;
         if (k != 0) {
             const uint32_t t = one ? t0 : table_of(off, A.ntables, (uint32_t)i);
             const uint32_t c0 = A.tcell_off[t], c1 = A.tcell_off[t + 1];
-            cell = claim_cell<KB>(A.cells, c0, c1 - c0, k);
+            cell = claim_cell<KB>(A.cells, c0, c1 - c0, k, rank);
         }
         A.op_cell[i] = cell;
+        A.op_rank[i] = rank;
     }
 }
 
@@ -302,8 +312,7 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
         const uint32_t cell = A.op_cell[i];
         if (cell == kNoCell) continue;
         const uint32_t d = *cell_word<KB>(A.cells, cell);
-        const unsigned long long o = atomicAdd(&A.dseg[d], 1ull);
-        A.seg[(uint32_t)(o >> 32) + (uint32_t)o] = (uint32_t)i;
+        A.seg[(uint32_t)(A.dseg[d] >> 32) + A.op_rank[i]] = (uint32_t)i;
     }
 }
 

@@ -58,9 +58,10 @@ struct ApplyScratch {
     // holds the cell's distinct-key id.
     void *cells;
     uint32_t *op_cell;         // cell of each op
+    uint32_t *op_rank;         // place of each op inside its key's segment
     void *dkey;                // distinct keys
     uint32_t *dcnt;            // per distinct key: ops
-    unsigned long long *dseg;  // per distinct key: segment start << 32 | fill cursor
+    unsigned long long *dseg;  // per distinct key: segment start << 32
     uint32_t *seg;             // op indices grouped by key
     void *pre_val;             // pre-batch value per distinct key
     uint32_t *pre_hit;         // pre-batch hit bits per distinct key
