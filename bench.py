@@ -265,6 +265,14 @@ def run_line_probe():
     print(json.dumps(d))
 
 
+def set_table_bytes(S, bucket_bytes=128):
+    """Device bytes of a set's subtables (from the members' slot capacities)."""
+    _, caps = S.sizes()
+    slot = 8 if S.key_bytes == 4 else 16
+    per_bucket = bucket_bytes // slot - (1 if bucket_bytes == 128 else 0)
+    return int(caps.sum()) // per_bucket * bucket_bytes
+
+
 def run_set_profile(args):
     """One table set (the multi-table workload with args.mt_tables tables),
     args.mt_rounds rounds of dyc_set_apply without graphs, each timed with
@@ -278,6 +286,7 @@ def run_set_profile(args):
     for t in range(w.ntables):
         k, v = w.preload(t)
         S.table(t).insert(k, v, new_keys=True, unique=True)
+    dg.pool_reserve(2 * set_table_bytes(S))  # growth headroom, mapped before the rounds
     n = w.n_ops
     out = torch.empty(n, dtype=torch.int32, device="cuda")
     bits = torch.empty((n + 31) // 32, dtype=torch.int32, device="cuda")
@@ -490,6 +499,9 @@ def run_multi_table(args, dev, torch, dg):
         k, v = w.preload(t)
         for S in sets:
             S.table(t).insert(k, v, new_keys=True, unique=True)
+    # growth headroom for both sets, mapped into the allocation pool before
+    # the rounds (the tables grow every round: hundreds of upsizes)
+    dg.pool_reserve(2 * sum(set_table_bytes(S) for S in sets), device=dev.index or 0)
     torch.cuda.synchronize()
     n = w.n_ops
     stream = torch.cuda.current_stream()

@@ -4,8 +4,11 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
+#include <memory>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "dycuckoo.h"
 #include "dyc_device.cuh"
@@ -249,6 +252,55 @@ dyc_status resize_up_impl(dyc_table *t, cudaStream_t s) {
     CK(cudaFreeAsync(old, s));
     t->capacity += (uint64_t)onb * t->slots;
     t->last.resizes_up++;
+    return DYC_OK;
+}
+
+// Host half of an upsize of subtable pick_up(): allocate the doubled
+// subtable, describe the move as a job and switch the descriptor to the new
+// subtable. The caller launches the move (resize_up_flush) before freeing
+// *old_out, both stream-ordered on s.
+dyc_status resize_up_prepare(dyc_table *t, cudaStream_t s, dyc::ResizeJob *job, void **old_out) {
+    const uint32_t ti = pick_up(t->D.nb, t->D.d);
+    const uint32_t onb = t->D.nb[ti];
+    if ((uint64_t)onb * 2 > 0xFFFFFFFFull) return fail(DYC_EINVAL, "subtable %u too large", ti);
+    const uint32_t nnb = onb * 2;
+    void *nw = nullptr;
+    CK(pool_alloc(t->device, &nw, (size_t)nnb * t->sb, s));
+    const uint64_t magic = dyc::fastmod_magic(nnb);
+    *job = dyc::ResizeJob{t->D.sub[ti], nw, magic, onb, ti, 0u, 0u};
+    *old_out = t->D.sub[ti];
+    t->D.sub[ti] = nw;
+    t->D.nb[ti] = nnb;
+    t->D.magic[ti] = magic;
+    t->capacity += (uint64_t)onb * t->slots;
+    t->last.resizes_up++;
+    return DYC_OK;
+}
+
+// The moves of prepared upsizes, kMaxResizeJobs per launch, then the old
+// subtables freed behind them.
+dyc_status resize_up_flush(int kb, int sb, int sms, cudaStream_t s,
+                           const std::vector<dyc::ResizeJob> &jobs, const std::vector<void *> &olds) {
+    static thread_local std::unique_ptr<dyc::ResizeJobs> J(new dyc::ResizeJobs());
+    const LaunchCtx L{sms, s};
+    const uint64_t g = (uint64_t)sb / 32;
+    for (size_t a = 0; a < jobs.size(); a += dyc::kMaxResizeJobs) {
+        const size_t m = std::min<size_t>(dyc::kMaxResizeJobs, jobs.size() - a);
+        uint64_t blocks = 0;
+        for (size_t i = 0; i < m; ++i) {
+            J->j[i] = jobs[a + i];
+            J->j[i].block0 = (uint32_t)blocks;
+            const uint64_t chunks = (uint64_t)J->j[i].old_nb * g;
+            blocks += (chunks + dyc::kResizeChunksPerBlock - 1) / dyc::kResizeChunksPerBlock;
+        }
+        if (blocks >= 0x7FFFFFFFull) return fail(DYC_EINVAL, "upsize wave too large");
+        J->n = (uint32_t)m;
+        J->blocks = (uint32_t)blocks;
+        const cudaError_t e = kb == 4 ? Ops<4>::resize_up_many(L, sb, *J)
+                                      : Ops<8>::resize_up_many(L, sb, *J);
+        if (e != cudaSuccess) return fail(DYC_ECUDA, "resize_up kernel: %s", cudaGetErrorString(e));
+    }
+    for (void *o : olds) CK(cudaFreeAsync(o, s));
     return DYC_OK;
 }
 
@@ -1573,20 +1625,40 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
         }
     bool moved = false;
     std::vector<uint8_t> grew;
+    // The policy's upsizes go out in waves of at most one per table, each
+    // wave one launch for all its tables (a round of many small tables
+    // upsizes hundreds of them).
     auto upsize_policy = [&]() -> dyc_status {
-        for (uint32_t t = 0; t < s->ntables; ++t) {
-            dyc_table *m = s->tables[t];
-            const uint64_t add = s->h_tup[t];
+        auto over = [&](uint32_t t) {
+            const dyc_table *m = s->tables[t];
             // the size the inserts meet: the table's erases go first, as in dyc_apply
             const double base = (double)m->size - (double)s->h_ter[t];
-            int guard = 0;
-            while (add && base + (double)add > m->cfg.upper_load * (double)m->capacity &&
-                   guard++ < 64) {
-                TRY(resize_up_impl(m, st));
-                moved = true;
+            return s->h_tup[t] &&
+                   base + (double)s->h_tup[t] > m->cfg.upper_load * (double)m->capacity;
+        };
+        std::vector<uint32_t> todo;
+        for (uint32_t t = 0; t < s->ntables; ++t)
+            if (over(t)) todo.push_back(t);
+        std::vector<dyc::ResizeJob> jobs;
+        std::vector<void *> olds;
+        for (int wave = 0; !todo.empty() && wave < 64; ++wave) {
+            jobs.clear();
+            olds.clear();
+            for (uint32_t t : todo) {
+                dyc::ResizeJob j;
+                void *old = nullptr;
+                TRY(resize_up_prepare(s->tables[t], st, &j, &old));
+                jobs.push_back(j);
+                olds.push_back(old);
                 if (grew.empty()) grew.assign(s->ntables, 0);
                 grew[t] = 1;
             }
+            moved = true;
+            TRY(resize_up_flush(s->kb, s->sb, s->sms, st, jobs, olds));
+            std::vector<uint32_t> next;
+            for (uint32_t t : todo)
+                if (over(t)) next.push_back(t);
+            todo.swap(next);
         }
         return DYC_OK;
     };

@@ -94,6 +94,23 @@ enum : int {
 };
 
 
+// Upsizes of many subtables (of different tables) in one launch: job j
+// doubles old_sub (old_nb buckets, subtable index t of its table) into
+// new_sub; its blocks are [block0, next job's block0). Passed by value as the
+// kernel's parameter block, so at most kMaxResizeJobs per launch.
+struct ResizeJob {
+    const void *old_sub;
+    void *new_sub;
+    uint64_t magic;  // fastmod reciprocal of 2 * old_nb
+    uint32_t old_nb, t, block0, pad;
+};
+constexpr uint32_t kMaxResizeJobs = 768;
+constexpr uint32_t kResizeChunksPerBlock = 2048;  // 32-byte chunks a block moves
+struct ResizeJobs {
+    uint32_t n, blocks;
+    ResizeJob j[kMaxResizeJobs];
+};
+static_assert(sizeof(ResizeJobs) <= 32000, "kernel parameter block limit");
 
 // Launch parameters picked once per kernel from the occupancy calculator.
 struct LaunchCtx {
@@ -130,6 +147,8 @@ template <int KB> struct Ops {
                              Counters *ctr);
     static cudaError_t resize_up(const LaunchCtx &L, int sb, uint32_t t, const void *old_sub,
                                  uint32_t old_nb, void *new_sub);
+    // J.n jobs in one launch of J.blocks blocks (job block ranges filled in)
+    static cudaError_t resize_up_many(const LaunchCtx &L, int sb, const ResizeJobs &J);
     // halve an even subtable: merged buckets to new_sub, leftovers to list
     static cudaError_t resize_down(const LaunchCtx &L, int sb, const void *old_sub,
                                    uint32_t old_nb, void *new_sub, void *list,

@@ -969,6 +969,55 @@ __global__ void __launch_bounds__(256) k_resize_up(uint32_t t, const char *__res
     }
 }
 
+// The same split for many subtables in one launch: each block finds its job
+// (a binary search over the jobs' first blocks, the same for every thread of
+// the block) and moves up to kResizeChunksPerBlock chunks of it.
+template <int KB, int SB>
+__global__ void __launch_bounds__(256) k_resize_up_many(const __grid_constant__ ResizeJobs J) {
+    using T = SlotT<KB>;
+    using Gm = Geo<KB, SB>;
+    constexpr int G = Gm::kG, SPC = Gm::kSPC, WPS = T::kBytes / 4;
+    uint32_t lo_j = 0, hi_j = J.n;
+    while (hi_j - lo_j > 1) {
+        const uint32_t mid = (lo_j + hi_j) >> 1;
+        if (J.j[mid].block0 <= blockIdx.x) lo_j = mid;
+        else hi_j = mid;
+    }
+    const ResizeJob &jb = J.j[lo_j];
+    const char *old_sub = (const char *)jb.old_sub;
+    char *new_sub = (char *)jb.new_sub;
+    const uint32_t old_nb = jb.old_nb, new_nb = 2u * jb.old_nb, t = jb.t;
+    const uint64_t chunks = (uint64_t)old_nb * G;
+    const uint64_t x0 = (uint64_t)(blockIdx.x - jb.block0) * kResizeChunksPerBlock;
+    const uint64_t x1 = x0 + kResizeChunksPerBlock < chunks ? x0 + kResizeChunksPerBlock : chunks;
+    for (uint64_t x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
+        const uint64_t b = x / G;
+        const int r = (int)(x % G);
+        uint32_t w[8], lo[8], hi[8];
+        ld_nc(old_sub + x * 32, w);
+#pragma unroll
+        for (int j = 0; j < SPC; ++j) {
+            typename T::S s;
+            T::from_words(w + j * WPS, s);
+            const int idx = r * SPC + j;
+            const bool is_meta = Gm::kMeta && idx == Gm::kTotal - 1;
+            bool to_lo = is_meta, to_hi = is_meta;
+            if (!is_meta && !T::is_empty(s)) {
+                const uint32_t nbk = fastmod(subtable_hash(fold(T::key(s)), t), jb.magic, new_nb);
+                to_lo = nbk == (uint32_t)b;
+                to_hi = !to_lo;
+            }
+#pragma unroll
+            for (int x2 = 0; x2 < WPS; ++x2) {
+                lo[j * WPS + x2] = to_lo ? w[j * WPS + x2] : 0u;
+                hi[j * WPS + x2] = to_hi ? w[j * WPS + x2] : 0u;
+            }
+        }
+        st_v8(new_sub + b * SB + r * 32, lo);
+        st_v8(new_sub + (b + old_nb) * SB + r * 32, hi);
+    }
+}
+
 // ----------------------------------------------------------------------------
 // Bulk-copy helpers (cp.async.bulk through an mbarrier) for streaming a
 // subtable through shared memory. Waits are bounded: a wait that gives up

@@ -115,6 +115,16 @@ cudaError_t Ops<KB>::erase(const LaunchCtx &L, const Desc &D, int sb, const Scra
 }
 
 template <int KB>
+cudaError_t Ops<KB>::resize_up_many(const LaunchCtx &L, int sb, const ResizeJobs &J) {
+    if (J.n == 0 || J.blocks == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_resize_up_many<KB, SB>;
+        k<<<J.blocks, 256, 0, L.stream>>>(J);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
 cudaError_t Ops<KB>::resize_up(const LaunchCtx &L, int sb, uint32_t t, const void *old_sub,
                                uint32_t old_nb, void *new_sub) {
     if (old_nb == 0) return cudaSuccess;
