@@ -297,7 +297,8 @@ def run_set_profile(args):
         e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(s)
-        S.apply(w.offsets, ops, keys, vals, out=out, bits=bits, h_offsets=w.offsets_host, stream=s)
+        S.apply(w.offsets, ops, keys, vals, out=out, bits=bits, h_offsets=w.offsets_host, stream=s,
+                graph=args.set_graph)
         e1.record(s)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
@@ -490,8 +491,9 @@ def run_multi_table(args, dev, torch, dg):
     """4096 independent u32 tables (log-uniform 2^8..2^20 keys), each with a
     log-uniform 16..2^16-op mixed batch per round (70/20/10, 50% find hits):
     the batched set path (one launch sequence per round, graph-replayed)
-    against one dyc_apply per table, on twin sets fed the same rounds; every
-    op's result must agree between the two."""
+    against one dyc_apply per table, on twin sets fed the same rounds (each
+    path runs its rounds back to back); every op's result must agree between
+    the two."""
     from databases_gpu_gb300.workloads import MultiTableWorkload
     w = MultiTableWorkload(args.mt_tables, seed=10327, device=dev)
     sets = [dg.DyCuckooSet(w.sizes.numpy(), device=dev.index or 0) for _ in range(2)]
@@ -513,10 +515,14 @@ def run_multi_table(args, dev, torch, dg):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     rounds = args.mt_rounds
-    for r in range(rounds + 2):  # two untimed rounds: scratch, graph capture
-        ops, keys, vals = w.round()
-        for which, S in (("batched", sets[0]), ("per_table", sets[1])):
-            i = 0 if which == "batched" else 1
+    # every path runs all its rounds back to back (two untimed: scratch, graph
+    # capture) on the same pre-generated rounds; the batched path's results
+    # are kept and compared op by op with the per-table path's
+    data = [w.round() for _ in range(rounds + 2)]
+    kept = []
+    for which, S in (("batched", sets[0]), ("per_table", sets[1])):
+        i = 0 if which == "batched" else 1
+        for r, (ops, keys, vals) in enumerate(data):
             torch.cuda.synchronize()
             e0.record(stream)
             S.apply(w.offsets, ops, keys, vals, out=outs[i], bits=bitss[i],
@@ -531,7 +537,11 @@ def run_multi_table(args, dev, torch, dg):
                     resized["up"] += st["resizes_up"]
                     resized["down"] += st["resizes_down"]
                     resized["split"] += st["split_phases"]
-        bad += int((outs[0] != outs[1]).sum()) + int((bitss[0] != bitss[1]).sum())
+            if which == "batched":
+                kept.append((outs[0].clone(), bitss[0].clone()))
+            else:
+                bad += int((kept[r][0] != outs[1]).sum()) + int((kept[r][1] != bitss[1]).sum())
+    del kept, data
     sa, ca = sets[0].sizes()
     sb, cb = sets[1].sizes()
     bad += int((sa != sb).sum())
@@ -637,6 +647,8 @@ def main():
     ap.add_argument("--skip-multi", action="store_true",
                     help="skip the batched multi-table workload")
     ap.add_argument("--skip-serve", action="store_true", help="skip the serving loop")
+    ap.add_argument("--set-graph", action="store_true",
+                    help="--set-profile rounds through graph replay")
     ap.add_argument("--serve-profile", action="store_true",
                     help="only serving-like set steps (the serving-step profiling command)")
     ap.add_argument("--serve-steps", type=int, default=300)
