@@ -912,7 +912,8 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
         multi ? ops * 4 : 0, multi ? ops * 4 : 0,     // up_tid, er_tid
         multi ? (size_t)ntables * 4 : 0,              // tup
         multi ? (size_t)ntables * 4 : 0,              // ter
-        multi ? ((size_t)ntables + 1) * 4 : 0};       // tcell_off
+        multi ? ((size_t)ntables + 1) * 4 : 0,        // tcell_off
+        multi ? (ops / dyc::kTidxStep + 1) * 4 : 0};  // tidx
     size_t need = 0;
     for (size_t b : sizes) need += (b + 255) & ~(size_t)255;
     if (*buf && *buf_bytes < need) {
@@ -954,6 +955,7 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
     A.tup = (uint32_t *)carve();
     A.ter = (uint32_t *)carve();
     A.tcell_off = (uint32_t *)carve();
+    A.tidx = (uint32_t *)carve();
     A.ntables = ntables;
     A.cap_cells = cells;
     A.cap_ops = ops;

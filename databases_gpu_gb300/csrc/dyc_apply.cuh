@@ -126,6 +126,19 @@ __device__ __forceinline__ uint32_t table_of(const uint32_t *__restrict__ off, u
     return lo;
 }
 
+// Table of op i through the coarse index tidx (the table of every
+// kTidxStep-th op, filled by k_set_prep): a lower bound, then a forward scan
+// over the offsets `bound` (off for ops; tcell_off for cells, with i the
+// cell index and the index entry of op i / 2). Replaces a binary search of
+// log2(ntables) dependent loads per lookup.
+__device__ __forceinline__ uint32_t table_at(const uint32_t *__restrict__ tidx,
+                                             const uint32_t *__restrict__ bound, uint32_t i,
+                                             uint32_t op) {
+    uint32_t t = __ldg(tidx + (op / kTidxStep));
+    while (__ldg(bound + t + 1) <= i) ++t;
+    return t;
+}
+
 // Many tables: ops of table t are [off[t], off[t+1]); its cells are
 // [tcell_off[t], tcell_off[t+1]), twice its ops.
 template <int KB>
@@ -139,13 +152,13 @@ __global__ void __launch_bounds__(256) k_set_group(const __grid_constant__ Apply
     for (uint64_t base = warp_base(); base < n; base += warp_stride()) {
         const uint64_t i = base + (threadIdx.x & 31);
         const uint64_t last = base + 31 < n ? base + 31 : n - 1;
-        const uint32_t t0 = table_of(off, A.ntables, (uint32_t)base);
+        const uint32_t t0 = table_at(A.tidx, off, (uint32_t)base, (uint32_t)base);
         const bool one = t0 == A.ntables - 1 || __ldg(off + t0 + 1) > (uint32_t)last;
         if (i >= n) continue;
         const K k = load_key<KB>(keys, i);
         uint32_t cell = kNoCell, rank = 0u;
         if (k != 0) {
-            const uint32_t t = one ? t0 : table_of(off, A.ntables, (uint32_t)i);
+            const uint32_t t = one ? t0 : table_at(A.tidx, off, (uint32_t)i, (uint32_t)i);
             const uint32_t c0 = A.tcell_off[t], c1 = A.tcell_off[t + 1];
             cell = claim_cell<KB>(A.cells, c0, c1 - c0, k, rank);
         }
@@ -174,6 +187,8 @@ __global__ void __launch_bounds__(256) k_set_prep(const __grid_constant__ ApplyS
         A.tcell_off[t] = 2u * off[t];
         if (t < A.ntables) A.tup[t] = A.ter[t] = 0u;
     }
+    for (uint64_t b = id; b * kTidxStep < n; b += stride)
+        A.tidx[b] = table_of(off, A.ntables, (uint32_t)(b * kTidxStep));
     const uint64_t words = 2 * n * (cell_bytes<KB>() / 8);
     for (uint64_t c = id; c < words; c += stride) ((unsigned long long *)A.cells)[c] = 0ull;
     if (bits != nullptr)
@@ -295,7 +310,8 @@ __global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ A
             ((typename SlotT<KB>::K *)A.dkey)[d] = cell_key<KB>(A.cells, c);
             A.dcnt[d] = cnt[k];
             A.dseg[d] = (unsigned long long)off << 32;
-            if (A.dtid) A.dtid[d] = table_of(A.tcell_off, A.ntables, (uint32_t)c);
+            if (A.dtid)
+                A.dtid[d] = table_at(A.tidx, A.tcell_off, (uint32_t)c, (uint32_t)(c >> 1));
         }
         __syncthreads();  // part / bases are reused by the next tile
     }

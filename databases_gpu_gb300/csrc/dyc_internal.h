@@ -79,8 +79,11 @@ struct ApplyScratch {
     uint32_t *tup;             // per table: upserts listed (the upsize policy's insert batch)
     uint32_t *ter;             // per table: erases listed (keys present before the batch)
     uint32_t *tcell_off;       // per table: first cell of its region (ntables + 1)
+    uint32_t *tidx;            // table of every kTidxStep-th op (cap_ops / kTidxStep + 1)
     uint32_t ntables;
 };
+
+constexpr uint32_t kTidxStep = 64;  // ops per entry of ApplyScratch::tidx
 
 // ApplyScratch::ctr slots
 enum : int {
