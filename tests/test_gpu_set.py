@@ -268,3 +268,48 @@ def test_set_deferred_upsize_matches_per_table_path(kind):
         assert_same_contents(A.table(t), maps[t], "table %d contents" % t)
     A.close()
     B.close()
+
+
+@pytest.mark.parametrize("bucket_bytes,key_bytes", [(128, 4), (64, 8)])
+def test_set_upsize_waves_match_per_table_path(bucket_bytes, key_bytes):
+    """Many tiny tables, each hit by enough inserts to need several upsizes in
+    one batch: the set issues them in waves (one launch per wave for all its
+    tables). Capacities, sizes, results and contents equal those of one
+    dyc_apply per table, which upsizes table by table."""
+    import torch
+    rng = np.random.default_rng(23)
+    nt = 200
+    A = _dg().DyCuckooSet([64] * nt, key_bytes=key_bytes, bucket_bytes=bucket_bytes)
+    B = _dg().DyCuckooSet([64] * nt, key_bytes=key_bytes, bucket_bytes=bucket_bytes)
+    maps = [O.Map() for _ in range(nt)]
+    for r in range(2):
+        cnt = rng.integers(0, 2000, nt)
+        off = np.zeros(nt + 1, np.uint32)
+        off[1:] = np.cumsum(cnt)
+        n = int(off[-1])
+        ops = rng.choice(np.array([0, 1, 2], np.uint8), size=n, p=[0.1, 0.8, 0.1])
+        if key_bytes == 4:
+            keys = rng.integers(1, 1 << 31, n).astype(np.uint32)
+            vals = rng.integers(0, 1 << 31, n).astype(np.uint32)
+            dk = torch.from_numpy(keys.view(np.int32)).cuda()
+            dv = torch.from_numpy(vals.view(np.int32)).cuda()
+        else:
+            keys = rng.integers(1, 1 << 62, n, dtype=np.int64).astype(np.uint64)
+            vals = rng.integers(0, 1 << 62, n, dtype=np.int64).astype(np.uint64)
+            dk = torch.from_numpy(keys.view(np.int64)).cuda()
+            dv = torch.from_numpy(vals.view(np.int64)).cuda()
+        do = torch.from_numpy(ops).cuda()
+        doff = torch.from_numpy(off.view(np.int32)).cuda()
+        oa, ba = A.apply(doff, do, dk, dv, h_offsets=off, graph=(r == 1))
+        st = A.stats()
+        ob, bb = B.apply(doff, do, dk, dv, h_offsets=off, each=True)
+        _check_round(A, maps, off, do, dk, dv, oa, ba, "waves round %d" % r)
+        assert bool((oa == ob).all()) and bool((ba == bb).all())
+        sza, capa = A.sizes()
+        szb, capb = B.sizes()
+        assert np.array_equal(sza, szb) and np.array_equal(capa, capb)
+        assert st["resizes_up"] > 2 * nt  # several upsizes per table
+    for t in (0, 99, nt - 1):
+        assert_same_contents(A.table(t), maps[t], "table %d contents" % t)
+    A.close()
+    B.close()
