@@ -574,11 +574,28 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
             else atomicAdd(&ctr->spill, 1ull);
         }
     }
-    agg_add(&ctr->inserted, n_ins);
-    agg_add(&ctr->size, n_ins);
-    agg_add(&ctr->updated, n_upd);
-    agg_add(&ctr->rejected, n_rej);
-    agg_add(&ctr->superseded, n_sup);
+    // one atomic per counter per block (the grid has many short-lived blocks)
+    __shared__ unsigned long long s_sum[4];
+    if (threadIdx.x < 4) s_sum[threadIdx.x] = 0ull;
+    __syncthreads();
+    const uint32_t w_ins = __reduce_add_sync(kFull, n_ins), w_upd = __reduce_add_sync(kFull, n_upd);
+    const uint32_t w_rej = __reduce_add_sync(kFull, n_rej), w_sup = __reduce_add_sync(kFull, n_sup);
+    if ((threadIdx.x & 31) == 0) {
+        if (w_ins) atomicAdd(&s_sum[0], (unsigned long long)w_ins);
+        if (w_upd) atomicAdd(&s_sum[1], (unsigned long long)w_upd);
+        if (w_rej) atomicAdd(&s_sum[2], (unsigned long long)w_rej);
+        if (w_sup) atomicAdd(&s_sum[3], (unsigned long long)w_sup);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_sum[0]) {
+            atomicAdd(&ctr->inserted, s_sum[0]);
+            atomicAdd(&ctr->size, s_sum[0]);
+        }
+        if (s_sum[1]) atomicAdd(&ctr->updated, s_sum[1]);
+        if (s_sum[2]) atomicAdd(&ctr->rejected, s_sum[2]);
+        if (s_sum[3]) atomicAdd(&ctr->superseded, s_sum[3]);
+    }
 }
 
 // Victim when a bucket is full: prefer a resident sitting in its second
@@ -912,15 +929,24 @@ __global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D,
         if (bits != nullptr && lane == 0) bits[base >> 5] = m;
         n_del += erased ? 1u : 0u;
     }
-    // loops are warp-uniform, so every lane of the warp is here
+    // loops are warp-uniform, so every lane of the warp is here; one atomic
+    // per counter per block (the grid has many short-lived blocks)
+    __shared__ unsigned long long s_sum[2];
+    if (threadIdx.x < 2) s_sum[threadIdx.x] = 0ull;
+    __syncthreads();
     const uint32_t del = __reduce_add_sync(kFull, n_del);
     const uint32_t sup = __reduce_add_sync(kFull, n_sup);
     if (lane == 0) {
-        if (del) {
-            atomicAdd(&ctr->erased, (unsigned long long)del);
-            atomicAdd(&ctr->size, (unsigned long long)(-(long long)del));  // size -= del
+        if (del) atomicAdd(&s_sum[0], (unsigned long long)del);
+        if (sup) atomicAdd(&s_sum[1], (unsigned long long)sup);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_sum[0]) {
+            atomicAdd(&ctr->erased, s_sum[0]);
+            atomicAdd(&ctr->size, (unsigned long long)(-(long long)s_sum[0]));  // size -= erased
         }
-        if (sup) atomicAdd(&ctr->superseded, (unsigned long long)sup);
+        if (s_sum[1]) atomicAdd(&ctr->superseded, s_sum[1]);
     }
 }
 

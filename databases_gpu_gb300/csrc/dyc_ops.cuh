@@ -80,8 +80,10 @@ cudaError_t Ops<KB>::place(const LaunchCtx &L, const Desc &D, int sb, const Scra
     if (n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_place<KB, SB>;
-        k<<<grid_for((const void *)k, L, n), 256, 0, L.stream>>>(
-            D, S, use_dedup ? 1 : 0, new_keys ? 1 : 0, keys, vals, vb, n, ctr);
+        // as for find: eight 32-key tiles per warp, as many blocks as that takes
+        const int g = (int)std::min<uint64_t>((n + 2047) / 2048, 0x7fffffffull);
+        k<<<g, 256, 0, L.stream>>>(D, S, use_dedup ? 1 : 0, new_keys ? 1 : 0, keys, vals, vb, n,
+                                   ctr);
     });
     return cudaGetLastError();
 }
@@ -108,8 +110,9 @@ cudaError_t Ops<KB>::erase(const LaunchCtx &L, const Desc &D, int sb, const Scra
     if (n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_erase<KB, SB>;
-        k<<<grid_for((const void *)k, L, n), 256, 0, L.stream>>>(D, S, use_dedup ? 1 : 0, keys,
-                                                                 n, bits, ctr);
+        // as for find: eight 32-key tiles per warp, as many blocks as that takes
+        const int g = (int)std::min<uint64_t>((n + 2047) / 2048, 0x7fffffffull);
+        k<<<g, 256, 0, L.stream>>>(D, S, use_dedup ? 1 : 0, keys, n, bits, ctr);
     });
     return cudaGetLastError();
 }
@@ -244,8 +247,9 @@ cudaError_t Ops<KB>::set_find(const LaunchCtx &L, const Desc *descs, int sb, con
     if (max_n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_set_find<KB, SB>;
-        k<<<grid_for((const void *)k, L, max_n), 256, 0, L.stream>>>(descs, keys, tids, n_ptr,
-                                                                      vals, vb, hits);
+        // eight 32-key tiles per warp of the bound, as for find
+        const int g = (int)std::min<uint64_t>((max_n + 2047) / 2048, 0x7fffffffull);
+        k<<<g, 256, 0, L.stream>>>(descs, keys, tids, n_ptr, vals, vb, hits);
     });
     return cudaGetLastError();
 }
@@ -260,7 +264,8 @@ cudaError_t Ops<KB>::set_mutate(const LaunchCtx &L, const Desc *descs, Counters 
     if (max_n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_set_mutate<KB, SB>;
-        k<<<grid_for((const void *)k, L, max_n + 32), 256, 0, L.stream>>>(
+        const int g = (int)std::min<uint64_t>((max_n + 32 + 2047) / 2048, 0x7fffffffull);
+        k<<<g, 256, 0, L.stream>>>(
             descs, tctr, er_keys, er_tids, ne_ptr, up_keys, up_vals, vb, up_tids, nu_ptr, list_a,
             list_a_tid, list_cap, gctr);
     });

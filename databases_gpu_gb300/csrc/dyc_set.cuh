@@ -209,9 +209,24 @@ __global__ void __launch_bounds__(256) k_set_mutate(
                                    list_a, list_a_tid, list_cap, gctr, stage, n_ins, n_upd);
         }
     }
-    agg_add(&gctr->erased, n_del);
-    agg_add(&gctr->inserted, n_ins);
-    agg_add(&gctr->updated, n_upd);
+    // one atomic per counter per block (the grid has many short-lived blocks)
+    __shared__ unsigned long long s_sum[3];
+    if (threadIdx.x < 3) s_sum[threadIdx.x] = 0ull;
+    __syncthreads();
+    n_del = __reduce_add_sync(kFull, n_del);
+    n_ins = __reduce_add_sync(kFull, n_ins);
+    n_upd = __reduce_add_sync(kFull, n_upd);
+    if ((threadIdx.x & 31) == 0) {
+        if (n_del) atomicAdd(&s_sum[0], (unsigned long long)n_del);
+        if (n_ins) atomicAdd(&s_sum[1], (unsigned long long)n_ins);
+        if (n_upd) atomicAdd(&s_sum[2], (unsigned long long)n_upd);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_sum[0]) atomicAdd(&gctr->erased, s_sum[0]);
+        if (s_sum[1]) atomicAdd(&gctr->inserted, s_sum[1]);
+        if (s_sum[2]) atomicAdd(&gctr->updated, s_sum[2]);
+    }
 }
 
 // eviction walks of src entries (k_walk per table, each with its own
