@@ -12,6 +12,27 @@
 
 namespace dyc {
 
+// Grid of a random-access kernel: one block of 256 threads per 2048 items,
+// so each warp takes eight 32-item tiles. Block
+// turnover keeps the SMs' fetch phases out of step, which sustains more
+// random line accesses than one resident wave (find on GB300: 39.3 vs 34.2
+// G/s).
+// A tuner's blocks-per-SM cap (L.max_blocks_per_sm) still bounds the grid;
+// the kernels are grid-stride loops.
+inline int tile_grid(const LaunchCtx &L, uint64_t n) {
+    uint64_t g = (n + 2047) / 2048;
+    // a small batch keeps one item per thread up to a full wave of 256-thread
+    // blocks (8 per SM): its latency, not the fetch rate, sets the time
+    const uint64_t one_each = (n + 255) / 256, wave = 8ull * (uint64_t)(L.sms > 0 ? L.sms : 1);
+    const uint64_t floor_g = one_each < wave ? one_each : wave;
+    if (g < floor_g) g = floor_g;
+    if (L.max_blocks_per_sm > 0) {
+        const uint64_t cap = (uint64_t)L.max_blocks_per_sm * (uint64_t)(L.sms > 0 ? L.sms : 1);
+        if (g > cap) g = cap;
+    }
+    return (int)(g < 1 ? 1 : (g > 0x7fffffffull ? 0x7fffffffull : g));
+}
+
 // Grid size for a grid-stride kernel: enough blocks for `work` threads, at
 // most one full wave of resident blocks (occupancy x SM count).
 inline int grid_for(const void *kernel, const LaunchCtx &L, uint64_t work, int block = 256) {
@@ -54,12 +75,7 @@ cudaError_t Ops<KB>::find(const LaunchCtx &L, const Desc &D, int sb, const void 
     if (n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_find<KB, SB>;
-        // eight 32-key tiles per warp and as many blocks as that takes: block
-        // turnover keeps the SMs' fetch phases out of step, which sustains
-        // more random line reads than a persistent grid (on GB300, 2^26
-        // finds: 39.3 G/s vs 34.2 G/s for one wave of resident blocks)
-        const int g = (int)std::min<uint64_t>((n + 2047) / 2048, 0x7fffffffull);
-        k<<<g, 256, 0, L.stream>>>(D, keys, vals, vb, hits, n);
+        k<<<tile_grid(L, n), 256, 0, L.stream>>>(D, keys, vals, vb, hits, n);
     });
     return cudaGetLastError();
 }
@@ -80,10 +96,8 @@ cudaError_t Ops<KB>::place(const LaunchCtx &L, const Desc &D, int sb, const Scra
     if (n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_place<KB, SB>;
-        // as for find: eight 32-key tiles per warp, as many blocks as that takes
-        const int g = (int)std::min<uint64_t>((n + 2047) / 2048, 0x7fffffffull);
-        k<<<g, 256, 0, L.stream>>>(D, S, use_dedup ? 1 : 0, new_keys ? 1 : 0, keys, vals, vb, n,
-                                   ctr);
+        k<<<tile_grid(L, n), 256, 0, L.stream>>>(D, S, use_dedup ? 1 : 0, new_keys ? 1 : 0, keys,
+                                                  vals, vb, n, ctr);
     });
     return cudaGetLastError();
 }
@@ -110,9 +124,7 @@ cudaError_t Ops<KB>::erase(const LaunchCtx &L, const Desc &D, int sb, const Scra
     if (n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_erase<KB, SB>;
-        // as for find: eight 32-key tiles per warp, as many blocks as that takes
-        const int g = (int)std::min<uint64_t>((n + 2047) / 2048, 0x7fffffffull);
-        k<<<g, 256, 0, L.stream>>>(D, S, use_dedup ? 1 : 0, keys, n, bits, ctr);
+        k<<<tile_grid(L, n), 256, 0, L.stream>>>(D, S, use_dedup ? 1 : 0, keys, n, bits, ctr);
     });
     return cudaGetLastError();
 }
@@ -175,7 +187,7 @@ cudaError_t Ops<KB>::apply_group(const LaunchCtx &L, const ApplyScratch &A, cons
                                  uint64_t n) {
     if (n == 0) return cudaSuccess;
     auto g = k_apply_group<KB>;
-    g<<<grid_for((const void *)g, L, n), 256, 0, L.stream>>>(A, keys, n);
+    g<<<tile_grid(L, n), 256, 0, L.stream>>>(A, keys, n);
     auto c = k_apply_compact<KB>;
     c<<<grid_for((const void *)c, L, 2 * n), 256, 0, L.stream>>>(A, 2 * n);
     return cudaGetLastError();
@@ -186,7 +198,7 @@ cudaError_t Ops<KB>::apply_scatter(const LaunchCtx &L, const ApplyScratch &A, ui
                                    const uint32_t *n_ptr) {
     if (n == 0) return cudaSuccess;
     auto sc = k_apply_scatter<KB>;
-    sc<<<grid_for((const void *)sc, L, n), 256, 0, L.stream>>>(A, n, n_ptr);
+    sc<<<tile_grid(L, n), 256, 0, L.stream>>>(A, n, n_ptr);
     return cudaGetLastError();
 }
 
@@ -198,8 +210,7 @@ cudaError_t Ops<KB>::apply_replay(const LaunchCtx &L, const ApplyScratch &A, con
     if (n == 0) return cudaSuccess;
     auto r = k_apply_replay<KB>;
     const uint64_t work = n > max_distinct ? n : max_distinct;
-    r<<<grid_for((const void *)r, L, work), 256, 0, L.stream>>>(A, ops, vals, vb, vals_out,
-                                                                 bits_out, n, n_ptr);
+    r<<<tile_grid(L, work), 256, 0, L.stream>>>(A, ops, vals, vb, vals_out, bits_out, n, n_ptr);
     // the segment classes are disjoint: with a side stream the warp and
     // block replays run beside the thread replay
     const bool forked = L.side != nullptr;
@@ -233,7 +244,7 @@ cudaError_t Ops<KB>::set_group(const LaunchCtx &L, const ApplyScratch &A, const 
         A, off, bits, (unsigned long long *)gctr, (uint32_t)(sizeof(Counters) / 8));
     if (n) {  // n sizes the grids; the kernels read the op count from off[ntables]
         auto g = k_set_group<KB>;
-        g<<<grid_for((const void *)g, L, n), 256, 0, L.stream>>>(A, off, keys);
+        g<<<tile_grid(L, n), 256, 0, L.stream>>>(A, off, keys);
         auto c = k_apply_compact<KB>;
         c<<<grid_for((const void *)c, L, 2 * n), 256, 0, L.stream>>>(A, 0);
     }
@@ -247,9 +258,7 @@ cudaError_t Ops<KB>::set_find(const LaunchCtx &L, const Desc *descs, int sb, con
     if (max_n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_set_find<KB, SB>;
-        // eight 32-key tiles per warp of the bound, as for find
-        const int g = (int)std::min<uint64_t>((max_n + 2047) / 2048, 0x7fffffffull);
-        k<<<g, 256, 0, L.stream>>>(descs, keys, tids, n_ptr, vals, vb, hits);
+        k<<<tile_grid(L, max_n), 256, 0, L.stream>>>(descs, keys, tids, n_ptr, vals, vb, hits);
     });
     return cudaGetLastError();
 }
@@ -264,8 +273,7 @@ cudaError_t Ops<KB>::set_mutate(const LaunchCtx &L, const Desc *descs, Counters 
     if (max_n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_set_mutate<KB, SB>;
-        const int g = (int)std::min<uint64_t>((max_n + 32 + 2047) / 2048, 0x7fffffffull);
-        k<<<g, 256, 0, L.stream>>>(
+        k<<<tile_grid(L, max_n + 32), 256, 0, L.stream>>>(
             descs, tctr, er_keys, er_tids, ne_ptr, up_keys, up_vals, vb, up_tids, nu_ptr, list_a,
             list_a_tid, list_cap, gctr);
     });
