@@ -35,6 +35,10 @@ enum : uint8_t { kOpFind = 0, kOpInsert = 1, kOpErase = 2 };
 constexpr uint32_t kShortSeg = 8;    // segments replayed by one thread
 constexpr uint32_t kWarpSeg = 256;   // segments sorted and replayed by one warp
 constexpr uint32_t kMidSeg = 4096;   // longest segment sorted in shared memory alone
+// Warp segments a warp replays in a row; lane j keeps segment j's final
+// state, so the upsert / erase lists take one warp-aggregated atomic per
+// task. Few segments per task keep more warps busy when segments are few.
+constexpr uint32_t kWarpTask = 8;
 constexpr uint32_t kNoCell = 0xffffffffu;
 
 // Cells: 4-byte keys {key (low word), count (high word)} in one 64-bit word;
@@ -532,10 +536,11 @@ __device__ __forceinline__ void bitonic_sort(uint32_t *s, uint32_t P, uint32_t t
 }
 
 // Warp segments (kShortSeg < ops <= kWarpSeg): one warp per segment sorts
-// it in its own shared memory and replays it. A warp takes 32 segments in a
-// row and keeps segment j's final state in lane j, so the erase / upsert
-// lists get one warp-aggregated allocation per 32 segments (one global
-// counter bumped per segment serialised this kernel).
+// it in its own shared memory and replays it. A warp takes kWarpTask
+// segments in a row and keeps segment j's final state in lane j, so the
+// erase / upsert lists get one warp-aggregated allocation per task (one
+// global counter bumped per segment serialised this kernel; tasks of 32
+// segments left most warps idle when a round had few warp segments).
 template <int KB>
 __global__ void __launch_bounds__(256) k_apply_replay_warp(const __grid_constant__ ApplyScratch A,
                                                            const uint8_t *__restrict__ ops,
@@ -549,11 +554,11 @@ __global__ void __launch_bounds__(256) k_apply_replay_warp(const __grid_constant
     const uint64_t nw = A.ctr[kCtrWarp];
     const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    for (uint64_t x0 = gw * 32; x0 < nw; x0 += warps * 32) {
+    for (uint64_t x0 = gw * kWarpTask; x0 < nw; x0 += warps * kWarpTask) {
         uint32_t rd = 0;
         bool rvalid = false, rpresent = false, rpre = false;
         uint64_t rvalue = 0ull, rpre_value = 0ull;
-        for (uint32_t j = 0; j < 32 && x0 + j < nw; ++j) {
+        for (uint32_t j = 0; j < kWarpTask && x0 + j < nw; ++j) {
             const uint32_t d = A.wseg[x0 + j];
             const uint32_t cnt = A.dcnt[d], off = seg_off(A, d);  // kShortSeg < cnt <= kWarpSeg
             uint32_t P = 32;

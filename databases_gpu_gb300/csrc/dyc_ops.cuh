@@ -221,8 +221,8 @@ cudaError_t Ops<KB>::apply_replay(const LaunchCtx &L, const ApplyScratch &A, con
         if (e != cudaSuccess) return e;
     }
     auto w = k_apply_replay_warp<KB>;
-    // one warp per 32 warp segments; at most n / (kShortSeg + 1) segments
-    w<<<grid_for((const void *)w, L, n / (kShortSeg + 1) + 32), 256, 0, s2>>>(
+    // one warp per kWarpTask warp segments; at most n / (kShortSeg + 1) segments
+    w<<<grid_for((const void *)w, L, (n / (kShortSeg + 1) / kWarpTask + 1) * 32), 256, 0, s2>>>(
         A, ops, vals, vb, vals_out, bits_out);
     auto m = k_apply_replay_mid<KB>;
     // one block per mid segment; at most n / (kWarpSeg + 1) of them
