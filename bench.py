@@ -437,8 +437,11 @@ def run_resize_stream(args, dev, torch, dg):
     ws = ResizeStream(B, nb // 2, nb - nb // 2, 1 << args.stream_log2_start,
                       1 << args.stream_log2_peak, dup=0.05, seed=10327, device=dev)
     t = dg.DyCuckoo(1 << args.stream_log2_start, key_bytes=8, value_bytes=8, upper_load=0.90,
-                    lower_load=0.35, min_downsize_capacity=0, max_evictions=args.max_evictions,
-                    device=dev.index or 0)
+                    lower_load=0.35, min_downsize_capacity=0,
+                    max_evictions=args.stream_max_evictions, device=dev.index or 0)
+    # 4 GiB mapped into the allocation pool up front, as the reference's
+    # hashAPI gives its CNMeM pool at construction (api.cpp:37-40)
+    dg.pool_reserve(4 << 30, device=dev.index or 0)
     k0, v0 = ws.preload()
     t.insert(k0, v0)
     del k0, v0
@@ -446,6 +449,7 @@ def run_resize_stream(args, dev, torch, dg):
     out = torch.empty(B, dtype=torch.int64, device=dev)
     bits = torch.empty((B + 31) // 32, dtype=torch.int32, device=dev)
     lat = []
+    kinds = []
     bad = 0
     ups = downs = 0
     peak_cap = 0
@@ -462,6 +466,7 @@ def run_resize_stream(args, dev, torch, dg):
         st = t.stats()
         ups += st["resizes_up"]
         downs += st["resizes_down"]
+        kinds.append((st["resizes_up"], st["resizes_down"], st["overflowed"]))
         peak_cap = max(peak_cap, t.capacity)
         hits = unpack_bits_dev(bits, B, torch)
         fh = int((hits & (sb.ops == 0)).sum())
@@ -478,6 +483,12 @@ def run_resize_stream(args, dev, torch, dg):
         "batch_ms_p50": round(lat_sorted[len(lat) // 2], 3),
         "batch_ms_p99": round(lat_sorted[min(len(lat) - 1, int(len(lat) * 0.99))], 3),
         "total_s": round(total_ms / 1e3, 3),
+        # the slowest batches: (ms, upsizes, downsizes, overflowed entries)
+        "slowest": [(round(lat[i], 3),) + kinds[i]
+                    for i in sorted(range(len(lat)), key=lambda i: -lat[i])[:8]],
+        "no_resize_batch_ms_p99": round(sorted(
+            [x for x, k in zip(lat, kinds) if k[0] == 0 and k[1] == 0] or [0.0])[
+            int(0.99 * max(0, sum(1 for k in kinds if k[0] == 0 and k[1] == 0) - 1))], 3),
         "resizes_up": ups, "resizes_down": downs, "peak_capacity": peak_cap,
         "final_capacity": t.capacity, "final_size": t.size,
         "check_failures": bad,
@@ -659,6 +670,7 @@ def main():
     ap.add_argument("--skip-tune", action="store_true", help="skip the tuned multi-table set")
     ap.add_argument("--mt-rounds", type=int, default=3)
     ap.add_argument("--stream-batches", type=int, default=512)
+    ap.add_argument("--stream-max-evictions", type=int, default=2048)
     ap.add_argument("--stream-log2-batch", type=int, default=22)
     ap.add_argument("--stream-log2-start", type=int, default=20)
     ap.add_argument("--stream-log2-peak", type=int, default=27)

@@ -255,6 +255,12 @@ dyc_status resize_up_impl(dyc_table *t, cudaStream_t s) {
     return DYC_OK;
 }
 
+// Highest load a batch may fill a table to before its upsize policy runs
+// (the policy then runs after the batch): halfway from the upper bound to
+// full. Past it eviction walks lengthen and fail (at 0.94 on 7-slot buckets
+// a walk of max_evictions 2048 steps took 4-6 ms before overflowing).
+double deferred_fill(const dyc_table *t) { return 0.5 * (1.0 + t->cfg.upper_load); }
+
 // Host half of an upsize of subtable pick_up(): allocate the doubled
 // subtable, describe the move as a job and switch the descriptor to the new
 // subtable. The caller launches the move (resize_up_flush) before freeing
@@ -1000,10 +1006,11 @@ dyc_status read_apply_counters(dyc_table *t, cudaStream_t s) {
 // device, so the host reads the counters once, at the end. The upsize
 // policy (api.cpp:359-369: the size after the batch's erases plus its
 // inserts above upper bound x capacity) needs the batch's upsert and erase
-// counts: where even n inserts fit the table's slots it is applied after the
-// batch with the same counts, so the capacity ends as if it had run first
-// (entries the fuller table could not place take the overflow path);
-// otherwise the host reads the counts after the replay and upsizes first.
+// counts: where even n inserts keep the table within deferred_fill() of its
+// slots it is applied after the batch with the same counts, so the capacity
+// ends as if it had run first (entries the fuller table could not place
+// take the overflow path); otherwise the host reads the counts after the
+// replay and upsizes first.
 dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const void *vals,
                        uint64_t n, void *vals_out, uint32_t *bits_out, uint32_t flags,
                        cudaStream_t s) {
@@ -1011,7 +1018,7 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     const LaunchCtx L = ctx(t, s);
     const uint32_t vb = (uint32_t)t->vb;
     const bool resize = t->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE);
-    const bool deferred = !resize || t->size + n <= t->capacity;
+    const bool deferred = !resize || (double)(t->size + n) <= deferred_fill(t) * (double)t->capacity;
     const uint64_t size0 = t->size;
     bool grew = false;
     auto upsize_policy = [&]() -> dyc_status {
@@ -1611,19 +1618,19 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
     // size + the batch's inserts > upper bound x capacity, upsize, where the
     // inserts are the table's upserts after the batch is reduced per key and
     // the size is the one after the table's erases (as in dyc_apply), both
-    // known on the device after phase A. Where even a batch of
-    // nothing but new keys stays within a table's slots, the batch runs both
-    // phases back to back and the policy is applied after it with the same
-    // sizes and counts, so capacities end as if it had run before the
-    // inserts (entries a fuller table could not place go through the
-    // overflow path). Otherwise the host reads the counts between the phases
-    // and upsizes first.
+    // known on the device after phase A. Where even a batch of nothing but
+    // new keys keeps every table within deferred_fill() of its slots, the
+    // batch runs both phases back to back and the policy is applied after it
+    // with the same sizes and counts, so capacities end as if it had run
+    // before the inserts (entries a fuller table could not place go through
+    // the overflow path). Otherwise the host reads the counts between the
+    // phases and upsizes first.
     bool deferred = true;
     if (resize)
         for (uint32_t t = 0; t < s->ntables && deferred; ++t) {
             const dyc_table *m = s->tables[t];
             const uint64_t cnt = h_offsets[t + 1] - h_offsets[t];
-            deferred = m->size + cnt <= m->capacity;
+            deferred = (double)(m->size + cnt) <= deferred_fill(m) * (double)m->capacity;
         }
     bool moved = false;
     std::vector<uint8_t> grew;

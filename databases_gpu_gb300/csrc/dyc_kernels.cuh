@@ -600,7 +600,20 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
 
 // Victim when a bucket is full: prefer a resident sitting in its second
 // bucket (evicting it sends it back to its first-probe bucket); the start
-// rotates with the step so chains do not cycle.
+// is a pseudo-random slot (victim_rot, mixed from the key and the step). The
+// preference holds for the first kPrefSteps steps of a chain (victim_pref):
+// a cluster of full buckets whose second-bucket residents all point at each
+// other can trap a walk that always takes them (at load 0.94 on 7-slot
+// buckets some walks ran out all 2048 steps), so a chain that long walks at
+// random. (Dropping the preference after 4 steps cost 32-byte buckets a
+// tenth of their first-probe hits.)
+constexpr uint32_t kPrefSteps = 32;
+__device__ __forceinline__ uint32_t victim_rot(uint32_t hk, uint32_t step) {
+    return mix32(hk ^ (step * 0x9E3779B9u));
+}
+__device__ __forceinline__ unsigned victim_pref(unsigned pref, uint32_t step) {
+    return step < kPrefSteps ? pref : 0u;
+}
 template <int KB, int SB>
 __device__ __forceinline__ int pick_victim(unsigned pref, uint32_t rot) {
     constexpr int B = Geo<KB, SB>::kSlots;
@@ -709,7 +722,8 @@ __device__ __forceinline__ WalkOut<KB> walk_lookahead(const Desc &D, typename Sl
                 pref |= ((second >> (x * G)) & 1u) << (q * RO + x);
             }
         }
-        const int j = pick_victim<KB, SB>(cand ? cand : pref, hk + level);
+        const int j = cand ? pick_victim<KB, SB>(cand, hk + level)
+                           : pick_victim<KB, SB>(victim_pref(pref, level), victim_rot(hk, level));
         const int src = (j % RO) * G;
         char *aj = nullptr;
         unsigned aem = 0u;
@@ -823,7 +837,8 @@ __global__ void __launch_bounds__(256) k_walk(const __grid_constant__ Desc D,
                     live = false;
                     fail = true;
                 } else {
-                    const int j = pick_victim<KB, SB>(r.pref, hk + evictions);
+                    const int j = pick_victim<KB, SB>(victim_pref(r.pref, evictions),
+                                                      victim_rot(hk, evictions));
                     if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
                     const Sl old = T::exch(slot_ptr<KB, SB>(bp, j), e);
                     ++evictions;

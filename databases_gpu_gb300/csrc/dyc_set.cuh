@@ -300,7 +300,8 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
                     live = false;
                     fail = true;
                 } else {
-                    const int j = pick_victim<KB, SB>(r.pref, hk + evictions);
+                    const int j = pick_victim<KB, SB>(victim_pref(r.pref, evictions),
+                                                      victim_rot(hk, evictions));
                     if (t != pe.first) mark_overflow<KB, SB>(fb, hk);
                     const Sl old = T::exch(slot_ptr<KB, SB>(bp, j), e);
                     ++evictions;

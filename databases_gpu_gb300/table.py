@@ -665,16 +665,21 @@ class hashAPI:  # noqa: N801 -- the reference's class name
     """The reference's hashAPI (GPU/dyhash/api.h:9-54, api.cpp) on GB300.
 
     Host arrays in, host arrays out, like the reference. Differences, all
-    deliberate: no memory pool and no leaked buffers; any number of live
-    tables; sizes are exact counts (the reference's num_size counts nominal
-    batch sizes, api.cpp:371, :490); insert is an upsert and no entry is ever
-    dropped (the reference drops entries at the end of long eviction chains,
+    deliberate: the 4 GiB the reference's constructor gives its CNMeM pool
+    (api.cpp:37-40) are mapped into the library's stream-ordered pool
+    (dyc_pool_reserve); no leaked buffers; any number of live tables; sizes
+    are exact counts (the reference's num_size counts nominal batch sizes,
+    api.cpp:371, :490); insert is an upsert and no entry is ever dropped (the
+    reference drops entries at the end of long eviction chains,
     cuckoo.cu:422-431).
     """
+
+    POOL_BYTES = 4 << 30
 
     def __init__(self, size: int, **cfg):
         cfg.setdefault("auto_resize", False)  # hash_insert has the check compiled out (api.cpp:185)
         self.t = DyCuckoo(int(size), **cfg)
+        pool_reserve(self.POOL_BYTES, device=self.t.device)
         self._pool_k = None
         self._pool_v = None
         self.batch_num_to_op = 0

@@ -15,7 +15,9 @@
 //   * any number of hashAPI objects may live at once (the reference keeps
 //     its table in one __constant__ symbol, cuckoo.cu:16);
 //   * num_size is the exact live count (the reference counts nominal batch
-//     sizes, api.cpp:371, :490).
+//     sizes, api.cpp:371, :490);
+//   * the 4 GiB the reference's CNMeM pool takes at construction are mapped
+//     into the library's stream-ordered pool instead (dyc_pool_reserve).
 #pragma once
 
 #include <cstdint>
@@ -56,18 +58,24 @@ class hashAPI {
   public:
     // api.cpp:26-91. Plain hash_insert applies no load-factor check (the
     // reference compiles it out, api.cpp:185-194); the batch calls do.
+    // Both constructors map 4 GiB into the library's allocation pool, as the
+    // reference's constructor sizes its CNMeM pool (api.cpp:37-40), so the
+    // first resizes do not map memory inside a call.
     explicit hashAPI(TYPE size) {
         dyc_config cfg;
         dyc_config_default(&cfg);
         cfg.initial_size = size;
         cfg.auto_resize = 0;
         check(dyc_create(&cfg, &t_), "hashAPI::hashAPI");
+        check(dyc_pool_reserve(cfg.device, kPoolBytes), "hashAPI::hashAPI");
     }
     hashAPI(TYPE size, const dyc_config &cfg_in) {
         dyc_config cfg = cfg_in;
         cfg.initial_size = size;
         check(dyc_create(&cfg, &t_), "hashAPI::hashAPI");
+        check(dyc_pool_reserve(cfg.device, kPoolBytes), "hashAPI::hashAPI");
     }
+    static constexpr uint64_t kPoolBytes = 4ull << 30;
     ~hashAPI() {
         if (d_pool_k_) cudaFree(d_pool_k_);
         if (d_pool_v_) cudaFree(d_pool_v_);

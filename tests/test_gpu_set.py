@@ -211,11 +211,12 @@ def test_set_graph_reuses_buffers_across_batch_sizes():
 
 @pytest.mark.parametrize("kind", ["new_keys", "half_updates"])
 def test_set_deferred_upsize_matches_per_table_path(kind):
-    """new_keys: tables preloaded to 75 % of their slots (below the 0.8 upper
-    bound), then a batch of new keys worth 20 % more. half_updates: preloaded
+    """new_keys: tables preloaded to 70 % of their slots (below the 0.8 upper
+    bound), then a batch of new keys worth 15 % more. half_updates: preloaded
     to 70 %, a batch worth 16 % of which half update present keys, so only
     counting every insert (as the reference's policy does) passes the bound.
-    Either batch fits the slots, so the set runs it without a host
+    Either batch keeps the tables within 90 % (halfway from the bound to
+    full) even if all its ops were new keys, so the set runs it without a host
     round trip and applies the upsize policy afterwards (entries the fuller
     tables could not place take the overflow path). Results, sizes,
     capacities and contents equal those of one dyc_apply per table, which
@@ -227,8 +228,8 @@ def test_set_deferred_upsize_matches_per_table_path(kind):
     B = _dg().DyCuckooSet([3000] * nt)
     _, caps = A.sizes()
     maps = [O.Map() for _ in range(nt)]
-    pre = 0.75 if kind == "new_keys" else 0.70
-    share = 0.2 if kind == "new_keys" else 0.16
+    pre = 0.70
+    share = 0.15 if kind == "new_keys" else 0.16
     preloaded = []
     for t in range(nt):
         m = int(pre * int(caps[t]))
@@ -264,6 +265,7 @@ def test_set_deferred_upsize_matches_per_table_path(kind):
     assert np.array_equal(sza, szb)
     assert np.array_equal(capa, capb), (capa, capb)
     assert sa["resizes_up"] >= nt
+    assert sa["split_phases"] == 0  # the policy ran after the batch
     for t in range(nt):
         assert_same_contents(A.table(t), maps[t], "table %d contents" % t)
     A.close()
