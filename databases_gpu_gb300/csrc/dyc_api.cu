@@ -1038,11 +1038,12 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     CK(cudaMemsetAsync(A.ctr, 0, dyc::kCtrSlots * sizeof(unsigned long long), s));
     if (bits_out) CK(cudaMemsetAsync(bits_out, 0, (size_t)((n + 31) / 32) * 4, s));
     cudaError_t e = KB_CALL(t, apply_group, L, A, keys, n);
-    if (e == cudaSuccess) e = KB_CALL(t, apply_scatter, L, A, n);
     // state of every distinct key before the batch
     if (e == cudaSuccess)
         e = KB_CALL(t, set_find, L, t->d_desc, t->sb, A.dkey, nullptr, &A.ctr[dyc::kCtrDistinct],
                     n, A.pre_val, vb, A.pre_hit);
+    if (e == cudaSuccess)
+        e = KB_CALL(t, apply_scatter, L, A, n, nullptr, ops, vals, vb, vals_out, bits_out);
     if (e == cudaSuccess) e = KB_CALL(t, apply_replay, L, A, ops, vals, vb, vals_out, bits_out, n, n);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "apply kernels: %s", cudaGetErrorString(e));
     if (!deferred) {
@@ -1337,10 +1338,11 @@ dyc_status set_phase_a(dyc_set *s, const uint32_t *d_off, const uint8_t *ops, co
     const uint32_t *d_n = d_off + s->ntables;
     // also zeroes phase B's counters (nothing between the phases uses them)
     cudaError_t e = SET_KB_CALL(s, set_group, L, A, d_off, keys, n, bits, s->d_gctr);
-    if (e == cudaSuccess) e = SET_KB_CALL(s, apply_scatter, L, A, n, d_n);
     if (e == cudaSuccess)
         e = SET_KB_CALL(s, set_find, L, s->d_desc, s->sb, A.dkey, A.dtid, &A.ctr[dyc::kCtrDistinct],
                         n, A.pre_val, vb, A.pre_hit);
+    if (e == cudaSuccess)
+        e = SET_KB_CALL(s, apply_scatter, L, A, n, d_n, ops, vals, vb, out, bits);
     if (e == cudaSuccess)
         e = SET_KB_CALL(s, apply_replay, L, A, ops, vals, vb, out, bits, n, n, d_n);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "set phase A kernels: %s", cudaGetErrorString(e));

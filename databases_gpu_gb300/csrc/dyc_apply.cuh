@@ -321,21 +321,6 @@ __global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ A
     }
 }
 
-// n_ptr (many tables: offsets[ntables]) gives the op count on the device
-// instead of n, so that a captured launch serves batches of any size.
-template <int KB>
-__global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ ApplyScratch A,
-                                                       uint64_t n, const uint32_t *n_ptr) {
-    if (n_ptr) n = *n_ptr;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint32_t cell = A.op_cell[i];
-        if (cell == kNoCell) continue;
-        const uint32_t d = *cell_word<KB>(A.cells, cell);
-        A.seg[(uint32_t)(A.dseg[d] >> 32) + A.op_rank[i]] = (uint32_t)i;
-    }
-}
-
 __device__ __forceinline__ uint32_t seg_off(const ApplyScratch &A, uint32_t d) {
     return (uint32_t)(A.dseg[d] >> 32);
 }
@@ -376,6 +361,81 @@ __device__ __forceinline__ void record_final_one(const ApplyScratch &A, uint32_t
         if (A.dtid) {
             A.er_tid[e] = A.dtid[d];
             atomicAdd(&A.ter[A.dtid[d]], 1u);
+        }
+    }
+}
+
+// The pass over the ops in op order, after the find of the distinct keys.
+// A key with a single op in the batch is resolved here: its result is the
+// key's state before the batch, written in op order (values coalesced, the
+// hit bits one word per warp by ballot), and its final state goes to the
+// upsert / erase lists. Ops of keys with several ops go into their key's
+// segment, at the rank the grouping handed them, for the replay kernels.
+// Key-0 ops (no cell) report a miss. Whole blocks step through the ops so
+// every thread reaches block_alloc. n_ptr (many tables: offsets[ntables])
+// gives the op count on the device instead of n, so that a captured launch
+// serves batches of any size.
+template <int KB>
+__global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ ApplyScratch A,
+                                                       uint64_t n, const uint32_t *n_ptr,
+                                                       const uint8_t *__restrict__ ops,
+                                                       const void *__restrict__ vals, uint32_t vb,
+                                                       void *__restrict__ vals_out,
+                                                       uint32_t *__restrict__ bits_out) {
+    using K = typename SlotT<KB>::K;
+    if (n_ptr) n = *n_ptr;
+    const int slots[2] = {kCtrUp, kCtrEr};
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        const uint64_t i = i0 + threadIdx.x;
+        bool up = false, er = false, hit = false;
+        K k = 0;
+        uint64_t value = 0ull;
+        uint32_t tid = 0u;
+        if (i < n) {
+            const uint32_t cell = A.op_cell[i];
+            if (cell == kNoCell) {
+                if (vals_out) store_val(vals_out, vb, i, 0ull);
+            } else {
+                const uint32_t d = *cell_word<KB>(A.cells, cell);
+                if (A.dcnt[d] == 1u) {
+                    const bool pre = (A.pre_hit[d >> 5] >> (d & 31)) & 1u;
+                    const uint64_t pre_value = load_val(A.pre_val, vb, d);
+                    if (vals_out) store_val(vals_out, vb, i, pre ? pre_value : 0ull);
+                    hit = pre;
+                    const uint8_t op = ops[i];
+                    bool present = pre;
+                    value = pre_value;
+                    replay_op(op, op == kOpInsert ? load_val(vals, vb, i) : 0ull, present, value);
+                    up = present && (!pre || value != pre_value);
+                    er = !present && pre;
+                    if (up || er) {
+                        k = ((const K *)A.dkey)[d];
+                        if (A.dtid) tid = A.dtid[d];
+                    }
+                } else {
+                    A.seg[seg_off(A, d) + A.op_rank[i]] = (uint32_t)i;
+                }
+            }
+        }
+        // i0 is a multiple of 256: a warp's 32 ops are one word of bits
+        const unsigned hits = __ballot_sync(kFull, hit);
+        if (bits_out && (threadIdx.x & 31) == 0 && i < n) bits_out[i >> 5] = hits;
+        uint32_t got[2];
+        block_alloc<2, 32>(A.ctr, slots, (unsigned long long)up | ((unsigned long long)er << 32),
+                           got);
+        if (A.tup) {
+            warp_count_by(A.tup, tid, up);
+            warp_count_by(A.ter, tid, er);
+        }
+        if (up) {
+            ((K *)A.up_key)[got[0]] = k;
+            if (vb == 4) ((uint32_t *)A.up_val)[got[0]] = (uint32_t)value;
+            else ((unsigned long long *)A.up_val)[got[0]] = value;
+            if (A.up_tid) A.up_tid[got[0]] = tid;
+        } else if (er) {
+            ((K *)A.er_key)[got[1]] = k;
+            if (A.er_tid) A.er_tid[got[1]] = tid;
         }
     }
 }
@@ -432,12 +492,10 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
                                                       uint32_t *__restrict__ bits_out, uint64_t n,
                                                       const uint32_t *n_ptr) {
     using K = typename SlotT<KB>::K;
-    if (n_ptr) n = *n_ptr;
+    (void)n;  // key-0 ops and single-op keys were resolved by the scatter pass
+    (void)n_ptr;
     const uint64_t nd = A.ctr[kCtrDistinct];
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    // key-0 ops (no cell): miss, output 0
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-        if (A.op_cell[i] == kNoCell && vals_out) store_val(vals_out, vb, i, 0ull);
     const int slots[4] = {kCtrUp, kCtrEr, kCtrWarp, kCtrMid};
     // whole blocks step through the distinct keys so every thread reaches
     // the block_alloc call
@@ -453,7 +511,7 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
                 md = true;
             } else if (cnt > kShortSeg) {
                 wp = true;
-            } else {
+            } else if (cnt > 1u) {
                 uint32_t s[kShortSeg];
                 const uint32_t off = seg_off(A, (uint32_t)d);
 #pragma unroll

@@ -162,14 +162,17 @@ template <int KB> struct Ops {
                                void *list, unsigned long long *list_count, uint64_t list_cap,
                                unsigned long long *spill);
     // mixed batches (dyc_apply.cuh). One table: apply_group (group +
-    // compact), apply_scatter, find of the distinct keys, apply_replay.
+    // compact), find of the distinct keys, apply_scatter, apply_replay.
     // Many tables (dyc_set.cuh): set_group replaces apply_group, and
     // set_find / set_mutate / set_walk replace find / erase + place / walk.
     static cudaError_t apply_group(const LaunchCtx &L, const ApplyScratch &A, const void *keys,
                                   uint64_t n);
-    // n_ptr (many tables): the op count on the device; n then only sizes grids
+    // after the find of the distinct keys: single-op keys resolved in op
+    // order, the other ops scattered into their keys' segments. n_ptr (many
+    // tables): the op count on the device; n then only sizes grids
     static cudaError_t apply_scatter(const LaunchCtx &L, const ApplyScratch &A, uint64_t n,
-                                     const uint32_t *n_ptr = nullptr);
+                                     const uint32_t *n_ptr, const uint8_t *ops, const void *vals,
+                                     uint32_t vb, void *vals_out, uint32_t *bits_out);
     static cudaError_t apply_replay(const LaunchCtx &L, const ApplyScratch &A, const uint8_t *ops,
                                    const void *vals, uint32_t vb, void *vals_out,
                                    uint32_t *bits_out, uint64_t n, uint64_t max_distinct,

@@ -195,10 +195,11 @@ cudaError_t Ops<KB>::apply_group(const LaunchCtx &L, const ApplyScratch &A, cons
 
 template <int KB>
 cudaError_t Ops<KB>::apply_scatter(const LaunchCtx &L, const ApplyScratch &A, uint64_t n,
-                                   const uint32_t *n_ptr) {
+                                   const uint32_t *n_ptr, const uint8_t *ops, const void *vals,
+                                   uint32_t vb, void *vals_out, uint32_t *bits_out) {
     if (n == 0) return cudaSuccess;
     auto sc = k_apply_scatter<KB>;
-    sc<<<tile_grid(L, n), 256, 0, L.stream>>>(A, n, n_ptr);
+    sc<<<tile_grid(L, n), 256, 0, L.stream>>>(A, n, n_ptr, ops, vals, vb, vals_out, bits_out);
     return cudaGetLastError();
 }
 
