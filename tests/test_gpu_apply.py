@@ -3,11 +3,12 @@
 For every op the value it saw (found / replaced / removed, 0 when absent) and
 its hit bit (key present just before the op) must equal the oracle's, which
 runs the same ops one at a time in index order; the table's full contents
-must equal the oracle's after every batch. Cases: unique keys, heavy
-repetition (segments replayed by one thread), keys repeated thousands of
-times (segments replayed by a warp after the radix sort), key 0, u64 keys,
-batches that span several internal chunks, and growth/shrink through the
-resize policy.
+must equal the oracle's after every batch. Cases: unique keys (resolved by
+the op-order scatter pass), heavy repetition (segments replayed by one
+thread), keys repeated tens to thousands of times (segments replayed by a
+warp, or sorted by a block in shared-memory chunks merged in global memory),
+key 0, u64 keys, batches that span several internal chunks, and
+growth/shrink through the resize policy.
 """
 import numpy as np
 import pytest

@@ -6,7 +6,10 @@ map after every round; the batched path, the per-table path
 (dyc_set_apply_each) and the graph-replayed path give identical results.
 Cases: tables of very different sizes, tables without ops in a round, small
 tables hit by large batches (segments of up to kMidSeg ops per key and one
-giant segment), key 0, u64 keys, growth through the per-table resize policy.
+longer, sorted in chunks and merged), key 0, u64 keys, growth through the
+per-table resize policy (before the inserts, or after the batch when it fits,
+in waves over many tables), graph replay from fixed buffers at varying op
+counts.
 """
 import numpy as np
 import pytest
@@ -105,7 +108,8 @@ def test_set_batched_equals_per_table_path():
 
 def test_set_long_segments_key_zero_and_empty_tables():
     """Table 0: a few keys hit thousands of times (mid segments) and one key
-    hit 6000 times (a giant segment); table 1 has no ops; table 2 gets key 0."""
+    hit 6000 times (longer than one shared-memory sort); table 1 has no ops;
+    table 2 gets key 0."""
     import torch
     rng = np.random.default_rng(4)
     S = _dg().DyCuckooSet([64, 1000, 5000])
