@@ -1612,7 +1612,9 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
     dyc_set::Graph *gr = nullptr;
     if (flags & DYC_FLAG_GRAPH)
         gr = set_graph_for(s, {(uintptr_t)d_offsets, (uintptr_t)d_ops, (uintptr_t)d_keys,
-                              (uintptr_t)d_vals, (uintptr_t)d_vals_out, (uintptr_t)d_bits_out});
+                              (uintptr_t)d_vals, (uintptr_t)d_vals_out, (uintptr_t)d_bits_out,
+                              // the sequence differs with the resize policy (count copies)
+                              (uintptr_t)(flags & DYC_FLAG_NO_RESIZE)});
     // under a graph the grids are sized by the scratch capacity, not by n
     const uint64_t ng = gr ? s->A.cap_ops : n;
     const bool resize = s->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE);

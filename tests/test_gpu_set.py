@@ -176,11 +176,16 @@ def test_set_graph_reuses_buffers_across_batch_sizes():
     count every round: the captured graphs read the count on the device, so
     each round replays the same graph. Rounds that cannot grow a table run
     both phases back to back; the growing rounds (small tables, many inserts)
-    take the path with an upsize between the phases, also under the graph."""
+    take the path with an upsize between the phases, also under the graph.
+    Two rounds skip the resize policy (a different captured sequence for the
+    same buffers). Capacities follow a twin set fed the same rounds through
+    one dyc_apply per table."""
     import torch
     rng = np.random.default_rng(13)
     nt = 48
-    S = _dg().DyCuckooSet(rng.integers(64, 4096, nt).tolist())
+    sizes = rng.integers(64, 4096, nt).tolist()
+    S = _dg().DyCuckooSet(sizes)
+    twin = _dg().DyCuckooSet(sizes)
     maps = [O.Map() for _ in range(nt)]
     cap = nt * 2500
     b_ops = torch.empty(cap, dtype=torch.uint8, device="cuda")
@@ -204,13 +209,18 @@ def test_set_graph_reuses_buffers_across_batch_sizes():
         b_vals[:n].copy_(torch.from_numpy(vals.view(np.int32)))
         b_off.copy_(torch.from_numpy(off.view(np.int32)))
         nw = (n + 31) // 32
+        fixed = r in (3, 6)
         out, bits = S.apply(b_off, b_ops[:n], b_keys[:n], b_vals[:n], out=b_out[:n],
-                            bits=b_bits[:nw], h_offsets=off, graph=True)
+                            bits=b_bits[:nw], h_offsets=off, graph=True, no_resize=fixed)
         _check_round(S, maps, off, b_ops[:n], b_keys[:n], b_vals[:n], out, bits,
                      "graph round %d (n=%d)" % (r, n))
+        twin.apply(b_off, b_ops[:n], b_keys[:n], b_vals[:n], h_offsets=off, each=True,
+                   no_resize=fixed)
+        assert np.array_equal(S.sizes()[1], twin.sizes()[1]), "round %d capacities" % r
     for t in (0, 21, nt - 1):
         assert_same_contents(S.table(t), maps[t], "table %d contents" % t)
     S.close()
+    twin.close()
 
 
 @pytest.mark.parametrize("kind", ["new_keys", "half_updates"])
