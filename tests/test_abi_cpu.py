@@ -36,22 +36,35 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_struct_layout_matches_header(tmp_path):
+    """Every struct the Python mirror declares has the header's size and field
+    offsets (gcc on the header against ctypes)."""
+    mirrors = [("dyc_config", _lib.DycConfig), ("dyc_op_stats", _lib.DycOpStats),
+               ("dyc_server_config", _lib.DycServerConfig),
+               ("dyc_server_stats", _lib.DycServerStats)]
+    lines, want = [], []
+    for cname, M in mirrors:
+        lines.append('printf("%%zu\\n", sizeof(%s));' % cname)
+        want.append(C.sizeof(M))
+        for f, _ in M._fields_:
+            lines.append('printf("%%zu\\n", offsetof(%s, %s));' % (cname, f))
+            want.append(getattr(M, f).offset)
     prog = tmp_path / "layout.c"
-    prog.write_text(
-        '#include <stdio.h>\n#include <stddef.h>\n#include "dycuckoo.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(dyc_config),"
-        " offsetof(dyc_config, initial_size), offsetof(dyc_config, upper_load),"
-        " offsetof(dyc_config, device), sizeof(dyc_op_stats),"
-        " offsetof(dyc_op_stats, resizes_down));return 0;}\n")
+    prog.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "dycuckoo.h"\n'
+                    "int main(void){" + "".join(lines) + "return 0;}\n")
     exe = tmp_path / "layout"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(prog), "-o", str(exe)],
                    check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
                                           check=True).stdout.split()]
-    D = _lib.DycConfig
-    S = _lib.DycOpStats
-    assert got == [C.sizeof(D), D.initial_size.offset, D.upper_load.offset, D.device.offset,
-                   C.sizeof(S), S.resizes_down.offset]
+    assert got == want
+
+
+def test_server_config_defaults():
+    L = _lib.lib()
+    c = _lib.DycServerConfig()
+    L.dyc_server_config_default(C.byref(c))
+    assert c.hbm_cap_bytes == 0 and c.max_step_ops == 1 << 22 and c.coalesce == 1
+    assert c.pool_reserve_bytes == (1 << 64) - 1  # DYC_POOL_RESERVE_AUTO
 
 
 def test_config_defaults():
