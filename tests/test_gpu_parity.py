@@ -12,7 +12,7 @@ import pytest
 
 from oracle import oracle as O
 from tests.helpers import (assert_same_contents, find_and_compare, first_probe_table, to_dev,
-                           unique_u32, unique_u64)
+                           to_host, unique_u32, unique_u64)
 
 pytestmark = pytest.mark.gpu
 
@@ -388,4 +388,24 @@ def test_host_forms_match_device_forms():
     _, eh = m.erase(keys[n // 2: n + n // 2])
     assert cnt == int(eh.sum())
     assert_same_contents(t, m, "host forms")
+    t.close()
+
+
+def test_host_find_pipeline_chunk_schedule():
+    """A host find spanning several pipeline chunks on all three streams and a
+    ragged last chunk: values and hit bits equal a device find of the same
+    keys."""
+    import torch
+    n = 3 * (1 << 22) + 4133
+    keys = unique_u32(n, seed=29)
+    t = _dg().DyCuckoo(n)
+    half = n // 2
+    t.insert(to_dev(keys[:half]), to_dev(keys[:half] ^ np.uint32(0x1234)))
+    out = np.zeros(n, np.uint32)
+    bits = np.zeros((n + 31) // 32, np.uint32)
+    t.find_host(keys, out, bits)
+    dv, db = t.find(to_dev(keys))
+    assert np.array_equal(out, to_host(dv, 4))
+    assert np.array_equal(bits.view(np.int32), db.cpu().numpy())
+    assert int(_bits_np(bits, n).sum()) == half
     t.close()
