@@ -33,6 +33,20 @@ inline int tile_grid(const LaunchCtx &L, uint64_t n) {
     return (int)(g < 1 ? 1 : (g > 0x7fffffffull ? 0x7fffffffull : g));
 }
 
+// Compaction: one block per tile of 256 * kCompactRun cells (a block's tile
+// ends in two barriers and two atomics, so many short blocks keep more tiles
+// in flight than one resident wave looping over them); the tuner's cap
+// applies as for tile_grid.
+inline int compact_grid(const LaunchCtx &L, uint64_t cells) {
+    const uint64_t tile = 256ull * kCompactRun;
+    uint64_t g = (cells + tile - 1) / tile;
+    if (L.max_blocks_per_sm > 0) {
+        const uint64_t cap = (uint64_t)L.max_blocks_per_sm * (uint64_t)(L.sms > 0 ? L.sms : 1);
+        if (g > cap) g = cap;
+    }
+    return (int)(g < 1 ? 1 : (g > 0x7fffffffull ? 0x7fffffffull : g));
+}
+
 // Grid size for a grid-stride kernel: enough blocks for `work` threads, at
 // most one full wave of resident blocks (occupancy x SM count).
 inline int grid_for(const void *kernel, const LaunchCtx &L, uint64_t work, int block = 256) {
@@ -189,7 +203,7 @@ cudaError_t Ops<KB>::apply_group(const LaunchCtx &L, const ApplyScratch &A, cons
     auto g = k_apply_group<KB>;
     g<<<tile_grid(L, n), 256, 0, L.stream>>>(A, keys, n);
     auto c = k_apply_compact<KB>;
-    c<<<grid_for((const void *)c, L, 2 * n), 256, 0, L.stream>>>(A, 2 * n);
+    c<<<compact_grid(L, 2 * n), 256, 0, L.stream>>>(A, 2 * n);
     return cudaGetLastError();
 }
 
@@ -247,7 +261,7 @@ cudaError_t Ops<KB>::set_group(const LaunchCtx &L, const ApplyScratch &A, const 
         auto g = k_set_group<KB>;
         g<<<tile_grid(L, n), 256, 0, L.stream>>>(A, off, keys);
         auto c = k_apply_compact<KB>;
-        c<<<grid_for((const void *)c, L, 2 * n), 256, 0, L.stream>>>(A, 0);
+        c<<<compact_grid(L, 2 * n), 256, 0, L.stream>>>(A, 0);
     }
     return cudaGetLastError();
 }
