@@ -152,12 +152,14 @@ def plan_set(sizes, batches, results: dict):
     return sb, d, ev
 
 
-def tune_launch(run_round, caps=(0, 2, 4, 8), repeats: int = 2) -> int:
+def tune_launch(run_round, caps=(0, 2, 4, 8), repeats: int = 2, margin: float = 0.03) -> int:
     """The blocks-per-SM cap (0: as many as fit) with the shortest round;
-    run_round(cap) runs one round with that cap and returns its time."""
-    best, best_t = 0, math.inf
-    for cap in caps:
-        t = min(run_round(cap) for _ in range(repeats))
-        if t < best_t:
-            best, best_t = cap, t
+    run_round(cap) runs one round with that cap and returns its time. A cap
+    is taken over the uncapped launches only when it is faster by more than
+    `margin` (round times vary by a few percent, and the random-access
+    kernels are sized for uncapped grids)."""
+    times = {cap: min(run_round(cap) for _ in range(repeats)) for cap in caps}
+    best = min(times, key=times.get)
+    if 0 in times and times[best] > times[0] * (1.0 - margin):
+        return 0
     return best
