@@ -374,13 +374,9 @@ __device__ __forceinline__ unsigned long long agg_inc(unsigned long long *ctr, b
     base = __shfl_sync(mask, base, leader);
     return base + __popc(vote & ((1u << lane) - 1u));
 }
-__device__ __forceinline__ void agg_add(unsigned long long *ctr, uint32_t x) {
-    const unsigned mask = __activemask();
-    const uint32_t sum = __reduce_add_sync(mask, x);
-    if ((int)(threadIdx.x & 31) == __ffs(mask) - 1 && sum) atomicAdd(ctr, (unsigned long long)sum);
-}
 
-// Dedup-table hash (independent of the subtable hashes).
+// Mixing hash of the batch-dedup table, the grouping cells and the eviction
+// victim choice (independent of the subtable hashes).
 __device__ __forceinline__ uint32_t mix32(uint32_t x) {
     x ^= x >> 16;
     x *= 0x7feb352du;
