@@ -897,12 +897,17 @@ def main():
         ct, cq, cexp, dropped, cbuild = cpu_table_and_sample(keys64, args.log2_keys, sample,
                                                              threads, torch)
         dt, cout = time_cpu_find(ct, cq, threads, reps=3)
+        # one thread as well, on an eighth of the sample
+        q1 = np.ascontiguousarray(cq[: max(1, sample // 8)])
+        dt1, _ = time_cpu_find(ct, q1, 1)
         cpu = {"value": round(sample / dt / 1e6, 2), "unit": "Mops/s", "cores": threads,
                "kind": "port",
                "sample": "%d uniform 100%%-hit finds on the full 2^%d-key table, best of 3 "
                          "(reference algorithm: 16-slot buckets, MAX_ITER 15; %d keys dropped "
                          "by its eviction bound; %d mismatches)"
-                         % (sample, args.log2_keys, dropped, int((cout != cexp).sum()))}
+                         % (sample, args.log2_keys, dropped, int((cout != cexp).sum())),
+               "single_thread_value": round(q1.size / dt1 / 1e6, 2),
+               "single_thread_sample": "%d of the same finds on 1 thread" % q1.size}
         ct.close()
 
     head = results["uniform100"]
