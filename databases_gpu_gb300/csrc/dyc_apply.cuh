@@ -6,21 +6,23 @@
 //
 // Steps (stream-ordered kernels):
 //   group   : each op claims its key's cell in an open-addressing scratch
-//             table, a {key, count} word updated by one atomic for a new key;
-//             for a batch over many tables every table has its own region of
-//             twice its ops in cells
+//             table, a {key, count} word updated by one atomic for a new key,
+//             and gets its rank (the count before it); for a batch over many
+//             tables every table has its own region of twice its ops in cells
 //   compact : each used cell gets a distinct-key id (written over its count),
 //             a segment of the op index array and the key itself
-//   scatter : op indices land in their key's segment (in no order)
-//   (the table's own find kernel reads the pre-batch state of every
-//    distinct key)
-//   replay  : one thread per distinct key replays a segment of at most
-//             kShortSeg ops after sorting it in registers; longer segments are
-//             sorted and replayed by a warp (up to kWarpSeg ops) or by one
-//             block (any length: shared-memory sort, merged in global memory
-//             beyond kMidSeg). Every op's result is written; keys whose state
-//             changed are listed as erases or upserts.
-//   (the table's erase and insert kernels apply the lists)
+//   (the find of dyc_set.cuh reads the pre-batch state of every distinct key)
+//   scatter : one pass in op order: a key with a single op in the batch is
+//             resolved there (result, hit bit, list entry); the other ops land
+//             in their key's segment at their rank
+//   replay  : one thread per distinct key replays a segment of 2 to kShortSeg
+//             ops after sorting it in registers; longer segments are sorted
+//             and replayed by a warp (up to kWarpSeg ops) or by one block (any
+//             length: shared-memory sort, merged in global memory beyond
+//             kMidSeg). Every op's result is written; keys whose state changed
+//             are listed as erases or upserts.
+//   (the erase + upsert and eviction-walk kernels of dyc_set.cuh apply the
+//    lists)
 // Only the lists touch the table, each key at most once, so the usual
 // insert/erase phases keep their guarantees. Counts the kernels need are read
 // from ApplyScratch::ctr on the device, so the sequence has no host reads.

@@ -22,6 +22,9 @@
 //     missing key.
 //   * Every loop is bounded: probe loops by the table size, walks by the
 //     eviction bound. Nothing spins on another thread.
+//   * Random-access kernels run one block per 2048 items (tile_grid in
+//     dyc_ops.cuh): many short blocks keep more line fetches in flight than
+//     one resident wave looping; their counters are added once per block.
 #pragma once
 
 #include "dyc_device.cuh"
