@@ -1,6 +1,8 @@
 // dyc_api.cu -- the C ABI of include/dycuckoo.h: table lifetime, sizing and
-// resize policy (GPU/dyhash/api.cpp), batch chunking, the no-loss overflow
-// loop, and the host-buffer forms of the hashAPI calls.
+// resize policy (GPU/dyhash/api.cpp), the library's allocation pool, batch
+// chunking, the no-loss overflow loop, mixed batches, table sets (their
+// launch graphs and upsize waves), snapshots, wide values, and the
+// host-buffer forms of the hashAPI calls.
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>

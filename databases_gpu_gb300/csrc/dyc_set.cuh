@@ -1,6 +1,7 @@
-// dyc_set.cuh -- probe kernels of a multi-table batch (a table set). They run
-// the find / erase / place / eviction-walk logic of the single-table kernels
-// in dyc_kernels.cuh, but every item carries a table id and reads that
+// dyc_set.cuh -- probe kernels of a multi-table batch (a table set): the find
+// of the distinct keys, one pass for the erases and upserts, and the eviction
+// walks, with the logic of the single-table kernels in dyc_kernels.cuh, but
+// every item carries a table id and reads that
 // table's descriptor from a device array, so one grid-stride launch serves
 // the work of every table in the set. Item counts are read on the device
 // (the counters the mixed-batch kernels fill), so a batch's launch sequence
