@@ -265,6 +265,51 @@ def run_line_probe():
     print(json.dumps(d))
 
 
+def run_copy_probe():
+    """Host <-> device copy rates behind the end-to-end find: 256 MiB between
+    pinned host memory and HBM, best of 5, one direction on 1/2/4/8 streams,
+    both directions at once, and host -> device in chunks of 4/16/64 MiB."""
+    import torch
+    nbytes = 256 << 20
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    h2 = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    streams = [torch.cuda.Stream() for _ in range(8)]
+
+    def timed(fn, reps=5):
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        return round(nbytes / best / 1e9, 1)
+
+    def split(dst, src, k, chunk=None):
+        part = chunk or nbytes // k
+        for j, a in enumerate(range(0, nbytes, part)):
+            with torch.cuda.stream(streams[j % k]):
+                dst[a:a + part].copy_(src[a:a + part], non_blocking=True)
+
+    out = {"bytes": nbytes}
+    for k in (1, 2, 4, 8):
+        out["h2d_gbs_%d_streams" % k] = timed(lambda: split(d, h, k))
+        out["d2h_gbs_%d_streams" % k] = timed(lambda: split(h, d, k))
+
+    def both():
+        with torch.cuda.stream(streams[0]):
+            d.copy_(h, non_blocking=True)
+        with torch.cuda.stream(streams[1]):
+            h2.copy_(d2, non_blocking=True)
+    out["both_directions_gbs_each"] = timed(both)
+    for mib in (4, 16, 64):
+        out["h2d_gbs_%dmib_chunks" % mib] = timed(lambda: split(d, h, 1, mib << 20))
+    print(json.dumps(out))
+
+
 def set_table_bytes(S, bucket_bytes=128):
     """Device bytes of a set's subtables (from the members' slot capacities)."""
     _, caps = S.sizes()
@@ -651,6 +696,8 @@ def main():
     ap.add_argument("--skip-variants", action="store_true")
     ap.add_argument("--line-probe", action="store_true",
                     help="measure the random 128-byte line ceiling of this GPU and exit")
+    ap.add_argument("--copy-probe", action="store_true",
+                    help="measure host <-> device copy rates (pinned memory) and exit")
     ap.add_argument("--set-profile", action="store_true",
                     help="run --mt-rounds untimed-graph rounds of the multi-table set and exit")
     ap.add_argument("--skip-stream", action="store_true",
@@ -680,6 +727,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.line_probe:
         return run_line_probe()
+    if args.copy_probe:
+        return run_copy_probe()
     if args.set_profile:
         return run_set_profile(args)
     if args.serve_profile:
