@@ -249,6 +249,65 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_reference_gpu(args, keys, batch, stream, torch):
+    """The reference's own GPU kernels on the same workload, on the same GPU:
+    cuckoo_insert builds a table of the same 2^N keys (hashAPI(N/0.9) sizing,
+    values 1..N), then cuckoo_search runs the headline batches (and the
+    uniform 10 %-hit ones), launched with the reference's grid, timed with
+    CUDA events on the launching stream like the library's find. Its output
+    buffer is zeroed once, not per batch (hashAPI::hash_search zeroes it on
+    every call, api.cpp:275). A baseline beside the measured value."""
+    from oracle import ref_gpu
+    if not ref_gpu.available():
+        return {"unavailable": "reference GPU kernels not staged (oracle/build_ref.py)"}
+    N = keys.numel()
+    Q = 1 << args.log2_batch
+    vals = torch.arange(1, N + 1, dtype=torch.int32, device=keys.device)
+    ref = ref_gpu.RefGpuTable(int(N / 0.9), device=keys.device.index or 0)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    flag = ref.insert(keys, vals, stream=stream)  # reads the flag after the kernel
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ins_ms = e0.elapsed_time(e1)
+    kept = sum(int((s != 0).sum()) for s in ref.subtables)
+    del ref.last_iter_counts, vals
+    blocks, threads, _, _ = ref_gpu.geometry()
+    res = {"kernel": "cuckoo_search (GPU/dyhash/cuckoo.cu:460-520) compiled for sm_103a, "
+                     "grid %dx%d as its wrapper launches it" % (blocks, threads),
+           "insert_mops": round(N / (ins_ms / 1e3) / 1e6, 1), "rehash_flag": flag,
+           "lost_keys": N - kept, "capacity": ref.capacity}
+    out = torch.zeros(Q, dtype=torch.int32, device=keys.device)
+    for mix in ("uniform100", "uniform10"):
+        qs = [batch(mix) for _ in range(2)]
+        for w in range(args.warmup):
+            ref.search(qs[w % 2][0], out=out, stream=stream)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for s in range(args.steps):
+            ref.search(qs[s % 2][0], out=out, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        # results of a fresh search of the last batch: a hit returns the
+        # key's value, a miss leaves 0; a key the reference lost reads 0
+        q, expv, _ = qs[(args.steps - 1) % 2]
+        out.zero_()
+        ref.search(q, out=out, stream=stream)
+        torch.cuda.synchronize()
+        wrong = int((out != expv).sum())
+        res[mix] = {"mops": round(args.steps * Q / (ms / 1e3) / 1e6, 1),
+                    "ms_per_batch": round(ms / args.steps, 4),
+                    "results_differing_from_expected": wrong}
+    res["value"] = res["uniform100"]["mops"]
+    res["unit"] = "Mops/s"
+    del ref
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_line_probe():
     """Random DRAM line ceiling (databases_gpu_gb300/csrc/dyc_line_probe.cu)."""
     from databases_gpu_gb300 import build as pkg_build
@@ -670,6 +729,10 @@ def run_tuned_set(args, w, dev, torch, dg):
                         for c, r in results.items()}}
 
 
+def head_mops(results):
+    return results["uniform100"]["mops"]
+
+
 def workload_config(args, lf):
     return {
         "workload": "large static table find: u32 keys/values, 4 subtables, 2^%d unique keys "
@@ -693,6 +756,8 @@ def main():
     ap.add_argument("--bucket-bytes", type=int, default=128)
     ap.add_argument("--max-evictions", type=int, default=2048)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-reference-gpu", action="store_true",
+                    help="skip timing the reference's own GPU kernels")
     ap.add_argument("--skip-variants", action="store_true")
     ap.add_argument("--line-probe", action="store_true",
                     help="measure the random 128-byte line ceiling of this GPU and exit")
@@ -938,6 +1003,16 @@ def main():
     e2e_bad = int((outh.to(dev) != qs_e2e[1]).sum())
     e2e_mops = ws * e2e_steps * Q / e2e_s / 1e6
 
+    # ---- the reference's own GPU kernels on the same table keys and batches
+    ref_gpu = None
+    if rank == 0 and ws == 1 and not args.skip_reference_gpu:
+        ref_gpu = run_reference_gpu(args, keys, batch, stream, torch)
+        if "value" in ref_gpu:
+            ref_gpu["ours_over_reference"] = round(head_mops(results) / ref_gpu["value"], 2)
+            if "uniform10" in results:
+                ref_gpu["ours_over_reference_uniform10"] = round(
+                    results["uniform10"]["mops"] / ref_gpu["uniform10"]["mops"], 2)
+
     # ---- CPU baseline: reference algorithm on the host cores (rank 0, N=1)
     cpu = None
     if rank == 0 and ws == 1 and not args.skip_cpu:
@@ -974,6 +1049,7 @@ def main():
                      "peak_kind": peak_kind,
                      "alg_bytes_per_op": head["alg_bytes_per_op"]},
         "cpu_baseline": cpu,
+        "reference_gpu": ref_gpu,
         "gpu_launches": args.steps,
         "clocks": clocks,
         "variants": results,
