@@ -1042,8 +1042,8 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     cudaError_t e = KB_CALL(t, apply_group, L, A, keys, n);
     // state of every distinct key before the batch
     if (e == cudaSuccess)
-        e = KB_CALL(t, set_find, L, t->d_desc, t->sb, A.dkey, nullptr, &A.ctr[dyc::kCtrDistinct],
-                    n, A.pre_val, vb, A.pre_hit);
+        e = KB_CALL(t, set_find, L, t->d_desc, 1u, t->sb, A.dkey, nullptr,
+                    &A.ctr[dyc::kCtrDistinct], n, A.pre_val, vb, A.pre_hit, &A.ctr[dyc::kCtrBad]);
     if (e == cudaSuccess)
         e = KB_CALL(t, apply_scatter, L, A, n, nullptr, ops, vals, vb, vals_out, bits_out);
     if (e == cudaSuccess) e = KB_CALL(t, apply_replay, L, A, ops, vals, vb, vals_out, bits_out, n, n);
@@ -1053,17 +1053,21 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
         TRY(upsize_policy());
         if (grew) TRY(push_desc(t, s));
     }
-    e = KB_CALL(t, set_mutate, L, t->d_desc, t->d_ctr, t->sb, A.er_key, nullptr,
+    e = KB_CALL(t, set_mutate, L, t->d_desc, 1u, t->d_ctr, t->sb, A.er_key, nullptr,
                 &A.ctr[dyc::kCtrEr], A.up_key, A.up_val, vb, nullptr, &A.ctr[dyc::kCtrUp], n,
-                t->S.list_a, nullptr, t->S.list_cap, t->d_ctr);
+                t->S.list_a, nullptr, t->S.list_cap, t->d_ctr, &A.ctr[dyc::kCtrBad]);
     if (e == cudaSuccess)
-        e = KB_CALL(t, set_walk, L, t->d_desc, t->d_ctr, t->sb, t->S.list_a, nullptr,
+        e = KB_CALL(t, set_walk, L, t->d_desc, 1u, t->d_ctr, t->sb, t->S.list_a, nullptr,
                     &t->d_ctr->pending, t->S.list_b, nullptr, &t->d_ctr->overflow,
-                    t->S.list_cap, t->cfg.max_evictions, t->d_ctr, t->S.list_cap);
+                    t->S.list_cap, t->cfg.max_evictions, t->d_ctr, t->S.list_cap,
+                    &A.ctr[dyc::kCtrBad]);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "apply probe kernels: %s", cudaGetErrorString(e));
     CK(cudaMemcpyAsync(t->h_actr, A.ctr, dyc::kCtrSlots * sizeof(unsigned long long),
                        cudaMemcpyDeviceToHost, s));
     TRY(read_counters(t, s));
+    if (t->h_actr[dyc::kCtrBad])
+        return fail(DYC_ECUDA, "mixed batch: %llu device counts or ids out of range",
+                    t->h_actr[dyc::kCtrBad]);
     if (deferred) TRY(upsize_policy());
     const Counters c = *t->h_ctr;
     dyc_op_stats &St = t->last;
@@ -1215,6 +1219,8 @@ struct dyc_set {
     Counters *d_tctr = nullptr, *h_tctr = nullptr;  // per-table counters
     Desc *d_desc = nullptr, *h_desc = nullptr;      // per-table descriptors (pinned mirror)
     Counters *d_gctr = nullptr, *h_gctr = nullptr;  // set-wide counters of one call
+    unsigned long long *h_actr = nullptr;   // pinned copy of the batch counters (A.ctr)
+    unsigned long long *h_hostn = nullptr;  // pinned: the op count of the current batch
     void *abuf = nullptr;
     size_t abytes = 0;
     dyc::ApplyScratch A{};
@@ -1338,11 +1344,16 @@ dyc_status set_phase_a(dyc_set *s, const uint32_t *d_off, const uint8_t *ops, co
     const LaunchCtx L{s->sms, st, (int)s->blocks_per_sm, s->side, s->fork, s->join};
     const uint32_t vb = (uint32_t)s->vb;
     const uint32_t *d_n = d_off + s->ntables;
+    // the op count the host's offsets declare, which bounds the device's
+    // (a pinned word: a captured graph copies its current value)
+    CK(cudaMemcpyAsync(&A.ctr[dyc::kCtrHostN], s->h_hostn, sizeof(unsigned long long),
+                       cudaMemcpyHostToDevice, st));
     // also zeroes phase B's counters (nothing between the phases uses them)
     cudaError_t e = SET_KB_CALL(s, set_group, L, A, d_off, keys, n, bits, s->d_gctr);
     if (e == cudaSuccess)
-        e = SET_KB_CALL(s, set_find, L, s->d_desc, s->sb, A.dkey, A.dtid, &A.ctr[dyc::kCtrDistinct],
-                        n, A.pre_val, vb, A.pre_hit);
+        e = SET_KB_CALL(s, set_find, L, s->d_desc, s->ntables, s->sb, A.dkey, A.dtid,
+                        &A.ctr[dyc::kCtrDistinct], n, A.pre_val, vb, A.pre_hit,
+                        &A.ctr[dyc::kCtrBad]);
     if (e == cudaSuccess)
         e = SET_KB_CALL(s, apply_scatter, L, A, n, d_n, ops, vals, vb, out, bits);
     if (e == cudaSuccess)
@@ -1360,15 +1371,18 @@ dyc_status set_phase_a(dyc_set *s, const uint32_t *d_off, const uint8_t *ops, co
 dyc_status set_phase_b(dyc_set *s, uint64_t n, cudaStream_t st) {
     const dyc::ApplyScratch &A = s->A;
     const LaunchCtx L{s->sms, st, (int)s->blocks_per_sm};
-    cudaError_t e = SET_KB_CALL(s, set_mutate, L, s->d_desc, s->d_tctr, s->sb, A.er_key,
-                                A.er_tid, &A.ctr[dyc::kCtrEr], A.up_key, A.up_val,
+    cudaError_t e = SET_KB_CALL(s, set_mutate, L, s->d_desc, s->ntables, s->d_tctr, s->sb,
+                                A.er_key, A.er_tid, &A.ctr[dyc::kCtrEr], A.up_key, A.up_val,
                                 (uint32_t)s->vb, A.up_tid, &A.ctr[dyc::kCtrUp], n, s->list_a,
-                                s->tid_a, s->list_cap, s->d_gctr);
+                                s->tid_a, s->list_cap, s->d_gctr, &A.ctr[dyc::kCtrBad]);
     if (e == cudaSuccess)
-        e = SET_KB_CALL(s, set_walk, L, s->d_desc, s->d_tctr, s->sb, s->list_a, s->tid_a,
-                        &s->d_gctr->pending, s->list_b, s->tid_b, &s->d_gctr->overflow,
-                        s->list_cap, s->max_evict_all, s->d_gctr, s->list_cap);
+        e = SET_KB_CALL(s, set_walk, L, s->d_desc, s->ntables, s->d_tctr, s->sb, s->list_a,
+                        s->tid_a, &s->d_gctr->pending, s->list_b, s->tid_b,
+                        &s->d_gctr->overflow, s->list_cap, s->max_evict_all, s->d_gctr,
+                        s->list_cap, &A.ctr[dyc::kCtrBad]);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "set phase B kernels: %s", cudaGetErrorString(e));
+    CK(cudaMemcpyAsync(s->h_actr, A.ctr, dyc::kCtrSlots * sizeof(unsigned long long),
+                       cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(s->h_gctr, s->d_gctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(s->h_tctr, s->d_tctr, sizeof(Counters) * s->ntables,
                        cudaMemcpyDeviceToHost, st));
@@ -1416,7 +1430,12 @@ dyc_status set_overflow(dyc_set *s, uint64_t cnt, const std::vector<uint8_t> &gr
     CK(cudaMemcpyAsync(tid.data(), s->tid_b, cnt * 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     std::vector<std::vector<uint64_t>> per(s->ntables);
-    for (uint64_t i = 0; i < cnt; ++i) per[tid[i]].push_back(i);
+    for (uint64_t i = 0; i < cnt; ++i) {
+        if (tid[i] >= s->ntables)
+            return fail(DYC_ECUDA, "overflow entry %llu names table %u of %u",
+                        (unsigned long long)i, tid[i], s->ntables);
+        per[tid[i]].push_back(i);
+    }
     for (uint32_t t = 0; t < s->ntables; ++t) {
         if (per[t].empty()) continue;
         dyc_table *m = s->tables[t];
@@ -1499,6 +1518,9 @@ dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_desc, sizeof(Desc) * ntables);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_gctr, sizeof(Counters));
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_gctr, sizeof(Counters));
+    if (e == cudaSuccess)
+        e = cudaMallocHost(&s->h_actr, sizeof(unsigned long long) * dyc::kCtrSlots);
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_hostn, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_tup, sizeof(uint32_t) * ntables);
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_ter, sizeof(uint32_t) * ntables);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
@@ -1540,6 +1562,8 @@ dyc_status dyc_set_destroy(dyc_set *s) {
     if (s->h_desc) cudaFreeHost(s->h_desc);
     if (s->d_gctr) cudaFree(s->d_gctr);
     if (s->h_gctr) cudaFreeHost(s->h_gctr);
+    if (s->h_actr) cudaFreeHost(s->h_actr);
+    if (s->h_hostn) cudaFreeHost(s->h_hostn);
     if (s->h_tup) cudaFreeHost(s->h_tup);
     if (s->h_ter) cudaFreeHost(s->h_ter);
     if (s->abuf) cudaFree(s->abuf);
@@ -1611,6 +1635,7 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
     // them: the kernels must see the current subtables
     TRY(set_refresh_descs(s, st));
     TRY(set_ensure_scratch(s, n));
+    *s->h_hostn = n;  // read by the copy at the start of phase A (the last call has synced)
     dyc_set::Graph *gr = nullptr;
     if (flags & DYC_FLAG_GRAPH)
         gr = set_graph_for(s, {(uintptr_t)d_offsets, (uintptr_t)d_ops, (uintptr_t)d_keys,
@@ -1698,6 +1723,13 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
         CK(cudaStreamSynchronize(st));
     }
     if (gr) gr->warm = true;
+    // Device offsets that disagree with h_offsets: the kernels clamped them
+    // and the batch ran; the bookkeeping below still follows the device's
+    // counters, and the call reports the disagreement at the end.
+    const unsigned long long bad_offsets = s->h_actr[dyc::kCtrBadOffsets];
+    if (s->h_actr[dyc::kCtrBad])
+        return fail(DYC_ECUDA, "set batch: %llu device counts or ids out of range",
+                    s->h_actr[dyc::kCtrBad]);
     const Counters g = *s->h_gctr;
     if (g.spill) return fail(DYC_EOVERFLOW, "internal list overflow (%llu entries)", g.spill);
     for (uint32_t t = 0; t < s->ntables; ++t) s->tables[t]->size = s->h_tctr[t].size;
@@ -1729,6 +1761,9 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
         }
     }
     if (moved) TRY(set_push_descs(s, st));
+    if (bad_offsets)
+        return fail(DYC_EINVAL, "device offsets disagree with h_offsets (%llu reports)",
+                    bad_offsets);
     return DYC_OK;
 }
 

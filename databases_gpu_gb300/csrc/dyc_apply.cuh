@@ -26,6 +26,12 @@
 // Only the lists touch the table, each key at most once, so the usual
 // insert/erase phases keep their guarantees. Counts the kernels need are read
 // from ApplyScratch::ctr on the device, so the sequence has no host reads.
+// Every such count, distinct-key id and segment range is checked against the
+// scratch capacity before it indexes anything (values out of range are
+// clamped or their item skipped and counted in ctr[kCtrBad]); a set batch's
+// op count is the smaller of its device offsets' total and the count the
+// host declared (ctr[kCtrHostN]), a disagreement counted in
+// ctr[kCtrBadOffsets].
 #pragma once
 
 #include "dyc_kernels.cuh"
@@ -60,6 +66,31 @@ __device__ __forceinline__ typename SlotT<KB>::K cell_key(const void *cells, uin
 template <int KB> __device__ __forceinline__ uint32_t *cell_word(void *cells, uint64_t c) {
     if constexpr (KB == 4) return (uint32_t *)cells + 2 * c + 1;
     else return (uint32_t *)((char *)cells + c * 16 + 8);
+}
+
+__device__ __forceinline__ void note_bad(const ApplyScratch &A, int slot = kCtrBad) {
+    atomicAdd(&A.ctr[slot], 1ull);
+}
+
+// Op count of a set batch: offsets[ntables], bounded by the count the host
+// declared for this batch and by the scratch.
+__device__ __forceinline__ uint64_t set_op_count(const ApplyScratch &A,
+                                                 const uint32_t *__restrict__ off) {
+    uint64_t n = off[A.ntables];
+    const uint64_t h = A.ctr[kCtrHostN];
+    if (n > h) n = h;
+    return n < A.cap_ops ? n : A.cap_ops;
+}
+
+// A device counter of listed items, clamped to the scratch's op capacity.
+__device__ __forceinline__ uint64_t ctr_count(const ApplyScratch &A, int slot) {
+    const uint64_t n = A.ctr[slot];
+    return n < A.cap_ops ? n : A.cap_ops;
+}
+
+// Segment [off, off + cnt) of a distinct key lies inside the op scratch.
+__device__ __forceinline__ bool seg_ok(const ApplyScratch &A, uint32_t off, uint32_t cnt) {
+    return (uint64_t)off + cnt <= A.cap_ops;
 }
 
 // Claim (or join) key k's cell in region [base, base + size): fastrange
@@ -152,7 +183,14 @@ __global__ void __launch_bounds__(256) k_set_group(const __grid_constant__ Apply
                                                    const uint32_t *__restrict__ off,
                                                    const void *__restrict__ keys) {
     using K = typename SlotT<KB>::K;
-    const uint64_t n = off[A.ntables];  // the op count, read on the device
+    const uint64_t n = set_op_count(A, off);  // the op count, read on the device
+    // offsets that disagree with the host's, or are out of order, are reported
+    // (every access below stays inside the scratch either way)
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid == 0 && ((uint64_t)off[A.ntables] != A.ctr[kCtrHostN] || off[0] != 0u))
+        note_bad(A, kCtrBadOffsets);
+    for (uint64_t t = gid; t < A.ntables; t += (uint64_t)gridDim.x * blockDim.x)
+        if (off[t] > off[t + 1]) note_bad(A, kCtrBadOffsets);
     // warp-uniform loop: a warp's 32 consecutive ops mostly belong to one
     // table, found by one search when the first and last lane's tables agree
     for (uint64_t base = warp_base(); base < n; base += warp_stride()) {
@@ -166,7 +204,8 @@ __global__ void __launch_bounds__(256) k_set_group(const __grid_constant__ Apply
         if (k != 0) {
             const uint32_t t = one ? t0 : table_at(A.tidx, off, (uint32_t)i, (uint32_t)i);
             const uint32_t c0 = A.tcell_off[t], c1 = A.tcell_off[t + 1];
-            cell = claim_cell<KB>(A.cells, c0, c1 - c0, k, rank);
+            if (c1 > c0) cell = claim_cell<KB>(A.cells, c0, c1 - c0, k, rank);
+            else note_bad(A, kCtrBadOffsets);  // offsets out of order: no region for the op
         }
         A.op_cell[i] = cell;
         A.op_rank[i] = rank;
@@ -174,9 +213,11 @@ __global__ void __launch_bounds__(256) k_set_group(const __grid_constant__ Apply
 }
 
 // Start of a set batch of off[ntables] ops, in one launch: zero the batch
-// counters, the probe phase's counters (gctr, gctr_words words) and the
-// result bits; cell regions of twice each table's ops, so table t's region
-// starts at tcell_off[t] = 2 * off[t]; zero the cells in use and the
+// counters (all but kCtrHostN, copied in before this kernel), the probe
+// phase's counters (gctr, gctr_words words) and the result bits; cell
+// regions of twice each table's ops, so table t's region starts at
+// tcell_off[t] = 2 * off[t] (offsets clamped to the op count, so every
+// region lies in the 2n cells zeroed here); zero the cells in use and the
 // per-table new-key counts.
 template <int KB>
 __global__ void __launch_bounds__(256) k_set_prep(const __grid_constant__ ApplyScratch A,
@@ -184,13 +225,13 @@ __global__ void __launch_bounds__(256) k_set_prep(const __grid_constant__ ApplyS
                                                   uint32_t *__restrict__ bits,
                                                   unsigned long long *__restrict__ gctr,
                                                   uint32_t gctr_words) {
-    const uint64_t n = off[A.ntables];
+    const uint64_t n = set_op_count(A, off);
     const uint64_t id = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    if (id < (uint64_t)kCtrSlots) A.ctr[id] = 0ull;
+    if (id < (uint64_t)kCtrSlots && id != (uint64_t)kCtrHostN) A.ctr[id] = 0ull;
     if (gctr != nullptr && id < gctr_words) gctr[id] = 0ull;
     for (uint64_t t = id; t <= A.ntables; t += stride) {
-        A.tcell_off[t] = 2u * off[t];
+        A.tcell_off[t] = 2u * (uint32_t)(off[t] < n ? off[t] : n);
         if (t < A.ntables) A.tup[t] = A.ter[t] = 0u;
     }
     for (uint64_t b = id; b * kTidxStep < n; b += stride)
@@ -266,6 +307,7 @@ __global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ A
     __shared__ unsigned long long part[kCompactRun * kWarpsPerBlock];  // ops << 32 | keys
     __shared__ unsigned long long base_keys, base_ops;
     if (A.tcell_off) nc = A.tcell_off[A.ntables];
+    if (nc > A.cap_cells) nc = A.cap_cells;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint64_t tile = (uint64_t)blockDim.x * kCompactRun;
     const uint64_t stride = (uint64_t)gridDim.x * tile;
@@ -309,9 +351,15 @@ __global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ A
         for (int k = 0; k < kCompactRun; ++k) {
             if (!cnt[k]) continue;
             const unsigned long long pk = part[k * kWarpsPerBlock + w];
-            const uint32_t d = (uint32_t)base_keys + (uint32_t)pk + ex_keys[k];
-            const uint32_t off = (uint32_t)base_ops + (uint32_t)(pk >> 32) + ex_ops[k];
+            const uint64_t d64 = base_keys + (uint32_t)pk + ex_keys[k];
+            const uint64_t off64 = base_ops + (uint32_t)(pk >> 32) + ex_ops[k];
             const uint64_t c = c0 + (uint64_t)k * blockDim.x + threadIdx.x;
+            if (d64 >= A.cap_ops || off64 + cnt[k] > A.cap_ops) {
+                *cell_word<KB>(A.cells, c) = kNoId;  // more keys or ops than the scratch holds
+                note_bad(A);
+                continue;
+            }
+            const uint32_t d = (uint32_t)d64, off = (uint32_t)off64;
             *cell_word<KB>(A.cells, c) = d;  // the count becomes the distinct id
             ((typename SlotT<KB>::K *)A.dkey)[d] = cell_key<KB>(A.cells, c);
             A.dcnt[d] = cnt[k];
@@ -349,7 +397,11 @@ __device__ __forceinline__ void record_final_one(const ApplyScratch &A, uint32_t
     using K = typename SlotT<KB>::K;
     const K k = ((const K *)A.dkey)[d];
     if (present && (!pre_present || value != pre_value)) {
-        const uint32_t u = (uint32_t)atomicAdd(&A.ctr[kCtrUp], 1ull);
+        const unsigned long long u = atomicAdd(&A.ctr[kCtrUp], 1ull);
+        if (u >= A.cap_ops) {
+            note_bad(A);
+            return;
+        }
         ((K *)A.up_key)[u] = k;
         if (vb == 4) ((uint32_t *)A.up_val)[u] = (uint32_t)value;
         else ((unsigned long long *)A.up_val)[u] = value;
@@ -358,7 +410,11 @@ __device__ __forceinline__ void record_final_one(const ApplyScratch &A, uint32_t
             atomicAdd(&A.tup[A.dtid[d]], 1u);
         }
     } else if (!present && pre_present) {
-        const uint32_t e = (uint32_t)atomicAdd(&A.ctr[kCtrEr], 1ull);
+        const unsigned long long e = atomicAdd(&A.ctr[kCtrEr], 1ull);
+        if (e >= A.cap_ops) {
+            note_bad(A);
+            return;
+        }
         ((K *)A.er_key)[e] = k;
         if (A.dtid) {
             A.er_tid[e] = A.dtid[d];
@@ -385,7 +441,7 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
                                                        void *__restrict__ vals_out,
                                                        uint32_t *__restrict__ bits_out) {
     using K = typename SlotT<KB>::K;
-    if (n_ptr) n = *n_ptr;
+    if (n_ptr) n = set_op_count(A, n_ptr - A.ntables);  // n_ptr = offsets + ntables
     const int slots[2] = {kCtrUp, kCtrEr};
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
@@ -396,10 +452,12 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
         uint32_t tid = 0u;
         if (i < n) {
             const uint32_t cell = A.op_cell[i];
-            if (cell == kNoCell) {
+            const uint32_t d = (cell == kNoCell || cell >= A.cap_cells)
+                                   ? kNoId : *cell_word<KB>(A.cells, cell);
+            if (d >= A.cap_ops) {  // key 0 (no cell), or a cell compaction could not list
+                if (cell != kNoCell) note_bad(A);
                 if (vals_out) store_val(vals_out, vb, i, 0ull);
             } else {
-                const uint32_t d = *cell_word<KB>(A.cells, cell);
                 const uint32_t cnt = A.dcnt[d];
                 if (cnt == 1u) {
                     const bool pre = (A.pre_hit[d >> 5] >> (d & 31)) & 1u;
@@ -422,7 +480,10 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
                     // if the grouping's state were not (as under a profiler
                     // replay of the grouping)
                     const uint32_t r = A.op_rank[i];
-                    if (r < cnt) A.seg[seg_off(A, d) + r] = (uint32_t)i;
+                    if (r < cnt && seg_ok(A, seg_off(A, d), r + 1))
+                        A.seg[seg_off(A, d) + r] = (uint32_t)i;
+                    else
+                        note_bad(A);
                 }
             }
         }
@@ -436,7 +497,9 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
             warp_count_by(A.tup, tid, up);
             warp_count_by(A.ter, tid, er);
         }
-        if (up) {
+        if ((up && got[0] >= A.cap_ops) || (er && got[1] >= A.cap_ops)) {
+            note_bad(A);
+        } else if (up) {
             ((K *)A.up_key)[got[0]] = k;
             if (vb == 4) ((uint32_t *)A.up_val)[got[0]] = (uint32_t)value;
             else ((unsigned long long *)A.up_val)[got[0]] = value;
@@ -502,7 +565,7 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
     using K = typename SlotT<KB>::K;
     (void)n;  // key-0 ops and single-op keys were resolved by the scatter pass
     (void)n_ptr;
-    const uint64_t nd = A.ctr[kCtrDistinct];
+    const uint64_t nd = ctr_count(A, kCtrDistinct);
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     const int slots[4] = {kCtrUp, kCtrEr, kCtrWarp, kCtrMid};
     // whole blocks step through the distinct keys so every thread reaches
@@ -519,6 +582,8 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
                 md = true;
             } else if (cnt > kShortSeg) {
                 wp = true;
+            } else if (cnt > 1u && !seg_ok(A, seg_off(A, (uint32_t)d), cnt)) {
+                note_bad(A);
             } else if (cnt > 1u) {
                 uint32_t s[kShortSeg];
                 const uint32_t off = seg_off(A, (uint32_t)d);
@@ -563,7 +628,10 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
             warp_count_by(A.tup, tid, up);
             warp_count_by(A.ter, tid, er);
         }
-        if (up) {
+        const uint32_t at = up ? got[0] : er ? got[1] : wp ? got[2] : got[3];
+        if ((up || er || wp || md) && at >= A.cap_ops) {
+            note_bad(A);
+        } else if (up) {
             ((K *)A.up_key)[got[0]] = k;
             if (vb == 4) ((uint32_t *)A.up_val)[got[0]] = (uint32_t)value;
             else ((unsigned long long *)A.up_val)[got[0]] = value;
@@ -617,7 +685,7 @@ __global__ void __launch_bounds__(256) k_apply_replay_warp(const __grid_constant
     __shared__ uint32_t s_all[kWarpsPerBlock][kWarpSeg];
     uint32_t *s = s_all[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31;
-    const uint64_t nw = A.ctr[kCtrWarp];
+    const uint64_t nw = ctr_count(A, kCtrWarp);
     const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     for (uint64_t x0 = gw * kWarpTask; x0 < nw; x0 += warps * kWarpTask) {
@@ -625,8 +693,16 @@ __global__ void __launch_bounds__(256) k_apply_replay_warp(const __grid_constant
         bool rvalid = false, rpresent = false, rpre = false;
         uint64_t rvalue = 0ull, rpre_value = 0ull;
         for (uint32_t j = 0; j < kWarpTask && x0 + j < nw; ++j) {
-            const uint32_t d = A.wseg[x0 + j];
+            const uint32_t d = A.wseg[x0 + j];  // d, cnt and off are warp-uniform
+            if (d >= A.cap_ops) {
+                if (lane == 0) note_bad(A);
+                continue;
+            }
             const uint32_t cnt = A.dcnt[d], off = seg_off(A, d);  // kShortSeg < cnt <= kWarpSeg
+            if (cnt <= kShortSeg || cnt > kWarpSeg || !seg_ok(A, off, cnt)) {
+                if (lane == 0) note_bad(A);
+                continue;
+            }
             uint32_t P = 32;
             while (P < cnt) P <<= 1;
             for (uint32_t q = lane; q < P; q += 32) s[q] = q < cnt ? A.seg[off + q] : 0xffffffffu;
@@ -650,13 +726,15 @@ __global__ void __launch_bounds__(256) k_apply_replay_warp(const __grid_constant
         const bool up = rvalid && rpresent && (!rpre || rvalue != rpre_value);
         const bool er = rvalid && !rpresent && rpre;
         const uint32_t tid = (rvalid && A.dtid) ? A.dtid[rd] : 0u;
-        const uint32_t u = (uint32_t)agg_inc(&A.ctr[kCtrUp], up);
-        const uint32_t e = (uint32_t)agg_inc(&A.ctr[kCtrEr], er);
+        const unsigned long long u = agg_inc(&A.ctr[kCtrUp], up);
+        const unsigned long long e = agg_inc(&A.ctr[kCtrEr], er);
         if (A.tup) {
             warp_count_by(A.tup, tid, up);
             warp_count_by(A.ter, tid, er);
         }
-        if (up) {
+        if ((up && u >= A.cap_ops) || (er && e >= A.cap_ops)) {
+            note_bad(A);
+        } else if (up) {
             ((K *)A.up_key)[u] = ((const K *)A.dkey)[rd];
             if (vb == 4) ((uint32_t *)A.up_val)[u] = (uint32_t)rvalue;
             else ((unsigned long long *)A.up_val)[u] = rvalue;
@@ -681,11 +759,19 @@ __global__ void __launch_bounds__(256) k_apply_replay_mid(const __grid_constant_
                                                           uint32_t vb, void *__restrict__ vals_out,
                                                           uint32_t *__restrict__ bits_out) {
     __shared__ uint32_t s[kMidSeg];
-    const uint64_t nmid = A.ctr[kCtrMid];
+    const uint64_t nmid = ctr_count(A, kCtrMid);
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
     for (uint64_t x = blockIdx.x; x < nmid; x += gridDim.x) {
-        const uint32_t d = A.mid[x];
+        const uint32_t d = A.mid[x];  // d, cnt and off are the same for the whole block
+        if (d >= A.cap_ops) {
+            if (tid == 0) note_bad(A);
+            continue;
+        }
         const uint32_t cnt = A.dcnt[d], off = seg_off(A, d);  // cnt > kWarpSeg
+        if (cnt <= kWarpSeg || !seg_ok(A, off, cnt)) {
+            if (tid == 0) note_bad(A);
+            continue;
+        }
         const uint32_t *sorted = s;
         if (cnt <= kMidSeg) {
             uint32_t P = 2u * kWarpSeg;

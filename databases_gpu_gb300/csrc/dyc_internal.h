@@ -85,16 +85,26 @@ struct ApplyScratch {
 
 constexpr uint32_t kTidxStep = 64;  // ops per entry of ApplyScratch::tidx
 
-// ApplyScratch::ctr slots
+// ApplyScratch::ctr slots. Every count and id the batch kernels read from
+// device memory is checked against the scratch capacity (and table ids
+// against the table count) before it indexes anything; a value out of range
+// is clamped or its item skipped, and counted in kCtrBad (an internal count
+// out of range) or kCtrBadOffsets (the device offsets of a set batch
+// disagree with the op count the host declared, kCtrHostN). The host turns
+// either count into an error.
 enum : int {
-    kCtrDistinct = 0,  // distinct keys
-    kCtrPlaced = 1,    // ops given a segment slot
-    kCtrUp = 2,        // upserts listed
-    kCtrEr = 3,        // erases listed
-    kCtrMid = 4,       // block segments
-    kCtrWarp = 5,      // warp segments
-    kCtrSlots = 8
+    kCtrDistinct = 0,    // distinct keys
+    kCtrPlaced = 1,      // ops given a segment slot
+    kCtrUp = 2,          // upserts listed
+    kCtrEr = 3,          // erases listed
+    kCtrMid = 4,         // block segments
+    kCtrWarp = 5,        // warp segments
+    kCtrBad = 6,         // device-read counts or ids out of range (must stay 0)
+    kCtrBadOffsets = 7,  // set batch: offsets[ntables] != kCtrHostN, or an op outside its table
+    kCtrHostN = 8,       // set batch: op count from the host's offsets (copied before the kernels)
+    kCtrSlots = 16
 };
+constexpr uint32_t kNoId = 0xffffffffu;  // a cell left without a distinct-key id
 
 
 // Upsizes of many subtables (of different tables) in one launch: job j
@@ -180,21 +190,28 @@ template <int KB> struct Ops {
     // prep (counters, gctr, result bits, cell regions) + grouping + compaction
     static cudaError_t set_group(const LaunchCtx &L, const ApplyScratch &A, const uint32_t *off,
                                  const void *keys, uint64_t n, uint32_t *bits, Counters *gctr);
-    static cudaError_t set_find(const LaunchCtx &L, const Desc *descs, int sb, const void *keys,
-                                const uint32_t *tids, const unsigned long long *n_ptr,
-                                uint64_t max_n, void *vals, uint32_t vb, uint32_t *hits);
+    // The set kernels below read their item counts from device memory and
+    // clamp them to max_n / max_entries (the capacity of the lists behind
+    // them); a table id at or above ntables skips its item. Either event is
+    // counted in *bad.
+    static cudaError_t set_find(const LaunchCtx &L, const Desc *descs, uint32_t ntables, int sb,
+                                const void *keys, const uint32_t *tids,
+                                const unsigned long long *n_ptr, uint64_t max_n, void *vals,
+                                uint32_t vb, uint32_t *hits, unsigned long long *bad);
     // erases and upserts of a set batch in one launch (max_n: both lists' bound)
-    static cudaError_t set_mutate(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
-                                  const void *er_keys, const uint32_t *er_tids,
-                                  const unsigned long long *ne_ptr, const void *up_keys,
-                                  const void *up_vals, uint32_t vb, const uint32_t *up_tids,
-                                  const unsigned long long *nu_ptr, uint64_t max_n, void *list_a,
-                                  uint32_t *list_a_tid, uint64_t list_cap, Counters *gctr);
-    static cudaError_t set_walk(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
-                                const void *src, const uint32_t *src_tid,
+    static cudaError_t set_mutate(const LaunchCtx &L, const Desc *descs, uint32_t ntables,
+                                  Counters *tctr, int sb, const void *er_keys,
+                                  const uint32_t *er_tids, const unsigned long long *ne_ptr,
+                                  const void *up_keys, const void *up_vals, uint32_t vb,
+                                  const uint32_t *up_tids, const unsigned long long *nu_ptr,
+                                  uint64_t max_n, void *list_a, uint32_t *list_a_tid,
+                                  uint64_t list_cap, Counters *gctr, unsigned long long *bad);
+    static cudaError_t set_walk(const LaunchCtx &L, const Desc *descs, uint32_t ntables,
+                                Counters *tctr, int sb, const void *src, const uint32_t *src_tid,
                                 const unsigned long long *src_count, void *dst, uint32_t *dst_tid,
                                 unsigned long long *dst_count, uint64_t dst_cap,
-                                uint32_t max_evict, Counters *gctr, uint64_t max_entries);
+                                uint32_t max_evict, Counters *gctr, uint64_t max_entries,
+                                unsigned long long *bad);
     // set every fingerprint bit of every bucket of a subtable
     static cudaError_t mark_all(const LaunchCtx &L, int sb, void *sub, uint32_t nb);
     static cudaError_t export_all(const LaunchCtx &L, const Desc &D, int sb, void *keys,

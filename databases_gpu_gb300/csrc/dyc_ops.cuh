@@ -267,46 +267,49 @@ cudaError_t Ops<KB>::set_group(const LaunchCtx &L, const ApplyScratch &A, const 
 }
 
 template <int KB>
-cudaError_t Ops<KB>::set_find(const LaunchCtx &L, const Desc *descs, int sb, const void *keys,
-                              const uint32_t *tids, const unsigned long long *n_ptr,
-                              uint64_t max_n, void *vals, uint32_t vb, uint32_t *hits) {
+cudaError_t Ops<KB>::set_find(const LaunchCtx &L, const Desc *descs, uint32_t ntables, int sb,
+                              const void *keys, const uint32_t *tids,
+                              const unsigned long long *n_ptr, uint64_t max_n, void *vals,
+                              uint32_t vb, uint32_t *hits, unsigned long long *bad) {
     if (max_n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_set_find<KB, SB>;
-        k<<<tile_grid(L, max_n), 256, 0, L.stream>>>(descs, keys, tids, n_ptr, vals, vb, hits);
+        k<<<tile_grid(L, max_n), 256, 0, L.stream>>>(descs, ntables, keys, tids, n_ptr, max_n,
+                                                     vals, vb, hits, bad);
     });
     return cudaGetLastError();
 }
 
 template <int KB>
-cudaError_t Ops<KB>::set_mutate(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
-                                const void *er_keys, const uint32_t *er_tids,
-                                const unsigned long long *ne_ptr, const void *up_keys,
-                                const void *up_vals, uint32_t vb, const uint32_t *up_tids,
-                                const unsigned long long *nu_ptr, uint64_t max_n, void *list_a,
-                                uint32_t *list_a_tid, uint64_t list_cap, Counters *gctr) {
+cudaError_t Ops<KB>::set_mutate(const LaunchCtx &L, const Desc *descs, uint32_t ntables,
+                                Counters *tctr, int sb, const void *er_keys,
+                                const uint32_t *er_tids, const unsigned long long *ne_ptr,
+                                const void *up_keys, const void *up_vals, uint32_t vb,
+                                const uint32_t *up_tids, const unsigned long long *nu_ptr,
+                                uint64_t max_n, void *list_a, uint32_t *list_a_tid,
+                                uint64_t list_cap, Counters *gctr, unsigned long long *bad) {
     if (max_n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_set_mutate<KB, SB>;
         k<<<tile_grid(L, max_n + 32), 256, 0, L.stream>>>(
-            descs, tctr, er_keys, er_tids, ne_ptr, up_keys, up_vals, vb, up_tids, nu_ptr, list_a,
-            list_a_tid, list_cap, gctr);
+            descs, ntables, tctr, er_keys, er_tids, ne_ptr, up_keys, up_vals, vb, up_tids, nu_ptr,
+            max_n, list_a, list_a_tid, list_cap, gctr, bad);
     });
     return cudaGetLastError();
 }
 
 template <int KB>
-cudaError_t Ops<KB>::set_walk(const LaunchCtx &L, const Desc *descs, Counters *tctr, int sb,
-                              const void *src, const uint32_t *src_tid,
+cudaError_t Ops<KB>::set_walk(const LaunchCtx &L, const Desc *descs, uint32_t ntables,
+                              Counters *tctr, int sb, const void *src, const uint32_t *src_tid,
                               const unsigned long long *src_count, void *dst, uint32_t *dst_tid,
                               unsigned long long *dst_count, uint64_t dst_cap, uint32_t max_evict,
-                              Counters *gctr, uint64_t max_entries) {
+                              Counters *gctr, uint64_t max_entries, unsigned long long *bad) {
     if (max_entries == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_set_walk<KB, SB>;
         k<<<grid_for((const void *)k, L, max_entries), 256, 0, L.stream>>>(
-            descs, tctr, src, src_tid, src_count, dst, dst_tid, dst_count, dst_cap, max_evict,
-            gctr, max_entries);
+            descs, ntables, tctr, src, src_tid, src_count, dst, dst_tid, dst_count, dst_cap,
+            max_evict, gctr, max_entries, bad);
     });
     return cudaGetLastError();
 }

@@ -5,9 +5,12 @@
 // table's descriptor from a device array, so one grid-stride launch serves
 // the work of every table in the set. Item counts are read on the device
 // (the counters the mixed-batch kernels fill), so a batch's launch sequence
-// needs no host reads and can be captured as a CUDA graph. A null table-id
-// array means table 0 for every item: a single table's mixed batch runs
-// through the same kernels with a one-entry descriptor array.
+// needs no host reads and can be captured as a CUDA graph. Such a count is
+// clamped to the capacity of the list behind it and a table id at or above
+// the table count skips its item; both are counted in *bad, which the host
+// turns into an error, so a wrong count can never index past a buffer. A
+// null table-id array means table 0 for every item: a single table's mixed
+// batch runs through the same kernels with a one-entry descriptor array.
 #pragma once
 
 #include "dyc_apply.cuh"
@@ -23,31 +26,55 @@ __device__ __forceinline__ void warp_size_add(Counters *tctr, uint32_t t, bool p
         atomicAdd(&tctr[t].size, (unsigned long long)(sign * (long long)__popc(peers)));
 }
 
+// A count read on the device, clamped to cap (the capacity of the list it
+// counts); an excess is recorded in *bad by one thread.
+__device__ __forceinline__ uint64_t clamped_count(const unsigned long long *p, uint64_t cap,
+                                                  unsigned long long *bad) {
+    const uint64_t n = *p;
+    if (n <= cap) return n;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(bad, 1ull);
+    return cap;
+}
+
+// Table id of item i (0 without an id array); an id at or above ntables is
+// recorded in *bad and the item is dropped from the pass (ok = false).
+__device__ __forceinline__ uint32_t checked_tid(const uint32_t *tids, uint64_t i,
+                                                uint32_t ntables, unsigned long long *bad,
+                                                bool &ok) {
+    const uint32_t t = tids ? tids[i] : 0u;
+    if (t < ntables) return t;
+    atomicAdd(bad, 1ull);
+    ok = false;
+    return 0u;
+}
+
 // find of keys[i] in table tids[i], i < *n_ptr (k_find per table)
 template <int KB, int SB>
-__global__ void __launch_bounds__(256) k_set_find(const Desc *__restrict__ descs,
+__global__ void __launch_bounds__(256) k_set_find(const Desc *__restrict__ descs, uint32_t ntables,
                                                   const void *__restrict__ keys,
                                                   const uint32_t *__restrict__ tids,
                                                   const unsigned long long *__restrict__ n_ptr,
-                                                  void *__restrict__ vals, uint32_t vb,
-                                                  uint32_t *__restrict__ hits) {
+                                                  uint64_t max_n, void *__restrict__ vals,
+                                                  uint32_t vb, uint32_t *__restrict__ hits,
+                                                  unsigned long long *bad) {
     using T = SlotT<KB>;
     using Gm = Geo<KB, SB>;
     __shared__ __align__(128) unsigned char s_stage[kWarpsPerBlock][32 * SB];
     unsigned char *stage = s_stage[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31;
-    const uint64_t n = *n_ptr;
+    const uint64_t n = clamped_count(n_ptr, max_n, bad);
     const uint64_t step = warp_stride();
     for (uint64_t base = warp_base(); base < n; base += step) {
         const uint64_t i = base + lane;
         typename T::K k = 0;
         uint32_t tb = 0u;
+        bool ok = true;
         if (i < n) {
             k = load_key<KB>(keys, i);
-            tb = tids ? tids[i] : 0u;
+            tb = checked_tid(tids, i, ntables, bad, ok);
         }
         const Desc &D = descs[tb];
-        const bool act = k != 0;
+        const bool act = ok && k != 0;
         const uint32_t hk = fold(k);
         const Pair p = pair_of(hk, D.d);
         const char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
@@ -73,22 +100,24 @@ __global__ void __launch_bounds__(256) k_set_find(const Desc *__restrict__ descs
 // below n (k_erase per table, no dedup). Warp-collective; returns whether
 // this lane erased its key.
 template <int KB, int SB>
-__device__ __forceinline__ bool set_erase_warp(const Desc *__restrict__ descs,
+__device__ __forceinline__ bool set_erase_warp(const Desc *__restrict__ descs, uint32_t ntables,
                                                Counters *__restrict__ tctr,
                                                const void *__restrict__ keys,
                                                const uint32_t *__restrict__ tids, uint64_t n,
-                                               uint64_t base, unsigned char *stage) {
+                                               uint64_t base, unsigned char *stage,
+                                               unsigned long long *bad) {
     using T = SlotT<KB>;
     using Gm = Geo<KB, SB>;
     const uint64_t i = base + (threadIdx.x & 31);
     typename T::K k = 0;
     uint32_t tb = 0u;
+    bool ok = true;
     if (i < n) {
         k = load_key<KB>(keys, i);
-        tb = tids ? tids[i] : 0u;
+        tb = checked_tid(tids, i, ntables, bad, ok);
     }
     const Desc &D = descs[tb];
-    const bool act = k != 0;
+    const bool act = ok && k != 0;
     const uint32_t hk = fold(k);
     const Pair p = pair_of(hk, D.d);
     char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
@@ -117,7 +146,7 @@ __device__ __forceinline__ bool set_erase_warp(const Desc *__restrict__ descs,
 // base + 32) and below n (k_place per table); ops left without a slot go to
 // list_a / list_a_tid. Warp-collective; adds to n_ins / n_upd.
 template <int KB, int SB>
-__device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs,
+__device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs, uint32_t ntables,
                                                Counters *__restrict__ tctr,
                                                const void *__restrict__ keys,
                                                const void *__restrict__ vals, uint32_t vb,
@@ -125,7 +154,7 @@ __device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs,
                                                uint64_t base, void *list_a, uint32_t *list_a_tid,
                                                uint64_t list_cap, Counters *gctr,
                                                unsigned char *stage, uint32_t &n_ins,
-                                               uint32_t &n_upd) {
+                                               uint32_t &n_upd, unsigned long long *bad) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
     using Gm = Geo<KB, SB>;
@@ -135,9 +164,10 @@ __device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs,
     uint32_t tb = 0u;
     Sl e = T::empty();
     if (i < n) {
+        bool ok = true;
         k = load_key<KB>(keys, i);
-        tb = tids ? tids[i] : 0u;
-        act = k != 0;
+        tb = checked_tid(tids, i, ntables, bad, ok);
+        act = ok && k != 0;
         if (act) e = T::make(k, load_val(vals, vb, i));
     }
     const Desc &D = descs[tb];
@@ -190,24 +220,28 @@ __device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs,
 // key; an erase only empties its own key's slot).
 template <int KB, int SB>
 __global__ void __launch_bounds__(256) k_set_mutate(
-    const Desc *__restrict__ descs, Counters *__restrict__ tctr, const void *__restrict__ er_keys,
-    const uint32_t *__restrict__ er_tids, const unsigned long long *__restrict__ ne_ptr,
-    const void *__restrict__ up_keys, const void *__restrict__ up_vals, uint32_t vb,
-    const uint32_t *__restrict__ up_tids, const unsigned long long *__restrict__ nu_ptr,
-    void *list_a, uint32_t *list_a_tid, uint64_t list_cap, Counters *gctr) {
+    const Desc *__restrict__ descs, uint32_t ntables, Counters *__restrict__ tctr,
+    const void *__restrict__ er_keys, const uint32_t *__restrict__ er_tids,
+    const unsigned long long *__restrict__ ne_ptr, const void *__restrict__ up_keys,
+    const void *__restrict__ up_vals, uint32_t vb, const uint32_t *__restrict__ up_tids,
+    const unsigned long long *__restrict__ nu_ptr, uint64_t max_n, void *list_a,
+    uint32_t *list_a_tid, uint64_t list_cap, Counters *gctr, unsigned long long *bad) {
     __shared__ __align__(128) unsigned char s_stage[kWarpsPerBlock][32 * SB];
     unsigned char *stage = s_stage[threadIdx.x >> 5];
-    const uint64_t ne = *ne_ptr, nu = *nu_ptr;
+    const uint64_t ne = clamped_count(ne_ptr, max_n, bad), nu = clamped_count(nu_ptr, max_n, bad);
     const uint64_t ne32 = (ne + 31) & ~(uint64_t)31;
     const uint64_t step = warp_stride();
     uint32_t n_del = 0, n_ins = 0, n_upd = 0;
     for (uint64_t base = warp_base(); base < ne32 + nu; base += step) {
         if (base < ne32) {  // warp-uniform: base is a multiple of 32
-            n_del += set_erase_warp<KB, SB>(descs, tctr, er_keys, er_tids, ne, base, stage) ? 1u
-                                                                                           : 0u;
+            n_del += set_erase_warp<KB, SB>(descs, ntables, tctr, er_keys, er_tids, ne, base,
+                                            stage, bad)
+                         ? 1u
+                         : 0u;
         } else {
-            set_place_warp<KB, SB>(descs, tctr, up_keys, up_vals, vb, up_tids, nu, base - ne32,
-                                   list_a, list_a_tid, list_cap, gctr, stage, n_ins, n_upd);
+            set_place_warp<KB, SB>(descs, ntables, tctr, up_keys, up_vals, vb, up_tids, nu,
+                                   base - ne32, list_a, list_a_tid, list_cap, gctr, stage, n_ins,
+                                   n_upd, bad);
         }
     }
     // one atomic per counter per block (the grid has many short-lived blocks)
@@ -234,19 +268,22 @@ __global__ void __launch_bounds__(256) k_set_mutate(
 // eviction bound; max_evict, the largest, bounds the cooperative loop);
 // failures go to dst
 template <int KB, int SB>
-__global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs,
+__global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs, uint32_t ntables,
                                                   Counters *__restrict__ tctr,
                                                   const void *__restrict__ src,
                                                   const uint32_t *__restrict__ src_tid,
                                                   const unsigned long long *src_count, void *dst,
                                                   uint32_t *dst_tid, unsigned long long *dst_count,
                                                   uint64_t dst_cap, uint32_t max_evict,
-                                                  Counters *gctr, uint64_t max_entries) {
+                                                  Counters *gctr, uint64_t max_entries,
+                                                  unsigned long long *bad) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
     __shared__ unsigned long long s_sum[2];
     if (threadIdx.x < 2) s_sum[threadIdx.x] = 0ull;
     __syncthreads();
+    // (more entries than max_entries means entries were already counted in
+    // spill by the kernel that listed them)
     uint64_t n = *src_count;
     if (n > max_entries) n = max_entries;
     const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -261,7 +298,7 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
             const uint64_t i = base + lane;
             bool live = i < n;
             Sl e = live ? ((const Sl *)src)[i] : T::empty();
-            const uint32_t tb = (live && src_tid) ? src_tid[i] : 0u;
+            const uint32_t tb = live ? checked_tid(src_tid, i, ntables, bad, live) : 0u;
             const Desc &D = descs[tb];
             uint32_t hk = 0;
             Pair pe{0u, 0u};
@@ -335,7 +372,11 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
     } else {
         for (uint64_t i = wid; i < n; i += warps) {
             const Sl e = ((const Sl *)src)[i];
-            const uint32_t tb = src_tid ? src_tid[i] : 0u;
+            const uint32_t tb = src_tid ? src_tid[i] : 0u;  // warp-uniform
+            if (tb >= ntables) {
+                if (lead) atomicAdd(bad, 1ull);
+                continue;
+            }
             const Desc &D = descs[tb];
             const WalkOut<KB> w = walk_lookahead<KB, SB>(D, e, D.max_evict);
             if (!lead) continue;

@@ -328,7 +328,13 @@ dyc_status dyc_set_table(dyc_set *s, uint32_t i, dyc_table **out);
 dyc_status dyc_set_sizes(dyc_set *s, uint64_t *h_sizes, uint64_t *h_capacities);
 
 /* Mixed batch over the set (see above). Returns when the batch is in the
- * tables. flags: DYC_FLAG_NO_RESIZE, DYC_FLAG_GRAPH. */
+ * tables. flags: DYC_FLAG_NO_RESIZE, DYC_FLAG_GRAPH. d_offsets must hold
+ * the same values as h_offsets: the kernels read the op count and the
+ * tables' ranges from d_offsets, clamp them to what h_offsets declared, and
+ * the call returns DYC_EINVAL after the batch when they disagree (or are
+ * out of order); the ops then went to the tables d_offsets named. A count
+ * or id the kernels read from device memory out of range (which no valid
+ * call produces) returns DYC_ECUDA. */
 dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *h_offsets,
                          const uint8_t *d_ops, const void *d_keys, const void *d_vals,
                          void *d_vals_out, uint32_t *d_bits_out, uint32_t flags, void *stream);

@@ -329,3 +329,69 @@ def test_set_upsize_waves_match_per_table_path(bucket_bytes, key_bytes):
         assert_same_contents(A.table(t), maps[t], "table %d contents" % t)
     A.close()
     B.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_set_device_offsets_disagreeing_with_host_offsets_are_reported(graph):
+    """The kernels read a set batch's op count and table ranges from the
+    device offsets, while the host sized everything from h_offsets. Device
+    offsets whose total is larger than the host's, or that are out of order,
+    are clamped by the kernels (every access stays inside the batch's
+    buffers) and the call returns DYC_EINVAL. With only the total too large
+    the batch is still applied exactly as the host's offsets describe it.
+    Under graph replay all calls use the same buffers, so the second and
+    third calls replay the captured graph with the offsets changed in place."""
+    import torch
+    from databases_gpu_gb300._lib import DYC_EINVAL
+    dg = _dg()
+    w = _small_workload(16, seed=11, log2_size=(4, 10), log2_batch=(4, 9))
+    S = dg.DyCuckooSet(w.sizes.numpy(), max_evictions=64)
+    maps = [O.Map() for _ in range(S.ntables)]
+    _preload(S, w, maps)
+    h_off = w.offsets_host
+    n = int(h_off[-1])
+    d_off = torch.empty(S.ntables + 1, dtype=torch.int32, device="cuda")
+    b_ops = torch.empty(n, dtype=torch.uint8, device="cuda")
+    b_keys = torch.empty(n, dtype=torch.int32, device="cuda")
+    b_vals = torch.empty(n, dtype=torch.int32, device="cuda")
+    out = torch.empty(n, dtype=torch.int32, device="cuda")
+    bits = torch.empty((n + 31) // 32, dtype=torch.int32, device="cuda")
+
+    def run(offsets):
+        ops, keys, vals = w.round()
+        b_ops.copy_(ops)
+        b_keys.copy_(keys)
+        b_vals.copy_(vals)
+        d_off.copy_(torch.from_numpy(np.asarray(offsets, np.int64).astype(np.uint32)
+                                     .view(np.int32)))
+        S.apply(d_off, b_ops, b_keys, b_vals, out=out, bits=bits, h_offsets=h_off, graph=graph)
+        return ops, keys, vals
+
+    # a clean round (warms the graph entry for these buffers)
+    ops, keys, vals = run(h_off)
+    _check_round(S, maps, h_off, ops, keys, vals, out, bits, "clean")
+    # the device total exceeds the host's op count: clamped to it, reported
+    big = h_off.astype(np.int64).copy()
+    big[-1] = n + 100
+    with pytest.raises(dg.DycError) as ei:
+        run(big)
+    assert ei.value.status == DYC_EINVAL, ei.value
+    o = b_ops.cpu().numpy()
+    k = to_host(b_keys, 4).astype(np.uint64)
+    v = to_host(b_vals, 4).astype(np.uint64)
+    for t in range(S.ntables):
+        a, b = int(h_off[t]), int(h_off[t + 1])
+        maps[t].apply(o[a:b], k[a:b], v[a:b])
+    for t in range(S.ntables):
+        assert_same_contents(S.table(t), maps[t], "table %d after the clamped round" % t)
+    # offsets out of order with the right total: reported (the tables got
+    # ops under the wrong ranges, so their contents are not checked)
+    bad = h_off.astype(np.int64).copy()
+    bad[1], bad[2] = bad[2], bad[1]
+    if bad[1] == bad[2]:
+        bad[1] = bad[2] + 1
+    with pytest.raises(dg.DycError) as ei:
+        run(bad)
+    assert ei.value.status == DYC_EINVAL, ei.value
+    torch.cuda.synchronize()
+    S.close()
