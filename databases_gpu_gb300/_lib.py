@@ -37,7 +37,7 @@ class DycConfig(C.Structure):
 class DycOpStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "inserted", "updated", "erased", "rejected", "superseded", "evict_steps",
-        "overflowed", "resizes_up", "resizes_down", "split_phases")]
+        "overflowed", "resizes_up", "resizes_down", "split_phases", "held")]
 
     def as_dict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
@@ -74,8 +74,10 @@ EXPORTS = [
     "dyc_server_wait", "dyc_server_stats_get", "dyc_server_set",
     "dyc_snapshot_bytes", "dyc_snapshot", "dyc_restore",
     "dyc_wide_create", "dyc_wide_destroy", "dyc_wide_insert", "dyc_wide_find", "dyc_wide_erase",
-    "dyc_wide_export", "dyc_wide_table", "dyc_wide_last_stats",
+    "dyc_wide_export", "dyc_wide_table", "dyc_wide_last_stats", "dyc_debug_inject",
+    "dyc_debug_alloc_count",
 ]
+INJECT_RESET, INJECT_POOL_ALLOC, INJECT_WAIT_TRIES = 0, 1, 2  # dyc_debug_inject kinds
 
 _lock = threading.Lock()
 _lib = None
@@ -133,6 +135,8 @@ def _declare(L):
         "dyc_wide_export": (st, [T, vp, vp, u64, C.POINTER(u64), vp]),
         "dyc_wide_table": (st, [T, C.POINTER(C.c_void_p)]),
         "dyc_wide_last_stats": (st, [T, C.POINTER(DycOpStats)]),
+        "dyc_debug_inject": (st, [u32, u64]),
+        "dyc_debug_alloc_count": (st, [C.POINTER(u64)]),
         "dyc_status_string": (C.c_char_p, [st]),
         "dyc_last_error": (C.c_char_p, []),
     }

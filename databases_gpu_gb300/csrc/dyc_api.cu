@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
+#include <atomic>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -21,6 +22,10 @@ using dyc::Desc;
 using dyc::LaunchCtx;
 using dyc::Ops;
 using dyc::Scratch;
+
+namespace dyc {
+std::atomic<unsigned long long> g_lib_allocs{0};
+}
 
 namespace {
 
@@ -160,6 +165,10 @@ struct dyc_table {
     size_t pipe_bytes = 0;
     uint64_t size = 0, capacity = 0;
     dyc_op_stats last{};
+    // entries a failed call could not place (slot images, held_n of them);
+    // not in the device size counter; the next call places them first
+    std::vector<unsigned char> held;
+    uint64_t held_n = 0;
 };
 
 namespace {
@@ -173,11 +182,25 @@ dyc_status set_device(dyc_table *t) {
 
 LaunchCtx ctx(dyc_table *t, void *stream) { return LaunchCtx{t->sms, (cudaStream_t)stream}; }
 
+// Failure injection for the tests of the error paths (dyc_debug_inject):
+// the n-th pool allocation from now fails as if the device were out of
+// memory; the downsize kernel's tile-copy waits give up after this many
+// polls. Process-wide.
+std::atomic<uint64_t> g_inject_alloc{0};
+std::atomic<uint32_t> g_inject_wait_tries{dyc::kWaitTries};
+
 // Stream-ordered allocation from the library pool of the table's device.
 cudaError_t pool_alloc(int device, void **p, size_t bytes, cudaStream_t s) {
+    for (uint64_t c = g_inject_alloc.load(); c != 0;) {
+        if (g_inject_alloc.compare_exchange_weak(c, c - 1)) {
+            if (c == 1) return cudaErrorMemoryAllocation;
+            break;
+        }
+    }
     cudaMemPool_t pool = nullptr;
     cudaError_t e = lib_pool(device, &pool);
     if (e != cudaSuccess) return e;
+    dyc::g_lib_allocs.fetch_add(1, std::memory_order_relaxed);
     return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 
@@ -198,7 +221,7 @@ dyc_status ensure_scratch(dyc_table *t, uint64_t n) {
         CK(cudaFree(t->scratch));
         t->scratch = nullptr;
     }
-    CK(cudaMalloc(&t->scratch, need));
+    CK(dyc::lib_malloc(&t->scratch, need));
     t->scratch_bytes = need;
     char *p = (char *)t->scratch;
     auto carve = [&](size_t bytes) {
@@ -231,6 +254,75 @@ dyc_status read_counters(dyc_table *t, cudaStream_t s) {
                     (unsigned long long)t->h_ctr->timeouts);
     t->size = t->h_ctr->size;
     return DYC_OK;
+}
+
+// ---- entries held outside the table after a failed call -------------------
+// An error path (an upsize the pool cannot serve, eviction overflow that
+// outlasts every round) keeps the entries it has not placed: they are copied
+// to the table's held list on the host instead of being dropped (the
+// reference drops them, cuckoo.cu:422-431, :714-722). Held entries are not
+// in the device size counter; dyc_size counts them, dyc_op_stats.held
+// reports them, and every later call on the table places them first
+// (settle_held).
+dyc_status hold_list(dyc_table *t, cudaStream_t s, const void *d_list, uint64_t count,
+                     bool counted) {
+    if (count == 0) return DYC_OK;
+    const size_t bytes = (size_t)count * t->slot_bytes, at = t->held.size();
+    t->held.resize(at + bytes);
+    cudaError_t e = cudaMemcpyAsync(t->held.data() + at, d_list, bytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        t->held.resize(at);
+        return fail(DYC_ECUDA, "copying %llu unplaced entries to the host: %s",
+                    (unsigned long long)count, cudaGetErrorString(e));
+    }
+    t->held_n += count;
+    if (counted) {  // moved residents (a downsize): the device size still counts them
+        t->size -= count;
+        t->h_ctr->size = t->size;
+        CK(cudaMemcpyAsync(&t->d_ctr->size, &t->h_ctr->size, sizeof(unsigned long long),
+                           cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    return DYC_OK;
+}
+
+// Hold `count` entries of d_list and return `why` (the failure that stopped
+// their placement), its message extended.
+dyc_status hold_failed(dyc_table *t, cudaStream_t s, const void *d_list, uint64_t count,
+                       bool counted, dyc_status why) {
+    const std::string msg = g_err;
+    TRY(hold_list(t, s, d_list, count, counted));
+    return fail(why, "%s; %llu entries held for the next call", msg.c_str(),
+                (unsigned long long)count);
+}
+
+dyc_status drain(dyc_table *t, cudaStream_t s, void *src, unsigned long long *src_ctr,
+                 void *dst, unsigned long long *dst_ctr, uint64_t cap, bool count_new,
+                 bool first_upsize);
+
+// Place the held entries (eviction walks, upsizing as needed). On failure
+// the ones still unplaced are held again.
+dyc_status settle_held(dyc_table *t, cudaStream_t s) {
+    if (t->held_n == 0) return DYC_OK;
+    const uint64_t n = t->held_n;
+    TRY(ensure_scratch(t, n));
+    CK(cudaMemcpyAsync(t->S.list_a, t->held.data(), (size_t)n * t->slot_bytes,
+                       cudaMemcpyHostToDevice, s));
+    TRY(reset_call_counters(t, s));
+    t->h_ctr->pending = n;
+    CK(cudaMemcpyAsync(&t->d_ctr->pending, &t->h_ctr->pending, sizeof(unsigned long long),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    std::vector<unsigned char>().swap(t->held);
+    t->held_n = 0;
+    const dyc_op_stats keep = t->last;
+    const dyc_status r = drain(t, s, t->S.list_a, &t->d_ctr->pending, t->S.list_b,
+                               &t->d_ctr->overflow, t->S.list_cap, true, false);
+    const uint64_t ups = t->last.resizes_up - keep.resizes_up;
+    t->last = keep;
+    t->last.resizes_up += ups;
+    return r;
 }
 
 // Double subtable pick_up(): allocate 2nb buckets, stream the old buckets
@@ -312,37 +404,45 @@ dyc_status resize_up_flush(int kb, int sb, int sms, cudaStream_t s,
     return DYC_OK;
 }
 
-// Place the entries of list `src` (count in counter *src_ctr) by eviction
-// walks; leftovers go to `dst`. Repeats with an upsize in between until
-// nothing is left. count_new: successes are new keys (insert) rather than
-// moved ones (downsize).
+// Place the entries of list `src` (count in counter *src_ctr, and in its
+// host mirror in t->h_ctr on entry) by eviction walks; leftovers go to
+// `dst`. Repeats with an upsize in between until nothing is left.
+// count_new: successes are new keys (insert) rather than moved ones
+// (downsize). If an upsize fails or the rounds run out, the entries not yet
+// placed are held (hold_list) and the error is returned: nothing is dropped.
 dyc_status drain(dyc_table *t, cudaStream_t s, void *src, unsigned long long *src_ctr,
                  void *dst, unsigned long long *dst_ctr, uint64_t cap, bool count_new,
                  bool first_upsize) {
+    auto host_count = [&](const unsigned long long *dc) {
+        return dc == &t->d_ctr->pending ? t->h_ctr->pending : t->h_ctr->overflow;
+    };
+    unsigned long long left = host_count(src_ctr);
     for (int round = 0; round < kMaxOverflowRounds; ++round) {
         if (round > 0 || first_upsize) {
             // grow to the upper load bound for everything placed or pending,
             // and by at least one subtable
-            const unsigned long long left = *(src_ctr == &t->d_ctr->pending ? &t->h_ctr->pending
-                                                                           : &t->h_ctr->overflow);
             int guard = 0;
             do {
-                TRY(resize_up_impl(t, s));
+                const dyc_status r = resize_up_impl(t, s);
+                if (r != DYC_OK) return hold_failed(t, s, src, left, !count_new, r);
             } while ((double)(t->size + left) > t->cfg.upper_load * (double)t->capacity &&
                      ++guard < 64);
         }
         CK(cudaMemsetAsync(dst_ctr, 0, sizeof(unsigned long long), s));
         cudaError_t e = KB_CALL(t, walk, ctx(t, s), t->D, t->sb, src, src_ctr, dst, dst_ctr, cap,
                                 t->cfg.max_evictions, count_new, t->d_ctr, cap);
-        if (e != cudaSuccess) return fail(DYC_ECUDA, "walk kernel: %s", cudaGetErrorString(e));
+        if (e != cudaSuccess)
+            return hold_failed(t, s, src, left, !count_new,
+                               fail(DYC_ECUDA, "walk kernel: %s", cudaGetErrorString(e)));
         TRY(read_counters(t, s));
-        const unsigned long long left =
-            dst_ctr == &t->d_ctr->pending ? t->h_ctr->pending : t->h_ctr->overflow;
+        left = host_count(dst_ctr);
         if (left == 0) return DYC_OK;
         std::swap(src, dst);
         std::swap(src_ctr, dst_ctr);
     }
-    return fail(DYC_EOVERFLOW, "eviction overflow persisted after %d upsizes", kMaxOverflowRounds);
+    return hold_failed(t, s, src, left, !count_new,
+                       fail(DYC_EOVERFLOW, "eviction overflow persisted after %d upsizes",
+                            kMaxOverflowRounds));
 }
 
 dyc_status insert_chunk(dyc_table *t, const void *keys, const void *vals, uint64_t n,
@@ -404,7 +504,12 @@ dyc_status erase_chunk(dyc_table *t, const void *keys, uint64_t n, uint32_t *bit
 // Halve subtable pick_down(). Even bucket counts merge bucket j with j+nb/2;
 // odd counts rehash the whole subtable into ceil(nb/2) buckets. Entries that
 // do not fit are placed by eviction walks (upsizing another subtable if
-// needed), so nothing is dropped.
+// needed), so nothing is dropped. The merge only reads the old subtable, and
+// the descriptor switches to the new one only after the merge's counters
+// are read: a failed allocation, a merge whose copy waits gave up
+// (DYC_ETIMEOUT) or a full list leave the table as it was. The lists hold
+// every entry that can be left over (even: one bucket's worth per merged
+// bucket; odd: the whole subtable), so a spill means a fault, not a load.
 dyc_status resize_down_impl(dyc_table *t, cudaStream_t s) {
     const uint32_t ti = pick_down(t->D.nb, t->D.d);
     const uint32_t onb = t->D.nb[ti];
@@ -413,32 +518,66 @@ dyc_status resize_down_impl(dyc_table *t, cudaStream_t s) {
     const uint32_t nnb = even ? onb / 2 : (onb + 1) / 2;
     const uint64_t list_cap = even ? (uint64_t)nnb * t->slots : (uint64_t)onb * t->slots;
     void *nw = nullptr, *la = nullptr, *lb = nullptr;
-    CK(pool_alloc(t->device, &nw, (size_t)nnb * t->sb, s));
-    CK(pool_alloc(t->device, &la, (size_t)list_cap * t->slot_bytes, s));
-    CK(pool_alloc(t->device, &lb, (size_t)list_cap * t->slot_bytes, s));
-    TRY(reset_call_counters(t, s));
+    auto release = [&]() {
+        if (nw) cudaFreeAsync(nw, s);
+        if (la) cudaFreeAsync(la, s);
+        if (lb) cudaFreeAsync(lb, s);
+    };
+    cudaError_t e = pool_alloc(t->device, &nw, (size_t)nnb * t->sb, s);
+    if (e == cudaSuccess) e = pool_alloc(t->device, &la, (size_t)list_cap * t->slot_bytes, s);
+    if (e == cudaSuccess) e = pool_alloc(t->device, &lb, (size_t)list_cap * t->slot_bytes, s);
+    if (e != cudaSuccess) {
+        release();
+        return fail(e == cudaErrorMemoryAllocation ? DYC_ENOMEM : DYC_ECUDA,
+                    "downsize of subtable %u: allocation: %s (table unchanged)", ti,
+                    cudaGetErrorString(e));
+    }
+    dyc_status r = reset_call_counters(t, s);
+    if (r != DYC_OK) {
+        release();
+        return r;
+    }
     void *old = t->D.sub[ti];
-    cudaError_t e;
     if (even) {
         e = KB_CALL(t, resize_down, ctx(t, s), t->sb, old, onb, nw, la, &t->d_ctr->pending,
-                    list_cap, &t->d_ctr->spill, &t->d_ctr->timeouts);
+                    list_cap, &t->d_ctr->spill, &t->d_ctr->timeouts, g_inject_wait_tries.load());
     } else {
-        CK(cudaMemsetAsync(nw, 0, (size_t)nnb * t->sb, s));
-        e = KB_CALL(t, collect, ctx(t, s), t->sb, old, onb, la, &t->d_ctr->pending, list_cap,
-                    &t->d_ctr->spill);
+        e = cudaMemsetAsync(nw, 0, (size_t)nnb * t->sb, s);
+        if (e == cudaSuccess)
+            e = KB_CALL(t, collect, ctx(t, s), t->sb, old, onb, la, &t->d_ctr->pending, list_cap,
+                        &t->d_ctr->spill);
         // keys of other subtables may have had their first-probe bucket here:
         // start every new bucket with all fingerprint bits set
         if (e == cudaSuccess) e = KB_CALL(t, mark_all, ctx(t, s), t->sb, nw, nnb);
     }
-    if (e != cudaSuccess) return fail(DYC_ECUDA, "downsize kernel: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        release();
+        return fail(DYC_ECUDA, "downsize kernel: %s", cudaGetErrorString(e));
+    }
+    e = cudaMemcpyAsync(t->h_ctr, t->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        release();
+        return fail(DYC_ECUDA, "downsize counters: %s", cudaGetErrorString(e));
+    }
+    if (t->h_ctr->timeouts || t->h_ctr->spill) {
+        const bool to = t->h_ctr->timeouts != 0;
+        const unsigned long long c = to ? t->h_ctr->timeouts : t->h_ctr->spill;
+        release();
+        CK(cudaMemsetAsync(&t->d_ctr->inserted, 0, sizeof(Counters) - sizeof(unsigned long long), s));
+        CK(cudaStreamSynchronize(s));
+        return fail(to ? DYC_ETIMEOUT : DYC_EOVERFLOW,
+                    "downsize of subtable %u: %llu %s; the table is unchanged", ti, c,
+                    to ? "bounded copy wait(s) gave up" : "leftover entries found no list slot");
+    }
     t->D.sub[ti] = nw;
     t->D.nb[ti] = nnb;
     t->D.magic[ti] = dyc::fastmod_magic(nnb);
     t->capacity -= (uint64_t)(onb - nnb) * t->slots;
     CK(cudaFreeAsync(old, s));
     t->last.resizes_down++;
-    dyc_status st = drain(t, s, la, &t->d_ctr->pending, lb, &t->d_ctr->overflow, list_cap, false,
-                          false);
+    const dyc_status st = drain(t, s, la, &t->d_ctr->pending, lb, &t->d_ctr->overflow, list_cap,
+                                false, false);
     cudaFreeAsync(la, s);
     cudaFreeAsync(lb, s);
     return st;
@@ -540,7 +679,7 @@ dyc_status create_impl(const dyc_config *cfg, Counters *ext_d, Counters *ext_h, 
     t->D.max_evict = cfg->max_evictions;
     for (uint32_t i = 0; i < t->D.d; ++i) {
         const uint32_t nb = nb_override ? nb_override[i] : nb_rule;
-        cudaError_t e = cudaMalloc(&t->D.sub[i], (size_t)nb * t->sb);
+        cudaError_t e = dyc::lib_malloc(&t->D.sub[i], (size_t)nb * t->sb);
         if (e != cudaSuccess) return undo(fail(DYC_ENOMEM, "subtable %u: %s", i, cudaGetErrorString(e)));
         e = cudaMemsetAsync(t->D.sub[i], 0, (size_t)nb * t->sb, 0);
         if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "memset: %s", cudaGetErrorString(e)));
@@ -554,9 +693,9 @@ dyc_status create_impl(const dyc_config *cfg, Counters *ext_d, Counters *ext_h, 
         t->d_ctr = ext_d;
         t->h_ctr = ext_h;
     } else {
-        e = cudaMalloc(&t->d_ctr, sizeof(Counters));
+        e = dyc::lib_malloc(&t->d_ctr, sizeof(Counters));
         if (e == cudaSuccess) e = cudaMemsetAsync(t->d_ctr, 0, sizeof(Counters), 0);
-        if (e == cudaSuccess) e = cudaMallocHost(&t->h_ctr, sizeof(Counters));
+        if (e == cudaSuccess) e = dyc::lib_malloc_host(&t->h_ctr, sizeof(Counters));
         if (e == cudaSuccess) memset(t->h_ctr, 0, sizeof(Counters));
     }
     if (e == cudaSuccess && sync) e = cudaDeviceSynchronize();
@@ -612,6 +751,7 @@ dyc_status dyc_pool_reserve(int32_t device, uint64_t bytes) {
     cudaStream_t s = nullptr;
     CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     void *p = nullptr;
+    dyc::g_lib_allocs.fetch_add(1, std::memory_order_relaxed);
     cudaError_t e = cudaMallocFromPoolAsync(&p, (size_t)bytes, pool, s);
     if (e == cudaSuccess) e = cudaFreeAsync(p, s);
     const cudaError_t e2 = cudaStreamSynchronize(s);
@@ -627,11 +767,12 @@ dyc_status dyc_pool_reserve(int32_t device, uint64_t bytes) {
 dyc_status dyc_insert(dyc_table *t, const void *d_keys, const void *d_vals, uint64_t n,
                       uint32_t flags, void *stream) {
     if (!t) return fail(DYC_EINVAL, "null table");
-    if (n == 0) return DYC_OK;
-    if (!d_keys || !d_vals) return fail(DYC_EINVAL, "null key or value array");
     TRY(set_device(t));
     cudaStream_t s = (cudaStream_t)stream;
     t->last = dyc_op_stats{};
+    TRY(settle_held(t, s));
+    if (n == 0) return DYC_OK;
+    if (!d_keys || !d_vals) return fail(DYC_EINVAL, "null key or value array");
     const uint64_t chunk = t->chunk;
     TRY(ensure_scratch(t, n < chunk ? n : chunk));
     for (uint64_t off = 0; off < n; off += chunk) {
@@ -651,9 +792,10 @@ dyc_status dyc_insert(dyc_table *t, const void *d_keys, const void *d_vals, uint
 dyc_status dyc_find(dyc_table *t, const void *d_keys, void *d_vals_out, uint32_t *d_hit_bits_out,
                     uint64_t n, void *stream) {
     if (!t) return fail(DYC_EINVAL, "null table");
+    TRY(set_device(t));
+    if (t->held_n) TRY(settle_held(t, (cudaStream_t)stream));
     if (n == 0) return DYC_OK;
     if (!d_keys || !d_vals_out) return fail(DYC_EINVAL, "null key or value array");
-    TRY(set_device(t));
     cudaError_t e = KB_CALL(t, find, ctx(t, stream), t->D, t->sb, d_keys, d_vals_out,
                             (uint32_t)t->vb, d_hit_bits_out, n);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "find kernel: %s", cudaGetErrorString(e));
@@ -664,11 +806,12 @@ dyc_status dyc_erase(dyc_table *t, const void *d_keys, uint64_t n, uint32_t *d_e
                      uint64_t *h_erased_count, uint32_t flags, void *stream) {
     if (!t) return fail(DYC_EINVAL, "null table");
     if (h_erased_count) *h_erased_count = 0;
-    if (n == 0) return DYC_OK;
-    if (!d_keys) return fail(DYC_EINVAL, "null key array");
     TRY(set_device(t));
     cudaStream_t s = (cudaStream_t)stream;
     t->last = dyc_op_stats{};
+    TRY(settle_held(t, s));
+    if (n == 0) return DYC_OK;
+    if (!d_keys) return fail(DYC_EINVAL, "null key array");
     const uint64_t chunk = t->chunk;
     TRY(ensure_scratch(t, n < chunk ? n : chunk));
     for (uint64_t off = 0; off < n; off += chunk) {
@@ -696,6 +839,7 @@ dyc_status dyc_resize_up(dyc_table *t, void *stream) {
     if (!t) return fail(DYC_EINVAL, "null table");
     TRY(set_device(t));
     t->last = dyc_op_stats{};
+    TRY(settle_held(t, (cudaStream_t)stream));
     TRY(resize_up_impl(t, (cudaStream_t)stream));
     CK(cudaStreamSynchronize((cudaStream_t)stream));
     return DYC_OK;
@@ -705,12 +849,13 @@ dyc_status dyc_resize_down(dyc_table *t, void *stream) {
     if (!t) return fail(DYC_EINVAL, "null table");
     TRY(set_device(t));
     t->last = dyc_op_stats{};
+    TRY(settle_held(t, (cudaStream_t)stream));
     return resize_down_impl(t, (cudaStream_t)stream);
 }
 
 dyc_status dyc_size(dyc_table *t, uint64_t *size) {
     if (!t || !size) return fail(DYC_EINVAL, "null argument");
-    *size = t->size;
+    *size = t->size + t->held_n;  // held entries are keys of the table too
     return DYC_OK;
 }
 
@@ -741,6 +886,7 @@ dyc_status dyc_export(dyc_table *t, void *d_keys_out, void *d_vals_out, uint64_t
     if (capacity && (!d_keys_out || !d_vals_out)) return fail(DYC_EINVAL, "null output array");
     TRY(set_device(t));
     cudaStream_t s = (cudaStream_t)stream;
+    TRY(settle_held(t, s));
     CK(cudaMemsetAsync(&t->d_ctr->pad[0], 0, sizeof(unsigned long long), s));
     cudaError_t e = KB_CALL(t, export_all, ctx(t, s), t->D, t->sb, d_keys_out, d_vals_out,
                             (uint32_t)t->vb, capacity, &t->d_ctr->pad[0]);
@@ -753,9 +899,33 @@ dyc_status dyc_export(dyc_table *t, void *d_keys_out, void *d_vals_out, uint64_t
     return DYC_OK;
 }
 
+dyc_status dyc_debug_alloc_count(uint64_t *count) {
+    if (!count) return fail(DYC_EINVAL, "null argument");
+    *count = dyc::g_lib_allocs.load();
+    return DYC_OK;
+}
+
+dyc_status dyc_debug_inject(uint32_t kind, uint64_t n) {
+    switch (kind) {
+    case DYC_INJECT_RESET:
+        g_inject_alloc.store(0);
+        g_inject_wait_tries.store(dyc::kWaitTries);
+        return DYC_OK;
+    case DYC_INJECT_POOL_ALLOC:
+        g_inject_alloc.store(n);
+        return DYC_OK;
+    case DYC_INJECT_WAIT_TRIES:
+        g_inject_wait_tries.store(n < dyc::kWaitTries ? (uint32_t)n : dyc::kWaitTries);
+        return DYC_OK;
+    default:
+        return fail(DYC_EINVAL, "unknown injection kind %u", kind);
+    }
+}
+
 dyc_status dyc_last_stats(dyc_table *t, dyc_op_stats *out) {
     if (!t || !out) return fail(DYC_EINVAL, "null argument");
     *out = t->last;
+    out->held = t->held_n;
     return DYC_OK;
 }
 
@@ -771,7 +941,7 @@ dyc_status ensure_io(dyc_table *t, size_t bytes) {
         CK(cudaFree(t->d_io));
         t->d_io = nullptr;
     }
-    CK(cudaMalloc(&t->d_io, bytes));
+    CK(dyc::lib_malloc(&t->d_io, bytes));
     t->d_io_bytes = bytes;
     return DYC_OK;
 }
@@ -831,7 +1001,7 @@ dyc_status dyc_find_host(dyc_table *t, const void *h_keys, void *h_vals_out,
         for (int i = 0; i < kStages; ++i) {
             if (!t->pipe_stream[i])
                 CK(cudaStreamCreateWithFlags(&t->pipe_stream[i], cudaStreamNonBlocking));
-            CK(cudaMalloc(&t->pipe_buf[i], need));
+            CK(dyc::lib_malloc(&t->pipe_buf[i], need));
         }
         t->pipe_bytes = need;
     }
@@ -930,7 +1100,7 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
         *buf = nullptr;
     }
     if (!*buf) {
-        CK(cudaMalloc(buf, need));
+        CK(dyc::lib_malloc(buf, need));
         *buf_bytes = need;
     }
     char *p = (char *)*buf;
@@ -975,12 +1145,12 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
 dyc_status ensure_apply(dyc_table *t, uint64_t n) {
     const uint64_t ops = n < 128 ? 128 : n;
     if (!t->d_desc) {
-        CK(cudaMalloc(&t->d_desc, sizeof(Desc)));
-        CK(cudaMallocHost(&t->h_desc, sizeof(Desc)));
+        CK(dyc::lib_malloc(&t->d_desc, sizeof(Desc)));
+        CK(dyc::lib_malloc_host(&t->h_desc, sizeof(Desc)));
         memset(t->h_desc, 0, sizeof(Desc));  // differs from any live D: the first push copies
     }
     if (t->apply_buf && t->A.cap_ops >= ops) return DYC_OK;
-    if (!t->h_actr) CK(cudaMallocHost(&t->h_actr, dyc::kCtrSlots * sizeof(unsigned long long)));
+    if (!t->h_actr) CK(dyc::lib_malloc_host(&t->h_actr, dyc::kCtrSlots * sizeof(unsigned long long)));
     return carve_apply(t->kb, t->vb, ops, 2 * ops, 0, &t->apply_buf, &t->apply_bytes, &t->A);
 }
 
@@ -1091,11 +1261,12 @@ extern "C" dyc_status dyc_apply(dyc_table *t, const uint8_t *d_ops, const void *
                                 const void *d_vals, uint64_t n, void *d_vals_out,
                                 uint32_t *d_bits_out, uint32_t flags, void *stream) {
     if (!t) return fail(DYC_EINVAL, "null table");
-    if (n == 0) return DYC_OK;
-    if (!d_ops || !d_keys || !d_vals) return fail(DYC_EINVAL, "null op, key or value array");
     TRY(set_device(t));
     cudaStream_t s = (cudaStream_t)stream;
     t->last = dyc_op_stats{};
+    TRY(settle_held(t, s));
+    if (n == 0) return DYC_OK;
+    if (!d_ops || !d_keys || !d_vals) return fail(DYC_EINVAL, "null op, key or value array");
     const uint64_t chunk = t->chunk;
     const uint64_t m0 = n < chunk ? n : chunk;
     TRY(ensure_apply(t, m0));
@@ -1172,21 +1343,27 @@ extern "C" dyc_status dyc_erase_noalloc(dyc_table *t, const void *d_keys, uint64
                     (unsigned long long)kNoAllocMaxKeys, (unsigned long long)n);
     if (n == 0) return DYC_OK;
     if (!d_keys) return fail(DYC_EINVAL, "null key array");
+    if (t->held_n)  // placing them may need memory: an allocating call must come first
+        return fail(DYC_ENOMEM, "%llu entries are held from a failed call; an allocating "
+                    "call on the table places them first", (unsigned long long)t->held_n);
     TRY(set_device(t));
     void *base = nullptr;
     TRY(noalloc_scratch(t->device, &base));
     cudaStream_t s = (cudaStream_t)stream;
+    // this call's dedup table: the first dedup_cap cells of the array (the
+    // kernels take their mask from dedup_cap), as the allocating path sizes
+    // its own; the index array of 8-byte keys keeps its fixed offset
     Scratch S{};
     S.dedup = base;
-    S.dedup_cap = kNoAllocCells;
+    S.dedup_cap = next_pow2(2 * (n < 16 ? 16 : n));  // <= kNoAllocCells for n <= the limit
     S.dedup_idx = t->kb == 8 ? (uint32_t *)((char *)base + kNoAllocCells * 8) : nullptr;
     const bool use_dedup = !(flags & DYC_FLAG_UNIQUE) && n > 1;
     t->last = dyc_op_stats{};
     TRY(reset_call_counters(t, s));
     if (use_dedup) {
-        // the array keeps the previous call's cells: clear the ones used
-        CK(cudaMemsetAsync(S.dedup, 0, (size_t)kNoAllocCells * 8, s));
-        if (S.dedup_idx) CK(cudaMemsetAsync(S.dedup_idx, 0xFF, (size_t)kNoAllocCells * 4, s));
+        // the array keeps the previous call's cells: clear the ones this call uses
+        CK(cudaMemsetAsync(S.dedup, 0, (size_t)S.dedup_cap * 8, s));
+        if (S.dedup_idx) CK(cudaMemsetAsync(S.dedup_idx, 0xFF, (size_t)S.dedup_cap * 4, s));
         cudaError_t e = KB_CALL(t, dedup, ctx(t, s), S, d_keys, n, dyc::kKeepFirst);
         if (e != cudaSuccess) return fail(DYC_ECUDA, "dedup kernel: %s", cudaGetErrorString(e));
     }
@@ -1320,7 +1497,7 @@ dyc_status set_ensure_scratch(dyc_set *s, uint64_t n) {
         CK(cudaFree(s->lbuf));
         s->lbuf = nullptr;
     }
-    CK(cudaMalloc(&s->lbuf, lb));
+    CK(dyc::lib_malloc(&s->lbuf, lb));
     s->lbytes = lb;
     char *p = (char *)s->lbuf;
     const size_t ls = (ops * slot + 255) & ~(size_t)255, lt = (ops * 4 + 255) & ~(size_t)255;
@@ -1447,16 +1624,37 @@ dyc_status set_overflow(dyc_set *s, uint64_t cnt, const std::vector<uint8_t> &gr
             memcpy(hk.data() + j * s->kb, e, s->kb);
             memcpy(hv.data() + j * s->vb, e + (s->kb == 4 ? 4 : 8), s->vb);
         }
-        TRY(ensure_io(m, c * (s->kb + s->vb) + 256));
+        // an upsize or scratch the pool cannot serve: this table's entries and
+        // those of the tables after it are held by their tables (not dropped)
+        auto hold_rest = [&](uint32_t from, dyc_status why) -> dyc_status {
+            const std::string msg = g_err;
+            uint64_t held = 0;
+            for (uint32_t u = from; u < s->ntables; ++u) {
+                dyc_table *mu = s->tables[u];
+                for (uint64_t i : per[u]) {
+                    const unsigned char *e = ent.data() + i * slot;
+                    mu->held.insert(mu->held.end(), e, e + slot);
+                }
+                mu->held_n += per[u].size();
+                held += per[u].size();
+            }
+            return fail(why, "%s; %llu entries held by their tables for the next call",
+                        msg.c_str(), (unsigned long long)held);
+        };
+        dyc_status r = ensure_io(m, c * (s->kb + s->vb) + 256);
+        if (r == DYC_OK) r = ensure_scratch(m, c);
+        if (r == DYC_OK && (grew.empty() || !grew[t])) r = resize_up_impl(m, st);
+        for (int guard = 0; r == DYC_OK && guard < 64 &&
+                            (double)(m->size + c) > m->cfg.upper_load * (double)m->capacity;
+             ++guard)
+            r = resize_up_impl(m, st);
+        if (r != DYC_OK) return hold_rest(t, r);
         char *dk = (char *)m->d_io, *dv = dk + ((c * s->kb + 255) & ~(uint64_t)255);
         CK(cudaMemcpyAsync(dk, hk.data(), c * s->kb, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(dv, hv.data(), c * s->vb, cudaMemcpyHostToDevice, st));
-        TRY(ensure_scratch(m, c));
-        int guard = 0;
-        if (grew.empty() || !grew[t]) TRY(resize_up_impl(m, st));
-        while ((double)(m->size + c) > m->cfg.upper_load * (double)m->capacity && ++guard < 64)
-            TRY(resize_up_impl(m, st));
-        TRY(insert_chunk(m, dk, dv, c, DYC_FLAG_UNIQUE | DYC_FLAG_NEW_KEYS, st));
+        // a failure inside holds this table's unplaced entries (drain)
+        r = insert_chunk(m, dk, dv, c, DYC_FLAG_UNIQUE | DYC_FLAG_NEW_KEYS, st);
+        if (r != DYC_OK) return hold_rest(t + 1, r);
         CK(cudaStreamSynchronize(st));  // hk / hv and the io buffer are reused
         s->last.resizes_up += m->last.resizes_up;
         m->last = dyc_op_stats{};
@@ -1511,18 +1709,18 @@ dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_
     cudaError_t e = cudaSetDevice(s->device);
     if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device);
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_tctr, sizeof(Counters) * ntables);
+    if (e == cudaSuccess) e = dyc::lib_malloc(&s->d_tctr, sizeof(Counters) * ntables);
     if (e == cudaSuccess) e = cudaMemset(s->d_tctr, 0, sizeof(Counters) * ntables);
-    if (e == cudaSuccess) e = cudaMallocHost(&s->h_tctr, sizeof(Counters) * ntables);
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_desc, sizeof(Desc) * ntables);
-    if (e == cudaSuccess) e = cudaMallocHost(&s->h_desc, sizeof(Desc) * ntables);
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_gctr, sizeof(Counters));
-    if (e == cudaSuccess) e = cudaMallocHost(&s->h_gctr, sizeof(Counters));
+    if (e == cudaSuccess) e = dyc::lib_malloc_host(&s->h_tctr, sizeof(Counters) * ntables);
+    if (e == cudaSuccess) e = dyc::lib_malloc(&s->d_desc, sizeof(Desc) * ntables);
+    if (e == cudaSuccess) e = dyc::lib_malloc_host(&s->h_desc, sizeof(Desc) * ntables);
+    if (e == cudaSuccess) e = dyc::lib_malloc(&s->d_gctr, sizeof(Counters));
+    if (e == cudaSuccess) e = dyc::lib_malloc_host(&s->h_gctr, sizeof(Counters));
     if (e == cudaSuccess)
-        e = cudaMallocHost(&s->h_actr, sizeof(unsigned long long) * dyc::kCtrSlots);
-    if (e == cudaSuccess) e = cudaMallocHost(&s->h_hostn, sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMallocHost(&s->h_tup, sizeof(uint32_t) * ntables);
-    if (e == cudaSuccess) e = cudaMallocHost(&s->h_ter, sizeof(uint32_t) * ntables);
+        e = dyc::lib_malloc_host(&s->h_actr, sizeof(unsigned long long) * dyc::kCtrSlots);
+    if (e == cudaSuccess) e = dyc::lib_malloc_host(&s->h_hostn, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = dyc::lib_malloc_host(&s->h_tup, sizeof(uint32_t) * ntables);
+    if (e == cudaSuccess) e = dyc::lib_malloc_host(&s->h_ter, sizeof(uint32_t) * ntables);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming);
@@ -1631,6 +1829,9 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
     }
     s->last = dyc_op_stats{};
     for (dyc_table *m : s->tables) m->last = dyc_op_stats{};
+    // entries a failed call left held by a member go back into it first
+    for (dyc_table *m : s->tables)
+        if (m->held_n) TRY(settle_held(m, st));
     // single-table calls on members since the last set call may have resized
     // them: the kernels must see the current subtables
     TRY(set_refresh_descs(s, st));
@@ -1784,7 +1985,7 @@ dyc_status dyc_set_apply_each(dyc_set *s, const uint32_t *d_offsets, const uint3
         if (s->bits_tmp_words < words) {
             if (s->d_bits_tmp) CK(cudaFree(s->d_bits_tmp));
             s->d_bits_tmp = nullptr;
-            CK(cudaMalloc(&s->d_bits_tmp, words * 4));
+            CK(dyc::lib_malloc(&s->d_bits_tmp, words * 4));
             s->bits_tmp_words = words;
         }
         CK(cudaMemsetAsync(d_bits_out, 0, (size_t)((n + 31) / 32) * 4, st));
@@ -1877,12 +2078,20 @@ extern "C" {
 
 dyc_status dyc_snapshot_bytes(dyc_table *t, uint64_t *bytes) {
     if (!t || !bytes) return fail(DYC_EINVAL, "null argument");
+    if (t->held_n) {  // held entries are placed first: the layout may grow
+        TRY(set_device(t));
+        TRY(settle_held(t, 0));
+    }
     *bytes = sizeof(dyc_snapshot_header) + snapshot_payload(t);
     return DYC_OK;
 }
 
 dyc_status dyc_snapshot(dyc_table *t, void *h_buf, uint64_t buf_bytes, void *stream) {
     if (!t || !h_buf) return fail(DYC_EINVAL, "null argument");
+    if (t->held_n) {  // placed first (may upsize: the size check below then sees it)
+        TRY(set_device(t));
+        TRY(settle_held(t, (cudaStream_t)stream));
+    }
     const uint64_t payload = snapshot_payload(t);
     if (buf_bytes < sizeof(dyc_snapshot_header) + payload)
         return fail(DYC_EINVAL, "snapshot buffer of %llu bytes, need %llu",
@@ -2018,7 +2227,7 @@ dyc_status wide_ensure_scratch(dyc_wide *w, uint64_t n) {
         CK(cudaFree(w->scr));
         w->scr = nullptr;
     }
-    CK(cudaMalloc(&w->scr, need));
+    CK(dyc::lib_malloc(&w->scr, need));
     char *p = (char *)w->scr;
     w->pre_h = (uint32_t *)p;
     p += al(m * 4);
@@ -2093,11 +2302,11 @@ dyc_status dyc_wide_create(const dyc_config *cfg, uint32_t value_bytes, dyc_wide
         delete w;
         return r;
     }
-    cudaError_t e = cudaMalloc(&w->d_alloc, sizeof(WideAlloc));
+    cudaError_t e = dyc::lib_malloc(&w->d_alloc, sizeof(WideAlloc));
     if (e == cudaSuccess) e = cudaMemset(w->d_alloc, 0, sizeof(WideAlloc));
-    if (e == cudaSuccess) e = cudaMallocHost(&w->h_alloc, sizeof(WideAlloc));
-    if (e == cudaSuccess) e = cudaMallocHost(&w->h_cnt, 2 * sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMallocHost(&w->h_cap, sizeof(uint32_t));
+    if (e == cudaSuccess) e = dyc::lib_malloc_host(&w->h_alloc, sizeof(WideAlloc));
+    if (e == cudaSuccess) e = dyc::lib_malloc_host(&w->h_cnt, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = dyc::lib_malloc_host(&w->h_cap, sizeof(uint32_t));
     if (e != cudaSuccess) {
         dyc_wide_destroy(w);
         return fail(DYC_ENOMEM, "wide table setup: %s", cudaGetErrorString(e));
@@ -2150,6 +2359,8 @@ dyc_status dyc_wide_insert(dyc_wide *w, const void *d_keys, const void *d_vals, 
     TRY(set_device(t));
     cudaStream_t s = (cudaStream_t)stream;
     w->last = dyc_op_stats{};
+    if (t->held_n) TRY(settle_held(t, s));
+    if (t->held_n) TRY(settle_held(t, s));  // (key, handle) slots a failed call held
     const uint64_t chunk = t->chunk;
     const uint64_t m0 = std::min(n, chunk);
     TRY(ensure_scratch(t, m0));
@@ -2213,6 +2424,7 @@ dyc_status dyc_wide_find(dyc_wide *w, const void *d_keys, void *d_vals_out, uint
     dyc_table *t = w->t;
     TRY(set_device(t));
     cudaStream_t s = (cudaStream_t)stream;
+    if (t->held_n) TRY(settle_held(t, s));
     const uint64_t chunk = t->chunk;
     TRY(wide_ensure_scratch(w, std::min(n, chunk)));
     for (uint64_t off = 0; off < n; off += chunk) {

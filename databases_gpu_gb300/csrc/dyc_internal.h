@@ -3,6 +3,7 @@
 // kernel launchers.
 #pragma once
 
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 
@@ -10,10 +11,25 @@
 
 namespace dyc {
 
+// Every device and pinned-host allocation the library makes goes through
+// these (counted for dyc_debug_alloc_count).
+extern std::atomic<unsigned long long> g_lib_allocs;
+template <class T> cudaError_t lib_malloc(T **p, size_t bytes) {
+    g_lib_allocs.fetch_add(1, std::memory_order_relaxed);
+    return cudaMalloc((void **)p, bytes);
+}
+template <class T> cudaError_t lib_malloc_host(T **p, size_t bytes) {
+    g_lib_allocs.fetch_add(1, std::memory_order_relaxed);
+    return cudaMallocHost((void **)p, bytes);
+}
+
 // The reference's modulus before the bucket modulo, written as in
 // GPU/dyhash/dy_hash.h:24 (294967291, not the prime 4294967291).
 constexpr uint32_t kPrime = 294967291u;
 constexpr int kMaxSub = 6;
+// Polls of a bounded device wait (mbarrier try_wait): far beyond any copy's
+// completion; a wait that runs out records a timeout instead of hanging.
+constexpr uint32_t kWaitTries = 1u << 22;
 
 // Table descriptor passed by value to every kernel (the reference keeps one
 // in __constant__ memory, cuckoo.cu:16, which limits a process to one table).
@@ -162,11 +178,14 @@ template <int KB> struct Ops {
                                  uint32_t old_nb, void *new_sub);
     // J.n jobs in one launch of J.blocks blocks (job block ranges filled in)
     static cudaError_t resize_up_many(const LaunchCtx &L, int sb, const ResizeJobs &J);
-    // halve an even subtable: merged buckets to new_sub, leftovers to list
+    // halve an even subtable: merged buckets to new_sub, leftovers to list;
+    // a tile-copy wait gives up after tile_wait_tries polls (counted in
+    // *timeouts; old_sub is only read)
     static cudaError_t resize_down(const LaunchCtx &L, int sb, const void *old_sub,
                                    uint32_t old_nb, void *new_sub, void *list,
                                    unsigned long long *list_count, uint64_t list_cap,
-                                   unsigned long long *spill, unsigned long long *timeouts);
+                                   unsigned long long *spill, unsigned long long *timeouts,
+                                   uint32_t tile_wait_tries);
     // every live slot of one subtable to list (general rehash)
     static cudaError_t collect(const LaunchCtx &L, int sb, const void *sub, uint32_t nb,
                                void *list, unsigned long long *list_count, uint64_t list_cap,

@@ -1087,10 +1087,10 @@ __device__ __forceinline__ void bulk_store(void *dst, uint32_t src, uint32_t byt
                  : "memory");
     asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
-// true when phase `parity` of the barrier completed within the bound
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    constexpr uint32_t kMaxTries = 1u << 22;  // far beyond any copy's completion
-    for (uint32_t i = 0; i < kMaxTries; ++i) {
+// true when phase `parity` of the barrier completed within `tries` polls
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
+                                          uint32_t tries = kWaitTries) {
+    for (uint32_t i = 0; i < tries; ++i) {
         uint32_t done;
         asm volatile(
             "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
@@ -1111,6 +1111,9 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 // buckets stream through shared memory by bulk copies: two loads (the tile
 // of each half) completing on an mbarrier, a merge by one thread per bucket
 // in place, one bulk store of the merged tile. The metadata words are OR-ed.
+// A tile wait that gives up after tile_wait_tries polls (kWaitTries unless a
+// test lowers it) is counted in *timeouts and the block stops; the old
+// subtable is only read, so the caller can keep it.
 // ----------------------------------------------------------------------------
 constexpr int kMergeTile = 128;  // buckets per tile = threads per block
 
@@ -1122,7 +1125,8 @@ __global__ void __launch_bounds__(kMergeTile) k_resize_down(const char *__restri
                                                             unsigned long long *list_count,
                                                             uint64_t list_cap,
                                                             unsigned long long *spill,
-                                                            unsigned long long *timeouts) {
+                                                            unsigned long long *timeouts,
+                                                            uint32_t tile_wait_tries) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
     using Gm = Geo<KB, SB>;
@@ -1155,7 +1159,7 @@ __global__ void __launch_bounds__(kMergeTile) k_resize_down(const char *__restri
             bulk_load(sa_addr, old_sub + j0 * SB, bytes, bar);
             bulk_load(sc_addr, old_sub + (j0 + new_nb) * SB, bytes, bar);
         }
-        const bool ok = mbar_wait(bar, parity);
+        const bool ok = mbar_wait(bar, parity, tile_wait_tries);
         parity ^= 1u;
         if (!ok) {
             if (tid == 0) atomicAdd(timeouts, 1ull);
@@ -1248,7 +1252,9 @@ __global__ void __launch_bounds__(kMergeTile) k_resize_down(const char *__restri
         if (tid == 0) bulk_store(new_sub + j0 * SB, sa_addr, bytes);
     }
     if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
-    if (failed && tid == 0) mbar_wait(bar, parity ^ 1u);  // copies of the failed tile, bounded
+    // the loads of a tile whose wait gave up are still in flight: wait for
+    // them (full bound) before the block's shared memory goes away
+    if (failed && tid == 0) mbar_wait(bar, parity ^ 1u);
 }
 
 // every live slot of one subtable into a list (odd-size downsize)

@@ -171,14 +171,15 @@ template <int KB>
 cudaError_t Ops<KB>::resize_down(const LaunchCtx &L, int sb, const void *old_sub,
                                  uint32_t old_nb, void *new_sub, void *list,
                                  unsigned long long *list_count, uint64_t list_cap,
-                                 unsigned long long *spill, unsigned long long *timeouts) {
+                                 unsigned long long *spill, unsigned long long *timeouts,
+                                 uint32_t tile_wait_tries) {
     const uint32_t new_nb = old_nb / 2u;
     if (new_nb == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_resize_down<KB, SB>;
         k<<<grid_for((const void *)k, L, new_nb, kMergeTile), kMergeTile, 0, L.stream>>>(
             (const char *)old_sub, new_nb, (char *)new_sub, list, list_count, list_cap, spill,
-            timeouts);
+            timeouts, tile_wait_tries);
     });
     return cudaGetLastError();
 }

@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include "dycuckoo.h"
+#include "dyc_internal.h"
 
 namespace {
 
@@ -456,8 +457,8 @@ dyc_status dyc_server_create(const dyc_config *table_cfg, uint32_t ntenants,
     for (int i = 0; i < kSlots && e == cudaSuccess; ++i) {
         Slot &sl = s->slot[i];
         void *h = nullptr, *d = nullptr;
-        e = cudaMallocHost(&h, bytes);
-        if (e == cudaSuccess) e = cudaMalloc(&d, bytes);
+        e = dyc::lib_malloc_host(&h, bytes);
+        if (e == cudaSuccess) e = dyc::lib_malloc(&d, bytes);
         if (e != cudaSuccess) {
             if (h) cudaFreeHost(h);
             break;

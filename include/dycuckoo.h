@@ -35,6 +35,20 @@
  *     erase batch only the first occurrence of a repeated key removes it.
  *   - no entry is ever dropped: an eviction chain that reaches its bound
  *     parks its entry, the table upsizes and the entry is placed again.
+ *
+ * Failures
+ *   - A call that fails after it has taken entries out of the table (an
+ *     upsize the device cannot serve: DYC_ENOMEM; eviction overflow that
+ *     outlasts every upsize round: DYC_EOVERFLOW) keeps the entries it could
+ *     not place on the host, "held" by the table, instead of dropping them
+ *     (the reference drops them: cuckoo.cu:422-431, :714-722). Held entries
+ *     are counted by dyc_size and reported in dyc_op_stats.held; finds do
+ *     not see them until they are placed. Every later call on the table
+ *     (any insert, find, erase, apply, resize, export or snapshot) places
+ *     them first, upsizing as needed, and fails the same way if it still
+ *     cannot; dyc_insert with n = 0 places them and nothing else.
+ *   - A downsize that cannot allocate, or whose bounded copy waits give up
+ *     (DYC_ETIMEOUT), leaves the table as it was.
  */
 #ifndef DYCUCKOO_H
 #define DYCUCKOO_H
@@ -94,6 +108,8 @@ typedef struct dyc_op_stats {
     uint64_t resizes_down;
     uint64_t split_phases; /* dyc_set_apply: 1 when the host read the batch's new-key
                               counts between its phases (a table could have filled) */
+    uint64_t held;         /* entries held outside the table after a failed call (see
+                              "Failures" below); the next call on the table places them */
 } dyc_op_stats;
 
 /* Defaults: 4-byte keys and values, d = 4, 128-byte buckets, bound 64,
@@ -459,6 +475,25 @@ dyc_status dyc_erase_noalloc(dyc_table *t, const void *d_keys, uint64_t n,
 
 const char *dyc_status_string(dyc_status s);
 const char *dyc_last_error(void);
+
+/* Failure injection for tests of the error paths above (no counterpart in
+ * the reference, which has no error paths). Process-wide, for tests only.
+ *   DYC_INJECT_RESET: clear every injection.
+ *   DYC_INJECT_POOL_ALLOC: the n-th allocation from the library pool from
+ *     now on (subtables of resizes, downsize lists) fails as if the device
+ *     were out of memory; n = 0 clears.
+ *   DYC_INJECT_WAIT_TRIES: the downsize kernel's bounded waits on its tile
+ *     copies give up after n polls (n = 0: at the first poll); the wait for
+ *     copies still in flight before a block exits keeps its full bound. */
+#define DYC_INJECT_RESET 0u
+#define DYC_INJECT_POOL_ALLOC 1u
+#define DYC_INJECT_WAIT_TRIES 2u
+dyc_status dyc_debug_inject(uint32_t kind, uint64_t n);
+
+/* Number of device and pinned-host allocations the library has made in this
+ * process (cudaMalloc, cudaMallocHost, allocations from its pool), for
+ * tests that a call allocates nothing. No counterpart in the reference. */
+dyc_status dyc_debug_alloc_count(uint64_t *count);
 
 #ifdef __cplusplus
 }

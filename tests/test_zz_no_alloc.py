@@ -6,8 +6,11 @@ allocation's synchronisation). For them dyc_erase_noalloc takes its
 batch-dedup scratch from a fixed array in the library. This checks, through
 the C ABI, that it returns exactly what dyc_erase returns -- erased bits,
 erased count and the table contents afterwards -- on two calls in a row,
-that device free memory does not move across those calls, and that a batch
-above the limit is refused without touching the table.
+that the library makes no device or pinned allocation during those calls
+(its own allocation counter, which also sees allocations its memory pool
+could serve without the device's free memory moving) and that device free
+memory does not move either, and that a batch above the limit is refused
+without touching the table.
 
 Kept in its own file so it is collected last.
 """
@@ -29,6 +32,12 @@ def _mem_free():
     free, total = C.c_size_t(), C.c_size_t()
     assert cudart.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
     return free.value
+
+
+def _allocs(L):
+    n = C.c_uint64()
+    assert L.dyc_debug_alloc_count(C.byref(n)) == 0
+    return n.value
 
 
 def _erase(L, fn, t, keys_dev, bits_dev, stream):
@@ -79,11 +88,14 @@ def test_noalloc_erase_matches_erase_on_two_calls(key_bytes):
     assert _erase(L, "dyc_erase_noalloc", b, warm, wbits, stream) == 0
     torch.cuda.synchronize()
 
-    free_before = _mem_free()
     got = []
+    new_allocs = []
+    free_before = _mem_free()
     for i, kb in enumerate(batches):
         c_ref = _erase(L, "dyc_erase", a, kb, bits[2 * i], stream)
+        n0 = _allocs(L)
         c_new = _erase(L, "dyc_erase_noalloc", b, kb, bits[2 * i + 1], stream)
+        new_allocs.append(_allocs(L) - n0)
         got.append((c_ref, c_new))
     torch.cuda.synchronize()
     free_after_b = _mem_free()
@@ -98,8 +110,10 @@ def test_noalloc_erase_matches_erase_on_two_calls(key_bytes):
         assert np.array_equal(dg.unpack_bits(bits[2 * i + 1], x.size), oh)
     assert_same_contents(a, m, "dyc_erase")
     assert_same_contents(b, m, "dyc_erase_noalloc")
-    # dyc_erase reuses scratch sized by its first call, so nothing in this
-    # window allocates; free device memory must not move
+    # the no-allocation calls made no allocation of the library's own
+    assert new_allocs == [0, 0], new_allocs
+    # and nothing in this window allocated device memory at all (dyc_erase
+    # reuses scratch sized by its first call): free memory must not move
     assert free_after_b == free_before, (free_before, free_after_b)
     a.close()
     b.close()
