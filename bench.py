@@ -15,10 +15,20 @@ excluded. Zipf ranks use the continuous inverse-CDF approximation.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--log2-keys 28] [--log2-batch 26] [--skip-cpu]
+                    [--only find|stream|multi|serve|serve-steps]
+
+Beside the headline the line carries: the same finds through the C ABI from
+host buffers (e2e) with the copies alone timed next to them; the same table
+at 32-byte buckets; erase, upsert, bulk-insert and mixed-batch rates with
+their random-sector rooflines; the reference's own GPU kernels
+(cuckoo_search / cuckoo_insert compiled for sm_103a) on the same keys; the
+reference algorithm on the host cores; and the other workloads of the
+measurement plan (resize stream, 4096-table batches, serving loop, serving
+steps). --only runs one of them.
 
 --impl reference times the reference's algorithm on the host cores (the
 oracle's restatement of GPU/dyhash: 16-slot buckets, the reference's hash
-functions and eviction rule), the only CPU form the reference's path has.
+functions and eviction rule), the CPU form of the reference's path.
 """
 from __future__ import annotations
 
@@ -308,67 +318,6 @@ def run_reference_gpu(args, keys, batch, stream, torch):
     return res
 
 
-def run_line_probe():
-    """Random DRAM line ceiling (databases_gpu_gb300/csrc/dyc_line_probe.cu)."""
-    from databases_gpu_gb300 import build as pkg_build
-    src = os.path.join(pkg_build.CSRC, "dyc_line_probe.cu")
-    exe = os.path.join(pkg_build.BUILD_DIR, "dyc_line_probe")
-    os.makedirs(pkg_build.BUILD_DIR, exist_ok=True)
-    if not os.path.exists(exe) or os.path.getmtime(exe) < os.path.getmtime(src):
-        subprocess.check_call([pkg_build.nvcc()] + pkg_build.ARCH + ["-O3", "-o", exe, src])
-    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.strip()
-    d = json.loads(out)
-    peak, kind = load_peaks()
-    d["line_bytes_frac_of_%s_hbm" % kind] = round(d["line_bytes_per_s"] / 1e9 / peak, 4)
-    d["find_hit_ceiling_ops_per_s"] = d["random_lines_per_s"]
-    print(json.dumps(d))
-
-
-def run_copy_probe():
-    """Host <-> device copy rates behind the end-to-end find: 256 MiB between
-    pinned host memory and HBM, best of 5, one direction on 1/2/4/8 streams,
-    both directions at once, and host -> device in chunks of 4/16/64 MiB."""
-    import torch
-    nbytes = 256 << 20
-    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
-    h2 = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
-    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
-    d2 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
-    streams = [torch.cuda.Stream() for _ in range(8)]
-
-    def timed(fn, reps=5):
-        best = None
-        for _ in range(reps):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            fn()
-            torch.cuda.synchronize()
-            dt = time.perf_counter() - t0
-            best = dt if best is None else min(best, dt)
-        return round(nbytes / best / 1e9, 1)
-
-    def split(dst, src, k, chunk=None):
-        part = chunk or nbytes // k
-        for j, a in enumerate(range(0, nbytes, part)):
-            with torch.cuda.stream(streams[j % k]):
-                dst[a:a + part].copy_(src[a:a + part], non_blocking=True)
-
-    out = {"bytes": nbytes}
-    for k in (1, 2, 4, 8):
-        out["h2d_gbs_%d_streams" % k] = timed(lambda: split(d, h, k))
-        out["d2h_gbs_%d_streams" % k] = timed(lambda: split(h, d, k))
-
-    def both():
-        with torch.cuda.stream(streams[0]):
-            d.copy_(h, non_blocking=True)
-        with torch.cuda.stream(streams[1]):
-            h2.copy_(d2, non_blocking=True)
-    out["both_directions_gbs_each"] = timed(both)
-    for mib in (4, 16, 64):
-        out["h2d_gbs_%dmib_chunks" % mib] = timed(lambda: split(d, h, 1, mib << 20))
-    print(json.dumps(out))
-
-
 def set_table_bytes(S, bucket_bytes=128):
     """Device bytes of a set's subtables (from the members' slot capacities)."""
     _, caps = S.sizes()
@@ -377,57 +326,16 @@ def set_table_bytes(S, bucket_bytes=128):
     return int(caps.sum()) // per_bucket * bucket_bytes
 
 
-def run_set_profile(args):
-    """One table set (the multi-table workload with args.mt_tables tables),
-    args.mt_rounds rounds of dyc_set_apply without graphs, each timed with
-    CUDA events: the command the set-path ncu captures run under."""
-    import torch
-
-    import databases_gpu_gb300 as dg
-    from databases_gpu_gb300.workloads import MultiTableWorkload
-    w = MultiTableWorkload(args.mt_tables, seed=10327, device="cuda")
-    S = dg.DyCuckooSet(w.sizes.numpy())
-    for t in range(w.ntables):
-        k, v = w.preload(t)
-        S.table(t).insert(k, v, new_keys=True, unique=True)
-    dg.pool_reserve(2 * set_table_bytes(S))  # growth headroom, mapped before the rounds
-    n = w.n_ops
-    out = torch.empty(n, dtype=torch.int32, device="cuda")
-    bits = torch.empty((n + 31) // 32, dtype=torch.int32, device="cuda")
-    s = torch.cuda.current_stream()
-    for r in range(args.mt_rounds):
-        ops, keys, vals = w.round()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record(s)
-        S.apply(w.offsets, ops, keys, vals, out=out, bits=bits, h_offsets=w.offsets_host, stream=s,
-                graph=args.set_graph)
-        e1.record(s)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        st = S.stats()
-        print(json.dumps({"round": r, "ms": round(ms, 3), "ops": n,
-                          "mops": round(n / ms / 1e3, 1), "tables": w.ntables,
-                          "resizes_up": st["resizes_up"], "resizes_down": st["resizes_down"],
-                          "split_phases": st["split_phases"]}))
-    S.close()
-
-
-def run_serve_profile(args):
-    """Serving steps without the server's threads: 64 u64/u32 tenant tables
-    (2^16..2^24 keys, preloaded), then args.serve_steps steps of about
-    args.serve_step_ops ops each, made of log-uniform 32..65536-op requests on
-    Zipf(0.9) tenants (70 % find on j < 2^17, 20 % insert on j < 2^25, 10 %
-    erase on j < 2^17), applied from fixed staging buffers through
-    dyc_set_apply with graph replay, as the server's executor does. Each step
-    is timed on the host around the call (which returns after its host read).
-    The command the serving-step ncu captures run under."""
-    import torch
-
-    import databases_gpu_gb300 as dg
+def run_serve_steps(args, dev, torch, dg):
+    """Serving steps without the server's threads (the executor's work
+    alone): 64 u64/u32 tenant tables (2^16..2^24 keys, preloaded), then
+    args.serve_steps steps of about args.serve_step_ops ops each, made of
+    log-uniform 32..65536-op requests on Zipf(0.9) tenants (70 % find on
+    j < 2^17, 20 % insert on j < 2^25, 10 % erase on j < 2^17), applied from
+    fixed staging buffers through dyc_set_apply with graph replay, as the
+    server's executor does. Each step is timed on the host around the call
+    (which returns after its host read): the fixed cost of a serving step."""
     from databases_gpu_gb300.workloads import splitmix64
-    dev = torch.device("cuda", 0)
     rng = np.random.default_rng(10327)
     nt = 64
     sizes = np.round(2.0 ** (16 + 8 * rng.random(nt))).astype(np.int64)
@@ -476,13 +384,17 @@ def run_serve_profile(args):
     a = np.array([r[0] for r in rows[3:]])
     rz = np.array([r[2] for r in rows[3:]])
     plain = a[rz == 0] if (rz == 0).any() else a
-    print(json.dumps({"steps": len(rows), "ops_per_step": target,
-                      "step_ms_median": round(float(np.median(a)), 4),
-                      "no_resize_step_ms_median": round(float(np.median(plain)), 4),
-                      "resize_steps": int((rz > 0).sum()),
-                      "split_steps": int(sum(r[3] for r in rows)),
-                      "no_resize_mops": round(target / float(np.median(plain)) / 1e3, 1)}))
     S.close()
+    return {"workload": "serving steps without the server threads: 64 u64/u32 tenants, "
+                        "~%d ops per step from 32..65536-op requests (70/20/10), graph replay"
+                        % target,
+            "steps": len(rows), "ops_per_step": target,
+            "step_ms_median": round(float(np.median(a)), 4),
+            "no_resize_step_ms_median": round(float(np.median(plain)), 4),
+            "resize_steps": int((rz > 0).sum()),
+            "split_steps": int(sum(r[3] for r in rows)),
+            "no_resize_mops": round(target / float(np.median(plain)) / 1e3, 1),
+            "api": "dyc_set_apply (graph replay, fixed staging buffers)"}
 
 
 def build_serve_load():
@@ -685,7 +597,10 @@ def run_multi_table(args, dev, torch, dg):
 def run_tuned_set(args, w, dev, torch, dg):
     """The same workload on a set configured by the tuner: per size class the
     bucket size, subtable count and eviction bound that ran the class's own
-    mixed batches fastest, then the blocks-per-SM cap with the fastest round."""
+    mixed batches fastest, then the blocks-per-SM cap with the fastest round.
+    The plan is then checked against an untuned set on the same held-out
+    rounds (alternating, both graph-replayed) and kept only if it wins by
+    more than 3 %; both rates are reported."""
     from databases_gpu_gb300 import tune
     sizes, batches = w.sizes.numpy(), w.batch.numpy()
     t0 = time.perf_counter()
@@ -693,40 +608,92 @@ def run_tuned_set(args, w, dev, torch, dg):
     sb, dsub, ev = tune.plan_set(sizes, batches, results)
     T = dg.DyCuckooSet(sizes, bucket_bytes=sb, num_subtables=dsub, device=dev.index or 0)
     T.configure(0, ev)
+    U = dg.DyCuckooSet(sizes, device=dev.index or 0)  # the untuned set
     for t in range(w.ntables):
         k, v = w.preload(t)
         T.table(t).insert(k, v, new_keys=True, unique=True)
+        U.table(t).insert(k, v, new_keys=True, unique=True)
+    dg.pool_reserve(2 * (set_table_bytes(T, sb) + set_table_bytes(U)), device=dev.index or 0)
     n = w.n_ops
-    out = torch.empty(n, dtype=torch.int32, device=dev)
-    bits = torch.empty((n + 31) // 32, dtype=torch.int32, device=dev)
+    outs = [torch.empty(n, dtype=torch.int32, device=dev) for _ in range(2)]
+    bitss = [torch.empty((n + 31) // 32, dtype=torch.int32, device=dev) for _ in range(2)]
     stream = torch.cuda.current_stream()
 
-    def run_round(cap, graph=False):
-        T.configure(cap, None)
-        ops, keys, vals = w.round()
+    def run_round(S, i, data, cap=None, graph=False):
+        if cap is not None:
+            S.configure(cap, None)
+        ops, keys, vals = data
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
-        T.apply(w.offsets, ops, keys, vals, out=out, bits=bits, h_offsets=w.offsets_host,
-                graph=graph, stream=stream)
+        S.apply(w.offsets, ops, keys, vals, out=outs[i], bits=bitss[i],
+                h_offsets=w.offsets_host, graph=graph, stream=stream)
         e1.record(stream)
         torch.cuda.synchronize()
         return e0.elapsed_time(e1)
 
-    run_round(0)  # scratch
-    cap = tune.tune_launch(run_round)
+    def tuning_round(c):
+        # the untuned twin gets every round too, so both sets hold the same
+        # keys and values and their held-out results must agree op for op
+        data = w.round()
+        ms = run_round(T, 0, data, cap=c)
+        run_round(U, 1, data)
+        return ms
+
+    tuning_round(0)  # scratch
+    cap = tune.tune_launch(tuning_round)
     tune_s = time.perf_counter() - t0
     T.configure(cap, None)
-    for _ in range(2):  # graph capture
-        run_round(cap, graph=True)
-    ms = sorted(run_round(cap, graph=True) for _ in range(args.mt_rounds))
+    for _ in range(2):  # graph capture on both sets
+        data = w.round()
+        run_round(T, 0, data, graph=True)
+        run_round(U, 1, data, graph=True)
+    held = [w.round() for _ in range(args.mt_rounds)]
+    mism = []
+
+    def plan(i):
+        return run_round(T, 0, held[i], graph=True)
+
+    def base(i):
+        ms = run_round(U, 1, held[i], graph=True)
+        mism.append(int((outs[0] != outs[1]).sum()) + int((bitss[0] != bitss[1]).sum()))
+        return ms
+    kept, pm, bm = tune.validate(plan, base, rounds=len(held))
     T.close()
-    return {"mops": round(n * len(ms) / (sum(ms) / 1e3) / 1e6, 1),
-            "round_ms_p50": round(ms[len(ms) // 2], 3), "bucket_bytes": int(sb),
-            "blocks_per_sm": int(cap), "tune_seconds": round(tune_s, 1),
+    U.close()
+    return {"plan_mops": round(n / pm / 1e3, 1), "untuned_mops": round(n / bm / 1e3, 1),
+            "kept": bool(kept), "mops": round(n / (pm if kept else bm) / 1e3, 1),
+            "plan_round_ms_p50": round(pm, 3), "untuned_round_ms_p50": round(bm, 3),
+            "held_out_rounds": len(held), "result_mismatches_plan_vs_untuned": sum(mism),
+            "bucket_bytes": int(sb), "blocks_per_sm": int(cap), "tune_seconds": round(tune_s, 1),
             "classes": {int(c): {"batch": r.batch, **r.best, "class_mops": r.mops}
                         for c, r in results.items()}}
+
+
+def copy_only_seconds(qh, outh, bitsh, Q, dev, torch, chunk=1 << 22, reps=3):
+    """dyc_find_host's transfers alone: per 4M-key chunk the key upload and
+    the value and hit-bit downloads, chunk c on stream c % 3 with its own
+    device buffers (as the library pipelines them), best of `reps`."""
+    streams = [torch.cuda.Stream(dev) for _ in range(3)]
+    bufs = [(torch.empty(chunk, dtype=torch.int32, device=dev),
+             torch.empty(chunk, dtype=torch.int32, device=dev),
+             torch.empty(chunk // 32 + 1, dtype=torch.int32, device=dev)) for _ in range(3)]
+    best = None
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for ci, off in enumerate(range(0, Q, chunk)):
+            m = min(chunk, Q - off)
+            dk, dv, db = bufs[ci % 3]
+            with torch.cuda.stream(streams[ci % 3]):
+                dk[:m].copy_(qh[off:off + m], non_blocking=True)
+                outh[off:off + m].copy_(dv[:m], non_blocking=True)
+                bitsh[off // 32:(off + m) // 32].copy_(db[:m // 32], non_blocking=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return best
 
 
 def head_mops(results):
@@ -759,21 +726,17 @@ def main():
     ap.add_argument("--skip-reference-gpu", action="store_true",
                     help="skip timing the reference's own GPU kernels")
     ap.add_argument("--skip-variants", action="store_true")
-    ap.add_argument("--line-probe", action="store_true",
-                    help="measure the random 128-byte line ceiling of this GPU and exit")
-    ap.add_argument("--copy-probe", action="store_true",
-                    help="measure host <-> device copy rates (pinned memory) and exit")
-    ap.add_argument("--set-profile", action="store_true",
-                    help="run --mt-rounds untimed-graph rounds of the multi-table set and exit")
     ap.add_argument("--skip-stream", action="store_true",
                     help="skip the dynamic resize stream workload")
     ap.add_argument("--skip-multi", action="store_true",
                     help="skip the batched multi-table workload")
-    ap.add_argument("--skip-serve", action="store_true", help="skip the serving loop")
-    ap.add_argument("--set-graph", action="store_true",
-                    help="--set-profile rounds through graph replay")
-    ap.add_argument("--serve-profile", action="store_true",
-                    help="only serving-like set steps (the serving-step profiling command)")
+    ap.add_argument("--skip-serve", action="store_true",
+                    help="skip the serving loop and the serving-step workload")
+    ap.add_argument("--only", default=None,
+                    choices=["find", "stream", "multi", "serve", "serve-steps"],
+                    help="run one workload: find (the headline line with its variants, ops "
+                         "and baselines, no other workloads) or one of the others alone, "
+                         "printing its own JSON object")
     ap.add_argument("--serve-steps", type=int, default=300)
     ap.add_argument("--serve-step-ops", type=int, default=363000)
     ap.add_argument("--serve-rate", type=float, default=2e5)
@@ -790,14 +753,6 @@ def main():
                     help="query mixes to time; the first is the headline")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.line_probe:
-        return run_line_probe()
-    if args.copy_probe:
-        return run_copy_probe()
-    if args.set_profile:
-        return run_set_profile(args)
-    if args.serve_profile:
-        return run_serve_profile(args)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -808,6 +763,17 @@ def main():
     ws, rank, local = dist_setup()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.only not in (None, "find"):
+        run = {"stream": lambda: run_resize_stream(args, dev, torch, dg),
+               "multi": lambda: run_multi_table(args, dev, torch, dg),
+               "serve": lambda: run_serving(args),
+               "serve-steps": lambda: run_serve_steps(args, dev, torch, dg)}[args.only]
+        res = run()
+        if rank == 0:
+            print(json.dumps({"workload_only": args.only, **res}))
+        return
+    if args.only == "find":
+        args.skip_stream = args.skip_multi = args.skip_serve = True
     N = 1 << args.log2_keys
     Q = 1 << args.log2_batch
     gen = torch.Generator(device=dev)
@@ -891,6 +857,37 @@ def main():
                         "alg_bytes_per_op": round(bytes_per_op, 2),
                         "achieved_gbs": round(achieved, 1), "frac": round(achieved / peak, 4),
                         "mismatches": bad_v + bad_h}
+        if mix == "uniform100":
+            head_qs = qs
+
+    # ---- the same keys in a table of 32-byte buckets (4 slots, no
+    # fingerprint word), the same uniform-hit batches: a probe reads one
+    # 32-byte sector instead of a 128-byte line, yet the find rate is the
+    # same when the GPU's random-access rate, not bytes, is the limit
+    if not args.skip_variants and args.bucket_bytes != 32 and ws == 1:
+        t32 = dg.DyCuckoo(int(N / 0.9), bucket_bytes=32, auto_resize=False,
+                          max_evictions=args.max_evictions, device=local)
+        t32.insert(keys, vals, unique=True, new_keys=True)
+        for w in range(args.warmup):
+            t32.find(head_qs[w % 2][0], out=out, hit_bits=bits, stream=stream)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for s in range(args.steps):
+            t32.find(head_qs[s % 2][0], out=out, hit_bits=bits, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        q, expv, hit = head_qs[(args.steps - 1) % 2]
+        results["uniform100_bucket32"] = {
+            "mops": round(args.steps * Q / (ms / 1e3) / 1e6, 1),
+            "ms_per_batch": round(ms / args.steps, 4), "bucket_bytes": 32,
+            "load_factor": round(t32.size / t32.capacity, 4),
+            "mismatches": int((out != expv).sum())}
+        t32.close()
+        del t32
+        torch.cuda.empty_cache()
 
     # ---- insert / erase on the same table (after the finds): erase 2^26
     # present keys, then upsert them back (dedup + update-or-place path)
@@ -929,6 +926,23 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
         ops["mixed_50f_30u_20e_mops"] = round(Q / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
+
+        def op_roofline(mops, bytes_per_op):
+            """The random-sector model's bytes per op (32 B per bucket read or
+            written, plus the op's key and value) at the measured rate."""
+            ach = mops * 1e6 * bytes_per_op / 1e9
+            return {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(ach / peak, 4), "alg_bytes_per_op": bytes_per_op,
+                    "peak_kind": peak_kind}
+        ops["roofline"] = {
+            "erase": op_roofline(ops["erase_mops"], 2 * SECTOR + 4),
+            "upsert": op_roofline(ops["upsert_mops"], 2 * SECTOR + 8),
+            "bulk_insert": op_roofline(ops["bulk_insert_mops"], 2 * SECTOR + 8),
+            # 50 % finds of present keys (40 B), 30 % upserts (72 B), 20 % erases (68 B)
+            "mixed_50f_30u_20e": op_roofline(ops["mixed_50f_30u_20e_mops"],
+                                             round(0.5 * (SECTOR + 8) + 0.3 * (2 * SECTOR + 8) +
+                                                   0.2 * (2 * SECTOR + 4), 2)),
+        }
         mst = t.stats()
         mbad = int((mout != vals[perm]).sum())  # every key was present: its old value
         n_er = int((mo == 2).sum())
@@ -981,6 +995,7 @@ def main():
         workloads["multi_table"] = run_multi_table(args, dev, torch, dg)
     if not args.skip_serve and not args.skip_variants and ws == 1:
         workloads["serving"] = run_serving(args)
+        workloads["serving_steps"] = run_serve_steps(args, dev, torch, dg)
 
     # ---- e2e: host buffers through the C ABI (dyc_find_host), pinned memory
     q0 = qs_e2e = batch("uniform100")
@@ -1002,6 +1017,7 @@ def main():
     e2e_s = barrier_max(time.perf_counter() - t0, ws)
     e2e_bad = int((outh.to(dev) != qs_e2e[1]).sum())
     e2e_mops = ws * e2e_steps * Q / e2e_s / 1e6
+    copy_mops = Q / copy_only_seconds(qh, outh, bitsh, Q, dev, torch) / 1e6
 
     # ---- the reference's own GPU kernels on the same table keys and batches
     ref_gpu = None
@@ -1043,7 +1059,10 @@ def main():
         "config": workload_config(args, round(lf, 4)),
         "e2e": {"value": round(e2e_mops, 1), "unit": "Mops/s",
                 "h2d_bytes_per_step": Q * 4, "d2h_bytes_per_step": Q * 4 + Q // 8,
-                "api": "dyc_find_host (pinned host buffers)", "mismatches": e2e_bad},
+                "api": "dyc_find_host (pinned host buffers)", "mismatches": e2e_bad,
+                "copy_only_mops": round(copy_mops, 1),
+                "copy_only": "the same transfers without the find kernel (same chunks, "
+                             "three streams, pinned buffers): the path's copy ceiling"},
         "roofline": {"bound": "hbm", "achieved": head["achieved_gbs"], "peak": peak,
                      "unit": "GB/s", "frac": head["frac"], "traffic": load_traffic(args),
                      "peak_kind": peak_kind,

@@ -470,9 +470,12 @@ __global__ void __launch_bounds__(256) k_dedup(const __grid_constant__ Scratch S
 // (32/64-byte buckets carry no metadata and always probe both on a miss).
 // Writes the value (0 on a miss) and one hit bit per key. (Queueing second
 // probes per warp, or prefetching the next tile's keys, measured slower.)
+// Five resident blocks per SM for 4-byte keys (48 registers, a 16-byte
+// spill): +1.7 % on uniform hits at 2^28 keys, 10 %-hit finds unchanged;
+// six blocks and larger or smaller tiles per block measured no better.
 // ----------------------------------------------------------------------------
 template <int KB, int SB>
-__global__ void __launch_bounds__(256) k_find(const __grid_constant__ Desc D,
+__global__ void __launch_bounds__(256, KB == 4 ? 5 : 1) k_find(const __grid_constant__ Desc D,
                                               const void *__restrict__ keys,
                                               void *__restrict__ vals, uint32_t vb,
                                               uint32_t *__restrict__ hits, uint64_t n) {

@@ -16,7 +16,10 @@ table's device bytes. A set uses one bucket size (its kernels are compiled
 per bucket size), so `plan_set` takes the bucket size that wins for most of
 the set's ops and, with it, each class's best subtable count and eviction
 bound; `tune_launch` then picks the set's blocks-per-SM cap by timing whole
-rounds. Everything runs through the public API, on the device given.
+rounds. A class is tuned on one table in isolation, which is not how a set
+round runs, so `validate` finally runs the tuned set and an untuned one on
+the same held-out rounds and keeps the plan only if it wins. Everything runs
+through the public API, on the device given.
 """
 from __future__ import annotations
 
@@ -163,3 +166,17 @@ def tune_launch(run_round, caps=(0, 2, 4, 8), repeats: int = 2, margin: float = 
     if 0 in times and times[best] > times[0] * (1.0 - margin):
         return 0
     return best
+
+
+def validate(run_plan, run_base, rounds: int = 4, margin: float = 0.03):
+    """Held-out A/B of a tuned set against the untuned one: run_plan(i) and
+    run_base(i) run held-out round i (the same ops for both) on their set and
+    return its time; they alternate, so drifting clocks hit both. The plan is
+    kept only when its median round is faster than the untuned median by
+    more than `margin`. Returns (kept, plan_ms, base_ms)."""
+    plan, base = [], []
+    for i in range(rounds):
+        plan.append(run_plan(i))
+        base.append(run_base(i))
+    pm, bm = float(np.median(plan)), float(np.median(base))
+    return pm < bm * (1.0 - margin), pm, bm
