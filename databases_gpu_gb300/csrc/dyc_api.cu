@@ -213,7 +213,8 @@ dyc_status ensure_scratch(dyc_table *t, uint64_t n) {
     const size_t dedup_bytes = (size_t)cap * 8;
     const size_t idx_bytes = t->kb == 8 ? (size_t)cap * 4 : 0;
     const size_t list_bytes = (size_t)n * t->slot_bytes;
-    const size_t need = dedup_bytes + idx_bytes + 2 * list_bytes + 3 * 256;
+    const size_t win_bytes = (size_t)(n / 32 + 1) * 4;
+    const size_t need = dedup_bytes + idx_bytes + 2 * list_bytes + win_bytes + 4 * 256;
     if (t->scratch && t->scratch_bytes >= need && t->S.list_cap >= n && t->S.dedup_cap >= cap)
         return DYC_OK;
     if (t->scratch) {
@@ -235,6 +236,7 @@ dyc_status ensure_scratch(dyc_table *t, uint64_t n) {
     t->S.list_a = carve(list_bytes);
     t->S.list_b = carve(list_bytes);
     t->S.list_cap = n;
+    t->S.winbits = (uint32_t *)carve(win_bytes);
     return DYC_OK;
 }
 

@@ -165,6 +165,11 @@ template <> struct SlotT<4> {
     __device__ static __forceinline__ bool same(S a, S b) { return a == b; }
     __device__ static __forceinline__ S cas(S *p, S cmp, S v) { return atomicCAS(p, cmp, v); }
     __device__ static __forceinline__ S exch(S *p, S v) { return atomicExch(p, v); }
+    // plain store of a whole slot: for a slot no other thread of the kernel
+    // can write (it holds a key the batch names once)
+    __device__ static __forceinline__ void store(S *p, S v) {
+        asm volatile("st.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+    }
     __device__ static __forceinline__ void from_words(const uint32_t *w, S &s) {
         s = (S)w[0] | ((S)w[1] << 32);
     }
@@ -208,6 +213,9 @@ template <> struct SlotT<8> {
             : "l"(v.lo), "l"(v.hi), "l"(p)
             : "memory");
         return r;
+    }
+    __device__ static __forceinline__ void store(S *p, S v) {
+        asm volatile("st.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(v.lo), "l"(v.hi) : "memory");
     }
     __device__ static __forceinline__ void from_words(const uint32_t *w, S &s) {
         s.lo = (unsigned long long)w[0] | ((unsigned long long)w[1] << 32);

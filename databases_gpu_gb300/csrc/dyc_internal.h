@@ -64,6 +64,10 @@ struct Scratch {
     void *list_a;           // pending entries (slots)
     void *list_b;           // overflow entries (slots)
     uint64_t list_cap;      // entries per list
+    // one bit per op of the chunk, set for the op its key's dedup cell names
+    // (filled from the dedup table after the claims); null: the winner is
+    // looked up in the dedup table by each op
+    uint32_t *winbits;
 };
 
 // Scratch of one mixed batch of at most `cap_ops` ops. The multi-table

@@ -412,6 +412,7 @@ template <> struct Dedup<4> {
         }
     }
     __device__ static __forceinline__ bool winner(const Scratch &S, uint32_t k, uint32_t i) {
+        if (S.winbits) return (S.winbits[i >> 5] >> (i & 31)) & 1u;
         const unsigned long long *tab = (const unsigned long long *)S.dedup;
         const uint64_t mask = S.dedup_cap - 1;
         uint64_t h = mix32(k) & mask;
@@ -441,6 +442,7 @@ template <> struct Dedup<8> {
         }
     }
     __device__ static __forceinline__ bool winner(const Scratch &S, uint64_t k, uint32_t i) {
+        if (S.winbits) return (S.winbits[i >> 5] >> (i & 31)) & 1u;
         const unsigned long long *tab = (const unsigned long long *)S.dedup;
         const uint64_t mask = S.dedup_cap - 1;
         uint64_t h = mix32(fold(k) ^ (uint32_t)(k >> 32)) & mask;
@@ -461,6 +463,25 @@ __global__ void __launch_bounds__(256) k_dedup(const __grid_constant__ Scratch S
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         typename SlotT<KB>::K k = load_key<KB>(keys, i);
         if (k != 0) Dedup<KB>::claim(S, k, (uint32_t)i, mode);
+    }
+}
+
+// After the claims: one pass over the dedup cells (sequential reads) sets
+// the winner bit of the op each used cell names (L2 atomics into a bitmap of
+// n bits), so the place and erase kernels read their op's bit coalesced
+// instead of probing the dedup table at random once more (the table of a
+// 4M-op chunk is 64 MB; those probes cost DRAM accesses beside the bucket
+// reads).
+template <int KB>
+__global__ void __launch_bounds__(256) k_dedup_winners(const __grid_constant__ Scratch S) {
+    const unsigned long long *tab = (const unsigned long long *)S.dedup;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t h = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; h < S.dedup_cap;
+         h += stride) {
+        const unsigned long long c = tab[h];
+        if (c == 0ull) continue;
+        const uint32_t i = KB == 4 ? (uint32_t)c : S.dedup_idx[h];
+        atomicOr(&S.winbits[i >> 5], 1u << (i & 31));
     }
 }
 
@@ -557,12 +578,17 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
             act && !found1 && ((!new_keys && (!Gm::kMeta || r1.overflow)) || r1.empty == 0u);
         KvOut r2{-1, 0ull, false, 0u};
         if (__any_sync(kFull, check2)) r2 = place_probe<KB, SB>(p2, k, check2, p.second, D.d, stage);
+        // An update rewrites the key's own slot with a plain store: the keys
+        // of the kernel are distinct (dedup, or the caller's promise) and
+        // its other writes only claim empty slots, so nothing else writes
+        // that slot while the kernel runs (a store does not wait for an L2
+        // round trip as an exchange does).
         bool pend = false;
         if (found1) {
-            T::exch(slot_ptr<KB, SB>(p1, r1.match), e);
+            T::store(slot_ptr<KB, SB>(p1, r1.match), e);
             ++n_upd;
         } else if (check2 && !new_keys && r2.match >= 0) {
-            T::exch(slot_ptr<KB, SB>(p2, r2.match), e);
+            T::store(slot_ptr<KB, SB>(p2, r2.match), e);
             ++n_upd;
         } else if (act) {
             bool ok = claim_empty<KB, SB>(p1, r1.empty, e);
@@ -930,20 +956,23 @@ __global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D,
         const Pair p = pair_of(hk, D.d);
         char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
         const KvOut r1 = kv_probe<KB, SB, 2>(p1, k, act, stage);
+        // A found key's slot is emptied with a plain store, as the reference
+        // does (cuckoo.cu:551): the kernel's keys are distinct (dedup, or the
+        // caller's promise) and nothing else runs on the table, so no other
+        // thread writes that slot; the store does not wait on an L2 round
+        // trip as a compare-and-swap does.
         bool erased = false;
         if (act && r1.match >= 0) {
-            const typename T::S cur = T::make(k, r1.value);
-            const typename T::S old = T::cas(slot_ptr<KB, SB>(p1, r1.match), cur, T::empty());
-            erased = T::same(old, cur);
+            T::store(slot_ptr<KB, SB>(p1, r1.match), T::empty());
+            erased = true;
         }
         const bool need2 = act && r1.match < 0 && (!Gm::kMeta || r1.overflow);
         if (__any_sync(kFull, need2)) {
             char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
             const KvOut r2 = kv_probe<KB, SB, 2>(p2, k, need2, stage);
             if (need2 && r2.match >= 0) {
-                const typename T::S cur = T::make(k, r2.value);
-                const typename T::S old = T::cas(slot_ptr<KB, SB>(p2, r2.match), cur, T::empty());
-                erased = T::same(old, cur);
+                T::store(slot_ptr<KB, SB>(p2, r2.match), T::empty());
+                erased = true;
             }
         }
         const unsigned m = __ballot_sync(kFull, erased);

@@ -98,8 +98,16 @@ template <int KB>
 cudaError_t Ops<KB>::dedup(const LaunchCtx &L, const Scratch &S, const void *keys, uint64_t n,
                            DedupMode mode) {
     if (n == 0) return cudaSuccess;
+    if (S.winbits) {
+        const cudaError_t e = cudaMemsetAsync(S.winbits, 0, (size_t)(n / 32 + 1) * 4, L.stream);
+        if (e != cudaSuccess) return e;
+    }
     auto k = k_dedup<KB>;
     k<<<grid_for((const void *)k, L, n), 256, 0, L.stream>>>(S, keys, n, mode);
+    if (S.winbits) {
+        auto w = k_dedup_winners<KB>;
+        w<<<grid_for((const void *)w, L, S.dedup_cap), 256, 0, L.stream>>>(S);
+    }
     return cudaGetLastError();
 }
 

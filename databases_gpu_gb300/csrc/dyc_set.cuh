@@ -122,20 +122,20 @@ __device__ __forceinline__ bool set_erase_warp(const Desc *__restrict__ descs, u
     const Pair p = pair_of(hk, D.d);
     char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
     const KvOut r1 = kv_probe<KB, SB, 2>(p1, k, act, stage);
+    // plain stores, as in k_erase: the erase and upsert lists name distinct
+    // keys, so no other thread of the pass writes a found key's slot
     bool erased = false;
     if (act && r1.match >= 0) {
-        const typename T::S cur = T::make(k, r1.value);
-        const typename T::S old = T::cas(slot_ptr<KB, SB>(p1, r1.match), cur, T::empty());
-        erased = T::same(old, cur);
+        T::store(slot_ptr<KB, SB>(p1, r1.match), T::empty());
+        erased = true;
     }
     const bool need2 = act && r1.match < 0 && (!Gm::kMeta || r1.overflow);
     if (__any_sync(kFull, need2)) {
         char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
         const KvOut r2 = kv_probe<KB, SB, 2>(p2, k, need2, stage);
         if (need2 && r2.match >= 0) {
-            const typename T::S cur = T::make(k, r2.value);
-            const typename T::S old = T::cas(slot_ptr<KB, SB>(p2, r2.match), cur, T::empty());
-            erased = T::same(old, cur);
+            T::store(slot_ptr<KB, SB>(p2, r2.match), T::empty());
+            erased = true;
         }
     }
     warp_size_add(tctr, tb, erased, -1);
@@ -181,11 +181,11 @@ __device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs, u
     KvOut r2{-1, 0ull, false, 0u};
     if (__any_sync(kFull, check2)) r2 = place_probe<KB, SB>(p2, k, check2, p.second, D.d, stage);
     bool pend = false, ins = false;
-    if (found1) {
-        T::exch(slot_ptr<KB, SB>(p1, r1.match), e);
+    if (found1) {  // the key's own slot: a plain store (distinct keys, as in k_place)
+        T::store(slot_ptr<KB, SB>(p1, r1.match), e);
         ++n_upd;
     } else if (check2 && r2.match >= 0) {
-        T::exch(slot_ptr<KB, SB>(p2, r2.match), e);
+        T::store(slot_ptr<KB, SB>(p2, r2.match), e);
         ++n_upd;
     } else if (act) {
         bool ok = claim_empty<KB, SB>(p1, r1.empty, e);

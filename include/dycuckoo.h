@@ -91,7 +91,9 @@ typedef struct dyc_config {
 } dyc_config;
 
 /* Per-call flags. */
-#define DYC_FLAG_UNIQUE 1u    /* caller promises no key repeats in this batch */
+#define DYC_FLAG_UNIQUE 1u    /* caller promises no key repeats in this batch (the batch
+                                 dedup is skipped; a batch that repeats a key anyway may
+                                 count it twice in the erased / updated counts) */
 #define DYC_FLAG_NEW_KEYS 2u  /* insert: caller promises no key of the batch is in the table */
 #define DYC_FLAG_NO_RESIZE 4u /* skip the load-factor policy for this call */
 
