@@ -30,7 +30,8 @@ class DycConfig(C.Structure):
         ("lower_load", C.c_double),
         ("min_downsize_capacity", C.c_uint64),
         ("device", C.c_int32),
-        ("reserved", C.c_uint32 * 7),
+        ("l2_resident", C.c_uint32),
+        ("reserved", C.c_uint32 * 6),
     ]
 
 

@@ -164,6 +164,7 @@ struct dyc_table {
     void *pipe_buf[3] = {nullptr, nullptr, nullptr};
     size_t pipe_bytes = 0;
     uint64_t size = 0, capacity = 0;
+    uint64_t l2_bytes = 0;  // the device's L2 (the residency rule of cfg.l2_resident)
     dyc_op_stats last{};
     // entries a failed call could not place (slot images, held_n of them);
     // not in the device size counter; the next call places them first
@@ -172,6 +173,21 @@ struct dyc_table {
 };
 
 namespace {
+
+// Desc::l2_keep from the table's current subtables (cfg.l2_resident: 0 when
+// they take at most 1.5x the L2, 1 never, 2 always); called whenever they
+// change. Measured on GB300 (2^26- and 2^20-key find batches): tables of up
+// to half the L2 stay there under any policy (54.7 G finds/s either way);
+// at 76 MB the policy gains 0.8 %, at 152 MB 0.6 % (2^26 batches) to 4.5 %
+// (2^20 batches); at 2.4 GB it changes nothing.
+bool l2_keep_rule(uint64_t bytes, uint64_t l2_bytes) { return 2 * bytes <= 3 * l2_bytes; }
+
+void refresh_l2(dyc_table *t) {
+    uint64_t bytes = 0;
+    for (uint32_t i = 0; i < t->D.d; ++i) bytes += (uint64_t)t->D.nb[i] * t->sb;
+    const uint32_t mode = t->cfg.l2_resident;
+    t->D.l2_keep = (mode == 2u || (mode == 0u && l2_keep_rule(bytes, t->l2_bytes))) ? 1u : 0u;
+}
 
 dyc_status set_device(dyc_table *t) {
     int cur = -1;
@@ -347,6 +363,7 @@ dyc_status resize_up_impl(dyc_table *t, cudaStream_t s) {
     t->D.magic[ti] = dyc::fastmod_magic(nnb);
     CK(cudaFreeAsync(old, s));
     t->capacity += (uint64_t)onb * t->slots;
+    refresh_l2(t);
     t->last.resizes_up++;
     return DYC_OK;
 }
@@ -375,6 +392,7 @@ dyc_status resize_up_prepare(dyc_table *t, cudaStream_t s, dyc::ResizeJob *job, 
     t->D.nb[ti] = nnb;
     t->D.magic[ti] = magic;
     t->capacity += (uint64_t)onb * t->slots;
+    refresh_l2(t);
     t->last.resizes_up++;
     return DYC_OK;
 }
@@ -576,6 +594,7 @@ dyc_status resize_down_impl(dyc_table *t, cudaStream_t s) {
     t->D.nb[ti] = nnb;
     t->D.magic[ti] = dyc::fastmod_magic(nnb);
     t->capacity -= (uint64_t)(onb - nnb) * t->slots;
+    refresh_l2(t);
     CK(cudaFreeAsync(old, s));
     t->last.resizes_down++;
     const dyc_status st = drain(t, s, la, &t->d_ctr->pending, lb, &t->d_ctr->overflow, list_cap,
@@ -598,6 +617,7 @@ bool valid_config(const dyc_config *c, char *why, size_t n) {
         return snprintf(why, n, "max_evictions must be 1..100000"), false;
     if (!(c->upper_load > 0.0 && c->upper_load <= 1.0) || !(c->lower_load >= 0.0 && c->lower_load < c->upper_load))
         return snprintf(why, n, "need 0 <= lower_load < upper_load <= 1"), false;
+    if (c->l2_resident > 2) return snprintf(why, n, "l2_resident must be 0, 1 or 2"), false;
     return true;
 }
 
@@ -668,7 +688,10 @@ dyc_status create_impl(const dyc_config *cfg, Counters *ext_d, Counters *ext_h, 
         cudaError_t e = cudaSetDevice(t->device);
         if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "cudaSetDevice(%d): %s", t->device, cudaGetErrorString(e)));
         e = cudaDeviceGetAttribute(&t->sms, cudaDevAttrMultiProcessorCount, t->device);
+        int l2 = 0;
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, t->device);
         if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "device attribute: %s", cudaGetErrorString(e)));
+        t->l2_bytes = (uint64_t)l2;
     }
     // hashAPI::hashAPI sizing (api.cpp:47-54) with this table's slots/bucket
     const uint64_t per = (uint64_t)cfg->num_subtables * t->slots;
@@ -689,6 +712,7 @@ dyc_status create_impl(const dyc_config *cfg, Counters *ext_d, Counters *ext_h, 
         t->D.magic[i] = dyc::fastmod_magic(nb);
         t->capacity += (uint64_t)nb * t->slots;
     }
+    refresh_l2(t);
     cudaError_t e = cudaSuccess;
     if (ext_d) {
         t->owns_ctr = false;
@@ -1735,6 +1759,19 @@ dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_
         if (num_subtables) c.num_subtables = num_subtables[t];
         dyc_status r = create_impl(&c, s->d_tctr + t, s->h_tctr + t, false, &s->tables[t]);
         if (r != DYC_OK) return undo(r);
+    }
+    // L2 residency of a set is decided by all its members together (their
+    // batches run in one pass): in the default mode they keep their lines
+    // only if the whole set passes the single-table rule
+    if (cfg->l2_resident == 0u) {
+        uint64_t bytes = 0;
+        for (dyc_table *m : s->tables)
+            for (uint32_t i = 0; i < m->D.d; ++i) bytes += (uint64_t)m->D.nb[i] * m->sb;
+        const uint32_t mode = l2_keep_rule(bytes, s->tables[0]->l2_bytes) ? 2u : 1u;
+        for (dyc_table *m : s->tables) {
+            m->cfg.l2_resident = mode;
+            refresh_l2(m);
+        }
     }
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "set setup: %s", cudaGetErrorString(e)));

@@ -255,6 +255,44 @@ __device__ __forceinline__ void st_v8(void *p, const uint32_t (&w)[8]) {
                  : "memory");
 }
 
+// ----------------------------------------------------------------------------
+// L2 residency. A table whose subtables fit in the L2 (Desc::l2_keep) reads
+// its buckets with an evict_last cache policy, and the kernels that stream a
+// batch through (find's keys, values and hit words) use evict_first, so the
+// batch does not push the table out of the L2 between probes (PTX
+// createpolicy + .L2::cache_hint: the eviction priorities an access-policy
+// window applies, given per access, so tables need not be contiguous and no
+// L2 set-aside is taken from the process). Other tables use evict_normal.
+// ----------------------------------------------------------------------------
+struct L2Pol {
+    unsigned long long table, stream;
+};
+__device__ __forceinline__ L2Pol l2_policies(bool keep) {
+    unsigned long long a, b;
+    if (keep) {
+        asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(a));
+        asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(b));
+    } else {
+        asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(a));
+        b = a;
+    }
+    return {a, b};
+}
+__device__ __forceinline__ void ld_nc_pol(const void *p, uint32_t (&w)[8], unsigned long long pol) {
+    asm volatile(
+        "ld.global.nc.L1::no_allocate.L2::cache_hint.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+        : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]),
+          "=r"(w[7])
+        : "l"(p), "l"(pol));
+}
+__device__ __forceinline__ void ld_cg_pol(const void *p, uint32_t (&w)[8], unsigned long long pol) {
+    asm volatile("ld.global.cg.L2::cache_hint.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+                 : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]),
+                   "=r"(w[6]), "=r"(w[7])
+                 : "l"(p), "l"(pol)
+                 : "memory");
+}
+
 __device__ __forceinline__ void ld_ca(const void *p, uint32_t (&w)[8]) {
     asm volatile("ld.global.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]),
@@ -367,6 +405,38 @@ __device__ __forceinline__ uint64_t load_val(const void *v, uint32_t vb, uint64_
 __device__ __forceinline__ void store_val(void *v, uint32_t vb, uint64_t i, uint64_t x) {
     if (vb == 4) ((uint32_t *)v)[i] = (uint32_t)x;
     else ((unsigned long long *)v)[i] = x;
+}
+// the same, with an L2 cache policy (a batch streaming past an L2-resident table)
+template <int KB>
+__device__ __forceinline__ typename SlotT<KB>::K load_key_pol(const void *k, uint64_t i,
+                                                             unsigned long long pol) {
+    if constexpr (KB == 4) {
+        uint32_t r;
+        asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;"
+                     : "=r"(r)
+                     : "l"((const uint32_t *)k + i), "l"(pol));
+        return r;
+    } else {
+        unsigned long long r;
+        asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u64 %0, [%1], %2;"
+                     : "=l"(r)
+                     : "l"((const unsigned long long *)k + i), "l"(pol));
+        return r;
+    }
+}
+__device__ __forceinline__ void store_u32_pol(uint32_t *p, uint32_t x, unsigned long long pol) {
+    asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(x), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ void store_val_pol(void *v, uint32_t vb, uint64_t i, uint64_t x,
+                                              unsigned long long pol) {
+    if (vb == 4) {
+        store_u32_pol((uint32_t *)v + i, (uint32_t)x, pol);
+    } else {
+        asm volatile("st.global.L2::cache_hint.u64 [%0], %1, %2;" ::"l"((unsigned long long *)v + i),
+                     "l"(x), "l"(pol)
+                     : "memory");
+    }
 }
 
 // Warp-aggregated counter increment: one atomic per warp for the lanes that

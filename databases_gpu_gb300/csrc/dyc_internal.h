@@ -39,6 +39,8 @@ struct Desc {
     uint32_t nb[kMaxSub];     // buckets per subtable
     uint32_t d;               // subtable count
     uint32_t max_evict;       // eviction bound of this table (read by the set kernels)
+    uint32_t l2_keep;         // 1: the table fits the L2; its bucket reads ask to stay there
+    uint32_t pad;
 };
 
 // Per-table device counters (one 128-byte block). `size` persists; the rest

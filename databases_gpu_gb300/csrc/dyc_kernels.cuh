@@ -136,9 +136,11 @@ template <int G> __device__ __forceinline__ unsigned group_or(unsigned v) {
     return v;
 }
 
-template <int KB, int SB, int MODE, bool WANT_EMPTY, bool WANT_PREF>
+// HINT: the bucket reads carry each op's L2 cache policy (pol, see l2_policies)
+template <int KB, int SB, int MODE, bool WANT_EMPTY, bool WANT_PREF, bool HINT = false>
 __device__ __forceinline__ ProbeOut<KB> probe(const char *p, typename SlotT<KB>::K key, bool act,
-                                              uint32_t t, uint32_t d) {
+                                              uint32_t t, uint32_t d,
+                                              unsigned long long pol = 0ull) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
     using K = typename T::K;
@@ -175,10 +177,16 @@ __device__ __forceinline__ ProbeOut<KB> probe(const char *p, typename SlotT<KB>:
             const bool have = ci < nact;
             src[qq] = all ? ci : (have ? nth_set(am, ci) : lane);
             const unsigned long long pq = shfl64((unsigned long long)p, src[qq]);
+            const unsigned long long polq = HINT ? shfl64(pol, src[qq]) : 0ull;
             if (have) {
                 const char *cp = (const char *)pq + r * 32;
-                if (MODE == 1) ld_nc(cp, w[qq]);
-                else ld_cg(cp, w[qq]);
+                if (HINT) {
+                    if (MODE == 1) ld_nc_pol(cp, w[qq], polq);
+                    else ld_cg_pol(cp, w[qq], polq);
+                } else {
+                    if (MODE == 1) ld_nc(cp, w[qq]);
+                    else ld_cg(cp, w[qq]);
+                }
             } else {
 #pragma unroll
                 for (int x = 0; x < 8; ++x) w[qq][x] = 0u;
@@ -275,6 +283,12 @@ constexpr int kWarpsPerBlock = kBlockThreads / 32;
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
+__device__ __forceinline__ void cp_async16_pol(uint32_t dst, const void *src,
+                                               unsigned long long pol) {
+    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(dst),
+                 "l"(src), "l"(pol)
+                 : "memory");
+}
 
 template <int SB> __device__ __forceinline__ uint32_t piece_off(int o, int s) {
     constexpr int P = SB / 16;  // 16-byte pieces per bucket
@@ -284,8 +298,9 @@ template <int SB> __device__ __forceinline__ uint32_t piece_off(int o, int s) {
 // Copy the bucket at p of every active lane into stage (lane-indexed).
 // ALL: every lane is active; otherwise active lanes are served in rank order
 // so few active lanes cost few rounds.
-template <int SB, bool ALL>
-__device__ __forceinline__ void stage_rounds(const char *p, unsigned am, unsigned char *stage) {
+template <int SB, bool ALL, bool HINT = false>
+__device__ __forceinline__ void stage_rounds(const char *p, unsigned am, unsigned char *stage,
+                                             unsigned long long pol = 0ull) {
     constexpr int G = SB / 32, RO = 32 / G;
     const int lane = threadIdx.x & 31, g = lane / G, r = lane % G;
     const int nact = ALL ? 32 : __popc(am);
@@ -297,7 +312,14 @@ __device__ __forceinline__ void stage_rounds(const char *p, unsigned am, unsigne
         const bool have = ALL ? true : ci < nact;
         const int o = ALL ? ci : (have ? nth_set(am, ci) : lane);
         const unsigned long long pq = shfl64((unsigned long long)p, o);
-        if (have) {
+        if (HINT) {
+            const unsigned long long polq = shfl64(pol, o);
+            if (have) {
+                cp_async16_pol(base + piece_off<SB>(o, r), (const char *)pq + r * 16, polq);
+                cp_async16_pol(base + piece_off<SB>(o, r + G), (const char *)pq + (r + G) * 16,
+                               polq);
+            }
+        } else if (have) {
             cp_async16(base + piece_off<SB>(o, r), (const char *)pq + r * 16);
             cp_async16(base + piece_off<SB>(o, r + G), (const char *)pq + (r + G) * 16);
         }
@@ -307,16 +329,17 @@ __device__ __forceinline__ void stage_rounds(const char *p, unsigned am, unsigne
     __syncwarp();  // other lanes' copies are visible after the warp barrier
 }
 
-template <int KB, int SB, bool WANT_EMPTY = false>
+template <int KB, int SB, bool WANT_EMPTY = false, bool HINT = false>
 __device__ __forceinline__ KvOut probe_staged(const char *p, typename SlotT<KB>::K key, bool act,
-                                              unsigned char *stage) {
+                                              unsigned char *stage,
+                                              unsigned long long pol = 0ull) {
     using T = SlotT<KB>;
     using Gm = Geo<KB, SB>;
     constexpr int P = SB / 16, SPP = 16 / T::kBytes > 0 ? 16 / T::kBytes : 1;
     const unsigned am = __ballot_sync(kFull, act);
     __syncwarp();  // the previous use of the stage is finished in every lane
-    if (am == kFull) stage_rounds<SB, true>(p, am, stage);
-    else if (am) stage_rounds<SB, false>(p, am, stage);
+    if (am == kFull) stage_rounds<SB, true, HINT>(p, am, stage, pol);
+    else if (am) stage_rounds<SB, false, HINT>(p, am, stage, pol);
     KvOut out{-1, 0ull, false, 0u};
     if (!act) return out;
     const int lane = threadIdx.x & 31;
@@ -352,13 +375,13 @@ __device__ __forceinline__ KvOut probe_staged(const char *p, typename SlotT<KB>:
 // buckets; 32-byte buckets (one lane per bucket, a single 256-bit load) read
 // straight into registers, since staging them would split each sector over
 // two 16-byte copies.
-template <int KB, int SB, int MODE>
+template <int KB, int SB, int MODE, bool HINT = false>
 __device__ __forceinline__ KvOut kv_probe(const char *p, typename SlotT<KB>::K key, bool act,
-                                          unsigned char *stage) {
+                                          unsigned char *stage, unsigned long long pol = 0ull) {
     if constexpr (SB >= 64) {
-        return probe_staged<KB, SB>(p, key, act, stage);
+        return probe_staged<KB, SB, false, HINT>(p, key, act, stage, pol);
     } else {
-        const ProbeOut<KB> r = probe<KB, SB, MODE, false, false>(p, key, act, 0u, 0u);
+        const ProbeOut<KB> r = probe<KB, SB, MODE, false, false, HINT>(p, key, act, 0u, 0u, pol);
         KvOut o;
         o.match = r.match;
         o.value = SlotT<KB>::val(r.mslot);
@@ -371,13 +394,14 @@ __device__ __forceinline__ KvOut kv_probe(const char *p, typename SlotT<KB>::K k
 // Probe used by insert placement: matching slot, empty entry slots and the
 // overflow bit, through the shared-memory stage for 64- and 128-byte buckets
 // (a coherent L2 snapshot: cp.async.cg), the register probe for 32-byte ones.
-template <int KB, int SB>
+template <int KB, int SB, bool HINT = false>
 __device__ __forceinline__ KvOut place_probe(const char *p, typename SlotT<KB>::K key, bool act,
-                                             uint32_t t, uint32_t d, unsigned char *stage) {
+                                             uint32_t t, uint32_t d, unsigned char *stage,
+                                             unsigned long long pol = 0ull) {
     if constexpr (SB >= 64) {
-        return probe_staged<KB, SB, true>(p, key, act, stage);
+        return probe_staged<KB, SB, true, HINT>(p, key, act, stage, pol);
     } else {
-        const ProbeOut<KB> r = probe<KB, SB, 2, true, false>(p, key, act, t, d);
+        const ProbeOut<KB> r = probe<KB, SB, 2, true, false, HINT>(p, key, act, t, d, pol);
         KvOut o;
         o.match = r.match;
         o.value = 0ull;
@@ -506,29 +530,30 @@ __global__ void __launch_bounds__(256, KB == 4 ? 5 : 1) k_find(const __grid_cons
     unsigned char *stage = s_stage[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t step = warp_stride();
+    const L2Pol pol = l2_policies(D.l2_keep != 0u);
     for (uint64_t base = warp_base(); base < n; base += step) {
         const uint64_t i = base + lane;
         typename T::K k = 0;
-        if (i < n) k = load_key<KB>(keys, i);
+        if (i < n) k = load_key_pol<KB>(keys, i, pol.stream);
         const bool act = k != 0;
         const uint32_t hk = fold(k);
         const Pair p = pair_of(hk, D.d);
         const char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
-        const KvOut r1 = kv_probe<KB, SB, 1>(p1, k, act, stage);
+        const KvOut r1 = kv_probe<KB, SB, 1, true>(p1, k, act, stage, pol.table);
         bool hit = act && r1.match >= 0;
         uint64_t v = hit ? r1.value : 0ull;
         const bool need2 = act && !hit && (!Gm::kMeta || r1.overflow);
         if (__any_sync(kFull, need2)) {
             const char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-            const KvOut r2 = kv_probe<KB, SB, 1>(p2, k, need2, stage);
+            const KvOut r2 = kv_probe<KB, SB, 1, true>(p2, k, need2, stage, pol.table);
             if (need2 && r2.match >= 0) {
                 hit = true;
                 v = r2.value;
             }
         }
-        if (i < n) store_val(vals, vb, i, v);
+        if (i < n) store_val_pol(vals, vb, i, v, pol.stream);
         const unsigned m = __ballot_sync(kFull, hit);
-        if (hits != nullptr && lane == 0) hits[base >> 5] = m;
+        if (hits != nullptr && lane == 0) store_u32_pol(hits + (base >> 5), m, pol.stream);
     }
 }
 
@@ -549,6 +574,7 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
     __shared__ __align__(128) unsigned char s_stage[SB >= 64 ? kWarpsPerBlock : 1][32 * SB];
     unsigned char *stage = s_stage[SB >= 64 ? (threadIdx.x >> 5) : 0];
     const uint64_t step = warp_stride();
+    const unsigned long long tpol = l2_policies(D.l2_keep != 0u).table;
     uint32_t n_ins = 0, n_upd = 0, n_rej = 0, n_sup = 0;
     for (uint64_t base = warp_base(); base < n; base += step) {
         const uint64_t i = base + (threadIdx.x & 31);
@@ -570,14 +596,15 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
         const Pair p = pair_of(hk, D.d);
         char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
         char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-        const KvOut r1 = place_probe<KB, SB>(p1, k, act, p.first, D.d, stage);
+        const KvOut r1 = place_probe<KB, SB, true>(p1, k, act, p.first, D.d, stage, tpol);
         const bool found1 = act && r1.match >= 0;
         // the second bucket is needed to look for the key (upsert, unless the
         // first bucket's overflow bit rules it out) or for an empty slot
         const bool check2 =
             act && !found1 && ((!new_keys && (!Gm::kMeta || r1.overflow)) || r1.empty == 0u);
         KvOut r2{-1, 0ull, false, 0u};
-        if (__any_sync(kFull, check2)) r2 = place_probe<KB, SB>(p2, k, check2, p.second, D.d, stage);
+        if (__any_sync(kFull, check2))
+            r2 = place_probe<KB, SB, true>(p2, k, check2, p.second, D.d, stage, tpol);
         // An update rewrites the key's own slot with a plain store: the keys
         // of the kernel are distinct (dedup, or the caller's promise) and
         // its other writes only claim empty slots, so nothing else writes
@@ -940,6 +967,7 @@ __global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D,
     unsigned char *stage = s_stage[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t step = warp_stride();
+    const unsigned long long tpol = l2_policies(D.l2_keep != 0u).table;
     uint32_t n_del = 0, n_sup = 0;
     for (uint64_t base = warp_base(); base < n; base += step) {
         const uint64_t i = base + lane;
@@ -955,7 +983,7 @@ __global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D,
         const uint32_t hk = fold(k);
         const Pair p = pair_of(hk, D.d);
         char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
-        const KvOut r1 = kv_probe<KB, SB, 2>(p1, k, act, stage);
+        const KvOut r1 = kv_probe<KB, SB, 2, true>(p1, k, act, stage, tpol);
         // A found key's slot is emptied with a plain store, as the reference
         // does (cuckoo.cu:551): the kernel's keys are distinct (dedup, or the
         // caller's promise) and nothing else runs on the table, so no other
@@ -969,7 +997,7 @@ __global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D,
         const bool need2 = act && r1.match < 0 && (!Gm::kMeta || r1.overflow);
         if (__any_sync(kFull, need2)) {
             char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-            const KvOut r2 = kv_probe<KB, SB, 2>(p2, k, need2, stage);
+            const KvOut r2 = kv_probe<KB, SB, 2, true>(p2, k, need2, stage, tpol);
             if (need2 && r2.match >= 0) {
                 T::store(slot_ptr<KB, SB>(p2, r2.match), T::empty());
                 erased = true;

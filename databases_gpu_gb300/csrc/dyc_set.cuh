@@ -75,16 +75,17 @@ __global__ void __launch_bounds__(256) k_set_find(const Desc *__restrict__ descs
         }
         const Desc &D = descs[tb];
         const bool act = ok && k != 0;
+        const unsigned long long tpol = l2_policies(D.l2_keep != 0u).table;
         const uint32_t hk = fold(k);
         const Pair p = pair_of(hk, D.d);
         const char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
-        const KvOut r1 = kv_probe<KB, SB, 1>(p1, k, act, stage);
+        const KvOut r1 = kv_probe<KB, SB, 1, true>(p1, k, act, stage, tpol);
         bool hit = act && r1.match >= 0;
         uint64_t v = hit ? r1.value : 0ull;
         const bool need2 = act && !hit && (!Gm::kMeta || r1.overflow);
         if (__any_sync(kFull, need2)) {
             const char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-            const KvOut r2 = kv_probe<KB, SB, 1>(p2, k, need2, stage);
+            const KvOut r2 = kv_probe<KB, SB, 1, true>(p2, k, need2, stage, tpol);
             if (need2 && r2.match >= 0) {
                 hit = true;
                 v = r2.value;
@@ -118,10 +119,11 @@ __device__ __forceinline__ bool set_erase_warp(const Desc *__restrict__ descs, u
     }
     const Desc &D = descs[tb];
     const bool act = ok && k != 0;
+    const unsigned long long tpol = l2_policies(D.l2_keep != 0u).table;
     const uint32_t hk = fold(k);
     const Pair p = pair_of(hk, D.d);
     char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
-    const KvOut r1 = kv_probe<KB, SB, 2>(p1, k, act, stage);
+    const KvOut r1 = kv_probe<KB, SB, 2, true>(p1, k, act, stage, tpol);
     // plain stores, as in k_erase: the erase and upsert lists name distinct
     // keys, so no other thread of the pass writes a found key's slot
     bool erased = false;
@@ -132,7 +134,7 @@ __device__ __forceinline__ bool set_erase_warp(const Desc *__restrict__ descs, u
     const bool need2 = act && r1.match < 0 && (!Gm::kMeta || r1.overflow);
     if (__any_sync(kFull, need2)) {
         char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-        const KvOut r2 = kv_probe<KB, SB, 2>(p2, k, need2, stage);
+        const KvOut r2 = kv_probe<KB, SB, 2, true>(p2, k, need2, stage, tpol);
         if (need2 && r2.match >= 0) {
             T::store(slot_ptr<KB, SB>(p2, r2.match), T::empty());
             erased = true;
@@ -171,15 +173,17 @@ __device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs, u
         if (act) e = T::make(k, load_val(vals, vb, i));
     }
     const Desc &D = descs[tb];
+    const unsigned long long tpol = l2_policies(D.l2_keep != 0u).table;
     const uint32_t hk = fold(k);
     const Pair p = pair_of(hk, D.d);
     char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
     char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-    const KvOut r1 = place_probe<KB, SB>(p1, k, act, p.first, D.d, stage);
+    const KvOut r1 = place_probe<KB, SB, true>(p1, k, act, p.first, D.d, stage, tpol);
     const bool found1 = act && r1.match >= 0;
     const bool check2 = act && !found1 && ((!Gm::kMeta || r1.overflow) || r1.empty == 0u);
     KvOut r2{-1, 0ull, false, 0u};
-    if (__any_sync(kFull, check2)) r2 = place_probe<KB, SB>(p2, k, check2, p.second, D.d, stage);
+    if (__any_sync(kFull, check2))
+        r2 = place_probe<KB, SB, true>(p2, k, check2, p.second, D.d, stage, tpol);
     bool pend = false, ins = false;
     if (found1) {  // the key's own slot: a plain store (distinct keys, as in k_place)
         T::store(slot_ptr<KB, SB>(p1, r1.match), e);

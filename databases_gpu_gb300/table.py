@@ -58,13 +58,16 @@ class DyCuckoo:
     """A GB300 DyCuckoo table; all arrays are CUDA tensors.
 
     size: number of keys to size the table for (the hashAPI(size) argument).
+    l2_resident: 0 keeps the buckets in the L2 when the table takes at most
+    1.5x of it, 1 never, 2 always (dyc_config.l2_resident).
     """
 
     def __init__(self, size: int, key_bytes: int = 4, value_bytes: int | None = None,
                  num_subtables: int = 4, bucket_bytes: int = 128, max_evictions: int = 64,
                  auto_resize: bool = True, upper_load: float = UPPER_BOUND,
                  lower_load: float = LOWER_BOUND,
-                 min_downsize_capacity: int = MIN_DOWNSIZE_CAPACITY, device: int = 0):
+                 min_downsize_capacity: int = MIN_DOWNSIZE_CAPACITY, device: int = 0,
+                 l2_resident: int = 0):
         L = _lib.lib()
         cfg = _lib.DycConfig()
         L.dyc_config_default(C.byref(cfg))
@@ -74,6 +77,7 @@ class DyCuckoo:
         cfg.bucket_bytes = bucket_bytes
         cfg.max_evictions = max_evictions
         cfg.auto_resize = 1 if auto_resize else 0
+        cfg.l2_resident = l2_resident
         cfg.initial_size = int(size)
         cfg.upper_load = upper_load
         cfg.lower_load = lower_load
@@ -340,10 +344,11 @@ class DyCuckooSet:
                  auto_resize: bool = True, upper_load: float = UPPER_BOUND,
                  lower_load: float = LOWER_BOUND,
                  min_downsize_capacity: int = MIN_DOWNSIZE_CAPACITY, device: int = 0,
-                 default_subtables: int = 4):
+                 default_subtables: int = 4, l2_resident: int = 0):
         L = _lib.lib()
         cfg = _lib.DycConfig()
         L.dyc_config_default(C.byref(cfg))
+        cfg.l2_resident = l2_resident
         cfg.key_bytes = key_bytes
         cfg.value_bytes = value_bytes if value_bytes is not None else key_bytes
         cfg.num_subtables = default_subtables

@@ -87,7 +87,14 @@ typedef struct dyc_config {
     double lower_load;       /* downsize below this after erase; default 0.5 */
     uint64_t min_downsize_capacity; /* no downsize at or below this capacity */
     int32_t device;          /* CUDA device ordinal; default 0 */
-    uint32_t reserved[7];
+    uint32_t l2_resident;    /* L2 residency of the buckets: 0 (default) when the
+                                subtables take at most 1.5x the device's L2 (for a table
+                                set: all its members together), 1 never, 2 always. A
+                                resident table reads its buckets with an evict_last L2
+                                cache policy and find streams its keys and results with
+                                evict_first, so a large batch does not push the table out
+                                of the L2. No counterpart in the reference. */
+    uint32_t reserved[6];
 } dyc_config;
 
 /* Per-call flags. */

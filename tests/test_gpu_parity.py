@@ -409,3 +409,25 @@ def test_host_find_pipeline_chunk_schedule():
     assert np.array_equal(bits.view(np.int32), db.cpu().numpy())
     assert int(_bits_np(bits, n).sum()) == half
     t.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_l2_residency_modes_give_the_same_results(mode):
+    """dyc_config.l2_resident only changes the L2 cache policy of the bucket
+    reads (evict_last for a resident table, evict_normal otherwise) and of
+    find's streaming keys and results: inserts, finds (hits and misses),
+    erases and the contents match the oracle in every mode."""
+    import databases_gpu_gb300 as dg
+    n = 1 << 16
+    pool = unique_u32(2 * n, seed=91)
+    keys, vals = pool[:n], np.arange(3, n + 3, dtype=np.uint32)
+    t = dg.DyCuckoo(int(n / 0.85), l2_resident=mode)
+    m = O.Map(n)
+    t.insert(to_dev(keys), to_dev(vals))
+    m.insert(keys, vals)
+    find_and_compare(t, m, pool, "find, l2_resident=%d" % mode)
+    assert t.erase(to_dev(keys[: n // 3])) == n // 3
+    m.erase(keys[: n // 3])
+    find_and_compare(t, m, pool, "find after erase, l2_resident=%d" % mode)
+    assert_same_contents(t, m, "contents, l2_resident=%d" % mode)
+    t.close()
