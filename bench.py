@@ -547,7 +547,9 @@ def run_multi_table(args, dev, torch, dg):
     # are kept and compared op by op with the per-table path's
     data = [w.round() for _ in range(rounds + 2)]
     kept = []
-    for which, S in (("batched", sets[0]), ("per_table", sets[1])):
+    paths = (("batched", sets[0]),) if args.mt_skip_per_table else \
+        (("batched", sets[0]), ("per_table", sets[1]))
+    for which, S in paths:
         i = 0 if which == "batched" else 1
         for r, (ops, keys, vals) in enumerate(data):
             torch.cuda.synchronize()
@@ -570,22 +572,25 @@ def run_multi_table(args, dev, torch, dg):
                 bad += int((kept[r][0] != outs[1]).sum()) + int((kept[r][1] != bitss[1]).sum())
     del kept, data
     sa, ca = sets[0].sizes()
-    sb, cb = sets[1].sizes()
-    bad += int((sa != sb).sum())
+    if not args.mt_skip_per_table:
+        sb, cb = sets[1].sizes()
+        bad += int((sa != sb).sum())
     res = {"workload": "batched multi-table: %d u32 tables, sizes log-uniform 2^8..2^20 keys, "
                        "per-table batches log-uniform 16..2^16 ops (70/20/10 find/insert/erase, "
                        "50%% find hits), %d ops per round" % (w.ntables, n),
            "tables": w.ntables, "ops_per_round": n, "rounds": rounds,
            "keys_total": int(sa.sum()), "capacity_total": int(ca.sum()),
            "result_mismatches": bad}
-    for which in ("batched", "per_table"):
+    for which in [p[0] for p in paths]:
         ms = sorted(lat[which])
         res[which] = {"mops": round(n * len(ms) / (sum(ms) / 1e3) / 1e6, 1),
                       "round_ms_p50": round(ms[len(ms) // 2], 3), "round_ms_max": round(ms[-1], 3)}
     res["batched"]["upsizes_per_round"] = round(resized["up"] / rounds, 1)
     res["batched"]["downsizes_per_round"] = round(resized["down"] / rounds, 1)
     res["batched"]["split_rounds"] = resized["split"]
-    res["batched_over_per_table"] = round(res["batched"]["mops"] / res["per_table"]["mops"], 2)
+    if not args.mt_skip_per_table:
+        res["batched_over_per_table"] = round(res["batched"]["mops"] / res["per_table"]["mops"],
+                                              2)
     res["api"] = "dyc_set_apply (graph replay) vs dyc_set_apply_each (one dyc_apply per table)"
     for S in sets:
         S.close()
@@ -743,6 +748,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=0.25)
     ap.add_argument("--mt-tables", type=int, default=4096)
     ap.add_argument("--skip-tune", action="store_true", help="skip the tuned multi-table set")
+    ap.add_argument("--mt-skip-per-table", action="store_true",
+                    help="multi-table workload without the one-dyc_apply-per-table rounds")
     ap.add_argument("--mt-rounds", type=int, default=3)
     ap.add_argument("--stream-batches", type=int, default=512)
     ap.add_argument("--stream-max-evictions", type=int, default=2048)

@@ -230,7 +230,7 @@ dyc_status ensure_scratch(dyc_table *t, uint64_t n) {
     const size_t idx_bytes = t->kb == 8 ? (size_t)cap * 4 : 0;
     const size_t list_bytes = (size_t)n * t->slot_bytes;
     const size_t win_bytes = (size_t)(n / 32 + 1) * 4;
-    const size_t need = dedup_bytes + idx_bytes + 2 * list_bytes + win_bytes + 4 * 256;
+    const size_t need = dedup_bytes + idx_bytes + 2 * list_bytes + win_bytes + 256 + 5 * 256;
     if (t->scratch && t->scratch_bytes >= need && t->S.list_cap >= n && t->S.dedup_cap >= cap)
         return DYC_OK;
     if (t->scratch) {
@@ -253,6 +253,7 @@ dyc_status ensure_scratch(dyc_table *t, uint64_t n) {
     t->S.list_b = carve(list_bytes);
     t->S.list_cap = n;
     t->S.winbits = (uint32_t *)carve(win_bytes);
+    t->S.dupseen = (uint32_t *)carve(4);
     return DYC_OK;
 }
 

@@ -70,6 +70,9 @@ struct Scratch {
     // (filled from the dedup table after the claims); null: the winner is
     // looked up in the dedup table by each op
     uint32_t *winbits;
+    // nonzero once the dedup claims met a key twice; while it stays zero
+    // every op of the chunk is its key's only op (no winner bits are needed)
+    uint32_t *dupseen;
 };
 
 // Scratch of one mixed batch of at most `cap_ops` ops. The multi-table

@@ -431,12 +431,16 @@ template <> struct Dedup<4> {
             if ((uint32_t)(old >> 32) == k) {
                 if (mode == kKeepLast) atomicMax(&tab[h], mine);
                 else atomicMin(&tab[h], mine);
+                if (S.dupseen) *(volatile uint32_t *)S.dupseen = 1u;
                 return;
             }
         }
     }
     __device__ static __forceinline__ bool winner(const Scratch &S, uint32_t k, uint32_t i) {
-        if (S.winbits) return (S.winbits[i >> 5] >> (i & 31)) & 1u;
+        if (S.winbits) {
+            if (S.dupseen && *S.dupseen == 0u) return true;  // no key repeats in the chunk
+            return (S.winbits[i >> 5] >> (i & 31)) & 1u;
+        }
         const unsigned long long *tab = (const unsigned long long *)S.dedup;
         const uint64_t mask = S.dedup_cap - 1;
         uint64_t h = mix32(k) & mask;
@@ -461,12 +465,16 @@ template <> struct Dedup<8> {
             if (old == 0ull || old == k) {
                 if (mode == kKeepLast) atomicMax(&S.dedup_idx[h], i);
                 else atomicMin(&S.dedup_idx[h], i);
+                if (old == k && S.dupseen) *(volatile uint32_t *)S.dupseen = 1u;
                 return;
             }
         }
     }
     __device__ static __forceinline__ bool winner(const Scratch &S, uint64_t k, uint32_t i) {
-        if (S.winbits) return (S.winbits[i >> 5] >> (i & 31)) & 1u;
+        if (S.winbits) {
+            if (S.dupseen && *S.dupseen == 0u) return true;  // no key repeats in the chunk
+            return (S.winbits[i >> 5] >> (i & 31)) & 1u;
+        }
         const unsigned long long *tab = (const unsigned long long *)S.dedup;
         const uint64_t mask = S.dedup_cap - 1;
         uint64_t h = mix32(fold(k) ^ (uint32_t)(k >> 32)) & mask;
@@ -495,9 +503,11 @@ __global__ void __launch_bounds__(256) k_dedup(const __grid_constant__ Scratch S
 // n bits), so the place and erase kernels read their op's bit coalesced
 // instead of probing the dedup table at random once more (the table of a
 // 4M-op chunk is 64 MB; those probes cost DRAM accesses beside the bucket
-// reads).
+// reads). A chunk whose claims met no key twice skips the pass: every op
+// wins (dupseen).
 template <int KB>
 __global__ void __launch_bounds__(256) k_dedup_winners(const __grid_constant__ Scratch S) {
+    if (S.dupseen && *S.dupseen == 0u) return;  // every op is its key's only one
     const unsigned long long *tab = (const unsigned long long *)S.dedup;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t h = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; h < S.dedup_cap;

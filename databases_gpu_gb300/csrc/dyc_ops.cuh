@@ -99,7 +99,8 @@ cudaError_t Ops<KB>::dedup(const LaunchCtx &L, const Scratch &S, const void *key
                            DedupMode mode) {
     if (n == 0) return cudaSuccess;
     if (S.winbits) {
-        const cudaError_t e = cudaMemsetAsync(S.winbits, 0, (size_t)(n / 32 + 1) * 4, L.stream);
+        cudaError_t e = cudaMemsetAsync(S.winbits, 0, (size_t)(n / 32 + 1) * 4, L.stream);
+        if (e == cudaSuccess && S.dupseen) e = cudaMemsetAsync(S.dupseen, 0, 4, L.stream);
         if (e != cudaSuccess) return e;
     }
     auto k = k_dedup<KB>;
