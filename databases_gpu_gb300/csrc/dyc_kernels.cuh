@@ -1200,7 +1200,7 @@ __global__ void __launch_bounds__(kMergeTile) k_resize_down(const char *__restri
     using T = SlotT<KB>;
     using Sl = typename T::S;
     using Gm = Geo<KB, SB>;
-    constexpr int B = Gm::kSlots, TOT = Gm::kTotal, W = T::kBytes / 4;
+    constexpr int B = Gm::kSlots, W = T::kBytes / 4;
     __shared__ __align__(128) unsigned char sa[kMergeTile * SB];
     __shared__ __align__(128) unsigned char sc[kMergeTile * SB];
     __shared__ __align__(8) unsigned long long bar_storage;
