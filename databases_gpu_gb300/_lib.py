@@ -31,7 +31,8 @@ class DycConfig(C.Structure):
         ("min_downsize_capacity", C.c_uint64),
         ("device", C.c_int32),
         ("l2_resident", C.c_uint32),
-        ("reserved", C.c_uint32 * 6),
+        ("device_upsize", C.c_uint32),
+        ("reserved", C.c_uint32 * 5),
     ]
 
 
@@ -70,7 +71,7 @@ EXPORTS = [
     "dyc_erase_host", "dyc_status_string", "dyc_last_error", "dyc_erase_noalloc", "dyc_apply",
     "dyc_pool_reserve",
     "dyc_set_create", "dyc_set_destroy", "dyc_set_table", "dyc_set_sizes", "dyc_set_apply",
-    "dyc_set_apply_each", "dyc_set_last_stats", "dyc_set_configure",
+    "dyc_set_apply_each", "dyc_set_last_stats", "dyc_set_configure", "dyc_set_spare_bytes",
     "dyc_server_config_default", "dyc_server_create", "dyc_server_destroy", "dyc_server_submit",
     "dyc_server_wait", "dyc_server_stats_get", "dyc_server_set",
     "dyc_snapshot_bytes", "dyc_snapshot", "dyc_restore",
@@ -113,6 +114,7 @@ def _declare(L):
         "dyc_set_destroy": (st, [T]),
         "dyc_set_table": (st, [T, u32, C.POINTER(C.c_void_p)]),
         "dyc_set_sizes": (st, [T, vp, vp]),
+        "dyc_set_spare_bytes": (st, [T, C.POINTER(C.c_uint64)]),
         "dyc_set_apply": (st, [T, vp, vp, vp, vp, vp, vp, vp, u32, vp]),
         "dyc_set_apply_each": (st, [T, vp, vp, vp, vp, vp, vp, vp, u32, vp]),
         "dyc_set_last_stats": (st, [T, C.POINTER(DycOpStats)]),

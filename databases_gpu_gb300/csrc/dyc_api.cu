@@ -68,12 +68,9 @@ uint32_t next_prime_ref(uint32_t n) {
     return n;
 }
 
-// resize target choice (api.cpp:115-122 and :147-153)
-uint32_t pick_up(const uint32_t *nb, uint32_t d) {
-    for (uint32_t i = 0; i + 1 < d; ++i)
-        if (nb[i] == 2u * nb[i + 1]) return i + 1;
-    return 0;
-}
+// resize target choice (api.cpp:115-122 and :147-153); the upsize rule is
+// shared with the device half of a set's policy (dyc::pick_up_index)
+uint32_t pick_up(const uint32_t *nb, uint32_t d) { return dyc::pick_up_index(nb, d); }
 uint32_t pick_down(const uint32_t *nb, uint32_t d) {
     for (uint32_t i = 0; i + 1 < d; ++i)
         if (nb[i] > nb[i + 1]) return i;
@@ -619,6 +616,7 @@ bool valid_config(const dyc_config *c, char *why, size_t n) {
     if (!(c->upper_load > 0.0 && c->upper_load <= 1.0) || !(c->lower_load >= 0.0 && c->lower_load < c->upper_load))
         return snprintf(why, n, "need 0 <= lower_load < upper_load <= 1"), false;
     if (c->l2_resident > 2) return snprintf(why, n, "l2_resident must be 0, 1 or 2"), false;
+    if (c->device_upsize > 1) return snprintf(why, n, "device_upsize must be 0 or 1"), false;
     return true;
 }
 
@@ -1441,7 +1439,8 @@ struct dyc_set {
     // their grids by the scratch capacity, so one graph serves any batch size
     struct Graph {
         std::vector<uintptr_t> key;
-        cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
+        // phase A, phase B, both, and the device policy + upsizes + phase B
+        cudaGraphExec_t exec[4] = {nullptr, nullptr, nullptr, nullptr};
         bool warm = false;
         uint64_t used = 0;
     };
@@ -1453,6 +1452,17 @@ struct dyc_set {
     uint32_t blocks_per_sm = 0;  // launch cap of the set kernels (0: as many as fit)
     uint32_t max_evict_all = 0;  // largest member eviction bound
     dyc_op_stats last{};
+    // device half of the upsize policy (cfg.device_upsize == 0, auto_resize):
+    // one upsize target per member, allocated ahead (h_spare, its device copy
+    // d_spare refreshed at every round), the moves k_set_policy lists, which
+    // members it upsized, and the buffers they replaced (freed at the next call)
+    bool spares = false;
+    dyc::Spare *d_spare = nullptr, *h_spare = nullptr;
+    dyc::ResizeJob *d_jobs = nullptr;
+    dyc::SetPolicyOut *d_pout = nullptr, *h_pout = nullptr;
+    uint8_t *d_grew = nullptr, *h_grew = nullptr;
+    std::vector<void *> free_later;
+    uint64_t free_later_bytes = 0;
 };
 
 namespace {
@@ -1572,13 +1582,15 @@ dyc_status set_phase_a(dyc_set *s, const uint32_t *d_off, const uint8_t *ops, co
 }
 
 // Phase B: erase list, upsert list, eviction walks; counters to the host.
-dyc_status set_phase_b(dyc_set *s, uint64_t n, cudaStream_t st) {
+// hold: a device word that, when nonzero, makes the pass do nothing (the
+// device policy found a member the host must upsize further first).
+dyc_status set_phase_b(dyc_set *s, uint64_t n, cudaStream_t st, const uint32_t *hold = nullptr) {
     const dyc::ApplyScratch &A = s->A;
     const LaunchCtx L{s->sms, st, (int)s->blocks_per_sm};
     cudaError_t e = SET_KB_CALL(s, set_mutate, L, s->d_desc, s->ntables, s->d_tctr, s->sb,
                                 A.er_key, A.er_tid, &A.ctr[dyc::kCtrEr], A.up_key, A.up_val,
                                 (uint32_t)s->vb, A.up_tid, &A.ctr[dyc::kCtrUp], n, s->list_a,
-                                s->tid_a, s->list_cap, s->d_gctr, &A.ctr[dyc::kCtrBad]);
+                                s->tid_a, s->list_cap, s->d_gctr, &A.ctr[dyc::kCtrBad], hold);
     if (e == cudaSuccess)
         e = SET_KB_CALL(s, set_walk, L, s->d_desc, s->ntables, s->d_tctr, s->sb, s->list_a,
                         s->tid_a, &s->d_gctr->pending, s->list_b, s->tid_b,
@@ -1591,6 +1603,85 @@ dyc_status set_phase_b(dyc_set *s, uint64_t n, cudaStream_t st) {
     CK(cudaMemcpyAsync(s->h_tctr, s->d_tctr, sizeof(Counters) * s->ntables,
                        cudaMemcpyDeviceToHost, st));
     return DYC_OK;
+}
+
+// ---- device half of the upsize policy ----------------------------------------
+// Replaced subtables and spares that no longer fit, freed (stream-ordered)
+// once the launches that could read them have been issued before.
+dyc_status set_release_later(dyc_set *s, cudaStream_t st) {
+    for (void *p : s->free_later) CK(cudaFreeAsync(p, st));
+    s->free_later.clear();
+    s->free_later_bytes = 0;
+    return DYC_OK;
+}
+
+// Give every member a spare that fits its next upsize (subtable pick_up with
+// its current bucket count, doubled). Issued while phase A runs on the
+// device; allocations are stream-ordered on st. A member whose spare cannot
+// be allocated has none this round: the device policy hands it to the host.
+void set_fill_spares(dyc_set *s, cudaStream_t st) {
+    for (uint32_t t = 0; t < s->ntables; ++t) {
+        const dyc_table *m = s->tables[t];
+        const uint32_t ti = pick_up(m->D.nb, m->D.d), onb = m->D.nb[ti];
+        dyc::Spare &sp = s->h_spare[t];
+        if (sp.new_sub && sp.ti == ti && sp.old_nb == onb) continue;
+        if (sp.new_sub) {
+            s->free_later.push_back(sp.new_sub);
+            s->free_later_bytes += 2ull * sp.old_nb * m->sb;
+        }
+        sp = dyc::Spare{nullptr, 0u, 0u};
+        if (onb == 0 || (uint64_t)onb * 2 > 0xFFFFFFFFull) continue;
+        void *p = nullptr;
+        if (pool_alloc(s->device, &p, 2ull * onb * m->sb, st) != cudaSuccess) {
+            (void)cudaGetLastError();
+            continue;
+        }
+        sp = dyc::Spare{p, ti, onb};
+    }
+}
+
+// Spare targets to the device, the policy, the listed upsizes, phase B
+// (held back when the host must finish the policy), and what the policy
+// did back to the host. One capturable sequence.
+dyc_status set_policy_and_b(dyc_set *s, uint64_t n, cudaStream_t st) {
+    const LaunchCtx L{s->sms, st, (int)s->blocks_per_sm};
+    CK(cudaMemcpyAsync(s->d_spare, s->h_spare, sizeof(dyc::Spare) * s->ntables,
+                       cudaMemcpyHostToDevice, st));
+    cudaError_t e = SET_KB_CALL(s, set_policy, L, s->d_desc, s->ntables, s->d_tctr, s->A.tup,
+                                s->A.ter, s->d_spare, s->cfg.upper_load,
+                                (uint32_t)s->tables[0]->slots, s->sb, s->d_jobs, s->d_grew,
+                                s->d_pout);
+    if (e == cudaSuccess)
+        e = SET_KB_CALL(s, resize_up_list, L, s->sb, s->d_jobs, s->d_pout, s->ntables);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "set upsize policy: %s", cudaGetErrorString(e));
+    TRY(set_phase_b(s, n, st, &s->d_pout->host));
+    CK(cudaMemcpyAsync(s->h_pout, s->d_pout, sizeof(dyc::SetPolicyOut), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(s->h_grew, s->d_grew, s->ntables, cudaMemcpyDeviceToHost, st));
+    return DYC_OK;
+}
+
+// The members the device upsized: their host descriptors follow the device
+// ones (the spare became subtable ti), the old subtable is freed at the next
+// call, and grew[t] is set as for a host upsize of the policy.
+void set_take_device_upsizes(dyc_set *s, std::vector<uint8_t> &grew) {
+    for (uint32_t t = 0; t < s->ntables; ++t) {
+        if (!s->h_grew[t]) continue;
+        dyc_table *m = s->tables[t];
+        dyc::Spare &sp = s->h_spare[t];
+        const uint32_t ti = sp.ti, nnb = 2u * sp.old_nb;
+        s->free_later.push_back(m->D.sub[ti]);
+        s->free_later_bytes += (uint64_t)sp.old_nb * m->sb;
+        m->D.sub[ti] = sp.new_sub;
+        m->D.nb[ti] = nnb;
+        m->D.magic[ti] = dyc::fastmod_magic(nnb);
+        m->capacity += (uint64_t)sp.old_nb * m->slots;
+        refresh_l2(m);
+        m->last.resizes_up++;
+        sp = dyc::Spare{nullptr, 0u, 0u};
+        s->h_desc[t] = m->D;  // the device descriptor is already this one
+        if (grew.empty()) grew.assign(s->ntables, 0);
+        grew[t] = 1;
+    }
 }
 
 // Run a launch sequence issue(stream) directly on st, or through its
@@ -1751,6 +1842,21 @@ dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming);
+    s->spares = cfg->auto_resize && cfg->device_upsize == 0u;
+    if (s->spares) {
+        if (e == cudaSuccess) e = dyc::lib_malloc(&s->d_spare, sizeof(dyc::Spare) * ntables);
+        if (e == cudaSuccess) e = dyc::lib_malloc_host(&s->h_spare, sizeof(dyc::Spare) * ntables);
+        if (e == cudaSuccess) e = dyc::lib_malloc(&s->d_jobs, sizeof(dyc::ResizeJob) * ntables);
+        if (e == cudaSuccess) e = dyc::lib_malloc(&s->d_pout, sizeof(dyc::SetPolicyOut));
+        if (e == cudaSuccess) e = dyc::lib_malloc_host(&s->h_pout, sizeof(dyc::SetPolicyOut));
+        if (e == cudaSuccess) e = dyc::lib_malloc(&s->d_grew, ntables);
+        if (e == cudaSuccess) e = dyc::lib_malloc_host(&s->h_grew, ntables);
+        if (e == cudaSuccess) {
+            memset(s->h_spare, 0, sizeof(dyc::Spare) * ntables);
+            memset(s->h_pout, 0, sizeof(dyc::SetPolicyOut));
+            memset(s->h_grew, 0, ntables);
+        }
+    }
     if (e != cudaSuccess) return undo(fail(DYC_ENOMEM, "set setup: %s", cudaGetErrorString(e)));
     memset(s->h_tctr, 0, sizeof(Counters) * ntables);
     s->tables.assign(ntables, nullptr);
@@ -1794,6 +1900,17 @@ dyc_status dyc_set_destroy(dyc_set *s) {
     if (s->join) cudaEventDestroy(s->join);
     for (dyc_table *t : s->tables)
         if (t) dyc_destroy(t);
+    if (s->h_spare)
+        for (uint32_t t = 0; t < s->ntables; ++t)
+            if (s->h_spare[t].new_sub) cudaFree(s->h_spare[t].new_sub);
+    for (void *p : s->free_later) cudaFree(p);
+    if (s->d_spare) cudaFree(s->d_spare);
+    if (s->h_spare) cudaFreeHost(s->h_spare);
+    if (s->d_jobs) cudaFree(s->d_jobs);
+    if (s->d_pout) cudaFree(s->d_pout);
+    if (s->h_pout) cudaFreeHost(s->h_pout);
+    if (s->d_grew) cudaFree(s->d_grew);
+    if (s->h_grew) cudaFreeHost(s->h_grew);
     if (s->d_tctr) cudaFree(s->d_tctr);
     if (s->h_tctr) cudaFreeHost(s->h_tctr);
     if (s->d_desc) cudaFree(s->d_desc);
@@ -1847,6 +1964,16 @@ dyc_status dyc_set_sizes(dyc_set *s, uint64_t *h_sizes, uint64_t *h_capacities) 
     return DYC_OK;
 }
 
+dyc_status dyc_set_spare_bytes(dyc_set *s, uint64_t *bytes) {
+    if (!s || !bytes) return fail(DYC_EINVAL, "null argument");
+    uint64_t b = s->free_later_bytes;
+    if (s->h_spare)
+        for (uint32_t t = 0; t < s->ntables; ++t)
+            b += 2ull * s->h_spare[t].old_nb * (s->h_spare[t].new_sub ? (uint64_t)s->sb : 0ull);
+    *bytes = b;
+    return DYC_OK;
+}
+
 dyc_status dyc_set_last_stats(dyc_set *s, dyc_op_stats *out) {
     if (!s || !out) return fail(DYC_EINVAL, "null argument");
     *out = s->last;
@@ -1896,9 +2023,11 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
     // with the same sizes and counts, so capacities end as if it had run
     // before the inserts (entries a fuller table could not place go through
     // the overflow path). Otherwise the host reads the counts between the
-    // phases and upsizes first.
+    // phases and upsizes first. With upsize targets kept ahead (spares), the
+    // policy runs on the device between the phases instead (k_set_policy),
+    // with no host read unless a member needs a second upsize in the batch.
     bool deferred = true;
-    if (resize)
+    if (resize && !s->spares)
         for (uint32_t t = 0; t < s->ntables && deferred; ++t) {
             const dyc_table *m = s->tables[t];
             const uint64_t cnt = h_offsets[t + 1] - h_offsets[t];
@@ -1943,7 +2072,29 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
         }
         return DYC_OK;
     };
-    if (deferred) {
+    if (resize && s->spares) {
+        // Phase A, then (while it runs) last round's replaced buffers freed and
+        // spares made to fit; then the device policy, its upsizes and phase B
+        // in one sequence. The host reads the counts between the phases only
+        // when a member needs more than its device upsize.
+        TRY(set_run(s, gr, 0, st, [&](cudaStream_t cs) {
+            return set_phase_a(s, d_offsets, d_ops, d_keys, d_vals, d_vals_out, d_bits_out, ng,
+                               true, cs);
+        }));
+        TRY(set_release_later(s, st));
+        set_fill_spares(s, st);
+        TRY(set_run(s, gr, 3, st, [&](cudaStream_t cs) { return set_policy_and_b(s, ng, cs); }));
+        CK(cudaStreamSynchronize(st));
+        set_take_device_upsizes(s, grew);
+        if (s->h_pout->host) {
+            s->last.split_phases = 1;
+            TRY(upsize_policy());
+            TRY(set_push_descs(s, st));
+            CK(cudaMemsetAsync(&s->d_pout->host, 0, sizeof(uint32_t), st));
+            TRY(set_run(s, gr, 1, st, [&](cudaStream_t cs) { return set_phase_b(s, ng, cs); }));
+            CK(cudaStreamSynchronize(st));
+        }
+    } else if (deferred) {
         TRY(set_run(s, gr, 2, st, [&](cudaStream_t cs) {
             TRY(set_phase_a(s, d_offsets, d_ops, d_keys, d_vals, d_vals_out, d_bits_out, ng,
                             resize, cs));

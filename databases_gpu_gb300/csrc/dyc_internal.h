@@ -140,7 +140,8 @@ struct ResizeJob {
     const void *old_sub;
     void *new_sub;
     uint64_t magic;  // fastmod reciprocal of 2 * old_nb
-    uint32_t old_nb, t, block0, pad;
+    uint32_t old_nb, t, block0;
+    uint32_t table;  // member of a table set (jobs the set's upsize policy lists on the device)
 };
 constexpr uint32_t kMaxResizeJobs = 768;
 constexpr uint32_t kResizeChunksPerBlock = 2048;  // 32-byte chunks a block moves
@@ -149,6 +150,30 @@ struct ResizeJobs {
     ResizeJob j[kMaxResizeJobs];
 };
 static_assert(sizeof(ResizeJobs) <= 32000, "kernel parameter block limit");
+
+// The subtable an upsize doubles (api.cpp:115-122): the first one after a
+// subtable twice its size, else subtable 0 (subtables grow in index order).
+__host__ __device__ inline uint32_t pick_up_index(const uint32_t *nb, uint32_t d) {
+    for (uint32_t i = 0; i + 1 < d; ++i)
+        if (nb[i] == 2u * nb[i + 1]) return i + 1;
+    return 0;
+}
+
+// A table-set member's next upsize target, allocated by the host ahead of
+// the round that needs it: new_sub holds 2 * old_nb buckets for subtable ti.
+// It fits only while subtable ti is the one pick_up_index names and still
+// has old_nb buckets.
+struct Spare {
+    void *new_sub;  // null: none
+    uint32_t ti, old_nb;
+};
+// What the device half of a set round's upsize policy did: jobs listed for
+// k_resize_up_list (tasks of kResizeChunksPerBlock chunks), and whether a
+// member needs more than its one device upsize (phase B then waits for the
+// host to apply the rest of the policy).
+struct SetPolicyOut {
+    uint32_t njobs, ntasks, host, pad;
+};
 
 // Launch parameters picked once per kernel from the occupancy calculator.
 struct LaunchCtx {
@@ -187,6 +212,17 @@ template <int KB> struct Ops {
                                  uint32_t old_nb, void *new_sub);
     // J.n jobs in one launch of J.blocks blocks (job block ranges filled in)
     static cudaError_t resize_up_many(const LaunchCtx &L, int sb, const ResizeJobs &J);
+    // the jobs a set's device policy listed (out->njobs of them, at most
+    // max_jobs, out->ntasks tasks), on a grid fixed at launch
+    static cudaError_t resize_up_list(const LaunchCtx &L, int sb, const ResizeJob *jobs,
+                                      const SetPolicyOut *out, uint32_t max_jobs);
+    // device half of a set round's upsize policy (one block): members whose
+    // upserts take them above upper x capacity switch to their spare subtable
+    // (descriptor rewritten, move listed in jobs, grew[t] = 1)
+    static cudaError_t set_policy(const LaunchCtx &L, Desc *descs, uint32_t ntables,
+                                  const Counters *tctr, const uint32_t *tup, const uint32_t *ter,
+                                  const Spare *spares, double upper, uint32_t slots, int sb,
+                                  ResizeJob *jobs, uint8_t *grew, SetPolicyOut *out);
     // halve an even subtable: merged buckets to new_sub, leftovers to list;
     // a tile-copy wait gives up after tile_wait_tries polls (counted in
     // *timeouts; old_sub is only read)
@@ -226,14 +262,16 @@ template <int KB> struct Ops {
                                 const void *keys, const uint32_t *tids,
                                 const unsigned long long *n_ptr, uint64_t max_n, void *vals,
                                 uint32_t vb, uint32_t *hits, unsigned long long *bad);
-    // erases and upserts of a set batch in one launch (max_n: both lists' bound)
+    // erases and upserts of a set batch in one launch (max_n: both lists'
+    // bound); nothing when *hold is nonzero (the host finishes the policy first)
     static cudaError_t set_mutate(const LaunchCtx &L, const Desc *descs, uint32_t ntables,
                                   Counters *tctr, int sb, const void *er_keys,
                                   const uint32_t *er_tids, const unsigned long long *ne_ptr,
                                   const void *up_keys, const void *up_vals, uint32_t vb,
                                   const uint32_t *up_tids, const unsigned long long *nu_ptr,
                                   uint64_t max_n, void *list_a, uint32_t *list_a_tid,
-                                  uint64_t list_cap, Counters *gctr, unsigned long long *bad);
+                                  uint64_t list_cap, Counters *gctr, unsigned long long *bad,
+                                  const uint32_t *hold = nullptr);
     static cudaError_t set_walk(const LaunchCtx &L, const Desc *descs, uint32_t ntables,
                                 Counters *tctr, int sb, const void *src, const uint32_t *src_tid,
                                 const unsigned long long *src_count, void *dst, uint32_t *dst_tid,

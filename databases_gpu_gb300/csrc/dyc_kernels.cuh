@@ -1046,16 +1046,19 @@ __global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D,
 // One thread per 32-byte chunk; the metadata word is copied to both halves
 // (keys displaced from old bucket b now have b or b+nb as first bucket).
 // ----------------------------------------------------------------------------
+// Chunks x0, x0 + step, ... below x1 of old subtable t (old_nb buckets) into
+// their low and high images in new_sub (2 * old_nb buckets, fastmod
+// reciprocal new_magic).
 template <int KB, int SB>
-__global__ void __launch_bounds__(256) k_resize_up(uint32_t t, const char *__restrict__ old_sub,
-                                                   uint32_t old_nb, char *__restrict__ new_sub,
-                                                   uint64_t new_magic, uint32_t new_nb) {
+__device__ __forceinline__ void upsize_chunks(uint32_t t, const char *__restrict__ old_sub,
+                                              uint32_t old_nb, char *__restrict__ new_sub,
+                                              uint64_t new_magic, uint64_t x0, uint64_t x1,
+                                              uint64_t step) {
     using T = SlotT<KB>;
     using Gm = Geo<KB, SB>;
     constexpr int G = Gm::kG, SPC = Gm::kSPC, WPS = T::kBytes / 4;
-    const uint64_t chunks = (uint64_t)old_nb * G;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < chunks; x += stride) {
+    const uint32_t new_nb = 2u * old_nb;
+    for (uint64_t x = x0; x < x1; x += step) {
         const uint64_t b = x / G;
         const int r = (int)(x % G);
         uint32_t w[8], lo[8], hi[8];
@@ -1083,52 +1086,59 @@ __global__ void __launch_bounds__(256) k_resize_up(uint32_t t, const char *__res
     }
 }
 
+template <int KB, int SB>
+__global__ void __launch_bounds__(256) k_resize_up(uint32_t t, const char *__restrict__ old_sub,
+                                                   uint32_t old_nb, char *__restrict__ new_sub,
+                                                   uint64_t new_magic) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    upsize_chunks<KB, SB>(t, old_sub, old_nb, new_sub, new_magic,
+                          (uint64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                          (uint64_t)old_nb * Geo<KB, SB>::kG, stride);
+}
+
 // The same split for many subtables in one launch: each block finds its job
 // (a binary search over the jobs' first blocks, the same for every thread of
 // the block) and moves up to kResizeChunksPerBlock chunks of it.
 template <int KB, int SB>
+__device__ __forceinline__ void upsize_task(const ResizeJob &jb, uint32_t task) {
+    const uint64_t chunks = (uint64_t)jb.old_nb * Geo<KB, SB>::kG;
+    const uint64_t x0 = (uint64_t)(task - jb.block0) * kResizeChunksPerBlock;
+    const uint64_t x1 = x0 + kResizeChunksPerBlock < chunks ? x0 + kResizeChunksPerBlock : chunks;
+    upsize_chunks<KB, SB>(jb.t, (const char *)jb.old_sub, jb.old_nb, (char *)jb.new_sub, jb.magic,
+                          x0 + threadIdx.x, x1, blockDim.x);
+}
+
+template <int KB, int SB>
 __global__ void __launch_bounds__(256) k_resize_up_many(const __grid_constant__ ResizeJobs J) {
-    using T = SlotT<KB>;
-    using Gm = Geo<KB, SB>;
-    constexpr int G = Gm::kG, SPC = Gm::kSPC, WPS = T::kBytes / 4;
     uint32_t lo_j = 0, hi_j = J.n;
     while (hi_j - lo_j > 1) {
         const uint32_t mid = (lo_j + hi_j) >> 1;
         if (J.j[mid].block0 <= blockIdx.x) lo_j = mid;
         else hi_j = mid;
     }
-    const ResizeJob &jb = J.j[lo_j];
-    const char *old_sub = (const char *)jb.old_sub;
-    char *new_sub = (char *)jb.new_sub;
-    const uint32_t old_nb = jb.old_nb, new_nb = 2u * jb.old_nb, t = jb.t;
-    const uint64_t chunks = (uint64_t)old_nb * G;
-    const uint64_t x0 = (uint64_t)(blockIdx.x - jb.block0) * kResizeChunksPerBlock;
-    const uint64_t x1 = x0 + kResizeChunksPerBlock < chunks ? x0 + kResizeChunksPerBlock : chunks;
-    for (uint64_t x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
-        const uint64_t b = x / G;
-        const int r = (int)(x % G);
-        uint32_t w[8], lo[8], hi[8];
-        ld_nc(old_sub + x * 32, w);
-#pragma unroll
-        for (int j = 0; j < SPC; ++j) {
-            typename T::S s;
-            T::from_words(w + j * WPS, s);
-            const int idx = r * SPC + j;
-            const bool is_meta = Gm::kMeta && idx == Gm::kTotal - 1;
-            bool to_lo = is_meta, to_hi = is_meta;
-            if (!is_meta && !T::is_empty(s)) {
-                const uint32_t nbk = fastmod(subtable_hash(fold(T::key(s)), t), jb.magic, new_nb);
-                to_lo = nbk == (uint32_t)b;
-                to_hi = !to_lo;
-            }
-#pragma unroll
-            for (int x2 = 0; x2 < WPS; ++x2) {
-                lo[j * WPS + x2] = to_lo ? w[j * WPS + x2] : 0u;
-                hi[j * WPS + x2] = to_hi ? w[j * WPS + x2] : 0u;
-            }
+    upsize_task<KB, SB>(J.j[lo_j], blockIdx.x);
+}
+
+// The jobs a table set's device policy listed (k_set_policy): their count
+// and task total are read on the device, so the grid is fixed and each
+// block takes tasks blockIdx.x, blockIdx.x + gridDim.x, ... The job count is
+// clamped to the list's capacity (max_jobs).
+template <int KB, int SB>
+__global__ void __launch_bounds__(256) k_resize_up_list(const ResizeJob *__restrict__ jobs,
+                                                        const SetPolicyOut *__restrict__ out,
+                                                        uint32_t max_jobs) {
+    const uint32_t nj = out->njobs < max_jobs ? out->njobs : max_jobs;
+    if (nj == 0) return;
+    const uint32_t ntask = out->ntasks;
+    for (uint32_t task = blockIdx.x; task < ntask; task += gridDim.x) {
+        uint32_t lo_j = 0, hi_j = nj;
+        while (hi_j - lo_j > 1) {
+            const uint32_t mid = (lo_j + hi_j) >> 1;
+            if (jobs[mid].block0 <= task) lo_j = mid;
+            else hi_j = mid;
         }
-        st_v8(new_sub + b * SB + r * 32, lo);
-        st_v8(new_sub + (b + old_nb) * SB + r * 32, hi);
+        const ResizeJob jb = jobs[lo_j];
+        if (task >= jb.block0) upsize_task<KB, SB>(jb, task);
     }
 }
 

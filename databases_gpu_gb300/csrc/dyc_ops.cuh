@@ -171,8 +171,30 @@ cudaError_t Ops<KB>::resize_up(const LaunchCtx &L, int sb, uint32_t t, const voi
     DYC_SB_DISPATCH(sb, {
         auto k = k_resize_up<KB, SB>;
         k<<<grid_for((const void *)k, L, (uint64_t)old_nb * (SB / 32)), 256, 0, L.stream>>>(
-            t, (const char *)old_sub, old_nb, (char *)new_sub, magic, new_nb);
+            t, (const char *)old_sub, old_nb, (char *)new_sub, magic);
     });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::resize_up_list(const LaunchCtx &L, int sb, const ResizeJob *jobs,
+                                    const SetPolicyOut *out, uint32_t max_jobs) {
+    if (max_jobs == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = k_resize_up_list<KB, SB>;
+        // one full wave; blocks loop over the listed tasks
+        k<<<grid_for((const void *)k, L, ~0ull >> 1), 256, 0, L.stream>>>(jobs, out, max_jobs);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::set_policy(const LaunchCtx &L, Desc *descs, uint32_t ntables,
+                                const Counters *tctr, const uint32_t *tup, const uint32_t *ter,
+                                const Spare *spares, double upper, uint32_t slots, int sb,
+                                ResizeJob *jobs, uint8_t *grew, SetPolicyOut *out) {
+    k_set_policy<KB><<<1, 1024, 0, L.stream>>>(descs, ntables, tctr, tup, ter, spares, upper, slots,
+                                               (uint32_t)sb / 32u, jobs, grew, out);
     return cudaGetLastError();
 }
 
@@ -297,13 +319,14 @@ cudaError_t Ops<KB>::set_mutate(const LaunchCtx &L, const Desc *descs, uint32_t 
                                 const void *up_keys, const void *up_vals, uint32_t vb,
                                 const uint32_t *up_tids, const unsigned long long *nu_ptr,
                                 uint64_t max_n, void *list_a, uint32_t *list_a_tid,
-                                uint64_t list_cap, Counters *gctr, unsigned long long *bad) {
+                                uint64_t list_cap, Counters *gctr, unsigned long long *bad,
+                                const uint32_t *hold) {
     if (max_n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = k_set_mutate<KB, SB>;
         k<<<tile_grid(L, max_n + 32), 256, 0, L.stream>>>(
             descs, ntables, tctr, er_keys, er_tids, ne_ptr, up_keys, up_vals, vb, up_tids, nu_ptr,
-            max_n, list_a, list_a_tid, list_cap, gctr, bad);
+            max_n, list_a, list_a_tid, list_cap, gctr, bad, hold);
     });
     return cudaGetLastError();
 }

@@ -189,7 +189,9 @@ uint64_t table_device_bytes(dyc_server *s) {
     for (uint64_t c : cap) slots += c;
     const uint64_t sb = s->tcfg.bucket_bytes;
     const uint64_t per_bucket = sb / s->slot_bytes - (sb == 128 ? 1 : 0);
-    return slots / per_bucket * sb;
+    uint64_t spare = 0;  // upsize targets kept ahead by the set
+    dyc_set_spare_bytes(s->set, &spare);
+    return slots / per_bucket * sb + spare;
 }
 
 void finish_slot_error(dyc_server *s, Slot &sl, dyc_status err) {

@@ -229,7 +229,9 @@ __global__ void __launch_bounds__(256) k_set_mutate(
     const unsigned long long *__restrict__ ne_ptr, const void *__restrict__ up_keys,
     const void *__restrict__ up_vals, uint32_t vb, const uint32_t *__restrict__ up_tids,
     const unsigned long long *__restrict__ nu_ptr, uint64_t max_n, void *list_a,
-    uint32_t *list_a_tid, uint64_t list_cap, Counters *gctr, unsigned long long *bad) {
+    uint32_t *list_a_tid, uint64_t list_cap, Counters *gctr, unsigned long long *bad,
+    const uint32_t *hold) {
+    if (hold != nullptr && *hold != 0u) return;  // the host applies the rest of the policy first
     __shared__ __align__(128) unsigned char s_stage[kWarpsPerBlock][32 * SB];
     unsigned char *stage = s_stage[threadIdx.x >> 5];
     const uint64_t ne = clamped_count(ne_ptr, max_n, bad), nu = clamped_count(nu_ptr, max_n, bad);
@@ -409,6 +411,126 @@ __global__ void __launch_bounds__(256) k_set_walk(const Desc *__restrict__ descs
     if (threadIdx.x == 0) {
         if (s_sum[0]) atomicAdd(&gctr->inserted, s_sum[0]);
         if (s_sum[1]) atomicAdd(&gctr->evict_steps, s_sum[1]);
+    }
+}
+
+// ----------------------------------------------------------------------------
+// Device half of a set round's upsize policy, between phase A (which counted
+// each member's upserts tup[t] and erases ter[t]) and phase B (which applies
+// them). The rule is the host's (hash_insert_batch, api.cpp:359-369, per
+// member): upsize while size - erases + upserts > upper x capacity. Here a
+// member over the bound is upsized once, into its spare (Spare: a subtable
+// of twice the buckets of the one pick_up_index names, allocated by the
+// host before the round); its descriptor switches to the spare at once and
+// the move is listed for k_resize_up_list, which runs before phase B. A
+// member still over the bound after that upsize, or without a fitting
+// spare, sets out->host: phase B's mutate kernel then does nothing and the
+// host applies the rest of the policy before running phase B itself. The
+// capacity and the comparison are the host's, in doubles. One block walks
+// the members in tiles of blockDim.x (a scan gives each listed move its
+// place and its first task).
+// ----------------------------------------------------------------------------
+template <int KB>
+__global__ void __launch_bounds__(1024) k_set_policy(Desc *__restrict__ descs, uint32_t ntables,
+                                                     const Counters *__restrict__ tctr,
+                                                     const uint32_t *__restrict__ tup,
+                                                     const uint32_t *__restrict__ ter,
+                                                     const Spare *__restrict__ spares, double upper,
+                                                     uint32_t slots, uint32_t chunks_per_bucket,
+                                                     ResizeJob *__restrict__ jobs,
+                                                     uint8_t *__restrict__ grew,
+                                                     SetPolicyOut *__restrict__ out) {
+    __shared__ uint32_t s_wj[32], s_wt[32];  // per-warp inclusive sums of the tile
+    __shared__ uint32_t s_cj, s_ct, s_host;   // jobs / tasks before the tile; host needed
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5, nw = blockDim.x >> 5;
+    if (tid == 0) {
+        s_cj = 0u;
+        s_ct = 0u;
+        s_host = 0u;
+    }
+    __syncthreads();
+    for (uint32_t base = 0; base < ntables; base += blockDim.x) {
+        const uint32_t t = base + tid;
+        uint32_t want = 0u, tasks = 0u, ti = 0u, onb = 0u;
+        if (t < ntables) {
+            const Desc &D = descs[t];
+            const uint32_t d = D.d < (uint32_t)kMaxSub ? D.d : (uint32_t)kMaxSub;
+            uint64_t nbs = 0;
+            for (uint32_t i = 0; i < d; ++i) nbs += D.nb[i];
+            const double cap = (double)(nbs * slots);
+            const double bse = (double)tctr[t].size - (double)ter[t];
+            const double up = (double)tup[t];
+            if (tup[t] != 0u && bse + up > upper * cap) {
+                ti = pick_up_index(D.nb, d);
+                onb = D.nb[ti];
+                const Spare sp = spares[t];
+                if (sp.new_sub != nullptr && sp.ti == ti && sp.old_nb == onb && onb != 0u &&
+                    onb <= 0x7fffffffu) {
+                    want = 1u;
+                    tasks = (uint32_t)(((uint64_t)onb * chunks_per_bucket + kResizeChunksPerBlock -
+                                        1) / kResizeChunksPerBlock);
+                    if (bse + up > upper * (cap + (double)((uint64_t)onb * slots))) s_host = 1u;
+                } else {
+                    s_host = 1u;
+                }
+            }
+            grew[t] = (uint8_t)want;
+        }
+        // place of this member's move among the tile's (exclusive scans)
+        uint32_t ij = want, it = tasks;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t a = __shfl_up_sync(kFull, ij, o), b = __shfl_up_sync(kFull, it, o);
+            if (lane >= (uint32_t)o) {
+                ij += a;
+                it += b;
+            }
+        }
+        if (lane == 31u) {
+            s_wj[w] = ij;
+            s_wt[w] = it;
+        }
+        __syncthreads();
+        if (w == 0) {
+            uint32_t vj = lane < nw ? s_wj[lane] : 0u, vt = lane < nw ? s_wt[lane] : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t a = __shfl_up_sync(kFull, vj, o), b = __shfl_up_sync(kFull, vt, o);
+                if (lane >= (uint32_t)o) {
+                    vj += a;
+                    vt += b;
+                }
+            }
+            if (lane < nw) {
+                s_wj[lane] = vj;
+                s_wt[lane] = vt;
+            }
+        }
+        __syncthreads();
+        if (want) {
+            const uint32_t pj = s_cj + (w ? s_wj[w - 1] : 0u) + ij - want;
+            const uint32_t pt = s_ct + (w ? s_wt[w - 1] : 0u) + it - tasks;
+            Desc &D = descs[t];
+            void *nw_sub = spares[t].new_sub;
+            const uint32_t nnb = 2u * onb;
+            const uint64_t mg = fastmod_magic(nnb);
+            jobs[pj] = ResizeJob{D.sub[ti], nw_sub, mg, onb, ti, pt, t};
+            D.sub[ti] = nw_sub;
+            D.nb[ti] = nnb;
+            D.magic[ti] = mg;
+        }
+        __syncthreads();  // the carries and the warp sums are read above
+        if (tid == 0) {
+            s_cj += s_wj[nw - 1];
+            s_ct += s_wt[nw - 1];
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        out->njobs = s_cj;
+        out->ntasks = s_ct;
+        out->host = s_host;
+        out->pad = 0u;
     }
 }
 

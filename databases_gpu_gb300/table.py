@@ -337,18 +337,22 @@ class DyCuckooSet:
     launch sequence per mixed batch for the whole set.
 
     sizes: per-table key counts to size for; num_subtables: optional
-    per-table subtable counts. Other arguments as for DyCuckoo (shared)."""
+    per-table subtable counts; device_upsize: 0 applies a round's upsize
+    policy on the device from upsize targets allocated ahead, 1 on the host
+    between the round's phases (dyc_config.device_upsize). Other arguments
+    as for DyCuckoo (shared)."""
 
     def __init__(self, sizes, key_bytes: int = 4, value_bytes: int | None = None,
                  num_subtables=None, bucket_bytes: int = 128, max_evictions: int = 64,
                  auto_resize: bool = True, upper_load: float = UPPER_BOUND,
                  lower_load: float = LOWER_BOUND,
                  min_downsize_capacity: int = MIN_DOWNSIZE_CAPACITY, device: int = 0,
-                 default_subtables: int = 4, l2_resident: int = 0):
+                 default_subtables: int = 4, l2_resident: int = 0, device_upsize: int = 0):
         L = _lib.lib()
         cfg = _lib.DycConfig()
         L.dyc_config_default(C.byref(cfg))
         cfg.l2_resident = l2_resident
+        cfg.device_upsize = device_upsize
         cfg.key_bytes = key_bytes
         cfg.value_bytes = value_bytes if value_bytes is not None else key_bytes
         cfg.num_subtables = default_subtables
@@ -416,6 +420,13 @@ class DyCuckooSet:
         st = _lib.DycOpStats()
         check(self.L.dyc_set_last_stats(self._h, C.byref(st)), "dyc_set_last_stats")
         return st.as_dict()
+
+    def spare_bytes(self) -> int:
+        """Device bytes held beside the members' subtables (upsize targets
+        allocated ahead, replaced subtables not yet freed)."""
+        b = C.c_uint64()
+        check(self.L.dyc_set_spare_bytes(self._h, C.byref(b)), "dyc_set_spare_bytes")
+        return int(b.value)
 
     def apply(self, offsets, ops, keys, values, out=None, bits=None, h_offsets=None,
               each: bool = False, graph: bool = False, no_resize: bool = False, stream=None):

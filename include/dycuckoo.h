@@ -94,7 +94,16 @@ typedef struct dyc_config {
                                 cache policy and find streams its keys and results with
                                 evict_first, so a large batch does not push the table out
                                 of the L2. No counterpart in the reference. */
-    uint32_t reserved[6];
+    uint32_t device_upsize;  /* table sets (dyc_set_apply with auto_resize): 0 (default)
+                                keeps one upsize target allocated ahead for every member,
+                                so a round's upsize policy runs on the device between the
+                                round's two phases, inside its launch sequence; a member
+                                that needs a second upsize in the round hands the rest of
+                                the policy to the host. Costs device memory: a spare holds
+                                twice the buckets of the member's next subtable to grow
+                                (dyc_set_spare_bytes). 1: the host applies the policy
+                                between the phases. Results are the same either way. */
+    uint32_t reserved[5];
 } dyc_config;
 
 /* Per-call flags. */
@@ -351,6 +360,11 @@ dyc_status dyc_set_table(dyc_set *s, uint32_t i, dyc_table **out);
 
 /* Live keys and slot capacity of every member (host arrays of ntables). */
 dyc_status dyc_set_sizes(dyc_set *s, uint64_t *h_sizes, uint64_t *h_capacities);
+
+/* Device bytes the set holds beside its members' subtables: the upsize
+ * targets of dyc_config.device_upsize (0 when it is 1 or auto_resize is off)
+ * and the subtables they replaced, freed at the next dyc_set_apply. */
+dyc_status dyc_set_spare_bytes(dyc_set *s, uint64_t *bytes);
 
 /* Mixed batch over the set (see above). Returns when the batch is in the
  * tables. flags: DYC_FLAG_NO_RESIZE, DYC_FLAG_GRAPH. d_offsets must hold

@@ -224,21 +224,24 @@ def test_set_graph_reuses_buffers_across_batch_sizes():
 
 
 @pytest.mark.parametrize("kind", ["new_keys", "half_updates"])
-def test_set_deferred_upsize_matches_per_table_path(kind):
+@pytest.mark.parametrize("device_upsize", [0, 1])
+def test_set_deferred_upsize_matches_per_table_path(kind, device_upsize):
     """new_keys: tables preloaded to 70 % of their slots (below the 0.8 upper
     bound), then a batch of new keys worth 15 % more. half_updates: preloaded
     to 70 %, a batch worth 16 % of which half update present keys, so only
     counting every insert (as the reference's policy does) passes the bound.
-    Either batch keeps the tables within 90 % (halfway from the bound to
-    full) even if all its ops were new keys, so the set runs it without a host
-    round trip and applies the upsize policy afterwards (entries the fuller
-    tables could not place take the overflow path). Results, sizes,
-    capacities and contents equal those of one dyc_apply per table, which
-    upsizes before inserting."""
+    One upsize per table brings each back under the bound. With upsize
+    targets kept ahead (device_upsize 0) the policy runs on the device
+    between the phases; without them (1) either batch keeps the tables within
+    90 % (halfway from the bound to full) even if all its ops were new keys,
+    so the set runs it without a host round trip and applies the upsize
+    policy afterwards (entries the fuller tables could not place take the
+    overflow path). Either way results, sizes, capacities and contents equal
+    those of one dyc_apply per table, which upsizes before inserting."""
     import torch
     rng = np.random.default_rng(21)
     nt = 8
-    A = _dg().DyCuckooSet([3000] * nt)
+    A = _dg().DyCuckooSet([3000] * nt, device_upsize=device_upsize)
     B = _dg().DyCuckooSet([3000] * nt)
     _, caps = A.sizes()
     maps = [O.Map() for _ in range(nt)]
@@ -279,7 +282,7 @@ def test_set_deferred_upsize_matches_per_table_path(kind):
     assert np.array_equal(sza, szb)
     assert np.array_equal(capa, capb), (capa, capb)
     assert sa["resizes_up"] >= nt
-    assert sa["split_phases"] == 0  # the policy ran after the batch
+    assert sa["split_phases"] == 0  # no host read between the phases
     for t in range(nt):
         assert_same_contents(A.table(t), maps[t], "table %d contents" % t)
     A.close()
@@ -287,15 +290,19 @@ def test_set_deferred_upsize_matches_per_table_path(kind):
 
 
 @pytest.mark.parametrize("bucket_bytes,key_bytes", [(128, 4), (64, 8)])
-def test_set_upsize_waves_match_per_table_path(bucket_bytes, key_bytes):
+@pytest.mark.parametrize("device_upsize", [0, 1])
+def test_set_upsize_waves_match_per_table_path(bucket_bytes, key_bytes, device_upsize):
     """Many tiny tables, each hit by enough inserts to need several upsizes in
     one batch: the set issues them in waves (one launch per wave for all its
-    tables). Capacities, sizes, results and contents equal those of one
-    dyc_apply per table, which upsizes table by table."""
+    tables; with upsize targets kept ahead the device makes the first upsize
+    of each table and the host the rest). Capacities, sizes, results and
+    contents equal those of one dyc_apply per table, which upsizes table by
+    table."""
     import torch
     rng = np.random.default_rng(23)
     nt = 200
-    A = _dg().DyCuckooSet([64] * nt, key_bytes=key_bytes, bucket_bytes=bucket_bytes)
+    A = _dg().DyCuckooSet([64] * nt, key_bytes=key_bytes, bucket_bytes=bucket_bytes,
+                          device_upsize=device_upsize)
     B = _dg().DyCuckooSet([64] * nt, key_bytes=key_bytes, bucket_bytes=bucket_bytes)
     maps = [O.Map() for _ in range(nt)]
     for r in range(2):
@@ -326,6 +333,90 @@ def test_set_upsize_waves_match_per_table_path(bucket_bytes, key_bytes):
         assert np.array_equal(sza, szb) and np.array_equal(capa, capb)
         assert st["resizes_up"] > 2 * nt  # several upsizes per table
     for t in (0, 99, nt - 1):
+        assert_same_contents(A.table(t), maps[t], "table %d contents" % t)
+    A.close()
+    B.close()
+
+
+@pytest.mark.parametrize("key_bytes", [4, 8])
+def test_set_device_upsize_policy_matches_host_policy(key_bytes):
+    """Tables of 2^5..2^9 keys preloaded near the 0.8 bound take six rounds
+    of mixed batches (from fixed buffers: the later rounds replay captured
+    graphs) that
+    make many of them grow: a set that keeps an upsize target ahead for every
+    member (the policy on the device, between the phases) and one that
+    applies the policy on the host between the phases give the same results,
+    sizes, capacities and contents, equal to the oracle's. Rounds in which
+    every growing table needs one upsize run with no host read between the
+    phases; the spare targets are counted by dyc_set_spare_bytes."""
+    import torch
+    rng = np.random.default_rng(41)
+    nt = 300
+    sizes = np.round(2.0 ** (5 + 4 * rng.random(nt))).astype(np.int64)
+    kw = dict(key_bytes=key_bytes, value_bytes=key_bytes)
+    A = _dg().DyCuckooSet(sizes, device_upsize=0, **kw)
+    B = _dg().DyCuckooSet(sizes, device_upsize=1, **kw)
+    maps = [O.Map() for _ in range(nt)]
+    npk, tdt = (np.uint32, np.int32) if key_bytes == 4 else (np.uint64, np.int64)
+    top = (1 << 31) if key_bytes == 4 else (1 << 62)
+    live = []
+    for t in range(nt):
+        k = np.unique(rng.integers(1, top, int(0.78 * sizes[t]) + 1, dtype=np.int64)).astype(npk)
+        v = rng.integers(0, top, k.size, dtype=np.int64).astype(npk)
+        dk = torch.from_numpy(k.view(tdt)).cuda()
+        dv = torch.from_numpy(v.view(tdt)).cuda()
+        A.table(t).insert(dk, dv)
+        B.table(t).insert(dk, dv)
+        maps[t].insert(k.astype(np.uint64), v.astype(np.uint64))
+        live.append(k)
+    # fixed buffers (rounds 2.. replay the captured graphs of each set)
+    cap = int(2 * (sizes // 8).sum()) + 32
+    tt = torch.int32 if key_bytes == 4 else torch.int64
+    b_ops = torch.empty(cap, dtype=torch.uint8, device="cuda")
+    b_keys = torch.empty(cap, dtype=tt, device="cuda")
+    b_vals = torch.empty(cap, dtype=tt, device="cuda")
+    b_off = torch.empty(nt + 1, dtype=torch.int32, device="cuda")
+    outs = [(torch.empty(cap, dtype=tt, device="cuda"),
+             torch.empty(cap // 32 + 1, dtype=torch.int32, device="cuda")) for _ in range(2)]
+    device_rounds = 0
+    for r in range(6):
+        cnt = rng.integers(0, 3, nt) * (sizes // 8)
+        off = np.zeros(nt + 1, np.uint32)
+        off[1:] = np.cumsum(cnt)
+        n = int(off[-1])
+        ops = rng.choice(np.array([0, 1, 2], np.uint8), size=n, p=[0.3, 0.6, 0.1])
+        keys = rng.integers(1, top, n, dtype=np.int64).astype(npk)
+        for t in range(nt):  # a third of each table's ops on its present keys
+            a, b = int(off[t]), int(off[t + 1])
+            m = (b - a) // 3
+            if m:
+                keys[a:a + m] = rng.choice(live[t], m)
+        vals = rng.integers(0, top, n, dtype=np.int64).astype(npk)
+        b_ops[:n].copy_(torch.from_numpy(ops))
+        b_keys[:n].copy_(torch.from_numpy(keys.view(tdt)))
+        b_vals[:n].copy_(torch.from_numpy(vals.view(tdt)))
+        b_off.copy_(torch.from_numpy(off.view(np.int32)))
+        do, dk, dv, nw = b_ops[:n], b_keys[:n], b_vals[:n], (n + 31) // 32
+        oa, ba = A.apply(b_off, do, dk, dv, out=outs[0][0][:n], bits=outs[0][1][:nw],
+                         h_offsets=off, graph=True)
+        sa = A.stats()
+        ob, bb = B.apply(b_off, do, dk, dv, out=outs[1][0][:n], bits=outs[1][1][:nw],
+                         h_offsets=off, graph=True)
+        _check_round(A, maps, off, do, dk, dv, oa, ba, "round %d" % r)
+        assert bool((oa == ob).all()) and bool((ba == bb).all()), "round %d" % r
+        sza, capa = A.sizes()
+        szb, capb = B.sizes()
+        assert np.array_equal(sza, szb) and np.array_equal(capa, capb), "round %d" % r
+        if sa["resizes_up"] > 0 and sa["split_phases"] == 0:
+            device_rounds += 1
+        for t in range(nt):
+            a, b = int(off[t]), int(off[t + 1])
+            ins = keys[a:b][ops[a:b] == 1]
+            if ins.size:
+                live[t] = np.union1d(live[t], ins)
+    assert device_rounds >= 2, device_rounds
+    assert A.spare_bytes() > 0 and B.spare_bytes() == 0
+    for t in range(0, nt, 23):
         assert_same_contents(A.table(t), maps[t], "table %d contents" % t)
     A.close()
     B.close()
