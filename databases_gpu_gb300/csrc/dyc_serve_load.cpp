@@ -63,6 +63,7 @@ int main(int argc, char **argv) {
     const uint64_t max_step = (uint64_t)arg(argc, argv, "--max-step-ops", 1 << 22);
     const int pool_log2 = (int)arg(argc, argv, "--pool-log2", 24);
     const uint64_t seed = (uint64_t)arg(argc, argv, "--seed", 10327);
+    const int device_upsize = (int)arg(argc, argv, "--device-upsize", 0);
     std::mt19937_64 rng(seed);
     std::uniform_real_distribution<double> U(0.0, 1.0);
 
@@ -73,6 +74,7 @@ int main(int argc, char **argv) {
     dyc_config_default(&cfg);
     cfg.key_bytes = 8;
     cfg.value_bytes = 4;
+    cfg.device_upsize = (uint32_t)device_upsize;
     dyc_server_config scfg;
     dyc_server_config_default(&scfg);
     scfg.hbm_cap_bytes = (uint64_t)(cap_gb * 1e9);
