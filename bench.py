@@ -727,6 +727,8 @@ def main():
     ap.add_argument("--log2-cpu-sample", type=int, default=24)
     ap.add_argument("--bucket-bytes", type=int, default=128)
     ap.add_argument("--max-evictions", type=int, default=2048)
+    ap.add_argument("--l2-resident", type=int, default=0, choices=[0, 1, 2],
+                    help="dyc_config.l2_resident of the find table (0: by its size)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-reference-gpu", action="store_true",
                     help="skip timing the reference's own GPU kernels")
@@ -791,7 +793,7 @@ def main():
     keys = as_i32(keys64, torch)
     vals = torch.arange(1, N + 1, dtype=torch.int32, device=dev)
     t = dg.DyCuckoo(int(N / 0.9), bucket_bytes=args.bucket_bytes, auto_resize=False,
-                    max_evictions=args.max_evictions, device=local)
+                    max_evictions=args.max_evictions, device=local, l2_resident=args.l2_resident)
     torch.cuda.synchronize()
     tb = time.perf_counter()
     st = t.insert(keys, vals, unique=True, new_keys=True)

@@ -161,7 +161,6 @@ struct dyc_table {
     void *pipe_buf[3] = {nullptr, nullptr, nullptr};
     size_t pipe_bytes = 0;
     uint64_t size = 0, capacity = 0;
-    uint64_t l2_bytes = 0;  // the device's L2 (the residency rule of cfg.l2_resident)
     dyc_op_stats last{};
     // entries a failed call could not place (slot images, held_n of them);
     // not in the device size counter; the next call places them first
@@ -171,20 +170,16 @@ struct dyc_table {
 
 namespace {
 
-// Desc::l2_keep from the table's current subtables (cfg.l2_resident: 0 when
-// they take at most 1.5x the L2, 1 never, 2 always); called whenever they
-// change. Measured on GB300 (2^26- and 2^20-key find batches): tables of up
-// to half the L2 stay there under any policy (54.7 G finds/s either way);
-// at 76 MB the policy gains 0.8 %, at 152 MB 0.6 % (2^26 batches) to 4.5 %
-// (2^20 batches); at 2.4 GB it changes nothing.
-bool l2_keep_rule(uint64_t bytes, uint64_t l2_bytes) { return 2 * bytes <= 3 * l2_bytes; }
-
-void refresh_l2(dyc_table *t) {
-    uint64_t bytes = 0;
-    for (uint32_t i = 0; i < t->D.d; ++i) bytes += (uint64_t)t->D.nb[i] * t->sb;
-    const uint32_t mode = t->cfg.l2_resident;
-    t->D.l2_keep = (mode == 2u || (mode == 0u && l2_keep_rule(bytes, t->l2_bytes))) ? 1u : 0u;
-}
+// Desc::l2_keep from cfg.l2_resident: 2 asks the L2 to keep the table's
+// bucket lines (evict_last hints on every probe, evict_first on the find's
+// key and result streams); 0 and 1 use plain accesses. Measured on GB300
+// with the find kernel: a table of 1.2x the L2 (2^24 keys) found 48.1 G/s
+// with the hints and 51.1 G/s with plain loads (Zipf 0.99: 35.0 both); at
+// 2^28 keys hinted loads even at evict_normal priority ran Zipf batches at
+// 15.6 G/s against 39.4 plain (many warps reading one hot line), and tables
+// of up to half the L2 stay resident under any policy. So the hints are
+// opt-in, and kernels take them only through their HINT instantiation.
+void refresh_l2(dyc_table *t) { t->D.l2_keep = t->cfg.l2_resident == 2u ? 1u : 0u; }
 
 dyc_status set_device(dyc_table *t) {
     int cur = -1;
@@ -687,10 +682,7 @@ dyc_status create_impl(const dyc_config *cfg, Counters *ext_d, Counters *ext_h, 
         cudaError_t e = cudaSetDevice(t->device);
         if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "cudaSetDevice(%d): %s", t->device, cudaGetErrorString(e)));
         e = cudaDeviceGetAttribute(&t->sms, cudaDevAttrMultiProcessorCount, t->device);
-        int l2 = 0;
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, t->device);
         if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "device attribute: %s", cudaGetErrorString(e)));
-        t->l2_bytes = (uint64_t)l2;
     }
     // hashAPI::hashAPI sizing (api.cpp:47-54) with this table's slots/bucket
     const uint64_t per = (uint64_t)cfg->num_subtables * t->slots;
@@ -1238,7 +1230,8 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     // state of every distinct key before the batch
     if (e == cudaSuccess)
         e = KB_CALL(t, set_find, L, t->d_desc, 1u, t->sb, A.dkey, nullptr,
-                    &A.ctr[dyc::kCtrDistinct], n, A.pre_val, vb, A.pre_hit, &A.ctr[dyc::kCtrBad]);
+                    &A.ctr[dyc::kCtrDistinct], n, A.pre_val, vb, A.pre_hit, &A.ctr[dyc::kCtrBad],
+                    t->D.l2_keep != 0u);
     if (e == cudaSuccess)
         e = KB_CALL(t, apply_scatter, L, A, n, nullptr, ops, vals, vb, vals_out, bits_out);
     if (e == cudaSuccess) e = KB_CALL(t, apply_replay, L, A, ops, vals, vb, vals_out, bits_out, n, n);
@@ -1250,7 +1243,8 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     }
     e = KB_CALL(t, set_mutate, L, t->d_desc, 1u, t->d_ctr, t->sb, A.er_key, nullptr,
                 &A.ctr[dyc::kCtrEr], A.up_key, A.up_val, vb, nullptr, &A.ctr[dyc::kCtrUp], n,
-                t->S.list_a, nullptr, t->S.list_cap, t->d_ctr, &A.ctr[dyc::kCtrBad]);
+                t->S.list_a, nullptr, t->S.list_cap, t->d_ctr, &A.ctr[dyc::kCtrBad], nullptr,
+                t->D.l2_keep != 0u);
     if (e == cudaSuccess)
         e = KB_CALL(t, set_walk, L, t->d_desc, 1u, t->d_ctr, t->sb, t->S.list_a, nullptr,
                     &t->d_ctr->pending, t->S.list_b, nullptr, &t->d_ctr->overflow,
@@ -1567,7 +1561,7 @@ dyc_status set_phase_a(dyc_set *s, const uint32_t *d_off, const uint8_t *ops, co
     if (e == cudaSuccess)
         e = SET_KB_CALL(s, set_find, L, s->d_desc, s->ntables, s->sb, A.dkey, A.dtid,
                         &A.ctr[dyc::kCtrDistinct], n, A.pre_val, vb, A.pre_hit,
-                        &A.ctr[dyc::kCtrBad]);
+                        &A.ctr[dyc::kCtrBad], s->tables[0]->D.l2_keep != 0u);
     if (e == cudaSuccess)
         e = SET_KB_CALL(s, apply_scatter, L, A, n, d_n, ops, vals, vb, out, bits);
     if (e == cudaSuccess)
@@ -1590,7 +1584,8 @@ dyc_status set_phase_b(dyc_set *s, uint64_t n, cudaStream_t st, const uint32_t *
     cudaError_t e = SET_KB_CALL(s, set_mutate, L, s->d_desc, s->ntables, s->d_tctr, s->sb,
                                 A.er_key, A.er_tid, &A.ctr[dyc::kCtrEr], A.up_key, A.up_val,
                                 (uint32_t)s->vb, A.up_tid, &A.ctr[dyc::kCtrUp], n, s->list_a,
-                                s->tid_a, s->list_cap, s->d_gctr, &A.ctr[dyc::kCtrBad], hold);
+                                s->tid_a, s->list_cap, s->d_gctr, &A.ctr[dyc::kCtrBad], hold,
+                                s->tables[0]->D.l2_keep != 0u);
     if (e == cudaSuccess)
         e = SET_KB_CALL(s, set_walk, L, s->d_desc, s->ntables, s->d_tctr, s->sb, s->list_a,
                         s->tid_a, &s->d_gctr->pending, s->list_b, s->tid_b,
@@ -1866,19 +1861,6 @@ dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_
         if (num_subtables) c.num_subtables = num_subtables[t];
         dyc_status r = create_impl(&c, s->d_tctr + t, s->h_tctr + t, false, &s->tables[t]);
         if (r != DYC_OK) return undo(r);
-    }
-    // L2 residency of a set is decided by all its members together (their
-    // batches run in one pass): in the default mode they keep their lines
-    // only if the whole set passes the single-table rule
-    if (cfg->l2_resident == 0u) {
-        uint64_t bytes = 0;
-        for (dyc_table *m : s->tables)
-            for (uint32_t i = 0; i < m->D.d; ++i) bytes += (uint64_t)m->D.nb[i] * m->sb;
-        const uint32_t mode = l2_keep_rule(bytes, s->tables[0]->l2_bytes) ? 2u : 1u;
-        for (dyc_table *m : s->tables) {
-            m->cfg.l2_resident = mode;
-            refresh_l2(m);
-        }
     }
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "set setup: %s", cudaGetErrorString(e)));

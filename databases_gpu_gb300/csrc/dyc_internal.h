@@ -257,11 +257,13 @@ template <int KB> struct Ops {
     // The set kernels below read their item counts from device memory and
     // clamp them to max_n / max_entries (the capacity of the lists behind
     // them); a table id at or above ntables skips its item. Either event is
-    // counted in *bad.
+    // counted in *bad. hint: the members keep their lines in the L2 (their
+    // probes carry L2 eviction-priority hints; plain loads otherwise).
     static cudaError_t set_find(const LaunchCtx &L, const Desc *descs, uint32_t ntables, int sb,
                                 const void *keys, const uint32_t *tids,
                                 const unsigned long long *n_ptr, uint64_t max_n, void *vals,
-                                uint32_t vb, uint32_t *hits, unsigned long long *bad);
+                                uint32_t vb, uint32_t *hits, unsigned long long *bad,
+                                bool hint = false);
     // erases and upserts of a set batch in one launch (max_n: both lists'
     // bound); nothing when *hold is nonzero (the host finishes the policy first)
     static cudaError_t set_mutate(const LaunchCtx &L, const Desc *descs, uint32_t ntables,
@@ -271,7 +273,7 @@ template <int KB> struct Ops {
                                   const uint32_t *up_tids, const unsigned long long *nu_ptr,
                                   uint64_t max_n, void *list_a, uint32_t *list_a_tid,
                                   uint64_t list_cap, Counters *gctr, unsigned long long *bad,
-                                  const uint32_t *hold = nullptr);
+                                  const uint32_t *hold = nullptr, bool hint = false);
     static cudaError_t set_walk(const LaunchCtx &L, const Desc *descs, uint32_t ntables,
                                 Counters *tctr, int sb, const void *src, const uint32_t *src_tid,
                                 const unsigned long long *src_count, void *dst, uint32_t *dst_tid,

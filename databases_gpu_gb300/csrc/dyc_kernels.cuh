@@ -528,8 +528,13 @@ __global__ void __launch_bounds__(256) k_dedup_winners(const __grid_constant__ S
 // Five resident blocks per SM for 4-byte keys (48 registers, a 16-byte
 // spill): +1.7 % on uniform hits at 2^28 keys, 10 %-hit finds unchanged;
 // six blocks and larger or smaller tiles per block measured no better.
+// HINT (a table that keeps its lines in the L2, Desc::l2_keep): loads and
+// stores carry L2 eviction-priority hints. Other tables use plain accesses:
+// hinted loads of a line many warps read at once (the hot keys of a Zipf
+// batch) measured 2.5x slower than plain ones (15.6 vs 39.4 G finds/s at
+// Zipf 0.99 on 2^28 keys; uniform 39.3 vs 40.4).
 // ----------------------------------------------------------------------------
-template <int KB, int SB>
+template <int KB, int SB, bool HINT>
 __global__ void __launch_bounds__(256, KB == 4 ? 5 : 1) k_find(const __grid_constant__ Desc D,
                                               const void *__restrict__ keys,
                                               void *__restrict__ vals, uint32_t vb,
@@ -540,30 +545,39 @@ __global__ void __launch_bounds__(256, KB == 4 ? 5 : 1) k_find(const __grid_cons
     unsigned char *stage = s_stage[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t step = warp_stride();
-    const L2Pol pol = l2_policies(D.l2_keep != 0u);
+    L2Pol pol{0ull, 0ull};
+    if constexpr (HINT) pol = l2_policies(true);
     for (uint64_t base = warp_base(); base < n; base += step) {
         const uint64_t i = base + lane;
         typename T::K k = 0;
-        if (i < n) k = load_key_pol<KB>(keys, i, pol.stream);
+        if (i < n) {
+            if constexpr (HINT) k = load_key_pol<KB>(keys, i, pol.stream);
+            else k = load_key<KB>(keys, i);
+        }
         const bool act = k != 0;
         const uint32_t hk = fold(k);
         const Pair p = pair_of(hk, D.d);
         const char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
-        const KvOut r1 = kv_probe<KB, SB, 1, true>(p1, k, act, stage, pol.table);
+        const KvOut r1 = kv_probe<KB, SB, 1, HINT>(p1, k, act, stage, pol.table);
         bool hit = act && r1.match >= 0;
         uint64_t v = hit ? r1.value : 0ull;
         const bool need2 = act && !hit && (!Gm::kMeta || r1.overflow);
         if (__any_sync(kFull, need2)) {
             const char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-            const KvOut r2 = kv_probe<KB, SB, 1, true>(p2, k, need2, stage, pol.table);
+            const KvOut r2 = kv_probe<KB, SB, 1, HINT>(p2, k, need2, stage, pol.table);
             if (need2 && r2.match >= 0) {
                 hit = true;
                 v = r2.value;
             }
         }
-        if (i < n) store_val_pol(vals, vb, i, v, pol.stream);
         const unsigned m = __ballot_sync(kFull, hit);
-        if (hits != nullptr && lane == 0) store_u32_pol(hits + (base >> 5), m, pol.stream);
+        if constexpr (HINT) {
+            if (i < n) store_val_pol(vals, vb, i, v, pol.stream);
+            if (hits != nullptr && lane == 0) store_u32_pol(hits + (base >> 5), m, pol.stream);
+        } else {
+            if (i < n) store_val(vals, vb, i, v);
+            if (hits != nullptr && lane == 0) hits[base >> 5] = m;
+        }
     }
 }
 
@@ -572,7 +586,7 @@ __global__ void __launch_bounds__(256, KB == 4 ? 5 : 1) k_find(const __grid_cons
 // the first-probe bucket, else in the second (marking the first bucket's
 // overflow bit first); ops left without a slot go to list_a.
 // ----------------------------------------------------------------------------
-template <int KB, int SB>
+template <int KB, int SB, bool HINT>
 __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
                                                const __grid_constant__ Scratch S, int use_dedup,
                                                int new_keys, const void *__restrict__ keys,
@@ -584,7 +598,7 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
     __shared__ __align__(128) unsigned char s_stage[SB >= 64 ? kWarpsPerBlock : 1][32 * SB];
     unsigned char *stage = s_stage[SB >= 64 ? (threadIdx.x >> 5) : 0];
     const uint64_t step = warp_stride();
-    const unsigned long long tpol = l2_policies(D.l2_keep != 0u).table;
+    const unsigned long long tpol = HINT ? l2_policies(true).table : 0ull;
     uint32_t n_ins = 0, n_upd = 0, n_rej = 0, n_sup = 0;
     for (uint64_t base = warp_base(); base < n; base += step) {
         const uint64_t i = base + (threadIdx.x & 31);
@@ -606,7 +620,7 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
         const Pair p = pair_of(hk, D.d);
         char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
         char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-        const KvOut r1 = place_probe<KB, SB, true>(p1, k, act, p.first, D.d, stage, tpol);
+        const KvOut r1 = place_probe<KB, SB, HINT>(p1, k, act, p.first, D.d, stage, tpol);
         const bool found1 = act && r1.match >= 0;
         // the second bucket is needed to look for the key (upsert, unless the
         // first bucket's overflow bit rules it out) or for an empty slot
@@ -614,7 +628,7 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Desc D,
             act && !found1 && ((!new_keys && (!Gm::kMeta || r1.overflow)) || r1.empty == 0u);
         KvOut r2{-1, 0ull, false, 0u};
         if (__any_sync(kFull, check2))
-            r2 = place_probe<KB, SB, true>(p2, k, check2, p.second, D.d, stage, tpol);
+            r2 = place_probe<KB, SB, HINT>(p2, k, check2, p.second, D.d, stage, tpol);
         // An update rewrites the key's own slot with a plain store: the keys
         // of the kernel are distinct (dedup, or the caller's promise) and
         // its other writes only claim empty slots, so nothing else writes
@@ -966,7 +980,7 @@ __global__ void __launch_bounds__(256) k_walk(const __grid_constant__ Desc D,
 // cleared with a CAS; the second bucket is only probed when the first one's
 // overflow bit allows the key to be there.
 // ----------------------------------------------------------------------------
-template <int KB, int SB>
+template <int KB, int SB, bool HINT>
 __global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D,
                                                const __grid_constant__ Scratch S, int use_dedup,
                                                const void *__restrict__ keys, uint64_t n,
@@ -977,7 +991,7 @@ __global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D,
     unsigned char *stage = s_stage[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t step = warp_stride();
-    const unsigned long long tpol = l2_policies(D.l2_keep != 0u).table;
+    const unsigned long long tpol = HINT ? l2_policies(true).table : 0ull;
     uint32_t n_del = 0, n_sup = 0;
     for (uint64_t base = warp_base(); base < n; base += step) {
         const uint64_t i = base + lane;
@@ -993,7 +1007,7 @@ __global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D,
         const uint32_t hk = fold(k);
         const Pair p = pair_of(hk, D.d);
         char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
-        const KvOut r1 = kv_probe<KB, SB, 2, true>(p1, k, act, stage, tpol);
+        const KvOut r1 = kv_probe<KB, SB, 2, HINT>(p1, k, act, stage, tpol);
         // A found key's slot is emptied with a plain store, as the reference
         // does (cuckoo.cu:551): the kernel's keys are distinct (dedup, or the
         // caller's promise) and nothing else runs on the table, so no other
@@ -1007,7 +1021,7 @@ __global__ void __launch_bounds__(256) k_erase(const __grid_constant__ Desc D,
         const bool need2 = act && r1.match < 0 && (!Gm::kMeta || r1.overflow);
         if (__any_sync(kFull, need2)) {
             char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-            const KvOut r2 = kv_probe<KB, SB, 2, true>(p2, k, need2, stage, tpol);
+            const KvOut r2 = kv_probe<KB, SB, 2, HINT>(p2, k, need2, stage, tpol);
             if (need2 && r2.match >= 0) {
                 T::store(slot_ptr<KB, SB>(p2, r2.match), T::empty());
                 erased = true;

@@ -88,7 +88,7 @@ cudaError_t Ops<KB>::find(const LaunchCtx &L, const Desc &D, int sb, const void 
                           uint32_t vb, uint32_t *hits, uint64_t n) {
     if (n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
-        auto k = k_find<KB, SB>;
+        auto k = D.l2_keep ? k_find<KB, SB, true> : k_find<KB, SB, false>;
         k<<<tile_grid(L, n), 256, 0, L.stream>>>(D, keys, vals, vb, hits, n);
     });
     return cudaGetLastError();
@@ -118,7 +118,7 @@ cudaError_t Ops<KB>::place(const LaunchCtx &L, const Desc &D, int sb, const Scra
                            uint32_t vb, uint64_t n, Counters *ctr) {
     if (n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
-        auto k = k_place<KB, SB>;
+        auto k = D.l2_keep ? k_place<KB, SB, true> : k_place<KB, SB, false>;
         k<<<tile_grid(L, n), 256, 0, L.stream>>>(D, S, use_dedup ? 1 : 0, new_keys ? 1 : 0, keys,
                                                   vals, vb, n, ctr);
     });
@@ -146,7 +146,7 @@ cudaError_t Ops<KB>::erase(const LaunchCtx &L, const Desc &D, int sb, const Scra
                            Counters *ctr) {
     if (n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
-        auto k = k_erase<KB, SB>;
+        auto k = D.l2_keep ? k_erase<KB, SB, true> : k_erase<KB, SB, false>;
         k<<<tile_grid(L, n), 256, 0, L.stream>>>(D, S, use_dedup ? 1 : 0, keys, n, bits, ctr);
     });
     return cudaGetLastError();
@@ -302,10 +302,10 @@ template <int KB>
 cudaError_t Ops<KB>::set_find(const LaunchCtx &L, const Desc *descs, uint32_t ntables, int sb,
                               const void *keys, const uint32_t *tids,
                               const unsigned long long *n_ptr, uint64_t max_n, void *vals,
-                              uint32_t vb, uint32_t *hits, unsigned long long *bad) {
+                              uint32_t vb, uint32_t *hits, unsigned long long *bad, bool hint) {
     if (max_n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
-        auto k = k_set_find<KB, SB>;
+        auto k = hint ? k_set_find<KB, SB, true> : k_set_find<KB, SB, false>;
         k<<<tile_grid(L, max_n), 256, 0, L.stream>>>(descs, ntables, keys, tids, n_ptr, max_n,
                                                      vals, vb, hits, bad);
     });
@@ -320,10 +320,10 @@ cudaError_t Ops<KB>::set_mutate(const LaunchCtx &L, const Desc *descs, uint32_t 
                                 const uint32_t *up_tids, const unsigned long long *nu_ptr,
                                 uint64_t max_n, void *list_a, uint32_t *list_a_tid,
                                 uint64_t list_cap, Counters *gctr, unsigned long long *bad,
-                                const uint32_t *hold) {
+                                const uint32_t *hold, bool hint) {
     if (max_n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
-        auto k = k_set_mutate<KB, SB>;
+        auto k = hint ? k_set_mutate<KB, SB, true> : k_set_mutate<KB, SB, false>;
         k<<<tile_grid(L, max_n + 32), 256, 0, L.stream>>>(
             descs, ntables, tctr, er_keys, er_tids, ne_ptr, up_keys, up_vals, vb, up_tids, nu_ptr,
             max_n, list_a, list_a_tid, list_cap, gctr, bad, hold);

@@ -49,7 +49,7 @@ __device__ __forceinline__ uint32_t checked_tid(const uint32_t *tids, uint64_t i
 }
 
 // find of keys[i] in table tids[i], i < *n_ptr (k_find per table)
-template <int KB, int SB>
+template <int KB, int SB, bool HINT>
 __global__ void __launch_bounds__(256) k_set_find(const Desc *__restrict__ descs, uint32_t ntables,
                                                   const void *__restrict__ keys,
                                                   const uint32_t *__restrict__ tids,
@@ -75,17 +75,17 @@ __global__ void __launch_bounds__(256) k_set_find(const Desc *__restrict__ descs
         }
         const Desc &D = descs[tb];
         const bool act = ok && k != 0;
-        const unsigned long long tpol = l2_policies(D.l2_keep != 0u).table;
+        const unsigned long long tpol = HINT ? l2_policies(D.l2_keep != 0u).table : 0ull;
         const uint32_t hk = fold(k);
         const Pair p = pair_of(hk, D.d);
         const char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
-        const KvOut r1 = kv_probe<KB, SB, 1, true>(p1, k, act, stage, tpol);
+        const KvOut r1 = kv_probe<KB, SB, 1, HINT>(p1, k, act, stage, tpol);
         bool hit = act && r1.match >= 0;
         uint64_t v = hit ? r1.value : 0ull;
         const bool need2 = act && !hit && (!Gm::kMeta || r1.overflow);
         if (__any_sync(kFull, need2)) {
             const char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-            const KvOut r2 = kv_probe<KB, SB, 1, true>(p2, k, need2, stage, tpol);
+            const KvOut r2 = kv_probe<KB, SB, 1, HINT>(p2, k, need2, stage, tpol);
             if (need2 && r2.match >= 0) {
                 hit = true;
                 v = r2.value;
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) k_set_find(const Desc *__restrict__ descs
 // erase of unique keys[i] from table tids[i], i in [base, base + 32) and
 // below n (k_erase per table, no dedup). Warp-collective; returns whether
 // this lane erased its key.
-template <int KB, int SB>
+template <int KB, int SB, bool HINT>
 __device__ __forceinline__ bool set_erase_warp(const Desc *__restrict__ descs, uint32_t ntables,
                                                Counters *__restrict__ tctr,
                                                const void *__restrict__ keys,
@@ -119,11 +119,11 @@ __device__ __forceinline__ bool set_erase_warp(const Desc *__restrict__ descs, u
     }
     const Desc &D = descs[tb];
     const bool act = ok && k != 0;
-    const unsigned long long tpol = l2_policies(D.l2_keep != 0u).table;
+    const unsigned long long tpol = HINT ? l2_policies(D.l2_keep != 0u).table : 0ull;
     const uint32_t hk = fold(k);
     const Pair p = pair_of(hk, D.d);
     char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
-    const KvOut r1 = kv_probe<KB, SB, 2, true>(p1, k, act, stage, tpol);
+    const KvOut r1 = kv_probe<KB, SB, 2, HINT>(p1, k, act, stage, tpol);
     // plain stores, as in k_erase: the erase and upsert lists name distinct
     // keys, so no other thread of the pass writes a found key's slot
     bool erased = false;
@@ -134,7 +134,7 @@ __device__ __forceinline__ bool set_erase_warp(const Desc *__restrict__ descs, u
     const bool need2 = act && r1.match < 0 && (!Gm::kMeta || r1.overflow);
     if (__any_sync(kFull, need2)) {
         char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-        const KvOut r2 = kv_probe<KB, SB, 2, true>(p2, k, need2, stage, tpol);
+        const KvOut r2 = kv_probe<KB, SB, 2, HINT>(p2, k, need2, stage, tpol);
         if (need2 && r2.match >= 0) {
             T::store(slot_ptr<KB, SB>(p2, r2.match), T::empty());
             erased = true;
@@ -147,7 +147,7 @@ __device__ __forceinline__ bool set_erase_warp(const Desc *__restrict__ descs, u
 // upsert of unique keys[i] -> vals[i] into table tids[i], i in [base,
 // base + 32) and below n (k_place per table); ops left without a slot go to
 // list_a / list_a_tid. Warp-collective; adds to n_ins / n_upd.
-template <int KB, int SB>
+template <int KB, int SB, bool HINT>
 __device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs, uint32_t ntables,
                                                Counters *__restrict__ tctr,
                                                const void *__restrict__ keys,
@@ -173,17 +173,17 @@ __device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs, u
         if (act) e = T::make(k, load_val(vals, vb, i));
     }
     const Desc &D = descs[tb];
-    const unsigned long long tpol = l2_policies(D.l2_keep != 0u).table;
+    const unsigned long long tpol = HINT ? l2_policies(D.l2_keep != 0u).table : 0ull;
     const uint32_t hk = fold(k);
     const Pair p = pair_of(hk, D.d);
     char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
     char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
-    const KvOut r1 = place_probe<KB, SB, true>(p1, k, act, p.first, D.d, stage, tpol);
+    const KvOut r1 = place_probe<KB, SB, HINT>(p1, k, act, p.first, D.d, stage, tpol);
     const bool found1 = act && r1.match >= 0;
     const bool check2 = act && !found1 && ((!Gm::kMeta || r1.overflow) || r1.empty == 0u);
     KvOut r2{-1, 0ull, false, 0u};
     if (__any_sync(kFull, check2))
-        r2 = place_probe<KB, SB, true>(p2, k, check2, p.second, D.d, stage, tpol);
+        r2 = place_probe<KB, SB, HINT>(p2, k, check2, p.second, D.d, stage, tpol);
     bool pend = false, ins = false;
     if (found1) {  // the key's own slot: a plain store (distinct keys, as in k_place)
         T::store(slot_ptr<KB, SB>(p1, r1.match), e);
@@ -222,7 +222,7 @@ __device__ __forceinline__ void set_place_warp(const Desc *__restrict__ descs, u
 // rest upsert. The keys of the two lists are distinct, so the two kinds may
 // run concurrently (an upsert only claims empty slots or rewrites its own
 // key; an erase only empties its own key's slot).
-template <int KB, int SB>
+template <int KB, int SB, bool HINT>
 __global__ void __launch_bounds__(256) k_set_mutate(
     const Desc *__restrict__ descs, uint32_t ntables, Counters *__restrict__ tctr,
     const void *__restrict__ er_keys, const uint32_t *__restrict__ er_tids,
@@ -240,12 +240,12 @@ __global__ void __launch_bounds__(256) k_set_mutate(
     uint32_t n_del = 0, n_ins = 0, n_upd = 0;
     for (uint64_t base = warp_base(); base < ne32 + nu; base += step) {
         if (base < ne32) {  // warp-uniform: base is a multiple of 32
-            n_del += set_erase_warp<KB, SB>(descs, ntables, tctr, er_keys, er_tids, ne, base,
+            n_del += set_erase_warp<KB, SB, HINT>(descs, ntables, tctr, er_keys, er_tids, ne, base,
                                             stage, bad)
                          ? 1u
                          : 0u;
         } else {
-            set_place_warp<KB, SB>(descs, ntables, tctr, up_keys, up_vals, vb, up_tids, nu,
+            set_place_warp<KB, SB, HINT>(descs, ntables, tctr, up_keys, up_vals, vb, up_tids, nu,
                                    base - ne32, list_a, list_a_tid, list_cap, gctr, stage, n_ins,
                                    n_upd, bad);
         }

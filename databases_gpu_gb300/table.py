@@ -58,8 +58,8 @@ class DyCuckoo:
     """A GB300 DyCuckoo table; all arrays are CUDA tensors.
 
     size: number of keys to size the table for (the hashAPI(size) argument).
-    l2_resident: 0 keeps the buckets in the L2 when the table takes at most
-    1.5x of it, 1 never, 2 always (dyc_config.l2_resident).
+    l2_resident: 2 asks the L2 to keep the buckets (eviction-priority
+    hints); 0 (default) and 1 use plain accesses (dyc_config.l2_resident).
     """
 
     def __init__(self, size: int, key_bytes: int = 4, value_bytes: int | None = None,

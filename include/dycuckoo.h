@@ -87,13 +87,14 @@ typedef struct dyc_config {
     double lower_load;       /* downsize below this after erase; default 0.5 */
     uint64_t min_downsize_capacity; /* no downsize at or below this capacity */
     int32_t device;          /* CUDA device ordinal; default 0 */
-    uint32_t l2_resident;    /* L2 residency of the buckets: 0 (default) when the
-                                subtables take at most 1.5x the device's L2 (for a table
-                                set: all its members together), 1 never, 2 always. A
-                                resident table reads its buckets with an evict_last L2
-                                cache policy and find streams its keys and results with
-                                evict_first, so a large batch does not push the table out
-                                of the L2. No counterpart in the reference. */
+    uint32_t l2_resident;    /* 2: ask the L2 to keep the buckets: probes carry an
+                                evict_last L2 cache hint and find streams its keys and
+                                results with evict_first. 0 (default) and 1: plain
+                                accesses, which measured faster on GB300 (a table of 1.2x
+                                the L2: 51.1 against 48.1 G finds/s with the hints; hinted
+                                loads of one hot line many warps read at once are 2.5x
+                                slower). A table set follows its configuration for all
+                                members. No counterpart in the reference. */
     uint32_t device_upsize;  /* table sets (dyc_set_apply with auto_resize): 0 (default)
                                 keeps one upsize target allocated ahead for every member,
                                 so a round's upsize policy runs on the device between the

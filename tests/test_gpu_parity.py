@@ -414,9 +414,9 @@ def test_host_find_pipeline_chunk_schedule():
 @pytest.mark.parametrize("mode", [0, 1, 2])
 def test_l2_residency_modes_give_the_same_results(mode):
     """dyc_config.l2_resident only changes the L2 cache policy of the bucket
-    reads (evict_last for a resident table, evict_normal otherwise) and of
-    find's streaming keys and results: inserts, finds (hits and misses),
-    erases and the contents match the oracle in every mode."""
+    reads (evict_last hints in mode 2, plain loads otherwise) and of find's
+    streaming keys and results: inserts, finds (hits and misses), erases and
+    the contents match the oracle in every mode."""
     import databases_gpu_gb300 as dg
     n = 1 << 16
     pool = unique_u32(2 * n, seed=91)

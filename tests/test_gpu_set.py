@@ -58,12 +58,16 @@ def _preload(S, w, maps):
         maps[t].insert(to_host(k, 4), to_host(v, 4))
 
 
-@pytest.mark.parametrize("graph,tuned", [(False, False), (True, False), (False, True)])
-def test_set_matches_oracle_per_table(graph, tuned):
+@pytest.mark.parametrize("graph,tuned,l2", [(False, False, 0), (True, False, 0), (False, True, 0),
+                                              (False, False, 2)])
+def test_set_matches_oracle_per_table(graph, tuned, l2):
     """tuned: per-table subtable counts and eviction bounds (2..4, 1..256, as
-    a tuner may pick), 64-byte buckets and a launch cap of 2 blocks per SM."""
+    a tuner may pick), 64-byte buckets and a launch cap of 2 blocks per SM.
+    l2 = 2: the members' probes carry L2 eviction-priority hints."""
     w = _small_workload(96, seed=5)
-    if tuned:
+    if l2:
+        S = _dg().DyCuckooSet(w.sizes.numpy(), max_evictions=64, l2_resident=l2)
+    elif tuned:
         rng = np.random.default_rng(2)
         S = _dg().DyCuckooSet(w.sizes.numpy(), bucket_bytes=64,
                               num_subtables=rng.integers(2, 5, 96))
