@@ -306,6 +306,7 @@ __global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ A
                                                        uint64_t nc) {
     __shared__ unsigned long long part[kCompactRun * kWarpsPerBlock];  // ops << 32 | keys
     __shared__ unsigned long long base_keys, base_ops;
+    __shared__ int tile_ok;  // the tile's key and op ranges lie inside the scratch
     if (A.tcell_off) nc = A.tcell_off[A.ntables];
     if (nc > A.cap_cells) nc = A.cap_cells;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -344,30 +345,41 @@ __global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ A
                 const unsigned long long nk = incl & 0xffffffffull, no = incl >> 32;
                 base_keys = nk ? atomicAdd(&A.ctr[kCtrDistinct], nk) : 0ull;
                 base_ops = no ? atomicAdd(&A.ctr[kCtrPlaced], no) : 0ull;
+                tile_ok = base_keys + nk <= A.cap_ops && base_ops + no <= A.cap_ops;
             }
         }
         __syncthreads();
+        if (tile_ok) {  // every id and segment of the tile is inside its range
 #pragma unroll
-        for (int k = 0; k < kCompactRun; ++k) {
-            if (!cnt[k]) continue;
-            const unsigned long long pk = part[k * kWarpsPerBlock + w];
-            const uint64_t d64 = base_keys + (uint32_t)pk + ex_keys[k];
-            const uint64_t off64 = base_ops + (uint32_t)(pk >> 32) + ex_ops[k];
-            const uint64_t c = c0 + (uint64_t)k * blockDim.x + threadIdx.x;
-            if (d64 >= A.cap_ops || off64 + cnt[k] > A.cap_ops) {
-                *cell_word<KB>(A.cells, c) = kNoId;  // more keys or ops than the scratch holds
-                note_bad(A);
-                continue;
+            for (int k = 0; k < kCompactRun; ++k) {
+                if (!cnt[k]) continue;
+                const unsigned long long pk = part[k * kWarpsPerBlock + w];
+                const uint32_t d = (uint32_t)base_keys + (uint32_t)pk + ex_keys[k];
+                const uint32_t off = (uint32_t)base_ops + (uint32_t)(pk >> 32) + ex_ops[k];
+                const uint64_t c = c0 + (uint64_t)k * blockDim.x + threadIdx.x;
+                *cell_word<KB>(A.cells, c) = d;  // the count becomes the distinct id
+                ((typename SlotT<KB>::K *)A.dkey)[d] = cell_key<KB>(A.cells, c);
+                A.dcnt[d] = cnt[k];
+                A.dseg[d] = (unsigned long long)off << 32;
+                if (A.dtid)
+                    A.dtid[d] = table_at(A.tidx, A.tcell_off, (uint32_t)c, (uint32_t)(c >> 1));
             }
-            const uint32_t d = (uint32_t)d64, off = (uint32_t)off64;
-            *cell_word<KB>(A.cells, c) = d;  // the count becomes the distinct id
-            ((typename SlotT<KB>::K *)A.dkey)[d] = cell_key<KB>(A.cells, c);
-            A.dcnt[d] = cnt[k];
-            A.dseg[d] = (unsigned long long)off << 32;
-            if (A.dtid)
-                A.dtid[d] = table_at(A.tidx, A.tcell_off, (uint32_t)c, (uint32_t)(c >> 1));
+        } else {
+            // more keys or ops than the scratch holds (counts this batch's
+            // grouping cannot have produced; the call reports them): the
+            // tile's cells get no id, and its ids inside the range a count
+            // of 0, so the later passes skip them and every id below the
+            // distinct count is written
+            if (threadIdx.x == 0) note_bad(A);
+            for (int k = 0; k < kCompactRun; ++k) {
+                if (!cnt[k]) continue;
+                const uint64_t d64 =
+                    base_keys + (uint32_t)part[k * kWarpsPerBlock + w] + ex_keys[k];
+                *cell_word<KB>(A.cells, c0 + (uint64_t)k * blockDim.x + threadIdx.x) = kNoId;
+                if (d64 < A.cap_ops) A.dcnt[d64] = 0u;
+            }
         }
-        __syncthreads();  // part / bases are reused by the next tile
+        __syncthreads();  // part / bases / tile_ok are reused by the next tile
     }
 }
 
@@ -582,9 +594,7 @@ __global__ void __launch_bounds__(256) k_apply_replay(const __grid_constant__ Ap
                 md = true;
             } else if (cnt > kShortSeg) {
                 wp = true;
-            } else if (cnt > 1u && !seg_ok(A, seg_off(A, (uint32_t)d), cnt)) {
-                note_bad(A);
-            } else if (cnt > 1u) {
+            } else if (cnt > 1u) {  // segment inside the op scratch: compaction checked it
                 uint32_t s[kShortSeg];
                 const uint32_t off = seg_off(A, (uint32_t)d);
 #pragma unroll
