@@ -104,7 +104,12 @@ class CopyPool {
     bool stop_ = false;
 };
 
-constexpr int kCopyHelpers = 7;  // per copying stage (assembler, completer)
+// Helper threads per copying stage (assembler, completer). Seven per stage
+// oversubscribed the 16 host cores the server shares with its clients: at
+// 1.72 G ops/s offered, request p50 ranged 0.9-5.9 ms and a client's own
+// submissions ran up to 8 ms late; with three, p50 0.63-0.93 ms, clients at
+// most 1.5 ms late, the same sustained rate.
+constexpr int kCopyHelpers = 3;
 
 struct Req {
     uint64_t ticket;

@@ -200,3 +200,63 @@ def test_set_places_a_members_held_entries_before_its_batch():
         assert_same_contents(S.table(t), maps[t], "table %d" % t)
     assert S.table(0).stats()["held"] == 0
     S.close()
+
+
+def test_set_member_without_a_spare_is_upsized_by_the_host():
+    """A table set applies its upsize policy on the device, from one upsize
+    target allocated ahead per member. When that allocation fails (injected:
+    the first pool allocation of the round), the member has no spare; the
+    device hands the policy to the host for that round, which upsizes it
+    before phase B. Every round's results, sizes and capacities equal those
+    of a twin set whose host applies the policy, and the oracle's."""
+    import torch
+    from databases_gpu_gb300 import _lib
+    from tests.helpers import to_host
+    dg = _dg()
+    rng = np.random.default_rng(77)
+    nt = 16
+    A = dg.DyCuckooSet([2000] * nt, device_upsize=0)
+    B = dg.DyCuckooSet([2000] * nt, device_upsize=1)
+    _, caps = A.sizes()
+    maps = [O.Map() for _ in range(nt)]
+    for t in range(nt):
+        k = unique_u32(int(0.78 * int(caps[t])), seed=100 + t)
+        v = rng.integers(0, 1 << 31, k.size).astype(np.uint32)
+        A.table(t).insert(to_dev(k), to_dev(v))
+        B.table(t).insert(to_dev(k), to_dev(v))
+        maps[t].insert(k, v)
+    splits = []
+    for r in range(2):
+        caps_now = A.sizes()[1].astype(np.int64)
+        cnt = (0.16 * caps_now).astype(np.int64)  # new keys: one upsize per member
+        off = np.zeros(nt + 1, np.uint32)
+        off[1:] = np.cumsum(cnt)
+        n = int(off[-1])
+        keys = rng.integers((1 << 31) + 1, (1 << 32) - 1, n, dtype=np.uint64).astype(np.uint32)
+        ops = np.ones(n, np.uint8)
+        vals = rng.integers(0, 1 << 31, n).astype(np.uint32)
+        d = lambda a: torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).cuda()
+        if r == 1:
+            _inject(_lib.INJECT_POOL_ALLOC, 1)
+        oa, ba = A.apply(d(off), d(ops), d(keys), d(vals), h_offsets=off)
+        _inject(_lib.INJECT_RESET, 0)
+        splits.append(A.stats()["split_phases"])
+        ob, bb = B.apply(d(off), d(ops), d(keys), d(vals), h_offsets=off)
+        assert bool((oa == ob).all()) and bool((ba == bb).all()), "round %d" % r
+        gv = to_host(oa, 4).astype(np.uint64)
+        gh = dg.unpack_bits(ba, n)
+        for t in range(nt):
+            a, b = int(off[t]), int(off[t + 1])
+            ov, oh = maps[t].apply(ops[a:b], keys[a:b].astype(np.uint64),
+                                   vals[a:b].astype(np.uint64))
+            assert np.array_equal(gh[a:b], oh) and np.array_equal(gv[a:b], ov), \
+                "round %d table %d" % (r, t)
+        sza, capa = A.sizes()
+        szb, capb = B.sizes()
+        assert np.array_equal(sza, szb) and np.array_equal(capa, capb), "round %d" % r
+    # round 0: every member upsized on the device; round 1: one had no spare
+    assert splits == [0, 1], splits
+    for t in range(nt):
+        assert_same_contents(A.table(t), maps[t], "table %d" % t)
+    A.close()
+    B.close()
