@@ -318,6 +318,72 @@ def run_reference_gpu(args, keys, batch, stream, torch):
     return res
 
 
+def run_reference_per_table(w, rnd, torch):
+    """The reference's own kernels on the same tables and one of the same
+    rounds, launched the way the reference serves many tables: its kernels
+    read one process-wide table descriptor (cuckoo.cu:16), so every table
+    takes a cudaMemcpyToSymbol of its descriptor (gpu_lp_set_table,
+    cuckoo.cu:918-923) and then one cuckoo_search, one cuckoo_insert and one
+    cuckoo_delete launch on its finds, inserts and erases (cuckoo.cu:324-587).
+    Tables are laid out as hashAPI(size) does and preloaded by cuckoo_insert.
+    A throughput baseline for the one-table-at-a-time launch path: a table's
+    three op kinds run as three kernels rather than in batch order, and the
+    reference's insert adds a second copy of a key already present."""
+    from oracle import ref_gpu
+    if not ref_gpu.available():
+        return {"unavailable": "reference GPU kernels not staged (oracle/build_ref.py)"}
+    import ctypes as C
+    L = ref_gpu.lib()
+    nt = w.ntables
+    dev = w.device
+    tabs = [ref_gpu.RefGpuTable(int(w.sizes[t]), device=dev.index or 0) for t in range(nt)]
+    descs = []
+    for tb in tabs:
+        descs.append(((C.c_void_p * 4)(*[s.data_ptr() for s in tb.subtables]),
+                      (C.c_uint32 * 4)(*[s.numel() for s in tb.subtables])))
+    legacy = C.c_void_p(0)  # the reference launches on the legacy default stream
+    rehash = torch.zeros(1, dtype=torch.int32, device=dev)
+    iters = torch.empty(int(w.sizes.max()) + 1, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    for t in range(nt):
+        k, v = w.preload(t)
+        assert L.refgpu_set_table(*descs[t]) == 0
+        assert L.refgpu_insert(k.data_ptr(), v.data_ptr(), k.numel(), rehash.data_ptr(),
+                               iters.data_ptr(), legacy) == 0
+    # the round's ops grouped by (table, op kind), untimed
+    ops, keys, vals = rnd
+    off = np.asarray(w.offsets_host, dtype=np.int64)
+    tid = torch.repeat_interleave(torch.arange(nt, device=dev),
+                                  torch.from_numpy(np.diff(off)).to(dev))
+    grp = tid * 3 + ops.long()
+    order = torch.argsort(grp, stable=True)
+    ks, vs = keys[order].contiguous(), vals[order].contiguous()
+    cnt = torch.bincount(grp, minlength=3 * nt).cpu().numpy().astype(np.int64)
+    start = np.concatenate([[0], np.cumsum(cnt)])
+    iters = torch.empty(int(cnt[1::3].max()) + 1, dtype=torch.int32, device=dev)
+    out = torch.zeros(ks.numel(), dtype=torch.int32, device=dev)
+    kp, vp, op_ = ks.data_ptr(), vs.data_ptr(), out.data_ptr()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for t in range(nt):
+        assert L.refgpu_set_table(*descs[t]) == 0
+        f, i, e = 3 * t, 3 * t + 1, 3 * t + 2
+        L.refgpu_search(kp + 4 * int(start[f]), op_ + 4 * int(start[f]), int(cnt[f]), legacy)
+        L.refgpu_insert(kp + 4 * int(start[i]), vp + 4 * int(start[i]), int(cnt[i]),
+                        rehash.data_ptr(), iters.data_ptr(), legacy)
+        L.refgpu_delete(kp + 4 * int(start[e]), int(cnt[e]), legacy)
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    n = int(start[-1])
+    del tabs
+    torch.cuda.empty_cache()
+    return {"kernels": "cuckoo_search / cuckoo_insert / cuckoo_delete (GPU/dyhash/cuckoo.cu) "
+                       "compiled for sm_103a, per table after gpu_lp_set_table's symbol upload",
+            "mops": round(n / sec / 1e6, 1), "round_ms": round(sec * 1e3, 2), "ops": n,
+            "note": "one round; per table one descriptor upload and three launches on the "
+                    "legacy default stream, host wall time"}
+
+
 def set_table_bytes(S, bucket_bytes=128):
     """Device bytes of a set's subtables (from the members' slot capacities)."""
     _, caps = S.sizes()
@@ -546,12 +612,18 @@ def run_multi_table(args, dev, torch, dg):
     # capture) on the same pre-generated rounds; the batched path's results
     # are kept and compared op by op with the per-table path's
     data = [w.round() for _ in range(rounds + 2)]
+    # each round is copied (untimed) into the same device buffers, so the
+    # batched path replays its captured graphs from the third round on
+    bufs = [torch.empty_like(x) for x in data[0]]
     kept = []
     paths = (("batched", sets[0]),) if args.mt_skip_per_table else \
         (("batched", sets[0]), ("per_table", sets[1]))
     for which, S in paths:
         i = 0 if which == "batched" else 1
-        for r, (ops, keys, vals) in enumerate(data):
+        for r, rnd in enumerate(data):
+            for b, x in zip(bufs, rnd):
+                b.copy_(x)
+            ops, keys, vals = bufs
             torch.cuda.synchronize()
             e0.record(stream)
             S.apply(w.offsets, ops, keys, vals, out=outs[i], bits=bitss[i],
@@ -570,7 +642,10 @@ def run_multi_table(args, dev, torch, dg):
                 kept.append((outs[0].clone(), bitss[0].clone()))
             else:
                 bad += int((kept[r][0] != outs[1]).sum()) + int((kept[r][1] != bitss[1]).sum())
-    del kept, data
+    ref_path = None
+    if not args.skip_reference_gpu:
+        ref_path = run_reference_per_table(w, data[2], torch)
+    del kept, data, bufs
     sa, ca = sets[0].sizes()
     if not args.mt_skip_per_table:
         sb, cb = sets[1].sizes()
@@ -592,6 +667,11 @@ def run_multi_table(args, dev, torch, dg):
         res["batched_over_per_table"] = round(res["batched"]["mops"] / res["per_table"]["mops"],
                                               2)
     res["api"] = "dyc_set_apply (graph replay) vs dyc_set_apply_each (one dyc_apply per table)"
+    if ref_path is not None:
+        res["reference_per_table"] = ref_path
+        if "mops" in ref_path:
+            res["batched_over_reference_per_table"] = round(
+                res["batched"]["mops"] / ref_path["mops"], 1)
     for S in sets:
         S.close()
     if not args.skip_tune:
