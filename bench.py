@@ -384,6 +384,107 @@ def run_reference_per_table(w, rnd, torch):
                     "legacy default stream, host wall time"}
 
 
+def run_small_table(args, dev, torch, dg):
+    """Config 1, the reference's own test scale: 2^20 unique u32 keys
+    (values 1..2^20, below 2^31) in a table sized for load factor 0.85
+    (hashAPI(2^20 / 0.85)). The library and the reference's own kernels
+    (cuckoo_insert / cuckoo_search / cuckoo_delete) on its own table run the
+    same sequence on the same keys, every step timed with CUDA events on the
+    launching stream:
+      insert the first half of the keys (untimed: the table's first call
+      sizes its scratch), insert the second half (timed, 2^19 keys), find
+      2^20 keys of which half hit (mean of 20 batches), erase 2^19 present
+      keys (timed), then re-insert them (timed; the library with
+      DYC_FLAG_UNIQUE, which skips the batch dedup the reference does not
+      have either).
+    The library's insert and erase calls dedup the batch (unless told the
+    keys are unique) and read their counters back before returning; the
+    reference's kernels do neither. The table takes ~10 MB, so it lives in
+    the L2."""
+    N = 1 << 20
+    H = N // 2
+    keys = as_i32(make_keys(0, N, torch, dev), torch)
+    vals = torch.arange(1, N + 1, dtype=torch.int32, device=dev)
+    miss = as_i32(make_keys(N, N + H, torch, dev), torch)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(10327)
+    q = torch.cat([keys[:H], miss])[torch.randperm(N, generator=gen, device=dev)]
+    # expected values by a sort-and-search of the inserted keys
+    srt, idx = torch.sort(keys.long())
+    pos = torch.searchsorted(srt, q.long()).clamp_(max=N - 1)
+    found = srt[pos] == q.long()
+    expv = torch.where(found, vals[idx[pos]], torch.zeros_like(vals))
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps=1):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    res = {"workload": "config 1: 2^20 unique u32 keys at load factor 0.85 (hashAPI(2^20/0.85)), "
+                       "insert of 2^19 keys into the half-full table, 2^20 finds (50 % hits), "
+                       "erase of 2^19 present keys, their re-insert; ~10 MB table"}
+    # no load-factor policy, as the reference's plain hash_insert (api.cpp:185-194)
+    t = dg.DyCuckoo(int(N / 0.85), auto_resize=False, device=dev.index or 0)
+    out = torch.empty(N, dtype=torch.int32, device=dev)
+    bits = torch.empty(N // 32, dtype=torch.int32, device=dev)
+    t.insert(keys[:H], vals[:H], stream=stream)
+    ins = timed(lambda: t.insert(keys[H:], vals[H:], stream=stream))
+    t.find(q, out=out, hit_bits=bits, stream=stream)
+    fnd = timed(lambda: t.find(q, out=out, hit_bits=bits, stream=stream), 20)
+    bad = int((out != expv).sum())
+    ers = timed(lambda: t.erase(keys[:H], stream=stream))
+    uins = timed(lambda: t.insert(keys[:H], vals[:H], unique=True, stream=stream))
+    res["library"] = {"insert_mops": round(H / ins / 1e3, 1), "find_mops": round(N / fnd / 1e3, 1),
+                      "erase_mops": round(H / ers / 1e3, 1),
+                      "insert_unique_mops": round(H / uins / 1e3, 1), "find_mismatches": bad,
+                      "size": t.size}
+    t.close()
+    if args.skip_reference_gpu:
+        return res
+    from oracle import ref_gpu
+    if not ref_gpu.available():
+        res["reference_gpu"] = {"unavailable": "reference GPU kernels not staged"}
+        return res
+    ref = ref_gpu.RefGpuTable(int(N / 0.85), device=dev.index or 0)
+    L = ref_gpu.lib()
+    import ctypes as C
+    rehash = torch.zeros(1, dtype=torch.int32, device=dev)
+    iters = torch.empty(H, dtype=torch.int32, device=dev)
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def rinsert(k, v):
+        assert L.refgpu_insert(k.data_ptr(), v.data_ptr(), k.numel(), rehash.data_ptr(),
+                               iters.data_ptr(), sp) == 0
+
+    rinsert(keys[:H], vals[:H])
+    rins = timed(lambda: rinsert(keys[H:], vals[H:]))
+    rout = torch.zeros(N, dtype=torch.int32, device=dev)
+    ref.search(q, out=rout, stream=stream)
+    rfnd = timed(lambda: ref.search(q, out=rout, stream=stream), 20)
+    rbad = int((rout != expv).sum())
+    rers = timed(lambda: ref.delete(keys[:H], stream=stream))
+    ruins = timed(lambda: rinsert(keys[:H], vals[:H]))
+    res["reference_gpu"] = {"insert_mops": round(H / rins / 1e3, 1),
+                            "find_mops": round(N / rfnd / 1e3, 1),
+                            "erase_mops": round(H / rers / 1e3, 1),
+                            "insert_unique_mops": round(H / ruins / 1e3, 1),
+                            "find_results_differing_from_expected": rbad,
+                            "rehash_flag": int(rehash.item())}
+    res["library_over_reference"] = {
+        k: round(res["library"][k] / res["reference_gpu"][k], 2)
+        for k in ("insert_mops", "find_mops", "erase_mops", "insert_unique_mops")}
+    del ref
+    torch.cuda.empty_cache()
+    return res
+
+
 def set_table_bytes(S, bucket_bytes=128):
     """Device bytes of a set's subtables (from the members' slot capacities)."""
     _, caps = S.sizes()
@@ -820,7 +921,7 @@ def main():
     ap.add_argument("--skip-serve", action="store_true",
                     help="skip the serving loop and the serving-step workload")
     ap.add_argument("--only", default=None,
-                    choices=["find", "stream", "multi", "serve", "serve-steps"],
+                    choices=["find", "small", "stream", "multi", "serve", "serve-steps"],
                     help="run one workload: find (the headline line with its variants, ops "
                          "and baselines, no other workloads) or one of the others alone, "
                          "printing its own JSON object")
@@ -853,7 +954,8 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     if args.only not in (None, "find"):
-        run = {"stream": lambda: run_resize_stream(args, dev, torch, dg),
+        run = {"small": lambda: run_small_table(args, dev, torch, dg),
+               "stream": lambda: run_resize_stream(args, dev, torch, dg),
                "multi": lambda: run_multi_table(args, dev, torch, dg),
                "serve": lambda: run_serving(args),
                "serve-steps": lambda: run_serve_steps(args, dev, torch, dg)}[args.only]
@@ -1078,6 +1180,8 @@ def main():
 
     # ---- dynamic resize stream (its own u64 table; the find table is kept)
     workloads = {}
+    if not args.skip_variants:
+        workloads["small_table"] = run_small_table(args, dev, torch, dg)
     if not args.skip_stream and not args.skip_variants:
         workloads["resize_stream"] = run_resize_stream(args, dev, torch, dg)
     if not args.skip_multi and not args.skip_variants:
