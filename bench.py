@@ -245,7 +245,7 @@ def run_reference(args):
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": workload_config(args, lf=None),
+        "config": workload_config(args),
         "cpu_baseline": {"value": round(value, 2), "unit": "Mops/s", "cores": threads,
                          "kind": "port",
                          "sample": "%d uniform 100%%-hit finds per step on the full %d-key table "
@@ -886,12 +886,15 @@ def head_mops(results):
     return results["uniform100"]["mops"]
 
 
-def workload_config(args, lf):
+def workload_config(args):
+    """The headline workload, the same for both arms (the load factor is the
+    target the table is sized for; the library's measured one is reported
+    under "build")."""
     return {
         "workload": "large static table find: u32 keys/values, 4 subtables, 2^%d unique keys "
                     "at load factor 0.90, find batches of 2^%d" % (args.log2_keys, args.log2_batch),
         "keys": 1 << args.log2_keys, "batch": 1 << args.log2_batch,
-        "load_factor": lf, "query_mix": "uniform, 100% hit",
+        "load_factor": 0.9, "query_mix": "uniform, 100% hit",
         "bucket_bytes": args.bucket_bytes, "subtables": 4,
         "l2": "inputs larger than L2 (table ~2.4 GB, batch 256 MB); no flush",
     }
@@ -1249,7 +1252,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_batch"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded bijective key permutation; Zipf by inverse CDF)",
-        "config": workload_config(args, round(lf, 4)),
+        "config": workload_config(args),
         "e2e": {"value": round(e2e_mops, 1), "unit": "Mops/s",
                 "h2d_bytes_per_step": Q * 4, "d2h_bytes_per_step": Q * 4 + Q // 8,
                 "api": "dyc_find_host (pinned host buffers)", "mismatches": e2e_bad,
@@ -1268,7 +1271,8 @@ def main():
         "ops": ops,
         "workloads": workloads,
         "build": {"seconds": round(build_s, 3), "evict_steps": st["evict_steps"],
-                  "overflowed": st["overflowed"], "capacity": t.capacity},
+                  "overflowed": st["overflowed"], "capacity": t.capacity,
+                  "load_factor": round(lf, 4)},
     }
     if rank == 0:
         print(json.dumps(line))
