@@ -254,7 +254,7 @@ def test_set_member_without_a_spare_is_upsized_by_the_host():
         sza, capa = A.sizes()
         szb, capb = B.sizes()
         assert np.array_equal(sza, szb) and np.array_equal(capa, capb), "round %d" % r
-    # round 0: every member upsized on the device; round 1: one had no spare
+    # first batch: every member upsized on the device; second: one member had no spare
     assert splits == [0, 1], splits
     for t in range(nt):
         assert_same_contents(A.table(t), maps[t], "table %d" % t)
