@@ -79,7 +79,7 @@ EXPORTS = [
     "dyc_wide_export", "dyc_wide_table", "dyc_wide_last_stats", "dyc_debug_inject",
     "dyc_debug_alloc_count",
 ]
-INJECT_RESET, INJECT_POOL_ALLOC, INJECT_WAIT_TRIES = 0, 1, 2  # dyc_debug_inject kinds
+INJECT_RESET, INJECT_POOL_ALLOC, INJECT_WAIT_TRIES, INJECT_CHUNK_OPS = 0, 1, 2, 3  # dyc_debug_inject kinds
 
 _lock = threading.Lock()
 _lib = None

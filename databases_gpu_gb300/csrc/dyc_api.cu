@@ -196,6 +196,7 @@ LaunchCtx ctx(dyc_table *t, void *stream) { return LaunchCtx{t->sms, (cudaStream
 // polls. Process-wide.
 std::atomic<uint64_t> g_inject_alloc{0};
 std::atomic<uint32_t> g_inject_wait_tries{dyc::kWaitTries};
+std::atomic<uint64_t> g_inject_chunk{0};  // ops per insert / erase chunk of new tables (0: default)
 
 // Stream-ordered allocation from the library pool of the table's device.
 cudaError_t pool_alloc(int device, void **p, size_t bytes, cudaStream_t s) {
@@ -458,17 +459,25 @@ dyc_status drain(dyc_table *t, cudaStream_t s, void *src, unsigned long long *sr
                             kMaxOverflowRounds));
 }
 
+// Batch dedup of one chunk into the dedup buffers of S, on stream s:
+// kKeepLast (insert) names each key's last op, kKeepFirst (erase) its first.
+dyc_status dedup_chunk(dyc_table *t, const Scratch &S, const void *keys, uint64_t n,
+                       dyc::DedupMode mode, cudaStream_t s) {
+    CK(cudaMemsetAsync(S.dedup, 0, (size_t)S.dedup_cap * 8, s));
+    if (S.dedup_idx)
+        CK(cudaMemsetAsync(S.dedup_idx, mode == dyc::kKeepLast ? 0 : 0xFF,
+                           (size_t)S.dedup_cap * 4, s));
+    cudaError_t e = KB_CALL(t, dedup, ctx(t, s), S, keys, n, mode);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "dedup kernel: %s", cudaGetErrorString(e));
+    return DYC_OK;
+}
+
 dyc_status insert_chunk(dyc_table *t, const void *keys, const void *vals, uint64_t n,
                         uint32_t flags, cudaStream_t s) {
     const bool use_dedup = !(flags & DYC_FLAG_UNIQUE) && n > 1;
     const bool new_keys = (flags & DYC_FLAG_NEW_KEYS) != 0;
     TRY(reset_call_counters(t, s));
-    if (use_dedup) {
-        CK(cudaMemsetAsync(t->S.dedup, 0, (size_t)t->S.dedup_cap * 8, s));
-        if (t->S.dedup_idx) CK(cudaMemsetAsync(t->S.dedup_idx, 0, (size_t)t->S.dedup_cap * 4, s));
-        cudaError_t e = KB_CALL(t, dedup, ctx(t, s), t->S, keys, n, dyc::kKeepLast);
-        if (e != cudaSuccess) return fail(DYC_ECUDA, "dedup kernel: %s", cudaGetErrorString(e));
-    }
+    if (use_dedup) TRY(dedup_chunk(t, t->S, keys, n, dyc::kKeepLast, s));
     cudaError_t e = KB_CALL(t, place, ctx(t, s), t->D, t->sb, t->S, use_dedup, new_keys, keys,
                             vals, (uint32_t)t->vb, n, t->d_ctr);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "place kernel: %s", cudaGetErrorString(e));
@@ -499,12 +508,7 @@ dyc_status erase_chunk(dyc_table *t, const void *keys, uint64_t n, uint32_t *bit
                        uint32_t flags, cudaStream_t s) {
     const bool use_dedup = !(flags & DYC_FLAG_UNIQUE) && n > 1;
     TRY(reset_call_counters(t, s));
-    if (use_dedup) {
-        CK(cudaMemsetAsync(t->S.dedup, 0, (size_t)t->S.dedup_cap * 8, s));
-        if (t->S.dedup_idx) CK(cudaMemsetAsync(t->S.dedup_idx, 0xFF, (size_t)t->S.dedup_cap * 4, s));
-        cudaError_t e = KB_CALL(t, dedup, ctx(t, s), t->S, keys, n, dyc::kKeepFirst);
-        if (e != cudaSuccess) return fail(DYC_ECUDA, "dedup kernel: %s", cudaGetErrorString(e));
-    }
+    if (use_dedup) TRY(dedup_chunk(t, t->S, keys, n, dyc::kKeepFirst, s));
     cudaError_t e = KB_CALL(t, erase, ctx(t, s), t->D, t->sb, t->S, use_dedup, keys, n, bits,
                             t->d_ctr);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "erase kernel: %s", cudaGetErrorString(e));
@@ -666,6 +670,7 @@ dyc_status create_impl(const dyc_config *cfg, Counters *ext_d, Counters *ext_h, 
     if (!valid_config(cfg, why, sizeof(why))) return fail(DYC_EINVAL, "%s", why);
     dyc_table *t = new (std::nothrow) dyc_table();
     if (!t) return fail(DYC_ENOMEM, "host allocation");
+    if (const uint64_t c = g_inject_chunk.load()) t->chunk = c;
     t->cfg = *cfg;
     t->kb = (int)cfg->key_bytes;
     t->vb = (int)cfg->value_bytes;
@@ -927,12 +932,20 @@ dyc_status dyc_debug_inject(uint32_t kind, uint64_t n) {
     case DYC_INJECT_RESET:
         g_inject_alloc.store(0);
         g_inject_wait_tries.store(dyc::kWaitTries);
+        g_inject_chunk.store(0);
         return DYC_OK;
     case DYC_INJECT_POOL_ALLOC:
         g_inject_alloc.store(n);
         return DYC_OK;
     case DYC_INJECT_WAIT_TRIES:
         g_inject_wait_tries.store(n < dyc::kWaitTries ? (uint32_t)n : dyc::kWaitTries);
+        return DYC_OK;
+    case DYC_INJECT_CHUNK_OPS:
+        // chunk offsets index per-op bit arrays by 32-bit word
+        if (n % 32 != 0 || n > kChunkDefault)
+            return fail(DYC_EINVAL, "chunk of %llu ops: a multiple of 32, at most %llu",
+                        (unsigned long long)n, (unsigned long long)kChunkDefault);
+        g_inject_chunk.store(n);
         return DYC_OK;
     default:
         return fail(DYC_EINVAL, "unknown injection kind %u", kind);

@@ -506,12 +506,16 @@ const char *dyc_last_error(void);
  *   DYC_INJECT_POOL_ALLOC: the n-th allocation from the library pool from
  *     now on (subtables of resizes, downsize lists) fails as if the device
  *     were out of memory; n = 0 clears.
+ *   DYC_INJECT_CHUNK_OPS: tables created from now on split inserts and
+ *     erases into chunks of n ops (a multiple of 32, at most 2^22; 0 = the
+ *     default 2^22), so that small tests reach the paths of many chunks.
  *   DYC_INJECT_WAIT_TRIES: the downsize kernel's bounded waits on its tile
  *     copies give up after n polls (n = 0: at the first poll); the wait for
  *     copies still in flight before a block exits keeps its full bound. */
 #define DYC_INJECT_RESET 0u
 #define DYC_INJECT_POOL_ALLOC 1u
 #define DYC_INJECT_WAIT_TRIES 2u
+#define DYC_INJECT_CHUNK_OPS 3u
 dyc_status dyc_debug_inject(uint32_t kind, uint64_t n);
 
 /* Number of device and pinned-host allocations the library has made in this

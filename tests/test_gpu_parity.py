@@ -431,3 +431,43 @@ def test_l2_residency_modes_give_the_same_results(mode):
     find_and_compare(t, m, pool, "find after erase, l2_resident=%d" % mode)
     assert_same_contents(t, m, "contents, l2_resident=%d" % mode)
     t.close()
+
+
+@pytest.mark.parametrize("key_bytes", [4, 8])
+def test_many_chunks_with_repeats_match_oracle(key_bytes):
+    """Inserts and erases split into many chunks (tables made with a
+    4096-op chunk, dyc_debug_inject): keys repeat within chunks and across
+    them, the table grows between chunks (auto resize), and erases include
+    misses. Every erase bit, the counts, the finds and the contents equal
+    the oracle's."""
+    import databases_gpu_gb300 as dg
+    from databases_gpu_gb300 import _lib
+    from tests.helpers import unique_u64
+    L = _lib.lib()
+    assert L.dyc_debug_inject(_lib.INJECT_CHUNK_OPS, 4096) == 0
+    try:
+        t = dg.DyCuckoo(1 << 12, key_bytes=key_bytes, value_bytes=key_bytes)
+    finally:
+        L.dyc_debug_inject(_lib.INJECT_RESET, 0)
+    rng = np.random.default_rng(61)
+    pool = (unique_u32(60000, seed=62) if key_bytes == 4 else unique_u64(60000, seed=62))
+    npk = np.uint32 if key_bytes == 4 else np.uint64
+    m = O.Map()
+    for r in range(3):
+        keys = pool[rng.integers(0, 40000 + 10000 * r, 50000)].astype(npk)
+        vals = rng.integers(1, 1 << 30, keys.size).astype(npk)
+        st = t.insert(to_dev(keys), to_dev(vals))
+        _, oh = m.insert(keys.astype(np.uint64), vals.astype(np.uint64))
+        assert st["inserted"] == int((~oh).sum()), (r, st)
+        assert t.size == len(m), (r, t.size, len(m))
+        ek = pool[rng.integers(0, 60000, 30000)].astype(npk)  # repeats and misses
+        import torch
+        bits = torch.zeros((ek.size + 31) // 32, dtype=torch.int32, device="cuda")
+        cnt = t.erase(to_dev(ek), erased_bits=bits)
+        _, eh = m.erase(ek.astype(np.uint64))
+        assert cnt == int(eh.sum()), (r, cnt, int(eh.sum()))
+        gh = dg.unpack_bits(bits, ek.size)
+        assert np.array_equal(gh, eh), "round %d: %d erase bits differ" % (r, int((gh != eh).sum()))
+        find_and_compare(t, m, pool, "chunks round %d" % r)
+    assert_same_contents(t, m, "chunked inserts and erases")
+    t.close()
