@@ -485,6 +485,80 @@ def run_small_table(args, dev, torch, dg):
     return res
 
 
+def run_features(args, dev, torch, dg):
+    """Rates of two extensions of the table.
+    Wide values (dyc_wide_*): 2^24 u32 keys with 32-byte values in a table
+    sized for load factor 0.85 (no resize policy): insert, find of every
+    key (mean of 5 batches), erase of half the keys, each timed with CUDA
+    events; every found value is checked.
+    Snapshot / restore (dyc_snapshot / dyc_restore): a 2^26-key u32 table
+    (LF 0.85) to a host buffer and back to a new table, host wall time; a
+    sample of finds on the restored table is checked."""
+    res = {}
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps=1):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    N, VB = 1 << 24, 32
+    keys = as_i32(make_keys(0, N, torch, dev), torch)
+    vals = (torch.arange(N * (VB // 4), dtype=torch.int64, device=dev) % (1 << 31)).to(
+        torch.int32).view(N, VB // 4)
+    w = dg.DyCuckooWide(int(N / 0.85), VB, auto_resize=False, device=dev.index or 0)
+    ins = timed(lambda: w.insert(keys, vals, stream=stream))
+    got = {}
+
+    def find():
+        got["v"] = w.find(keys, stream=stream)
+
+    fnd = timed(find, 5)
+    bad = int((got["v"][0] != vals).any(dim=1).sum())
+    ers = timed(lambda: w.erase(keys[: N // 2], stream=stream))
+    res["wide_values"] = {
+        "workload": "2^24 u32 keys, 32-byte values, load factor 0.85",
+        "insert_mops": round(N / ins / 1e3, 1), "find_mops": round(N / fnd / 1e3, 1),
+        "erase_mops": round(N // 2 / ers / 1e3, 1),
+        "find_value_gbs": round(N * VB / (fnd / 1e3) / 1e9, 1), "find_mismatches": bad}
+    w.close()
+    del keys, vals, got
+    torch.cuda.empty_cache()
+
+    N = 1 << 26
+    keys = as_i32(make_keys(0, N, torch, dev), torch)
+    vals = torch.arange(1, N + 1, dtype=torch.int32, device=dev)
+    t = dg.DyCuckoo(int(N / 0.85), auto_resize=False, device=dev.index or 0)
+    t.insert(keys, vals, unique=True, new_keys=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    buf = t.snapshot()
+    snap_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    r = dg.DyCuckoo.restore(buf, device=dev.index or 0)
+    torch.cuda.synchronize()
+    rest_s = time.perf_counter() - t0
+    q = keys[: 1 << 20]
+    out, _ = r.find(q)
+    bad = int((out != vals[: 1 << 20]).sum())
+    res["snapshot"] = {"workload": "2^26 u32 keys at load factor 0.85, to a host buffer and back",
+                       "bytes": int(buf.size), "snapshot_gbs": round(buf.size / snap_s / 1e9, 2),
+                       "restore_gbs": round(buf.size / rest_s / 1e9, 2),
+                       "restored_find_mismatches": bad,
+                       "note": "host wall time; the buffer is pageable host memory"}
+    t.close()
+    r.close()
+    del keys, vals, buf
+    torch.cuda.empty_cache()
+    return res
+
+
 def set_table_bytes(S, bucket_bytes=128):
     """Device bytes of a set's subtables (from the members' slot capacities)."""
     _, caps = S.sizes()
@@ -924,7 +998,8 @@ def main():
     ap.add_argument("--skip-serve", action="store_true",
                     help="skip the serving loop and the serving-step workload")
     ap.add_argument("--only", default=None,
-                    choices=["find", "small", "stream", "multi", "serve", "serve-steps"],
+                    choices=["find", "small", "features", "stream", "multi", "serve",
+                             "serve-steps"],
                     help="run one workload: find (the headline line with its variants, ops "
                          "and baselines, no other workloads) or one of the others alone, "
                          "printing its own JSON object")
@@ -958,6 +1033,7 @@ def main():
     dev = torch.device("cuda", local)
     if args.only not in (None, "find"):
         run = {"small": lambda: run_small_table(args, dev, torch, dg),
+               "features": lambda: run_features(args, dev, torch, dg),
                "stream": lambda: run_resize_stream(args, dev, torch, dg),
                "multi": lambda: run_multi_table(args, dev, torch, dg),
                "serve": lambda: run_serving(args),
@@ -1185,6 +1261,7 @@ def main():
     workloads = {}
     if not args.skip_variants:
         workloads["small_table"] = run_small_table(args, dev, torch, dg)
+        workloads["features"] = run_features(args, dev, torch, dg)
     if not args.skip_stream and not args.skip_variants:
         workloads["resize_stream"] = run_resize_stream(args, dev, torch, dg)
     if not args.skip_multi and not args.skip_variants:
