@@ -1223,6 +1223,25 @@ def main():
                  stream=stream)
         torch.cuda.synchronize()
         assert t.size == N
+        # the same batch with DYC_FLAG_UNIQUE (its keys are distinct): one probe
+        # pass, no batch dedup; restored untimed after
+        mout.zero_()
+        e0.record(stream)
+        t.apply(mo, mk, mv, out=mout, bits=mbits, no_resize=True, unique=True, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ops["mixed_unique_50f_30u_20e_mops"] = round(Q / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
+        ops["roofline"]["mixed_unique_50f_30u_20e"] = op_roofline(
+            ops["mixed_unique_50f_30u_20e_mops"], ops["roofline"]["mixed_50f_30u_20e"]["alg_bytes_per_op"])
+        ust = t.stats()
+        ubad = int((mout != vals[perm]).sum())
+        ops["checks"]["mixed_unique"] = {"value_mismatches": ubad, "erased": ust["erased"],
+                                         "updated": ust["updated"]}
+        assert ubad == 0 and ust["erased"] == n_er and t.size == N - n_er
+        t.insert(keys[perm].contiguous(), vals[perm].contiguous(), unique=True, no_resize=True,
+                 stream=stream)
+        torch.cuda.synchronize()
+        assert t.size == N
         # ---- resize: double the subtable the reference would pick, then
         # halve it back (even bucket count: bucket j merges with j + nb/2);
         # algorithmic bytes: upsize reads S and writes 2S, downsize reads 2S

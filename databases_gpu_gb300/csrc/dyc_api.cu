@@ -1287,6 +1287,59 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     return DYC_OK;
 }
 
+// One chunk of a mixed batch whose keys are all distinct (DYC_FLAG_UNIQUE):
+// the one-pass kernel, then eviction walks for the inserts it left without a
+// slot. The upsize policy counts every insert op of the chunk before it, as
+// dyc_insert does (api.cpp:359-369), unless even a chunk of nothing but new
+// keys keeps the table within deferred_fill() of its slots; then it runs
+// after the chunk on the table's size.
+dyc_status apply_unique_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const void *vals,
+                              uint64_t n, void *vals_out, uint32_t *bits_out, uint32_t flags,
+                              cudaStream_t s) {
+    const bool resize = t->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE);
+    const bool before = resize && (double)(t->size + n) > deferred_fill(t) * (double)t->capacity;
+    TRY(reset_call_counters(t, s));
+    if (before) {
+        cudaError_t e = KB_CALL(t, count_inserts, ctx(t, s), ops, n, &t->d_ctr->nins);
+        if (e != cudaSuccess) return fail(DYC_ECUDA, "count kernel: %s", cudaGetErrorString(e));
+        TRY(read_counters(t, s));
+        const uint64_t nins = t->h_ctr->nins;
+        int guard = 0;
+        while (nins && (double)(t->size + nins) > t->cfg.upper_load * (double)t->capacity &&
+               guard++ < 64)
+            TRY(resize_up_impl(t, s));
+    }
+    cudaError_t e = KB_CALL(t, apply_unique, ctx(t, s), t->D, t->sb, t->S, ops, keys, vals,
+                            (uint32_t)t->vb, vals_out, bits_out, n, t->d_ctr);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "apply kernel: %s", cudaGetErrorString(e));
+    e = KB_CALL(t, walk, ctx(t, s), t->D, t->sb, t->S.list_a, &t->d_ctr->pending, t->S.list_b,
+                &t->d_ctr->overflow, t->S.list_cap, t->cfg.max_evictions, true, t->d_ctr,
+                t->S.list_cap);
+    if (e != cudaSuccess) return fail(DYC_ECUDA, "walk kernel: %s", cudaGetErrorString(e));
+    TRY(read_counters(t, s));
+    const Counters c = *t->h_ctr;
+    dyc_op_stats &St = t->last;
+    St.inserted += c.inserted;
+    St.updated += c.updated;
+    St.erased += c.erased;
+    St.evict_steps += c.evict_steps;
+    St.overflowed += c.overflow;
+    bool grew = false;
+    if (c.overflow) {
+        TRY(drain(t, s, t->S.list_b, &t->d_ctr->overflow, t->S.list_a, &t->d_ctr->pending,
+                  t->S.list_cap, true, true));
+        St.inserted += t->h_ctr->inserted - c.inserted;
+        St.evict_steps += t->h_ctr->evict_steps - c.evict_steps;
+        grew = true;
+    }
+    if (resize && !before && !grew) {
+        int guard = 0;
+        while ((double)t->size > t->cfg.upper_load * (double)t->capacity && guard++ < 64)
+            TRY(resize_up_impl(t, s));
+    }
+    return DYC_OK;
+}
+
 }  // namespace
 
 extern "C" dyc_status dyc_apply(dyc_table *t, const uint8_t *d_ops, const void *d_keys,
@@ -1301,14 +1354,16 @@ extern "C" dyc_status dyc_apply(dyc_table *t, const uint8_t *d_ops, const void *
     if (!d_ops || !d_keys || !d_vals) return fail(DYC_EINVAL, "null op, key or value array");
     const uint64_t chunk = t->chunk;
     const uint64_t m0 = n < chunk ? n : chunk;
-    TRY(ensure_apply(t, m0));
+    const bool unique = (flags & DYC_FLAG_UNIQUE) != 0;
+    if (!unique) TRY(ensure_apply(t, m0));
     TRY(ensure_scratch(t, m0));
     for (uint64_t off = 0; off < n; off += chunk) {
         const uint64_t m = (n - off) < chunk ? (n - off) : chunk;
-        TRY(apply_chunk(t, d_ops + off, (const char *)d_keys + off * t->kb,
-                        (const char *)d_vals + off * t->vb, m,
-                        d_vals_out ? (char *)d_vals_out + off * t->vb : nullptr,
-                        d_bits_out ? d_bits_out + off / 32 : nullptr, flags, s));
+        const char *k = (const char *)d_keys + off * t->kb, *v = (const char *)d_vals + off * t->vb;
+        void *o = d_vals_out ? (char *)d_vals_out + off * t->vb : nullptr;
+        uint32_t *b = d_bits_out ? d_bits_out + off / 32 : nullptr;
+        if (unique) TRY(apply_unique_chunk(t, d_ops + off, k, v, m, o, b, flags, s));
+        else TRY(apply_chunk(t, d_ops + off, k, v, m, o, b, flags, s));
     }
     // downsize check after the batch, as after an erase batch (api.cpp:494-505)
     if (t->cfg.auto_resize && !(flags & DYC_FLAG_NO_RESIZE) &&

@@ -835,4 +835,131 @@ __global__ void __launch_bounds__(256) k_apply_replay_mid(const __grid_constant_
     }
 }
 
+// ----------------------------------------------------------------------------
+// Mixed batch whose keys are all distinct (dyc_apply with DYC_FLAG_UNIQUE):
+// with one op per key no op depends on another, so each is resolved and
+// applied in a single pass, without the grouping, compaction and replay the
+// general path needs for repeated keys. An op probes its key's first bucket,
+// and the second one where the key or (for an insert) an empty slot may be
+// there; it reports the key's state before it, as the general path does.
+// Then an insert updates the key's own slot or claims an empty one (ops left
+// without a slot go to list_a for the eviction walks that follow the pass),
+// and an erase clears the key's slot. Ops on different keys run side by
+// side: nothing in the pass moves an entry, so a find never misses a key
+// that is present, and a key's own slot is written only by its own op.
+// ----------------------------------------------------------------------------
+template <int KB, int SB, bool HINT>
+__global__ void __launch_bounds__(256) k_apply_unique(
+    const __grid_constant__ Desc D, const __grid_constant__ Scratch S,
+    const uint8_t *__restrict__ ops, const void *__restrict__ keys,
+    const void *__restrict__ vals, uint32_t vb, void *__restrict__ vals_out,
+    uint32_t *__restrict__ bits_out, uint64_t n, Counters *ctr) {
+    using T = SlotT<KB>;
+    using Sl = typename T::S;
+    using Gm = Geo<KB, SB>;
+    __shared__ __align__(128) unsigned char s_stage[SB >= 64 ? kWarpsPerBlock : 1][32 * SB];
+    unsigned char *stage = s_stage[SB >= 64 ? (threadIdx.x >> 5) : 0];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t step = warp_stride();
+    const unsigned long long tpol = HINT ? l2_policies(true).table : 0ull;
+    uint32_t n_ins = 0, n_upd = 0, n_del = 0;
+    for (uint64_t base = warp_base(); base < n; base += step) {
+        const uint64_t i = base + lane;
+        typename T::K k = 0;
+        uint8_t op = kOpFind;
+        Sl e = T::empty();
+        if (i < n) {
+            k = load_key<KB>(keys, i);
+            op = ops[i];
+        }
+        const bool act = k != 0;  // ops on key 0 miss and change nothing
+        const bool ins = act && op == kOpInsert, del = act && op == kOpErase;
+        if (ins) e = T::make(k, load_val(vals, vb, i));
+        const uint32_t hk = fold(k);
+        const Pair p = pair_of(hk, D.d);
+        char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
+        char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
+        const KvOut r1 = place_probe<KB, SB, HINT>(p1, k, act, p.first, D.d, stage, tpol);
+        const bool found1 = act && r1.match >= 0;
+        // the second bucket holds the key only if the first one's fingerprint
+        // bit allows it (always without metadata); an insert also looks there
+        // for an empty slot when the first bucket is full
+        const bool check2 =
+            act && !found1 && ((!Gm::kMeta || r1.overflow) || (ins && r1.empty == 0u));
+        KvOut r2{-1, 0ull, false, 0u};
+        if (__any_sync(kFull, check2))
+            r2 = place_probe<KB, SB, HINT>(p2, k, check2, p.second, D.d, stage, tpol);
+        const bool found2 = check2 && r2.match >= 0;
+        const bool present = found1 || found2;
+        const uint64_t before = found1 ? r1.value : (found2 ? r2.value : 0ull);
+        bool pend = false;
+        if (ins) {
+            if (found1) {
+                T::store(slot_ptr<KB, SB>(p1, r1.match), e);
+                ++n_upd;
+            } else if (found2) {
+                T::store(slot_ptr<KB, SB>(p2, r2.match), e);
+                ++n_upd;
+            } else {
+                bool ok = claim_empty<KB, SB>(p1, r1.empty, e);
+                if (!ok && check2 && r2.empty) {
+                    mark_overflow<KB, SB>(p1, hk);
+                    ok = claim_empty<KB, SB>(p2, r2.empty, e);
+                }
+                if (ok) ++n_ins;
+                else pend = true;
+            }
+        } else if (del && present) {
+            T::store(found1 ? slot_ptr<KB, SB>(p1, r1.match) : slot_ptr<KB, SB>(p2, r2.match),
+                     T::empty());
+            ++n_del;
+        }
+        if (vals_out != nullptr && i < n) store_val(vals_out, vb, i, before);
+        const unsigned m = __ballot_sync(kFull, present);
+        if (bits_out != nullptr && lane == 0) bits_out[base >> 5] = m;
+        __syncwarp();
+        const unsigned long long at = agg_inc(&ctr->pending, pend);
+        if (pend) {
+            if (at < S.list_cap) ((Sl *)S.list_a)[at] = e;
+            else atomicAdd(&ctr->spill, 1ull);
+        }
+    }
+    // one atomic per counter per block
+    __shared__ unsigned long long s_sum[3];
+    if (threadIdx.x < 3) s_sum[threadIdx.x] = 0ull;
+    __syncthreads();
+    const uint32_t w_ins = __reduce_add_sync(kFull, n_ins), w_upd = __reduce_add_sync(kFull, n_upd);
+    const uint32_t w_del = __reduce_add_sync(kFull, n_del);
+    if (lane == 0) {
+        if (w_ins) atomicAdd(&s_sum[0], (unsigned long long)w_ins);
+        if (w_upd) atomicAdd(&s_sum[1], (unsigned long long)w_upd);
+        if (w_del) atomicAdd(&s_sum[2], (unsigned long long)w_del);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_sum[0]) atomicAdd(&ctr->inserted, s_sum[0]);
+        if (s_sum[1]) atomicAdd(&ctr->updated, s_sum[1]);
+        if (s_sum[2]) atomicAdd(&ctr->erased, s_sum[2]);
+        const long long net = (long long)s_sum[0] - (long long)s_sum[2];
+        if (net) atomicAdd(&ctr->size, (unsigned long long)net);  // size += inserted - erased
+    }
+}
+
+// *count += the INSERT ops among ops[0..n) (one atomic per block).
+template <int KB>
+__global__ void __launch_bounds__(256) k_count_inserts(const uint8_t *__restrict__ ops, uint64_t n,
+                                                       unsigned long long *count) {
+    uint32_t c = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        c += ops[i] == kOpInsert ? 1u : 0u;
+    __shared__ unsigned long long s_c;
+    if (threadIdx.x == 0) s_c = 0ull;
+    __syncthreads();
+    c = __reduce_add_sync(kFull, c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(&s_c, (unsigned long long)c);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_c) atomicAdd(count, s_c);
+}
+
 }  // namespace dyc

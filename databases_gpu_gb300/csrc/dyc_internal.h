@@ -52,7 +52,8 @@ struct Counters {
     unsigned long long spill;  // pending entries a list could not hold (must stay 0)
     unsigned long long pad[2];      // scratch words of dyc_export and dyc_snapshot
     unsigned long long timeouts;    // bounded device waits that gave up (must stay 0)
-    unsigned long long pad2[3];
+    unsigned long long nins;        // scratch word: insert ops of a dyc_apply batch
+    unsigned long long pad2[2];
 };
 static_assert(sizeof(Counters) == 128, "Counters is one 128-byte block");
 
@@ -241,6 +242,15 @@ template <int KB> struct Ops {
     // set_find / set_mutate / set_walk replace find / erase + place / walk.
     static cudaError_t apply_group(const LaunchCtx &L, const ApplyScratch &A, const void *keys,
                                   uint64_t n);
+    // a mixed batch whose keys are all distinct, in one probe pass (ops left
+    // without a slot go to S.list_a, counted in ctr->pending)
+    static cudaError_t apply_unique(const LaunchCtx &L, const Desc &D, int sb, const Scratch &S,
+                                    const uint8_t *ops, const void *keys, const void *vals,
+                                    uint32_t vb, void *vals_out, uint32_t *bits_out, uint64_t n,
+                                    Counters *ctr);
+    // *count += the INSERT ops among ops[0..n)
+    static cudaError_t count_inserts(const LaunchCtx &L, const uint8_t *ops, uint64_t n,
+                                     unsigned long long *count);
     // after the find of the distinct keys: single-op keys resolved in op
     // order, the other ops scattered into their keys' segments. n_ptr (many
     // tables): the op count on the device; n then only sizes grids

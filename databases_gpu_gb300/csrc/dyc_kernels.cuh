@@ -404,7 +404,7 @@ __device__ __forceinline__ KvOut place_probe(const char *p, typename SlotT<KB>::
         const ProbeOut<KB> r = probe<KB, SB, 2, true, false, HINT>(p, key, act, t, d, pol);
         KvOut o;
         o.match = r.match;
-        o.value = 0ull;
+        o.value = SlotT<KB>::val(r.mslot);
         o.overflow = (r.meta & fp_bit(fold(key))) != 0ull;
         o.empty = r.empty;
         return o;

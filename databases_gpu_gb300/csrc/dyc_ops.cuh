@@ -153,6 +153,29 @@ cudaError_t Ops<KB>::erase(const LaunchCtx &L, const Desc &D, int sb, const Scra
 }
 
 template <int KB>
+cudaError_t Ops<KB>::apply_unique(const LaunchCtx &L, const Desc &D, int sb, const Scratch &S,
+                                  const uint8_t *ops, const void *keys, const void *vals,
+                                  uint32_t vb, void *vals_out, uint32_t *bits_out, uint64_t n,
+                                  Counters *ctr) {
+    if (n == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = D.l2_keep ? k_apply_unique<KB, SB, true> : k_apply_unique<KB, SB, false>;
+        k<<<tile_grid(L, n), 256, 0, L.stream>>>(D, S, ops, keys, vals, vb, vals_out, bits_out, n,
+                                                  ctr);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
+cudaError_t Ops<KB>::count_inserts(const LaunchCtx &L, const uint8_t *ops, uint64_t n,
+                                   unsigned long long *count) {
+    if (n == 0) return cudaSuccess;
+    auto k = k_count_inserts<KB>;
+    k<<<grid_for((const void *)k, L, n), 256, 0, L.stream>>>(ops, n, count);
+    return cudaGetLastError();
+}
+
+template <int KB>
 cudaError_t Ops<KB>::resize_up_many(const LaunchCtx &L, int sb, const ResizeJobs &J) {
     if (J.n == 0 || J.blocks == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {

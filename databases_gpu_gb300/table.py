@@ -176,11 +176,13 @@ class DyCuckoo:
         return int(cnt.value)
 
     def apply(self, ops, keys, values, out=None, bits=None, no_resize: bool = False,
-              stream=None):
+              unique: bool = False, stream=None):
         """Mixed batch (dyc_apply): ops is a uint8 tensor of OP_FIND /
         OP_INSERT / OP_ERASE, applied in index order. Returns (out, bits):
         the value each op saw (found / previous / removed, 0 if absent) and
-        one bit per op, set when the key was present before the op."""
+        one bit per op, set when the key was present before the op.
+        unique: the caller promises no key repeats in the batch (one probe
+        pass per op, DYC_FLAG_UNIQUE)."""
         torch = _torch()
         n = keys.numel()
         if ops.numel() != n or values.numel() != n:
@@ -194,7 +196,8 @@ class DyCuckoo:
         check(self.L.dyc_apply(self._h, _ptr(ops, "ops", 1), _ptr(keys, "keys", self.key_bytes),
                                _ptr(values, "values", self.value_bytes),
                                n, _ptr(out, "out", self.value_bytes), _ptr(bits, "bits", 4),
-                               FLAG_NO_RESIZE if no_resize else 0, _stream_ptr(stream)),
+                               (FLAG_NO_RESIZE if no_resize else 0) |
+                               (FLAG_UNIQUE if unique else 0), _stream_ptr(stream)),
               "dyc_apply")
         return out, bits
 

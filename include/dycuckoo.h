@@ -108,9 +108,11 @@ typedef struct dyc_config {
 } dyc_config;
 
 /* Per-call flags. */
-#define DYC_FLAG_UNIQUE 1u    /* caller promises no key repeats in this batch (the batch
-                                 dedup is skipped; a batch that repeats a key anyway may
-                                 count it twice in the erased / updated counts) */
+#define DYC_FLAG_UNIQUE 1u    /* caller promises no key repeats in this batch: inserts and
+                                 erases skip the batch dedup, dyc_apply resolves every op in
+                                 one probe pass. A batch that repeats a key anyway gets
+                                 unspecified results: a new key inserted twice may be
+                                 stored twice, and counts may include it twice */
 #define DYC_FLAG_NEW_KEYS 2u  /* insert: caller promises no key of the batch is in the table */
 #define DYC_FLAG_NO_RESIZE 4u /* skip the load-factor policy for this call */
 
@@ -241,7 +243,11 @@ dyc_status dyc_erase_host(dyc_table *t, const void *h_keys, uint64_t n,
  * d_bits_out (ceil(n/32) words) are optional. Ops other than 0/1/2 are
  * treated as FIND. Inserts may upsize first (projected load above
  * upper_load); the batch may downsize after (load below lower_load), unless
- * DYC_FLAG_NO_RESIZE. Returns after the batch is in the table. */
+ * DYC_FLAG_NO_RESIZE. Returns after the batch is in the table.
+ * DYC_FLAG_UNIQUE (no key repeats in the batch): every op is resolved and
+ * applied in one probe pass of its key's buckets. There is no grouping of
+ * the batch by key. The results are the same. The upsize policy then
+ * counts every INSERT op as a possible new key, as dyc_insert does. */
 dyc_status dyc_apply(dyc_table *t, const uint8_t *d_ops, const void *d_keys, const void *d_vals,
                      uint64_t n, void *d_vals_out, uint32_t *d_bits_out, uint32_t flags,
                      void *stream);

@@ -24,8 +24,8 @@ def _dg():
     return dg
 
 
-def _apply_and_compare(t, m, ops, keys, vals, label):
-    out, bits = t.apply(to_dev(ops), to_dev(keys), to_dev(vals))
+def _apply_and_compare(t, m, ops, keys, vals, label, unique=False):
+    out, bits = t.apply(to_dev(ops), to_dev(keys), to_dev(vals), unique=unique)
     gv = to_host(out, t.value_bytes).astype(np.uint64)
     gh = _dg().unpack_bits(bits, keys.size)
     ov, oh = m.apply(ops, keys.astype(np.uint64), vals.astype(np.uint64))
@@ -186,3 +186,45 @@ def test_resize_stream_u64_matches_oracle_every_batch():
     assert ups > 0 and downs > 0
     assert t.capacity < peak_cap
     t.close()
+
+
+@pytest.mark.parametrize("key_bytes,bucket_bytes,chunk", [(4, 128, 0), (8, 128, 0), (4, 32, 0),
+                                                         (8, 64, 4096)])
+def test_apply_distinct_keys_one_pass_matches_oracle(key_bytes, bucket_bytes, chunk):
+    """dyc_apply with DYC_FLAG_UNIQUE (no key repeats in a batch): every op
+    resolved and applied in one probe pass. Five batches of distinct keys on
+    a growing table: finds, upserts and erases of present keys, inserts of
+    new keys (enough to fill buckets and need eviction walks and upsizes),
+    erases and finds of absent keys, ops on key 0. Every op's value and hit
+    bit and the contents after every batch equal the oracle's; with chunk,
+    batches span many 4096-op chunks."""
+    from databases_gpu_gb300 import _lib
+    dg = _dg()
+    L = _lib.lib()
+    if chunk:
+        assert L.dyc_debug_inject(_lib.INJECT_CHUNK_OPS, chunk) == 0
+    try:
+        t = dg.DyCuckoo(1 << 12, key_bytes=key_bytes, value_bytes=key_bytes,
+                        bucket_bytes=bucket_bytes)
+    finally:
+        L.dyc_debug_inject(_lib.INJECT_RESET, 0)
+    m = O.Map()
+    rng = np.random.default_rng(83)
+    pool = unique_u32(1 << 17, seed=84) if key_bytes == 4 else unique_u64(1 << 17, seed=84)
+    npk = np.uint32 if key_bytes == 4 else np.uint64
+    used = 0
+    for r in range(5):
+        present = m.export()[0].astype(npk)
+        nold = min(present.size, 6000)
+        old = rng.choice(present, nold, replace=False) if nold else np.zeros(0, npk)
+        fresh = pool[used:used + 9000].astype(npk)
+        used += 9000
+        keys = np.concatenate([old[old != 0], fresh[fresh != 0], np.zeros(1, npk)])
+        rng.shuffle(keys)
+        n = keys.size
+        ops = rng.choice(np.array([0, 1, 2], np.uint8), n, p=[0.3, 0.5, 0.2])
+        vals = rng.integers(1, 1 << 30, n).astype(npk)
+        _apply_and_compare(t, m, ops, keys, vals, "unique batch %d" % r, unique=True)
+    assert len(m) > 15000 and t.capacity > (1 << 12)
+    t.close()
+
