@@ -392,17 +392,19 @@ def run_small_table(args, dev, torch, dg):
     same sequence on the same keys, every step timed with CUDA events on the
     launching stream:
       insert the first half of the keys (untimed: the table's first call
-      sizes its scratch), insert the second half (timed, 2^19 keys), find
-      2^20 keys of which half hit (mean of 20 batches), erase 2^19 present
-      keys (timed), then re-insert them (timed; the library with
-      DYC_FLAG_UNIQUE, which skips the batch dedup the reference does not
-      have either).
+      sizes its scratch); then REPS cycles of: insert the second half
+      (2^19 new keys into the half-full table), erase it again; then find
+      2^20 keys of which half hit (mean of 20 batches) on the full table;
+      then REPS cycles of: erase the second half (untimed), re-insert it
+      (the library with DYC_FLAG_UNIQUE, which skips the batch dedup the
+      reference does not have either). Each rate is the median cycle.
     The library's insert and erase calls dedup the batch (unless told the
     keys are unique) and read their counters back before returning; the
     reference's kernels do neither. The table takes ~10 MB, so it lives in
     the L2."""
     N = 1 << 20
     H = N // 2
+    REPS = 9
     keys = as_i32(make_keys(0, N, torch, dev), torch)
     vals = torch.arange(1, N + 1, dtype=torch.int32, device=dev)
     miss = as_i32(make_keys(N, N + H, torch, dev), torch)
@@ -417,6 +419,8 @@ def run_small_table(args, dev, torch, dg):
     stream = torch.cuda.current_stream()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    k1, k2 = keys[:H].contiguous(), keys[H:].contiguous()
+    v1, v2 = vals[:H].contiguous(), vals[H:].contiguous()
 
     def timed(fn, reps=1):
         torch.cuda.synchronize()
@@ -427,20 +431,42 @@ def run_small_table(args, dev, torch, dg):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
+    def median(xs):
+        xs = sorted(xs)
+        return xs[len(xs) // 2]
+
+    def sequence(insert, insert_unique, erase, erase_untimed, find):
+        """The timed sequence on a table holding the first half: medians in ms."""
+        ins, ers, uins = [], [], []
+        for _ in range(REPS):
+            ins.append(timed(lambda: insert(k2, v2)))
+            ers.append(timed(lambda: erase(k2)))
+        insert(k2, v2)
+        find()
+        fnd = timed(find, 20)
+        for _ in range(REPS):
+            erase_untimed(k2)
+            uins.append(timed(lambda: insert_unique(k2, v2)))
+        return median(ins), fnd, median(ers), median(uins)
+
     res = {"workload": "config 1: 2^20 unique u32 keys at load factor 0.85 (hashAPI(2^20/0.85)), "
                        "insert of 2^19 keys into the half-full table, 2^20 finds (50 % hits), "
-                       "erase of 2^19 present keys, their re-insert; ~10 MB table"}
+                       "erase of 2^19 present keys, their re-insert; ~10 MB table; median of "
+                       "%d cycles per step" % REPS}
     # no load-factor policy, as the reference's plain hash_insert (api.cpp:185-194)
     t = dg.DyCuckoo(int(N / 0.85), auto_resize=False, device=dev.index or 0)
     out = torch.empty(N, dtype=torch.int32, device=dev)
     bits = torch.empty(N // 32, dtype=torch.int32, device=dev)
-    t.insert(keys[:H], vals[:H], stream=stream)
-    ins = timed(lambda: t.insert(keys[H:], vals[H:], stream=stream))
+    t.insert(k1, v1, stream=stream)
+    ins, fnd, ers, uins = sequence(
+        lambda k, v: t.insert(k, v, stream=stream),
+        lambda k, v: t.insert(k, v, unique=True, stream=stream),
+        lambda k: t.erase(k, stream=stream),
+        lambda k: t.erase(k, unique=True, stream=stream),
+        lambda: t.find(q, out=out, hit_bits=bits, stream=stream))
     t.find(q, out=out, hit_bits=bits, stream=stream)
-    fnd = timed(lambda: t.find(q, out=out, hit_bits=bits, stream=stream), 20)
+    torch.cuda.synchronize()
     bad = int((out != expv).sum())
-    ers = timed(lambda: t.erase(keys[:H], stream=stream))
-    uins = timed(lambda: t.insert(keys[:H], vals[:H], unique=True, stream=stream))
     res["library"] = {"insert_mops": round(H / ins / 1e3, 1), "find_mops": round(N / fnd / 1e3, 1),
                       "erase_mops": round(H / ers / 1e3, 1),
                       "insert_unique_mops": round(H / uins / 1e3, 1), "find_mismatches": bad,
@@ -463,14 +489,17 @@ def run_small_table(args, dev, torch, dg):
         assert L.refgpu_insert(k.data_ptr(), v.data_ptr(), k.numel(), rehash.data_ptr(),
                                iters.data_ptr(), sp) == 0
 
-    rinsert(keys[:H], vals[:H])
-    rins = timed(lambda: rinsert(keys[H:], vals[H:]))
+    def rerase(k):
+        ref.delete(k, stream=stream)
+
     rout = torch.zeros(N, dtype=torch.int32, device=dev)
+    rinsert(k1, v1)
+    rins, rfnd, rers, ruins = sequence(rinsert, rinsert, rerase, rerase,
+                                       lambda: ref.search(q, out=rout, stream=stream))
+    rout.zero_()
     ref.search(q, out=rout, stream=stream)
-    rfnd = timed(lambda: ref.search(q, out=rout, stream=stream), 20)
+    torch.cuda.synchronize()
     rbad = int((rout != expv).sum())
-    rers = timed(lambda: ref.delete(keys[:H], stream=stream))
-    ruins = timed(lambda: rinsert(keys[:H], vals[:H]))
     res["reference_gpu"] = {"insert_mops": round(H / rins / 1e3, 1),
                             "find_mops": round(N / rfnd / 1e3, 1),
                             "erase_mops": round(H / rers / 1e3, 1),
