@@ -461,13 +461,22 @@ dyc_status drain(dyc_table *t, cudaStream_t s, void *src, unsigned long long *sr
 
 // Batch dedup of one chunk into the dedup buffers of S, on stream s:
 // kKeepLast (insert) names each key's last op, kKeepFirst (erase) its first.
+// The table's scratch as one chunk of n ops uses it: the dedup table sized
+// for n (as ensure_scratch sizes it for the largest chunk), so a small call
+// on a table that once took a large batch clears and probes a small table.
+Scratch chunk_scratch(const dyc_table *t, uint64_t n) {
+    Scratch S = t->S;
+    const uint64_t cap = next_pow2(2 * (n < 16 ? 16 : n));
+    if (cap < S.dedup_cap) S.dedup_cap = cap;
+    return S;
+}
+
+// The batch dedup of a chunk: one launch clears its cells and the call
+// counters (what reset_call_counters does), then the claims.
 dyc_status dedup_chunk(dyc_table *t, const Scratch &S, const void *keys, uint64_t n,
                        dyc::DedupMode mode, cudaStream_t s) {
-    CK(cudaMemsetAsync(S.dedup, 0, (size_t)S.dedup_cap * 8, s));
-    if (S.dedup_idx)
-        CK(cudaMemsetAsync(S.dedup_idx, mode == dyc::kKeepLast ? 0 : 0xFF,
-                           (size_t)S.dedup_cap * 4, s));
-    cudaError_t e = KB_CALL(t, dedup, ctx(t, s), S, keys, n, mode);
+    cudaError_t e = KB_CALL(t, dedup, ctx(t, s), S, keys, n, mode, &t->d_ctr->inserted,
+                            (uint32_t)(sizeof(Counters) / 8 - 1));
     if (e != cudaSuccess) return fail(DYC_ECUDA, "dedup kernel: %s", cudaGetErrorString(e));
     return DYC_OK;
 }
@@ -476,9 +485,10 @@ dyc_status insert_chunk(dyc_table *t, const void *keys, const void *vals, uint64
                         uint32_t flags, cudaStream_t s) {
     const bool use_dedup = !(flags & DYC_FLAG_UNIQUE) && n > 1;
     const bool new_keys = (flags & DYC_FLAG_NEW_KEYS) != 0;
-    TRY(reset_call_counters(t, s));
-    if (use_dedup) TRY(dedup_chunk(t, t->S, keys, n, dyc::kKeepLast, s));
-    cudaError_t e = KB_CALL(t, place, ctx(t, s), t->D, t->sb, t->S, use_dedup, new_keys, keys,
+    const Scratch S = chunk_scratch(t, n);
+    if (use_dedup) TRY(dedup_chunk(t, S, keys, n, dyc::kKeepLast, s));
+    else TRY(reset_call_counters(t, s));
+    cudaError_t e = KB_CALL(t, place, ctx(t, s), t->D, t->sb, S, use_dedup, new_keys, keys,
                             vals, (uint32_t)t->vb, n, t->d_ctr);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "place kernel: %s", cudaGetErrorString(e));
     // walks for the ops whose buckets were full: list_a -> list_b
@@ -507,9 +517,10 @@ dyc_status insert_chunk(dyc_table *t, const void *keys, const void *vals, uint64
 dyc_status erase_chunk(dyc_table *t, const void *keys, uint64_t n, uint32_t *bits,
                        uint32_t flags, cudaStream_t s) {
     const bool use_dedup = !(flags & DYC_FLAG_UNIQUE) && n > 1;
-    TRY(reset_call_counters(t, s));
-    if (use_dedup) TRY(dedup_chunk(t, t->S, keys, n, dyc::kKeepFirst, s));
-    cudaError_t e = KB_CALL(t, erase, ctx(t, s), t->D, t->sb, t->S, use_dedup, keys, n, bits,
+    const Scratch S = chunk_scratch(t, n);
+    if (use_dedup) TRY(dedup_chunk(t, S, keys, n, dyc::kKeepFirst, s));
+    else TRY(reset_call_counters(t, s));
+    cudaError_t e = KB_CALL(t, erase, ctx(t, s), t->D, t->sb, S, use_dedup, keys, n, bits,
                             t->d_ctr);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "erase kernel: %s", cudaGetErrorString(e));
     TRY(read_counters(t, s));
@@ -2614,22 +2625,21 @@ dyc_status dyc_wide_insert(dyc_wide *w, const void *d_keys, const void *d_vals, 
         cudaError_t e = KB_CALL(t, find, ctx(t, s), t->D, t->sb, k, w->pre_h, 4u, w->bits, m);
         if (e != cudaSuccess) return fail(DYC_ECUDA, "wide find: %s", cudaGetErrorString(e));
         const bool use_dedup = !(flags & DYC_FLAG_UNIQUE) && m > 1;
-        if (use_dedup) {
-            CK(cudaMemsetAsync(t->S.dedup, 0, (size_t)t->S.dedup_cap * 8, s));
-            if (t->S.dedup_idx) CK(cudaMemsetAsync(t->S.dedup_idx, 0, (size_t)t->S.dedup_cap * 4, s));
-            e = KB_CALL(t, dedup, ctx(t, s), t->S, k, m, dyc::kKeepLast);
+        const Scratch S = chunk_scratch(t, m);
+        if (use_dedup) {  // clears the chunk's cells first
+            e = KB_CALL(t, dedup, ctx(t, s), S, k, m, dyc::kKeepLast);
             if (e != cudaSuccess) return fail(DYC_ECUDA, "dedup kernel: %s", cudaGetErrorString(e));
         }
         TRY(wide_ensure_heap(w, m, s));
         CK(cudaMemsetAsync(w->cnt, 0, 2 * sizeof(unsigned long long), s));
         const unsigned grid = wide_grid(w, m);
         if (t->kb == 4)
-            dyc::k_wide_stage<4><<<grid, 256, 0, s>>>(t->S, use_dedup ? 1 : 0, k, v, w->words, m,
+            dyc::k_wide_stage<4><<<grid, 256, 0, s>>>(S, use_dedup ? 1 : 0, k, v, w->words, m,
                                                       w->pre_h, w->bits, w->heap, w->stack,
                                                       w->d_alloc, w->new_keys, w->new_h, w->cnt,
                                                       w->cnt + 1);
         else
-            dyc::k_wide_stage<8><<<grid, 256, 0, s>>>(t->S, use_dedup ? 1 : 0, k, v, w->words, m,
+            dyc::k_wide_stage<8><<<grid, 256, 0, s>>>(S, use_dedup ? 1 : 0, k, v, w->words, m,
                                                       w->pre_h, w->bits, w->heap, w->stack,
                                                       w->d_alloc, w->new_keys, w->new_h, w->cnt,
                                                       w->cnt + 1);

@@ -76,6 +76,15 @@ struct Scratch {
     uint32_t *dupseen;
 };
 
+// Dedup tables of at least this many cells get the winners pass (winbits);
+// smaller ones fit in the L2 beside the bucket lines, so an op of a chunk
+// with repeats looks its winner up in the table instead, and the pass's
+// launch is saved.
+constexpr uint64_t kWinnersMinCap = 1ull << 22;
+__host__ __device__ inline bool winners_pass(const Scratch &S) {
+    return S.winbits != nullptr && S.dedup_cap >= kWinnersMinCap;
+}
+
 // Scratch of one mixed batch of at most `cap_ops` ops. The multi-table
 // fields are null for a single table.
 struct ApplyScratch {
@@ -192,8 +201,13 @@ struct LaunchCtx {
 template <int KB> struct Ops {
     static cudaError_t find(const LaunchCtx &L, const Desc &D, int sb, const void *keys,
                             void *vals, uint32_t vb, uint32_t *hits, uint64_t n);
+    // the batch dedup of a chunk. With the table's own scratch (winbits
+    // set) it first clears the chunk's cells, winner bits and repeat flag,
+    // and `nzero` 64-bit words at `zero` (the call counters), in one launch;
+    // without, the caller has cleared the cells.
     static cudaError_t dedup(const LaunchCtx &L, const Scratch &S, const void *keys, uint64_t n,
-                             DedupMode mode);
+                             DedupMode mode, unsigned long long *zero = nullptr,
+                             uint32_t nzero = 0);
     // insert: place or update every op; ops whose two buckets are full go to
     // list_a (counted in pending). new_keys = caller promises absent keys.
     static cudaError_t place(const LaunchCtx &L, const Desc &D, int sb, const Scratch &S,

@@ -437,10 +437,8 @@ template <> struct Dedup<4> {
         }
     }
     __device__ static __forceinline__ bool winner(const Scratch &S, uint32_t k, uint32_t i) {
-        if (S.winbits) {
-            if (S.dupseen && *S.dupseen == 0u) return true;  // no key repeats in the chunk
-            return (S.winbits[i >> 5] >> (i & 31)) & 1u;
-        }
+        if (S.dupseen && *S.dupseen == 0u) return true;  // no key repeats in the chunk
+        if (winners_pass(S)) return (S.winbits[i >> 5] >> (i & 31)) & 1u;
         const unsigned long long *tab = (const unsigned long long *)S.dedup;
         const uint64_t mask = S.dedup_cap - 1;
         uint64_t h = mix32(k) & mask;
@@ -471,10 +469,8 @@ template <> struct Dedup<8> {
         }
     }
     __device__ static __forceinline__ bool winner(const Scratch &S, uint64_t k, uint32_t i) {
-        if (S.winbits) {
-            if (S.dupseen && *S.dupseen == 0u) return true;  // no key repeats in the chunk
-            return (S.winbits[i >> 5] >> (i & 31)) & 1u;
-        }
+        if (S.dupseen && *S.dupseen == 0u) return true;  // no key repeats in the chunk
+        if (winners_pass(S)) return (S.winbits[i >> 5] >> (i & 31)) & 1u;
         const unsigned long long *tab = (const unsigned long long *)S.dedup;
         const uint64_t mask = S.dedup_cap - 1;
         uint64_t h = mix32(fold(k) ^ (uint32_t)(k >> 32)) & mask;
@@ -486,6 +482,30 @@ template <> struct Dedup<8> {
         return false;
     }
 };
+
+// Clears one chunk's dedup state in one launch: the key cells (16-byte
+// stores; dedup_cap is a power of two >= 32 and the cells are 256-byte
+// aligned), the op-index cells of 8-byte keys (to idx_fill), win_words
+// winner-bit words, the repeat flag, and nzero 64-bit words at zero.
+template <int KB>
+__global__ void __launch_bounds__(256) k_dedup_clear(const __grid_constant__ Scratch S,
+                                                     uint32_t idx_fill, uint64_t win_words,
+                                                     unsigned long long *zero, uint32_t nzero) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint4 *cells = (uint4 *)S.dedup;
+    const uint64_t n16 = S.dedup_cap / 2;  // two 8-byte cells per store
+    for (uint64_t i = tid; i < n16; i += stride) cells[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (KB == 8 && S.dedup_idx != nullptr) {
+        uint4 *ix = (uint4 *)S.dedup_idx;
+        const uint4 f = make_uint4(idx_fill, idx_fill, idx_fill, idx_fill);
+        for (uint64_t i = tid; i < S.dedup_cap / 4; i += stride) ix[i] = f;
+    }
+    if (S.winbits != nullptr)
+        for (uint64_t i = tid; i < win_words; i += stride) S.winbits[i] = 0u;
+    if (tid == 0 && S.dupseen != nullptr) *S.dupseen = 0u;
+    if (tid < nzero) zero[tid] = 0ull;
+}
 
 template <int KB>
 __global__ void __launch_bounds__(256) k_dedup(const __grid_constant__ Scratch S,

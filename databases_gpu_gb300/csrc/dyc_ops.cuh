@@ -96,16 +96,16 @@ cudaError_t Ops<KB>::find(const LaunchCtx &L, const Desc &D, int sb, const void 
 
 template <int KB>
 cudaError_t Ops<KB>::dedup(const LaunchCtx &L, const Scratch &S, const void *keys, uint64_t n,
-                           DedupMode mode) {
+                           DedupMode mode, unsigned long long *zero, uint32_t nzero) {
     if (n == 0) return cudaSuccess;
     if (S.winbits) {
-        cudaError_t e = cudaMemsetAsync(S.winbits, 0, (size_t)(n / 32 + 1) * 4, L.stream);
-        if (e == cudaSuccess && S.dupseen) e = cudaMemsetAsync(S.dupseen, 0, 4, L.stream);
-        if (e != cudaSuccess) return e;
+        auto c = k_dedup_clear<KB>;
+        c<<<grid_for((const void *)c, L, S.dedup_cap / 2), 256, 0, L.stream>>>(
+            S, mode == kKeepLast ? 0u : 0xFFFFFFFFu, n / 32 + 1, zero, nzero);
     }
     auto k = k_dedup<KB>;
     k<<<grid_for((const void *)k, L, n), 256, 0, L.stream>>>(S, keys, n, mode);
-    if (S.winbits) {
+    if (winners_pass(S)) {
         auto w = k_dedup_winners<KB>;
         w<<<grid_for((const void *)w, L, S.dedup_cap), 256, 0, L.stream>>>(S);
     }
