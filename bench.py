@@ -450,7 +450,7 @@ def run_small_table(args, dev, torch, dg):
         return median(ins), fnd, median(ers), median(uins)
 
     res = {"workload": "config 1: 2^20 unique u32 keys at load factor 0.85 (hashAPI(2^20/0.85)), "
-                       "insert of 2^19 keys into the half-full table, 2^20 finds (50 % hits), "
+                       "insert of 2^19 keys into the half-full table, 2^20 finds (50 %% hits), "
                        "erase of 2^19 present keys, their re-insert; ~10 MB table; median of "
                        "%d cycles per step" % REPS}
     # no load-factor policy, as the reference's plain hash_insert (api.cpp:185-194)
@@ -1271,6 +1271,31 @@ def main():
                  stream=stream)
         torch.cuda.synchronize()
         assert t.size == N
+        # the same op mix on 2^26 keys drawn with replacement from the table
+        # (about 12 % of the ops share their key with another op): the
+        # general path, batch order per key; restored untimed after
+        ridx = torch.randint(0, N, (Q,), generator=gen, device=dev)
+        rk = keys[ridx].contiguous()
+        rv = (vals[ridx] + 1).contiguous()
+        e0.record(stream)
+        t.apply(mo, rk, rv, out=mout, bits=mbits, no_resize=True, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ops["mixed_repeats_50f_30u_20e_mops"] = round(Q / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
+        ops["roofline"]["mixed_repeats_50f_30u_20e"] = op_roofline(
+            ops["mixed_repeats_50f_30u_20e_mops"], ops["roofline"]["mixed_50f_30u_20e"]["alg_bytes_per_op"])
+        # every key's first op saw its original value (present before the batch)
+        first = torch.full((N,), Q, dtype=torch.int64, device=dev)
+        first.scatter_reduce_(0, ridx, torch.arange(Q, device=dev), reduce="amin")
+        fo = first[first < Q]
+        rbad = int((mout[fo] != vals[ridx[fo]]).sum())
+        ops["checks"]["mixed_repeats"] = {"distinct_keys": int(fo.numel()),
+                                          "first_op_value_mismatches": rbad}
+        assert rbad == 0
+        t.insert(rk, vals[ridx].contiguous(), no_resize=True, stream=stream)
+        torch.cuda.synchronize()
+        assert t.size == N
+        del first, fo, rk, rv, ridx
         # ---- resize: double the subtable the reference would pick, then
         # halve it back (even bucket count: bucket j merges with j + nb/2);
         # algorithmic bytes: upsize reads S and writes 2S, downsize reads 2S

@@ -1234,8 +1234,8 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     const bool deferred = !resize || (double)(t->size + n) <= deferred_fill(t) * (double)t->capacity;
     const uint64_t size0 = t->size;
     bool grew = false;
-    auto upsize_policy = [&]() -> dyc_status {
-        const uint64_t nu = t->h_actr[dyc::kCtrUp], ne = t->h_actr[dyc::kCtrEr];
+    // nu upserts and ne erases of present keys
+    auto upsize_policy = [&](uint64_t nu, uint64_t ne) -> dyc_status {
         int guard = 0;
         while (resize && nu &&
                (double)size0 - (double)ne + (double)nu > t->cfg.upper_load * (double)t->capacity &&
@@ -1245,24 +1245,35 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
         }
         return DYC_OK;
     };
+    // With the policy deferred, the batch picks its path on the device: a
+    // chunk whose keys are all distinct (k_apply_group met no key twice) runs
+    // the one-pass kernel, and the grouping's compaction and scatter return
+    // at once; otherwise the one-pass kernel does. The kernels after them
+    // read counts the skipped ones leave at 0, so one launch sequence serves
+    // both and the host reads nothing in between.
+    dyc::ApplyScratch Ag = A;
+    if (deferred) Ag.gate = &A.ctr[dyc::kCtrRepeat];
     TRY(push_desc(t, s));
     TRY(reset_call_counters(t, s));
     CK(cudaMemsetAsync(A.cells, 0, (size_t)(2 * n) * (t->kb == 4 ? 8 : 16), s));  // 2n cells used
     CK(cudaMemsetAsync(A.ctr, 0, dyc::kCtrSlots * sizeof(unsigned long long), s));
     if (bits_out) CK(cudaMemsetAsync(bits_out, 0, (size_t)((n + 31) / 32) * 4, s));
-    cudaError_t e = KB_CALL(t, apply_group, L, A, keys, n);
+    cudaError_t e = KB_CALL(t, apply_group, L, Ag, keys, n);
     // state of every distinct key before the batch
     if (e == cudaSuccess)
         e = KB_CALL(t, set_find, L, t->d_desc, 1u, t->sb, A.dkey, nullptr,
                     &A.ctr[dyc::kCtrDistinct], n, A.pre_val, vb, A.pre_hit, &A.ctr[dyc::kCtrBad],
                     t->D.l2_keep != 0u);
     if (e == cudaSuccess)
-        e = KB_CALL(t, apply_scatter, L, A, n, nullptr, ops, vals, vb, vals_out, bits_out);
-    if (e == cudaSuccess) e = KB_CALL(t, apply_replay, L, A, ops, vals, vb, vals_out, bits_out, n, n);
+        e = KB_CALL(t, apply_scatter, L, Ag, n, nullptr, ops, vals, vb, vals_out, bits_out);
+    if (e == cudaSuccess) e = KB_CALL(t, apply_replay, L, Ag, ops, vals, vb, vals_out, bits_out, n, n);
+    if (e == cudaSuccess && deferred)
+        e = KB_CALL(t, apply_unique, L, t->D, t->sb, t->S, ops, keys, vals, vb, vals_out, bits_out,
+                    n, t->d_ctr, Ag.gate);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "apply kernels: %s", cudaGetErrorString(e));
     if (!deferred) {
         TRY(read_apply_counters(t, s));
-        TRY(upsize_policy());
+        TRY(upsize_policy(t->h_actr[dyc::kCtrUp], t->h_actr[dyc::kCtrEr]));
         if (grew) TRY(push_desc(t, s));
     }
     e = KB_CALL(t, set_mutate, L, t->d_desc, 1u, t->d_ctr, t->sb, A.er_key, nullptr,
@@ -1281,8 +1292,13 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     if (t->h_actr[dyc::kCtrBad])
         return fail(DYC_ECUDA, "mixed batch: %llu device counts or ids out of range",
                     t->h_actr[dyc::kCtrBad]);
-    if (deferred) TRY(upsize_policy());
     const Counters c = *t->h_ctr;
+    if (deferred) {
+        if (t->h_actr[dyc::kCtrRepeat])
+            TRY(upsize_policy(t->h_actr[dyc::kCtrUp], t->h_actr[dyc::kCtrEr]));
+        else  // the one-pass path: every insert op upserted, erases counted as they hit
+            TRY(upsize_policy(c.inserted + c.updated, c.erased));
+    }
     dyc_op_stats &St = t->last;
     St.inserted += c.inserted;
     St.updated += c.updated;

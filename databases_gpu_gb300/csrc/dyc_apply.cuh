@@ -142,12 +142,15 @@ __global__ void __launch_bounds__(256) k_apply_group(const __grid_constant__ App
     using K = typename SlotT<KB>::K;
     const uint64_t size = 2 * n;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    bool repeat = false;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const K k = load_key<KB>(keys, i);
         uint32_t rank = 0u;
         A.op_cell[i] = k == 0 ? kNoCell : claim_cell<KB>(A.cells, 0, size, k, rank);  // key 0: none
         A.op_rank[i] = rank;
+        repeat |= rank != 0u;
     }
+    if (repeat && A.gate != nullptr) *(volatile unsigned long long *)A.gate = 1ull;
 }
 
 // Largest t < ntables with off[t] <= i (for cell offsets: the table owning
@@ -307,6 +310,7 @@ __global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ A
     __shared__ unsigned long long part[kCompactRun * kWarpsPerBlock];  // ops << 32 | keys
     __shared__ unsigned long long base_keys, base_ops;
     __shared__ int tile_ok;  // the tile's key and op ranges lie inside the scratch
+    if (A.gate != nullptr && *A.gate == 0ull) return;  // no key repeats: one-pass path
     if (A.tcell_off) nc = A.tcell_off[A.ntables];
     if (nc > A.cap_cells) nc = A.cap_cells;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -453,6 +457,7 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
                                                        void *__restrict__ vals_out,
                                                        uint32_t *__restrict__ bits_out) {
     using K = typename SlotT<KB>::K;
+    if (A.gate != nullptr && *A.gate == 0ull) return;  // no key repeats: one-pass path
     if (n_ptr) n = set_op_count(A, n_ptr - A.ntables);  // n_ptr = offsets + ntables
     const int slots[2] = {kCtrUp, kCtrEr};
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -853,10 +858,11 @@ __global__ void __launch_bounds__(256) k_apply_unique(
     const __grid_constant__ Desc D, const __grid_constant__ Scratch S,
     const uint8_t *__restrict__ ops, const void *__restrict__ keys,
     const void *__restrict__ vals, uint32_t vb, void *__restrict__ vals_out,
-    uint32_t *__restrict__ bits_out, uint64_t n, Counters *ctr) {
+    uint32_t *__restrict__ bits_out, uint64_t n, Counters *ctr, const unsigned long long *gate) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
     using Gm = Geo<KB, SB>;
+    if (gate != nullptr && *gate != 0ull) return;  // the batch repeats a key: general path
     __shared__ __align__(128) unsigned char s_stage[SB >= 64 ? kWarpsPerBlock : 1][32 * SB];
     unsigned char *stage = s_stage[SB >= 64 ? (threadIdx.x >> 5) : 0];
     const uint32_t lane = threadIdx.x & 31;

@@ -116,6 +116,12 @@ struct ApplyScratch {
     uint32_t *tcell_off;       // per table: first cell of its region (ntables + 1)
     uint32_t *tidx;            // table of every kTidxStep-th op (cap_ops / kTidxStep + 1)
     uint32_t ntables;
+    // one table's batch that picks its path on the device (null: none).
+    // k_apply_group sets *gate once it meets a key twice; compaction and the
+    // scatter pass then run only when *gate != 0, the one-pass kernel only
+    // when it is 0. Every other kernel of the general path reads counts the
+    // skipped kernels leave at 0.
+    unsigned long long *gate;
 };
 
 constexpr uint32_t kTidxStep = 64;  // ops per entry of ApplyScratch::tidx
@@ -137,6 +143,7 @@ enum : int {
     kCtrBad = 6,         // device-read counts or ids out of range (must stay 0)
     kCtrBadOffsets = 7,  // set batch: offsets[ntables] != kCtrHostN, or an op outside its table
     kCtrHostN = 8,       // set batch: op count from the host's offsets (copied before the kernels)
+    kCtrRepeat = 9,      // one table's batch: nonzero once k_apply_group met a key twice
     kCtrSlots = 16
 };
 constexpr uint32_t kNoId = 0xffffffffu;  // a cell left without a distinct-key id
@@ -257,11 +264,12 @@ template <int KB> struct Ops {
     static cudaError_t apply_group(const LaunchCtx &L, const ApplyScratch &A, const void *keys,
                                   uint64_t n);
     // a mixed batch whose keys are all distinct, in one probe pass (ops left
-    // without a slot go to S.list_a, counted in ctr->pending)
+    // without a slot go to S.list_a, counted in ctr->pending); with a gate,
+    // only when *gate == 0 (ApplyScratch::gate)
     static cudaError_t apply_unique(const LaunchCtx &L, const Desc &D, int sb, const Scratch &S,
                                     const uint8_t *ops, const void *keys, const void *vals,
                                     uint32_t vb, void *vals_out, uint32_t *bits_out, uint64_t n,
-                                    Counters *ctr);
+                                    Counters *ctr, const unsigned long long *gate = nullptr);
     // *count += the INSERT ops among ops[0..n)
     static cudaError_t count_inserts(const LaunchCtx &L, const uint8_t *ops, uint64_t n,
                                      unsigned long long *count);

@@ -188,16 +188,19 @@ def test_resize_stream_u64_matches_oracle_every_batch():
     t.close()
 
 
+@pytest.mark.parametrize("flag", [True, False], ids=["flag", "detected"])
 @pytest.mark.parametrize("key_bytes,bucket_bytes,chunk", [(4, 128, 0), (8, 128, 0), (4, 32, 0),
                                                          (8, 64, 4096)])
-def test_apply_distinct_keys_one_pass_matches_oracle(key_bytes, bucket_bytes, chunk):
-    """dyc_apply with DYC_FLAG_UNIQUE (no key repeats in a batch): every op
-    resolved and applied in one probe pass. Five batches of distinct keys on
-    a growing table: finds, upserts and erases of present keys, inserts of
-    new keys (enough to fill buckets and need eviction walks and upsizes),
-    erases and finds of absent keys, ops on key 0. Every op's value and hit
-    bit and the contents after every batch equal the oracle's; with chunk,
-    batches span many 4096-op chunks."""
+def test_apply_distinct_keys_one_pass_matches_oracle(key_bytes, bucket_bytes, chunk, flag):
+    """Batches without key repeats take the one-pass path: with
+    DYC_FLAG_UNIQUE by the caller's word, without it when the grouping meets
+    no key twice (the path is picked on the device; chunks near the upsize
+    bound take the general path). Five batches of distinct keys on a growing
+    table: finds, upserts and erases of present keys, inserts of new keys
+    (enough to fill buckets and need eviction walks and upsizes), erases and
+    finds of absent keys, an op on key 0. Every op's value and hit bit and
+    the contents after every batch equal the oracle's; with chunk, batches
+    span many 4096-op chunks."""
     from databases_gpu_gb300 import _lib
     dg = _dg()
     L = _lib.lib()
@@ -224,7 +227,7 @@ def test_apply_distinct_keys_one_pass_matches_oracle(key_bytes, bucket_bytes, ch
         n = keys.size
         ops = rng.choice(np.array([0, 1, 2], np.uint8), n, p=[0.3, 0.5, 0.2])
         vals = rng.integers(1, 1 << 30, n).astype(npk)
-        _apply_and_compare(t, m, ops, keys, vals, "unique batch %d" % r, unique=True)
+        _apply_and_compare(t, m, ops, keys, vals, "distinct batch %d" % r, unique=flag)
     assert len(m) > 15000 and t.capacity > (1 << 12)
     t.close()
 
