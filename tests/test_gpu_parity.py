@@ -97,6 +97,44 @@ def test_repeated_keys_first_erase_removes():
     t.close()
 
 
+@pytest.mark.parametrize("key_bytes", [4, 8])
+def test_repeats_in_large_chunks_use_the_winner_bits(key_bytes):
+    """Insert and erase chunks of 2^21 + 5 ops, whose dedup tables (2^22
+    cells) get the winners pass, against chunks of 2^16 ops, which look
+    their winners up in the dedup table: keys repeat within the batch (a
+    pool of 2^20 keys), the last insert of a key wins and the first erase
+    removes it; counts, erase bits and contents equal the oracle's."""
+    import torch
+    rng = np.random.default_rng(91 + key_bytes)
+    npk = np.uint32 if key_bytes == 4 else np.uint64
+    pool = (unique_u32(1 << 20, seed=92) if key_bytes == 4 else
+            unique_u64(1 << 20, seed=92)).astype(npk)
+    n = (1 << 21) + 5
+    t = _dg().DyCuckoo(1 << 21, key_bytes=key_bytes, value_bytes=key_bytes)
+    m = O.Map()
+    keys = pool[rng.integers(0, pool.size, n)]
+    vals = rng.integers(1, 1 << 30, n).astype(npk)
+    st = t.insert(to_dev(keys), to_dev(vals))
+    _, oh = m.insert(keys.astype(np.uint64), vals.astype(np.uint64))
+    assert st["inserted"] == int((~oh).sum()) and st["superseded"] > 0
+    assert_same_contents(t, m, "large insert with repeats")
+    for size in (n, 1 << 16):
+        ek = pool[rng.integers(0, pool.size, size)]
+        ek[::97] = rng.integers(1, 1 << 30, ek[::97].size).astype(npk)  # misses, mostly
+        bits = torch.zeros((size + 31) // 32, dtype=torch.int32, device="cuda")
+        cnt = t.erase(to_dev(ek), erased_bits=bits, no_resize=True)
+        _, eh = m.erase(ek.astype(np.uint64))
+        assert cnt == int(eh.sum())
+        assert np.array_equal(_bits_np(bits, size), eh), "erase of %d: bits differ" % size
+        assert_same_contents(t, m, "erase of %d with repeats" % size)
+        re = pool[rng.integers(0, pool.size, size)]
+        rv = rng.integers(1, 1 << 30, size).astype(npk)
+        t.insert(to_dev(re), to_dev(rv))
+        m.insert(re.astype(np.uint64), rv.astype(np.uint64))
+        assert_same_contents(t, m, "re-insert of %d with repeats" % size)
+    t.close()
+
+
 def test_key_zero_is_never_stored():
     keys = np.array([0, 5, 0, 9, 11], np.uint32)
     vals = np.array([1, 2, 3, 4, 5], np.uint32)
@@ -391,12 +429,13 @@ def test_host_forms_match_device_forms():
     t.close()
 
 
-def test_host_find_pipeline_chunk_schedule():
-    """A host find spanning several pipeline chunks on all three streams and a
-    ragged last chunk: values and hit bits equal a device find of the same
-    keys."""
+@pytest.mark.parametrize("chunks", [3, 5])
+def test_host_find_pipeline_chunk_schedule(chunks):
+    """A host find spanning several pipeline chunks on all three streams
+    (each stream reused when there are five) and a ragged last chunk: values
+    and hit bits equal a device find of the same keys."""
     import torch
-    n = 3 * (1 << 22) + 4133
+    n = chunks * (1 << 22) + 4133
     keys = unique_u32(n, seed=29)
     t = _dg().DyCuckoo(n)
     half = n // 2
