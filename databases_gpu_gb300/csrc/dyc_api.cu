@@ -11,6 +11,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "dycuckoo.h"
@@ -1550,8 +1551,14 @@ struct dyc_set {
     dyc::ResizeJob *d_jobs = nullptr;
     dyc::SetPolicyOut *d_pout = nullptr, *h_pout = nullptr;
     uint8_t *d_grew = nullptr, *h_grew = nullptr;
-    std::vector<void *> free_later;
+    std::vector<std::pair<void *, uint64_t>> free_later;  // (block, bytes)
     uint64_t free_later_bytes = 0;
+    // replaced subtables kept for reuse as later spares, by size, up to
+    // spare_cache_cap bytes: a stream-ordered allocation or free costs the
+    // host ~1.7 us when it next synchronises, and a round upsizes hundreds
+    // of members
+    std::multimap<uint64_t, void *> spare_cache;
+    uint64_t spare_cache_bytes = 0, spare_cache_cap = 0;
 };
 
 namespace {
@@ -1696,13 +1703,32 @@ dyc_status set_phase_b(dyc_set *s, uint64_t n, cudaStream_t st, const uint32_t *
 }
 
 // ---- device half of the upsize policy ----------------------------------------
-// Replaced subtables and spares that no longer fit, freed (stream-ordered)
-// once the launches that could read them have been issued before.
+// Replaced subtables and spares that no longer fit, from the previous call
+// (no kernel of this call reads them): kept in the spare cache while it has
+// room, else freed (stream-ordered).
 dyc_status set_release_later(dyc_set *s, cudaStream_t st) {
-    for (void *p : s->free_later) CK(cudaFreeAsync(p, st));
+    for (const auto &b : s->free_later) {
+        if (s->spare_cache_bytes + b.second <= s->spare_cache_cap) {
+            s->spare_cache.emplace(b.second, b.first);
+            s->spare_cache_bytes += b.second;
+        } else {
+            CK(cudaFreeAsync(b.first, st));
+        }
+    }
     s->free_later.clear();
     s->free_later_bytes = 0;
     return DYC_OK;
+}
+
+// A block of at least `bytes` (and at most a quarter more) from the spare
+// cache, or null.
+void *set_cached_block(dyc_set *s, uint64_t bytes) {
+    auto it = s->spare_cache.lower_bound(bytes);
+    if (it == s->spare_cache.end() || it->first - bytes > bytes / 4) return nullptr;
+    void *p = it->second;
+    s->spare_cache_bytes -= it->first;
+    s->spare_cache.erase(it);
+    return p;
 }
 
 // Give every member a spare that fits its next upsize (subtable pick_up with
@@ -1716,13 +1742,14 @@ void set_fill_spares(dyc_set *s, cudaStream_t st) {
         dyc::Spare &sp = s->h_spare[t];
         if (sp.new_sub && sp.ti == ti && sp.old_nb == onb) continue;
         if (sp.new_sub) {
-            s->free_later.push_back(sp.new_sub);
+            s->free_later.emplace_back(sp.new_sub, 2ull * sp.old_nb * m->sb);
             s->free_later_bytes += 2ull * sp.old_nb * m->sb;
         }
         sp = dyc::Spare{nullptr, 0u, 0u};
         if (onb == 0 || (uint64_t)onb * 2 > 0xFFFFFFFFull) continue;
-        void *p = nullptr;
-        if (pool_alloc(s->device, &p, 2ull * onb * m->sb, st) != cudaSuccess) {
+        const uint64_t need = 2ull * onb * m->sb;
+        void *p = set_cached_block(s, need);
+        if (!p && pool_alloc(s->device, &p, need, st) != cudaSuccess) {
             (void)cudaGetLastError();
             continue;
         }
@@ -1759,7 +1786,7 @@ void set_take_device_upsizes(dyc_set *s, std::vector<uint8_t> &grew) {
         dyc_table *m = s->tables[t];
         dyc::Spare &sp = s->h_spare[t];
         const uint32_t ti = sp.ti, nnb = 2u * sp.old_nb;
-        s->free_later.push_back(m->D.sub[ti]);
+        s->free_later.emplace_back(m->D.sub[ti], (uint64_t)sp.old_nb * m->sb);
         s->free_later_bytes += (uint64_t)sp.old_nb * m->sb;
         m->D.sub[ti] = sp.new_sub;
         m->D.nb[ti] = nnb;
@@ -1957,6 +1984,12 @@ dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_
         dyc_status r = create_impl(&c, s->d_tctr + t, s->h_tctr + t, false, &s->tables[t]);
         if (r != DYC_OK) return undo(r);
     }
+    if (s->spares) {  // the spare cache keeps up to a quarter of the members' bytes
+        uint64_t bytes = 0;
+        for (const dyc_table *m : s->tables)
+            for (uint32_t k = 0; k < m->D.d; ++k) bytes += (uint64_t)m->D.nb[k] * m->sb;
+        s->spare_cache_cap = std::max<uint64_t>(bytes / 4, 64ull << 20);
+    }
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "set setup: %s", cudaGetErrorString(e)));
     s->max_evict_all = cfg->max_evictions;
@@ -1980,7 +2013,8 @@ dyc_status dyc_set_destroy(dyc_set *s) {
     if (s->h_spare)
         for (uint32_t t = 0; t < s->ntables; ++t)
             if (s->h_spare[t].new_sub) cudaFree(s->h_spare[t].new_sub);
-    for (void *p : s->free_later) cudaFree(p);
+    for (const auto &b : s->free_later) cudaFree(b.first);
+    for (const auto &b : s->spare_cache) cudaFree(b.second);
     if (s->d_spare) cudaFree(s->d_spare);
     if (s->h_spare) cudaFreeHost(s->h_spare);
     if (s->d_jobs) cudaFree(s->d_jobs);
@@ -2043,7 +2077,7 @@ dyc_status dyc_set_sizes(dyc_set *s, uint64_t *h_sizes, uint64_t *h_capacities) 
 
 dyc_status dyc_set_spare_bytes(dyc_set *s, uint64_t *bytes) {
     if (!s || !bytes) return fail(DYC_EINVAL, "null argument");
-    uint64_t b = s->free_later_bytes;
+    uint64_t b = s->free_later_bytes + s->spare_cache_bytes;
     if (s->h_spare)
         for (uint32_t t = 0; t < s->ntables; ++t)
             b += 2ull * s->h_spare[t].old_nb * (s->h_spare[t].new_sub ? (uint64_t)s->sb : 0ull);

@@ -373,7 +373,9 @@ dyc_status dyc_set_sizes(dyc_set *s, uint64_t *h_sizes, uint64_t *h_capacities);
 
 /* Device bytes the set holds beside its members' subtables: the upsize
  * targets of dyc_config.device_upsize (0 when it is 1 or auto_resize is off)
- * and the subtables they replaced, freed at the next dyc_set_apply. */
+ * and the subtables they replaced. At the next dyc_set_apply a replaced
+ * subtable is either freed or kept to serve as a later upsize target. The
+ * kept ones are at most a quarter of the members' bytes (64 MiB at least). */
 dyc_status dyc_set_spare_bytes(dyc_set *s, uint64_t *bytes);
 
 /* Mixed batch over the set (see above). Returns when the batch is in the
