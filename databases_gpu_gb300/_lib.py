@@ -72,6 +72,7 @@ EXPORTS = [
     "dyc_pool_reserve",
     "dyc_set_create", "dyc_set_destroy", "dyc_set_table", "dyc_set_sizes", "dyc_set_apply",
     "dyc_set_apply_each", "dyc_set_last_stats", "dyc_set_configure", "dyc_set_spare_bytes",
+    "dyc_set_spare_cache",
     "dyc_server_config_default", "dyc_server_create", "dyc_server_destroy", "dyc_server_submit",
     "dyc_server_wait", "dyc_server_stats_get", "dyc_server_set",
     "dyc_snapshot_bytes", "dyc_snapshot", "dyc_restore",
@@ -115,6 +116,7 @@ def _declare(L):
         "dyc_set_table": (st, [T, u32, C.POINTER(C.c_void_p)]),
         "dyc_set_sizes": (st, [T, vp, vp]),
         "dyc_set_spare_bytes": (st, [T, C.POINTER(C.c_uint64)]),
+        "dyc_set_spare_cache": (st, [T, u64]),
         "dyc_set_apply": (st, [T, vp, vp, vp, vp, vp, vp, vp, u32, vp]),
         "dyc_set_apply_each": (st, [T, vp, vp, vp, vp, vp, vp, vp, u32, vp]),
         "dyc_set_last_stats": (st, [T, C.POINTER(DycOpStats)]),

@@ -1988,7 +1988,7 @@ dyc_status dyc_set_create(const dyc_config *cfg, uint32_t ntables, const uint64_
         uint64_t bytes = 0;
         for (const dyc_table *m : s->tables)
             for (uint32_t k = 0; k < m->D.d; ++k) bytes += (uint64_t)m->D.nb[k] * m->sb;
-        s->spare_cache_cap = std::max<uint64_t>(bytes / 4, 64ull << 20);
+        s->spare_cache_cap = bytes / 4;
     }
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return undo(fail(DYC_ECUDA, "set setup: %s", cudaGetErrorString(e)));
@@ -2082,6 +2082,23 @@ dyc_status dyc_set_spare_bytes(dyc_set *s, uint64_t *bytes) {
         for (uint32_t t = 0; t < s->ntables; ++t)
             b += 2ull * s->h_spare[t].old_nb * (s->h_spare[t].new_sub ? (uint64_t)s->sb : 0ull);
     *bytes = b;
+    return DYC_OK;
+}
+
+dyc_status dyc_set_spare_cache(dyc_set *s, uint64_t max_bytes) {
+    if (!s) return fail(DYC_EINVAL, "null set");
+    {
+        int cur = -1;
+        CK(cudaGetDevice(&cur));
+        if (cur != s->device) CK(cudaSetDevice(s->device));
+    }
+    s->spare_cache_cap = max_bytes;
+    while (s->spare_cache_bytes > max_bytes && !s->spare_cache.empty()) {
+        auto it = std::prev(s->spare_cache.end());  // largest first
+        CK(cudaFreeAsync(it->second, 0));
+        s->spare_cache_bytes -= it->first;
+        s->spare_cache.erase(it);
+    }
     return DYC_OK;
 }
 

@@ -498,6 +498,17 @@ dyc_status dyc_server_create(const dyc_config *table_cfg, uint32_t ntenants,
     // step size) count against the cap from the start
     s->fixed_bytes = kSlots * bytes + m * 160;
     s->table_bytes = table_device_bytes(s);
+    // replaced subtables the set keeps for reuse count against the cap: at
+    // most an eighth of the headroom goes to them
+    if (s->scfg.hbm_cap_bytes) {
+        const uint64_t used = s->fixed_bytes + s->table_bytes;
+        const uint64_t head = s->scfg.hbm_cap_bytes > used ? s->scfg.hbm_cap_bytes - used : 0;
+        r = dyc_set_spare_cache(s->set, std::min<uint64_t>(head / 8, s->table_bytes / 4));
+        if (r != DYC_OK) {
+            free_server(s);
+            return r;
+        }
+    }
     // growth headroom mapped into the allocation pool now rather than by the
     // first resizes inside steps
     uint64_t reserve = s->scfg.pool_reserve_bytes;

@@ -431,6 +431,11 @@ class DyCuckooSet:
         check(self.L.dyc_set_spare_bytes(self._h, C.byref(b)), "dyc_set_spare_bytes")
         return int(b.value)
 
+    def spare_cache(self, max_bytes: int) -> None:
+        """Bound the replaced subtables kept for reuse as upsize targets
+        (dyc_set_spare_cache; 0 keeps none)."""
+        check(self.L.dyc_set_spare_cache(self._h, int(max_bytes)), "dyc_set_spare_cache")
+
     def apply(self, offsets, ops, keys, values, out=None, bits=None, h_offsets=None,
               each: bool = False, graph: bool = False, no_resize: bool = False, stream=None):
         """Mixed batch: ops of table t are [offsets[t], offsets[t+1]) of the

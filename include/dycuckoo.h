@@ -374,9 +374,17 @@ dyc_status dyc_set_sizes(dyc_set *s, uint64_t *h_sizes, uint64_t *h_capacities);
 /* Device bytes the set holds beside its members' subtables: the upsize
  * targets of dyc_config.device_upsize (0 when it is 1 or auto_resize is off)
  * and the subtables they replaced. At the next dyc_set_apply a replaced
- * subtable is either freed or kept to serve as a later upsize target. The
- * kept ones are at most a quarter of the members' bytes (64 MiB at least). */
+ * subtable is either freed or kept to serve as a later upsize target
+ * (dyc_set_spare_cache). */
 dyc_status dyc_set_spare_bytes(dyc_set *s, uint64_t *bytes);
+
+/* Bound on the replaced subtables a set keeps for reuse as upsize targets
+ * (default: a quarter of the members' bytes at creation; 0 keeps none).
+ * A kept block serves a later target of at most a quarter fewer bytes, so
+ * a round's upsizes make no allocation or free on a hit. Blocks above a
+ * lowered bound are freed at once (stream-ordered on the legacy stream).
+ * The request server lowers it to an eighth of its HBM headroom. */
+dyc_status dyc_set_spare_cache(dyc_set *s, uint64_t max_bytes);
 
 /* Mixed batch over the set (see above). Returns when the batch is in the
  * tables. flags: DYC_FLAG_NO_RESIZE, DYC_FLAG_GRAPH. d_offsets must hold

@@ -342,8 +342,9 @@ def test_set_upsize_waves_match_per_table_path(bucket_bytes, key_bytes, device_u
     B.close()
 
 
+@pytest.mark.parametrize("keep", [True, False], ids=["spare_cache", "no_cache"])
 @pytest.mark.parametrize("key_bytes", [4, 8])
-def test_set_device_upsize_policy_matches_host_policy(key_bytes):
+def test_set_device_upsize_policy_matches_host_policy(key_bytes, keep):
     """Tables of 2^5..2^9 keys preloaded near the 0.8 bound take six rounds
     of mixed batches (from fixed buffers: the later rounds replay captured
     graphs) that
@@ -352,13 +353,17 @@ def test_set_device_upsize_policy_matches_host_policy(key_bytes):
     applies the policy on the host between the phases give the same results,
     sizes, capacities and contents, equal to the oracle's. Rounds in which
     every growing table needs one upsize run with no host read between the
-    phases; the spare targets are counted by dyc_set_spare_bytes."""
+    phases; the spare targets are counted by dyc_set_spare_bytes. With the
+    spare cache (the default) replaced subtables serve as later spares;
+    without it (dyc_set_spare_cache 0) every spare is a fresh allocation."""
     import torch
     rng = np.random.default_rng(41)
     nt = 300
     sizes = np.round(2.0 ** (5 + 4 * rng.random(nt))).astype(np.int64)
     kw = dict(key_bytes=key_bytes, value_bytes=key_bytes)
     A = _dg().DyCuckooSet(sizes, device_upsize=0, **kw)
+    if not keep:
+        A.spare_cache(0)
     B = _dg().DyCuckooSet(sizes, device_upsize=1, **kw)
     maps = [O.Map() for _ in range(nt)]
     npk, tdt = (np.uint32, np.int32) if key_bytes == 4 else (np.uint64, np.int64)
