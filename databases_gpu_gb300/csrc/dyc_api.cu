@@ -460,8 +460,6 @@ dyc_status drain(dyc_table *t, cudaStream_t s, void *src, unsigned long long *sr
                             kMaxOverflowRounds));
 }
 
-// Batch dedup of one chunk into the dedup buffers of S, on stream s:
-// kKeepLast (insert) names each key's last op, kKeepFirst (erase) its first.
 // The table's scratch as one chunk of n ops uses it: the dedup table sized
 // for n (as ensure_scratch sizes it for the largest chunk), so a small call
 // on a table that once took a large batch clears and probes a small table.
@@ -472,8 +470,10 @@ Scratch chunk_scratch(const dyc_table *t, uint64_t n) {
     return S;
 }
 
-// The batch dedup of a chunk: one launch clears its cells and the call
-// counters (what reset_call_counters does), then the claims.
+// Batch dedup of one chunk into the dedup buffers of S, on stream s:
+// kKeepLast (insert) names each key's last op, kKeepFirst (erase) its first.
+// One launch clears the chunk's cells and the call counters (what
+// reset_call_counters does), then the claims run.
 dyc_status dedup_chunk(dyc_table *t, const Scratch &S, const void *keys, uint64_t n,
                        dyc::DedupMode mode, cudaStream_t s) {
     cudaError_t e = KB_CALL(t, dedup, ctx(t, s), S, keys, n, mode, &t->d_ctr->inserted,
