@@ -218,8 +218,20 @@ cudaError_t pool_alloc(int device, void **p, size_t bytes, cudaStream_t s) {
 #define KB_CALL(t, fn, ...) ((t)->kb == 4 ? Ops<4>::fn(__VA_ARGS__) : Ops<8>::fn(__VA_ARGS__))
 
 // Make the scratch lists hold `n` ops (grow only).
+// Dedup cells for a chunk of n ops: a power of two, at most half full, and
+// at most a quarter full while that stays within 2^22 cells (32 MB of 8-byte
+// cells, which stay in the L2 beside the bucket lines). Fewer probes per
+// claim pay there: 2^19-key calls on an L2-resident table went from 5.1 to
+// 5.9 G ops/s (insert) and 8.2 to 8.8 (erase). A larger table at a quarter
+// load spills the L2: 4M-op chunks on a 2^28-key table lost 10 %.
+uint64_t dedup_cells(uint64_t n) {
+    const uint64_t m = n < 16 ? 16 : n;
+    const uint64_t quarter = next_pow2(4 * m);
+    return quarter <= (1ull << 22) ? quarter : next_pow2(2 * m);
+}
+
 dyc_status ensure_scratch(dyc_table *t, uint64_t n) {
-    const uint64_t cap = next_pow2(2 * (n < 16 ? 16 : n));
+    const uint64_t cap = dedup_cells(n);
     const size_t dedup_bytes = (size_t)cap * 8;
     const size_t idx_bytes = t->kb == 8 ? (size_t)cap * 4 : 0;
     const size_t list_bytes = (size_t)n * t->slot_bytes;
@@ -465,7 +477,7 @@ dyc_status drain(dyc_table *t, cudaStream_t s, void *src, unsigned long long *sr
 // on a table that once took a large batch clears and probes a small table.
 Scratch chunk_scratch(const dyc_table *t, uint64_t n) {
     Scratch S = t->S;
-    const uint64_t cap = next_pow2(2 * (n < 16 ? 16 : n));
+    const uint64_t cap = dedup_cells(n);
     if (cap < S.dedup_cap) S.dedup_cap = cap;
     return S;
 }
