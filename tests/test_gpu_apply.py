@@ -231,3 +231,33 @@ def test_apply_distinct_keys_one_pass_matches_oracle(key_bytes, bucket_bytes, ch
     assert len(m) > 15000 and t.capacity > (1 << 12)
     t.close()
 
+
+
+@pytest.mark.parametrize("repeats", [False, True], ids=["distinct", "repeats"])
+def test_apply_without_outputs(repeats):
+    """dyc_apply with no value or bit output (both optional): a batch of
+    distinct keys (the one-pass path) and one with repeats (the general
+    path) leave the same contents as the oracle."""
+    import ctypes as C
+    import torch
+    from databases_gpu_gb300 import _lib
+    rng = np.random.default_rng(121)
+    pool = unique_u32(1 << 16, seed=122)
+    t = _dg().DyCuckoo(1 << 15)
+    m = O.Map()
+    t.insert(to_dev(pool[: 1 << 14]), to_dev(pool[: 1 << 14]))
+    m.insert(pool[: 1 << 14], pool[: 1 << 14])
+    n = 1 << 15
+    keys = pool[rng.integers(0, pool.size, n)] if repeats else rng.permutation(pool)[:n]
+    ops = rng.choice(np.array([0, 1, 2], np.uint8), n, p=[0.3, 0.5, 0.2])
+    vals = rng.integers(1, 1 << 30, n).astype(np.uint32)
+    dops, dkeys, dvals = to_dev(ops), to_dev(keys), to_dev(vals)
+    L = _lib.lib()
+    st = L.dyc_apply(t.handle, C.c_void_p(dops.data_ptr()), C.c_void_p(dkeys.data_ptr()),
+                     C.c_void_p(dvals.data_ptr()), n, None, None, 0,
+                     C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0
+    torch.cuda.synchronize()
+    m.apply(ops, keys.astype(np.uint64), vals.astype(np.uint64))
+    assert_same_contents(t, m, "apply without outputs")
+    t.close()
