@@ -1258,14 +1258,19 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
         }
         return DYC_OK;
     };
-    // With the policy deferred, the batch picks its path on the device: a
-    // chunk whose keys are all distinct (k_apply_group met no key twice) runs
-    // the one-pass kernel, and the grouping's compaction and scatter return
-    // at once; otherwise the one-pass kernel does. The kernels after them
-    // read counts the skipped ones leave at 0, so one launch sequence serves
-    // both and the host reads nothing in between.
+    // With the policy deferred, keys with a single op in the chunk (most keys
+    // of a random batch) skip the per-key passes: compaction lists only keys
+    // with several ops, the find, scatter, replays and mutation handle those,
+    // and after the replays the one-pass kernel resolves every other op in
+    // one probe of its key's buckets (it touches no key the others do). A
+    // chunk in which no key repeats (k_apply_group sets the gate) skips
+    // compaction and the scatter altogether. The host reads nothing in
+    // between; later kernels read counts the skipped ones leave at 0.
     dyc::ApplyScratch Ag = A;
-    if (deferred) Ag.gate = &A.ctr[dyc::kCtrRepeat];
+    if (deferred) {
+        Ag.gate = &A.ctr[dyc::kCtrRepeat];
+        Ag.single_pass = 1u;
+    }
     TRY(push_desc(t, s));
     TRY(reset_call_counters(t, s));
     CK(cudaMemsetAsync(A.cells, 0, (size_t)(2 * n) * (t->kb == 4 ? 8 : 16), s));  // 2n cells used
@@ -1282,7 +1287,7 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     if (e == cudaSuccess) e = KB_CALL(t, apply_replay, L, Ag, ops, vals, vb, vals_out, bits_out, n, n);
     if (e == cudaSuccess && deferred)
         e = KB_CALL(t, apply_unique, L, t->D, t->sb, t->S, ops, keys, vals, vb, vals_out, bits_out,
-                    n, t->d_ctr, Ag.gate);
+                    n, t->d_ctr, A.op_cell, A.cells);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "apply kernels: %s", cudaGetErrorString(e));
     if (!deferred) {
         TRY(read_apply_counters(t, s));
@@ -1306,12 +1311,10 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
         return fail(DYC_ECUDA, "mixed batch: %llu device counts or ids out of range",
                     t->h_actr[dyc::kCtrBad]);
     const Counters c = *t->h_ctr;
-    if (deferred) {
-        if (t->h_actr[dyc::kCtrRepeat])
-            TRY(upsize_policy(t->h_actr[dyc::kCtrUp], t->h_actr[dyc::kCtrEr]));
-        else  // the one-pass path: every insert op upserted, erases counted as they hit
-            TRY(upsize_policy(c.inserted + c.updated, c.erased));
-    }
+    // both paths' upserts and erases of present keys, as the table counted
+    // them (the one-pass kernel counts an insert on a present key as an
+    // update even when the value is the same)
+    if (deferred) TRY(upsize_policy(c.inserted + c.updated, c.erased));
     dyc_op_stats &St = t->last;
     St.inserted += c.inserted;
     St.updated += c.updated;

@@ -340,6 +340,7 @@ __global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ A
         for (int k = 0; k < kCompactRun; ++k) {
             const uint64_t c = c0 + (uint64_t)k * blockDim.x + threadIdx.x;
             cnt[k] = c < nc ? *cell_word<KB>(A.cells, c) : 0u;
+            if (A.single_pass && cnt[k] == 1u) cnt[k] = 0u;  // left to the one-pass kernel
             const unsigned used = __ballot_sync(kFull, cnt[k] != 0u);
             ex_keys[k] = __popc(used & ((1u << lane) - 1u));
             uint32_t incl = cnt[k];
@@ -379,7 +380,7 @@ __global__ void __launch_bounds__(256) k_apply_compact(const __grid_constant__ A
                 const uint32_t d = (uint32_t)base_keys + (uint32_t)pk + ex_keys[k];
                 const uint32_t off = (uint32_t)base_ops + (uint32_t)(pk >> 32) + ex_ops[k];
                 const uint64_t c = c0 + (uint64_t)k * blockDim.x + threadIdx.x;
-                *cell_word<KB>(A.cells, c) = d;  // the count becomes the distinct id
+                *cell_word<KB>(A.cells, c) = kIdBit | d;  // the count becomes the distinct id
                 ((typename SlotT<KB>::K *)A.dkey)[d] = cell_key<KB>(A.cells, c);
                 A.dcnt[d] = cnt[k];
                 A.dseg[d] = (unsigned long long)off << 32;
@@ -487,9 +488,12 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
         uint32_t tid = 0u;
         if (i < n) {
             const uint32_t cell = A.op_cell[i];
-            const uint32_t d = (cell == kNoCell || cell >= A.cap_cells)
-                                   ? kNoId : *cell_word<KB>(A.cells, cell);
-            if (d >= A.cap_ops) {  // key 0 (no cell), or a cell compaction could not list
+            uint32_t d = (cell == kNoCell || cell >= A.cap_cells)
+                             ? kNoId : *cell_word<KB>(A.cells, cell);
+            if (d != kNoId) d = (d & kIdBit) ? (d & ~kIdBit) : kNoId - 1u;  // no bit: one op
+            if (A.single_pass && (cell == kNoCell || d == kNoId - 1u)) {
+                // key 0 or a key with one op: resolved by the one-pass kernel
+            } else if (d >= A.cap_ops) {  // key 0 (no cell), or a cell compaction could not list
                 if (cell != kNoCell) note_bad(A);
                 if (vals_out) store_val(vals_out, vb, i, 0ull);
             } else {
@@ -876,11 +880,11 @@ __global__ void __launch_bounds__(256) k_apply_unique(
     const __grid_constant__ Desc D, const __grid_constant__ Scratch S,
     const uint8_t *__restrict__ ops, const void *__restrict__ keys,
     const void *__restrict__ vals, uint32_t vb, void *__restrict__ vals_out,
-    uint32_t *__restrict__ bits_out, uint64_t n, Counters *ctr, const unsigned long long *gate) {
+    uint32_t *__restrict__ bits_out, uint64_t n, Counters *ctr, const uint32_t *op_cell,
+    const void *cells) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
     using Gm = Geo<KB, SB>;
-    if (gate != nullptr && *gate != 0ull) return;  // the batch repeats a key: general path
     __shared__ __align__(128) unsigned char s_stage[SB >= 64 ? kWarpsPerBlock : 1][32 * SB];
     unsigned char *stage = s_stage[SB >= 64 ? (threadIdx.x >> 5) : 0];
     const uint32_t lane = threadIdx.x & 31;
@@ -892,7 +896,12 @@ __global__ void __launch_bounds__(256) k_apply_unique(
         typename T::K k = 0;
         uint8_t op = kOpFind;
         Sl e = T::empty();
-        if (i < n) {
+        bool mine = i < n;  // this kernel resolves op i
+        if (mine && cells != nullptr) {  // after a grouping: keys with one op, and key 0
+            const uint32_t c = op_cell[i];
+            mine = c == kNoCell || (*cell_word<KB>(const_cast<void *>(cells), c) & kIdBit) == 0u;
+        }
+        if (mine) {
             k = load_key<KB>(keys, i);
             op = ops[i];
         }
@@ -938,9 +947,12 @@ __global__ void __launch_bounds__(256) k_apply_unique(
                      T::empty());
             ++n_del;
         }
-        if (vals_out != nullptr && i < n) store_val(vals_out, vb, i, before);
+        if (vals_out != nullptr && mine) store_val(vals_out, vb, i, before);
         const unsigned m = __ballot_sync(kFull, present);
-        if (bits_out != nullptr && lane == 0) bits_out[base >> 5] = m;
+        if (bits_out != nullptr && lane == 0) {
+            if (cells == nullptr) bits_out[base >> 5] = m;
+            else if (m) atomicOr(&bits_out[base >> 5], m);  // the replays own the other bits
+        }
         __syncwarp();
         const unsigned long long at = agg_inc(&ctr->pending, pend);
         if (pend) {

@@ -116,13 +116,20 @@ struct ApplyScratch {
     uint32_t *tcell_off;       // per table: first cell of its region (ntables + 1)
     uint32_t *tidx;            // table of every kTidxStep-th op (cap_ops / kTidxStep + 1)
     uint32_t ntables;
-    // one table's batch that picks its path on the device (null: none).
-    // k_apply_group sets *gate once it meets a key twice; compaction and the
-    // scatter pass then run only when *gate != 0, the one-pass kernel only
-    // when it is 0. Every other kernel of the general path reads counts the
-    // skipped kernels leave at 0.
+    // one table's batch (null: none): k_apply_group sets *gate once it meets
+    // a key twice; compaction and the scatter pass run only when it did.
     unsigned long long *gate;
+    // nonzero: keys with a single op in the batch, and key-0 ops, are left
+    // to the one-pass kernel (k_apply_unique with op_cell / cells), which
+    // runs after the replays. Compaction lists only keys with several ops,
+    // so the find of the distinct keys, the scatter, the replays and the
+    // mutation see those alone.
+    uint32_t single_pass;
 };
+
+// Cell words after compaction: kIdBit | distinct id. A word without the bit
+// in a single_pass batch is a count of 1 (a key compaction left alone).
+constexpr uint32_t kIdBit = 0x80000000u;
 
 constexpr uint32_t kTidxStep = 64;  // ops per entry of ApplyScratch::tidx
 
@@ -264,12 +271,14 @@ template <int KB> struct Ops {
     static cudaError_t apply_group(const LaunchCtx &L, const ApplyScratch &A, const void *keys,
                                   uint64_t n);
     // a mixed batch whose keys are all distinct, in one probe pass (ops left
-    // without a slot go to S.list_a, counted in ctr->pending); with a gate,
-    // only when *gate == 0 (ApplyScratch::gate)
+    // without a slot go to S.list_a, counted in ctr->pending). With cells
+    // (a single_pass batch after its grouping), only the ops whose key has
+    // no other op in the batch, and key-0 ops; their hit bits are ORed in.
     static cudaError_t apply_unique(const LaunchCtx &L, const Desc &D, int sb, const Scratch &S,
                                     const uint8_t *ops, const void *keys, const void *vals,
                                     uint32_t vb, void *vals_out, uint32_t *bits_out, uint64_t n,
-                                    Counters *ctr, const unsigned long long *gate = nullptr);
+                                    Counters *ctr, const uint32_t *op_cell = nullptr,
+                                    const void *cells = nullptr);
     // *count += the INSERT ops among ops[0..n)
     static cudaError_t count_inserts(const LaunchCtx &L, const uint8_t *ops, uint64_t n,
                                      unsigned long long *count);
