@@ -248,9 +248,9 @@ dyc_status dyc_erase_host(dyc_table *t, const void *h_keys, uint64_t n,
  * applied in one probe pass of its key's buckets. There is no grouping of
  * the batch by key. The results are the same. The upsize policy then
  * counts every INSERT op as a possible new key, as dyc_insert does.
- * Without the flag the batch is grouped by key, and a chunk in which no key
- * repeats takes the same one-pass kernel after the grouping (picked on the
- * device, no host round trip). */
+ * Without the flag the batch is grouped by key on the device: keys with
+ * one op in the chunk take the same one-pass kernel, and only repeated keys
+ * go through the per-key replay (no host round trip in between). */
 dyc_status dyc_apply(dyc_table *t, const uint8_t *d_ops, const void *d_keys, const void *d_vals,
                      uint64_t n, void *d_vals_out, uint32_t *d_bits_out, uint32_t flags,
                      void *stream);
