@@ -1574,6 +1574,15 @@ struct dyc_set {
     // of members
     std::multimap<uint64_t, void *> spare_cache;
     uint64_t spare_cache_bytes = 0, spare_cache_cap = 0;
+    // the batch of the current dyc_set_apply (phase B resolves its keys with
+    // one op there; a captured graph is keyed by these pointers)
+    struct Batch {
+        const uint32_t *off = nullptr;
+        const uint8_t *ops = nullptr;
+        const void *keys = nullptr, *vals = nullptr;
+        void *out = nullptr;
+        uint32_t *bits = nullptr;
+    } cur;
 };
 
 namespace {
@@ -1638,6 +1647,7 @@ dyc_status set_ensure_scratch(dyc_set *s, uint64_t n) {
     if (s->abuf && s->A.cap_ops >= ops) return DYC_OK;
     set_drop_graphs(s);
     TRY(carve_apply(s->kb, s->vb, ops, 2 * ops, s->ntables, &s->abuf, &s->abytes, &s->A));
+    s->A.single_pass = 1u;  // keys with one op in a batch: k_set_unique in phase B
     const size_t slot = s->kb == 4 ? 8 : 16;
     const size_t lb = ((ops * slot + 255) & ~(size_t)255) * 2 + ((ops * 4 + 255) & ~(size_t)255) * 2;
     if (s->lbuf) {
@@ -1698,11 +1708,17 @@ dyc_status set_phase_a(dyc_set *s, const uint32_t *d_off, const uint8_t *ops, co
 dyc_status set_phase_b(dyc_set *s, uint64_t n, cudaStream_t st, const uint32_t *hold = nullptr) {
     const dyc::ApplyScratch &A = s->A;
     const LaunchCtx L{s->sms, st, (int)s->blocks_per_sm};
-    cudaError_t e = SET_KB_CALL(s, set_mutate, L, s->d_desc, s->ntables, s->d_tctr, s->sb,
-                                A.er_key, A.er_tid, &A.ctr[dyc::kCtrEr], A.up_key, A.up_val,
-                                (uint32_t)s->vb, A.up_tid, &A.ctr[dyc::kCtrUp], n, s->list_a,
-                                s->tid_a, s->list_cap, s->d_gctr, &A.ctr[dyc::kCtrBad], hold,
-                                s->tables[0]->D.l2_keep != 0u);
+    cudaError_t e = cudaSuccess;
+    if (A.single_pass)  // keys with one op in the batch, after the policy's upsizes
+        e = SET_KB_CALL(s, set_unique, L, A, s->cur.off, s->d_desc, s->ntables, s->d_tctr, s->sb,
+                        s->cur.ops, s->cur.keys, s->cur.vals, (uint32_t)s->vb, s->cur.out,
+                        s->cur.bits, n, s->list_a, s->tid_a, s->list_cap, s->d_gctr, hold,
+                        s->tables[0]->D.l2_keep != 0u);
+    if (e == cudaSuccess)
+        e = SET_KB_CALL(s, set_mutate, L, s->d_desc, s->ntables, s->d_tctr, s->sb, A.er_key,
+                        A.er_tid, &A.ctr[dyc::kCtrEr], A.up_key, A.up_val, (uint32_t)s->vb,
+                        A.up_tid, &A.ctr[dyc::kCtrUp], n, s->list_a, s->tid_a, s->list_cap,
+                        s->d_gctr, &A.ctr[dyc::kCtrBad], hold, s->tables[0]->D.l2_keep != 0u);
     if (e == cudaSuccess)
         e = SET_KB_CALL(s, set_walk, L, s->d_desc, s->ntables, s->d_tctr, s->sb, s->list_a,
                         s->tid_a, &s->d_gctr->pending, s->list_b, s->tid_b,
@@ -2147,6 +2163,7 @@ dyc_status dyc_set_apply(dyc_set *s, const uint32_t *d_offsets, const uint32_t *
     TRY(set_refresh_descs(s, st));
     TRY(set_ensure_scratch(s, n));
     *s->h_hostn = n;  // read by the copy at the start of phase A (the last call has synced)
+    s->cur = dyc_set::Batch{d_offsets, d_ops, d_keys, d_vals, d_vals_out, d_bits_out};
     dyc_set::Graph *gr = nullptr;
     if (flags & DYC_FLAG_GRAPH)
         gr = set_graph_for(s, {(uintptr_t)d_offsets, (uintptr_t)d_ops, (uintptr_t)d_keys,

@@ -477,12 +477,14 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
                                                        uint32_t *__restrict__ bits_out) {
     using K = typename SlotT<KB>::K;
     if (A.gate != nullptr && *A.gate == 0ull) return;  // no key repeats: one-pass path
-    if (n_ptr) n = set_op_count(A, n_ptr - A.ntables);  // n_ptr = offsets + ntables
+    const uint32_t *off = n_ptr ? n_ptr - A.ntables : nullptr;  // n_ptr = offsets + ntables
+    if (n_ptr) n = set_op_count(A, off);
     const int slots[2] = {kCtrUp, kCtrEr};
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
         const uint64_t i = i0 + threadIdx.x;
         bool up = false, er = false, hit = false;
+        bool one_up = false;  // an insert the one-pass kernel resolves (a table's upsert count)
         K k = 0;
         uint64_t value = 0ull;
         uint32_t tid = 0u;
@@ -492,7 +494,13 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
                              ? kNoId : *cell_word<KB>(A.cells, cell);
             if (d != kNoId) d = (d & kIdBit) ? (d & ~kIdBit) : kNoId - 1u;  // no bit: one op
             if (A.single_pass && (cell == kNoCell || d == kNoId - 1u)) {
-                // key 0 or a key with one op: resolved by the one-pass kernel
+                // key 0 or a key with one op: resolved by the one-pass kernel;
+                // a set's upsize policy counts the insert of a key with one op
+                // as an upsert of its table
+                if (A.tup && cell != kNoCell && ops[i] == kOpInsert) {
+                    one_up = true;
+                    tid = table_at(A.tidx, off, (uint32_t)i, (uint32_t)i);
+                }
             } else if (d >= A.cap_ops) {  // key 0 (no cell), or a cell compaction could not list
                 if (cell != kNoCell) note_bad(A);
                 if (vals_out) store_val(vals_out, vb, i, 0ull);
@@ -533,7 +541,7 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
         block_alloc<2, 32>(A.ctr, slots, (unsigned long long)up | ((unsigned long long)er << 32),
                            got);
         if (A.tup) {
-            warp_count_by(A.tup, tid, up);
+            warp_count_by(A.tup, tid, up || one_up);
             warp_count_by(A.ter, tid, er);
         }
         if ((up && got[0] >= A.cap_ops) || (er && got[1] >= A.cap_ops)) {

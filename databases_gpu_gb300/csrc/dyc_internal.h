@@ -315,6 +315,16 @@ template <int KB> struct Ops {
                                   uint64_t max_n, void *list_a, uint32_t *list_a_tid,
                                   uint64_t list_cap, Counters *gctr, unsigned long long *bad,
                                   const uint32_t *hold = nullptr, bool hint = false);
+    // the ops of a single_pass set batch whose key has no other op in it
+    // (and key-0 ops), one probe each (k_set_unique); max_n bounds the grid,
+    // the op count is read on the device; nothing when *hold is nonzero
+    static cudaError_t set_unique(const LaunchCtx &L, const ApplyScratch &A, const uint32_t *off,
+                                  const Desc *descs, uint32_t ntables, Counters *tctr, int sb,
+                                  const uint8_t *ops, const void *keys, const void *vals,
+                                  uint32_t vb, void *vals_out, uint32_t *bits_out,
+                                  uint64_t max_n, void *list_a, uint32_t *list_a_tid,
+                                  uint64_t list_cap, Counters *gctr, const uint32_t *hold,
+                                  bool hint);
     static cudaError_t set_walk(const LaunchCtx &L, const Desc *descs, uint32_t ntables,
                                 Counters *tctr, int sb, const void *src, const uint32_t *src_tid,
                                 const unsigned long long *src_count, void *dst, uint32_t *dst_tid,

@@ -355,6 +355,23 @@ cudaError_t Ops<KB>::set_mutate(const LaunchCtx &L, const Desc *descs, uint32_t 
 }
 
 template <int KB>
+cudaError_t Ops<KB>::set_unique(const LaunchCtx &L, const ApplyScratch &A, const uint32_t *off,
+                                const Desc *descs, uint32_t ntables, Counters *tctr, int sb,
+                                const uint8_t *ops, const void *keys, const void *vals,
+                                uint32_t vb, void *vals_out, uint32_t *bits_out, uint64_t max_n,
+                                void *list_a, uint32_t *list_a_tid, uint64_t list_cap,
+                                Counters *gctr, const uint32_t *hold, bool hint) {
+    if (max_n == 0) return cudaSuccess;
+    DYC_SB_DISPATCH(sb, {
+        auto k = hint ? k_set_unique<KB, SB, true> : k_set_unique<KB, SB, false>;
+        k<<<tile_grid(L, max_n), 256, 0, L.stream>>>(A, off, descs, ntables, tctr, ops, keys,
+                                                      vals, vb, vals_out, bits_out, list_a,
+                                                      list_a_tid, list_cap, gctr, hold);
+    });
+    return cudaGetLastError();
+}
+
+template <int KB>
 cudaError_t Ops<KB>::set_walk(const LaunchCtx &L, const Desc *descs, uint32_t ntables,
                               Counters *tctr, int sb, const void *src, const uint32_t *src_tid,
                               const unsigned long long *src_count, void *dst, uint32_t *dst_tid,

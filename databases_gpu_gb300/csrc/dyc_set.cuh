@@ -270,6 +270,141 @@ __global__ void __launch_bounds__(256) k_set_mutate(
     }
 }
 
+// The ops of a set batch whose key has no other op in it (and key-0 ops),
+// after the device policy's upsizes and before the mutation of the repeated
+// keys (ApplyScratch::single_pass): each resolved in one probe of its
+// table's buckets, as k_apply_unique does for one table. The result is the
+// key's state before the batch; an insert updates in place or claims an
+// empty slot, else goes to list_a with its table; an erase of a present key
+// clears its slot. Hit bits are ORed in (the scatter and the replays wrote
+// the repeated keys' bits). The other phase-B kernels touch only repeated
+// keys, so no key is probed by two kernels at once.
+template <int KB, int SB, bool HINT>
+__global__ void __launch_bounds__(256) k_set_unique(
+    const __grid_constant__ ApplyScratch A, const uint32_t *__restrict__ off,
+    const Desc *__restrict__ descs, uint32_t ntables, Counters *__restrict__ tctr,
+    const uint8_t *__restrict__ ops, const void *__restrict__ keys, const void *__restrict__ vals,
+    uint32_t vb, void *__restrict__ vals_out, uint32_t *__restrict__ bits_out, void *list_a,
+    uint32_t *list_a_tid, uint64_t list_cap, Counters *gctr, const uint32_t *hold) {
+    using T = SlotT<KB>;
+    using Sl = typename T::S;
+    using Gm = Geo<KB, SB>;
+    if (hold != nullptr && *hold != 0u) return;  // the host applies the rest of the policy first
+    __shared__ __align__(128) unsigned char s_stage[kWarpsPerBlock][32 * SB];
+    unsigned char *stage = s_stage[threadIdx.x >> 5];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t n = set_op_count(A, off);
+    const uint64_t step = warp_stride();
+    uint32_t n_ins = 0, n_upd = 0, n_del = 0;
+    for (uint64_t base = warp_base(); base < n; base += step) {
+        const uint64_t i = base + lane;
+        bool mine = i < n;
+        uint32_t tb = 0u;
+        if (mine) {
+            const uint32_t c = A.op_cell[i];
+            if (c != kNoCell && c >= A.cap_cells) {
+                note_bad(A);
+                mine = false;
+            } else if (c != kNoCell) {
+                mine = (*cell_word<KB>(A.cells, c) & kIdBit) == 0u;
+            }
+        }
+        typename T::K k = 0;
+        uint8_t op = kOpFind;
+        Sl e = T::empty();
+        if (mine) {
+            tb = table_at(A.tidx, off, (uint32_t)i, (uint32_t)i);
+            if (tb >= ntables) {
+                note_bad(A);
+                mine = false;
+                tb = 0u;
+            } else {
+                k = load_key<KB>(keys, i);
+                op = ops[i];
+            }
+        }
+        const Desc &D = descs[tb];
+        const unsigned long long tpol = HINT ? l2_policies(D.l2_keep != 0u).table : 0ull;
+        const bool act = mine && k != 0;  // ops on key 0 miss and change nothing
+        const bool ins = act && op == kOpInsert, del = act && op == kOpErase;
+        if (ins) e = T::make(k, load_val(vals, vb, i));
+        const uint32_t hk = fold(k);
+        const Pair p = pair_of(hk, D.d);
+        char *p1 = bucket_ptr<KB, SB>(D, p.first, bucket_index(D, p.first, hk));
+        char *p2 = bucket_ptr<KB, SB>(D, p.second, bucket_index(D, p.second, hk));
+        const KvOut r1 = place_probe<KB, SB, HINT>(p1, k, act, p.first, D.d, stage, tpol);
+        const bool found1 = act && r1.match >= 0;
+        const bool check2 =
+            act && !found1 && ((!Gm::kMeta || r1.overflow) || (ins && r1.empty == 0u));
+        KvOut r2{-1, 0ull, false, 0u};
+        if (__any_sync(kFull, check2))
+            r2 = place_probe<KB, SB, HINT>(p2, k, check2, p.second, D.d, stage, tpol);
+        const bool found2 = check2 && r2.match >= 0;
+        const bool present = found1 || found2;
+        const uint64_t before = found1 ? r1.value : (found2 ? r2.value : 0ull);
+        bool pend = false, placed = false, gone = false;
+        if (ins) {
+            if (found1) {
+                T::store(slot_ptr<KB, SB>(p1, r1.match), e);
+                ++n_upd;
+            } else if (found2) {
+                T::store(slot_ptr<KB, SB>(p2, r2.match), e);
+                ++n_upd;
+            } else {
+                bool ok = claim_empty<KB, SB>(p1, r1.empty, e);
+                if (!ok && check2 && r2.empty) {
+                    mark_overflow<KB, SB>(p1, hk);
+                    ok = claim_empty<KB, SB>(p2, r2.empty, e);
+                }
+                if (ok) {
+                    ++n_ins;
+                    placed = true;
+                } else {
+                    pend = true;
+                }
+            }
+        } else if (del && present) {
+            T::store(found1 ? slot_ptr<KB, SB>(p1, r1.match) : slot_ptr<KB, SB>(p2, r2.match),
+                     T::empty());
+            ++n_del;
+            gone = true;
+        }
+        if (vals_out != nullptr && mine) store_val(vals_out, vb, i, before);
+        const unsigned m = __ballot_sync(kFull, present);
+        if (bits_out != nullptr && lane == 0 && m) atomicOr(&bits_out[base >> 5], m);
+        __syncwarp();
+        warp_size_add(tctr, tb, placed, 1);
+        warp_size_add(tctr, tb, gone, -1);
+        const unsigned long long at = agg_inc(&gctr->pending, pend);
+        if (pend) {
+            if (at < list_cap) {
+                ((Sl *)list_a)[at] = e;
+                if (list_a_tid) list_a_tid[at] = tb;
+            } else {
+                atomicAdd(&gctr->spill, 1ull);
+            }
+        }
+    }
+    // one atomic per counter per block
+    __shared__ unsigned long long s_sum[3];
+    if (threadIdx.x < 3) s_sum[threadIdx.x] = 0ull;
+    __syncthreads();
+    n_del = __reduce_add_sync(kFull, n_del);
+    n_ins = __reduce_add_sync(kFull, n_ins);
+    n_upd = __reduce_add_sync(kFull, n_upd);
+    if (lane == 0) {
+        if (n_del) atomicAdd(&s_sum[0], (unsigned long long)n_del);
+        if (n_ins) atomicAdd(&s_sum[1], (unsigned long long)n_ins);
+        if (n_upd) atomicAdd(&s_sum[2], (unsigned long long)n_upd);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_sum[0]) atomicAdd(&gctr->erased, s_sum[0]);
+        if (s_sum[1]) atomicAdd(&gctr->inserted, s_sum[1]);
+        if (s_sum[2]) atomicAdd(&gctr->updated, s_sum[2]);
+    }
+}
+
 // eviction walks of src entries (k_walk per table, each with its own
 // eviction bound; max_evict, the largest, bounds the cooperative loop);
 // failures go to dst
