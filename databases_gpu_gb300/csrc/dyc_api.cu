@@ -1287,7 +1287,7 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     if (e == cudaSuccess) e = KB_CALL(t, apply_replay, L, Ag, ops, vals, vb, vals_out, bits_out, n, n);
     if (e == cudaSuccess && deferred)
         e = KB_CALL(t, apply_unique, L, t->D, t->sb, t->S, ops, keys, vals, vb, vals_out, bits_out,
-                    n, t->d_ctr, A.op_cell, A.cells);
+                    n, t->d_ctr, A.op_cell, A.cells, Ag.gate);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "apply kernels: %s", cudaGetErrorString(e));
     if (!deferred) {
         TRY(read_apply_counters(t, s));

@@ -889,10 +889,14 @@ __global__ void __launch_bounds__(256) k_apply_unique(
     const uint8_t *__restrict__ ops, const void *__restrict__ keys,
     const void *__restrict__ vals, uint32_t vb, void *__restrict__ vals_out,
     uint32_t *__restrict__ bits_out, uint64_t n, Counters *ctr, const uint32_t *op_cell,
-    const void *cells) {
+    const void *cells, const unsigned long long *gate) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
     using Gm = Geo<KB, SB>;
+    // no key repeated in the chunk (the grouping's flag): every op is ours,
+    // and the cell words need not be read
+    if (cells != nullptr && gate != nullptr && *gate == 0ull) cells = nullptr;
+    const bool all_ops = cells == nullptr;
     __shared__ __align__(128) unsigned char s_stage[SB >= 64 ? kWarpsPerBlock : 1][32 * SB];
     unsigned char *stage = s_stage[SB >= 64 ? (threadIdx.x >> 5) : 0];
     const uint32_t lane = threadIdx.x & 31;
@@ -958,7 +962,7 @@ __global__ void __launch_bounds__(256) k_apply_unique(
         if (vals_out != nullptr && mine) store_val(vals_out, vb, i, before);
         const unsigned m = __ballot_sync(kFull, present);
         if (bits_out != nullptr && lane == 0) {
-            if (cells == nullptr) bits_out[base >> 5] = m;
+            if (all_ops) bits_out[base >> 5] = m;
             else if (m) atomicOr(&bits_out[base >> 5], m);  // the replays own the other bits
         }
         __syncwarp();

@@ -278,7 +278,8 @@ template <int KB> struct Ops {
                                     const uint8_t *ops, const void *keys, const void *vals,
                                     uint32_t vb, void *vals_out, uint32_t *bits_out, uint64_t n,
                                     Counters *ctr, const uint32_t *op_cell = nullptr,
-                                    const void *cells = nullptr);
+                                    const void *cells = nullptr,
+                                    const unsigned long long *gate = nullptr);
     // *count += the INSERT ops among ops[0..n)
     static cudaError_t count_inserts(const LaunchCtx &L, const uint8_t *ops, uint64_t n,
                                      unsigned long long *count);
