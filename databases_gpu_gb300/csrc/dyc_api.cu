@@ -1145,7 +1145,8 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
         multi ? (size_t)ntables * 4 : 0,              // tup
         multi ? (size_t)ntables * 4 : 0,              // ter
         multi ? ((size_t)ntables + 1) * 4 : 0,        // tcell_off
-        multi ? (ops / dyc::kTidxStep + 1) * 4 : 0};  // tidx
+        multi ? (ops / dyc::kTidxStep + 1) * 4 : 0,   // tidx
+        (ops / 32 + 1) * 4};                          // single
     size_t need = 0;
     for (size_t b : sizes) need += (b + 255) & ~(size_t)255;
     if (*buf && *buf_bytes < need) {
@@ -1188,6 +1189,7 @@ dyc_status carve_apply(int kb, int vb, uint64_t ops, uint64_t cells, uint32_t nt
     A.ter = (uint32_t *)carve();
     A.tcell_off = (uint32_t *)carve();
     A.tidx = (uint32_t *)carve();
+    A.single = (uint32_t *)carve();
     A.ntables = ntables;
     A.cap_cells = cells;
     A.cap_ops = ops;
@@ -1287,7 +1289,7 @@ dyc_status apply_chunk(dyc_table *t, const uint8_t *ops, const void *keys, const
     if (e == cudaSuccess) e = KB_CALL(t, apply_replay, L, Ag, ops, vals, vb, vals_out, bits_out, n, n);
     if (e == cudaSuccess && deferred)
         e = KB_CALL(t, apply_unique, L, t->D, t->sb, t->S, ops, keys, vals, vb, vals_out, bits_out,
-                    n, t->d_ctr, A.op_cell, A.cells, Ag.gate);
+                    n, t->d_ctr, A.single, Ag.gate);
     if (e != cudaSuccess) return fail(DYC_ECUDA, "apply kernels: %s", cudaGetErrorString(e));
     if (!deferred) {
         TRY(read_apply_counters(t, s));

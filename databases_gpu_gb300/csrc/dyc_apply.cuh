@@ -485,6 +485,7 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
         const uint64_t i = i0 + threadIdx.x;
         bool up = false, er = false, hit = false;
         bool one_up = false;  // an insert the one-pass kernel resolves (a table's upsert count)
+        bool left = false;    // op i is left to the one-pass kernel
         K k = 0;
         uint64_t value = 0ull;
         uint32_t tid = 0u;
@@ -494,6 +495,7 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
                              ? kNoId : *cell_word<KB>(A.cells, cell);
             if (d != kNoId) d = (d & kIdBit) ? (d & ~kIdBit) : kNoId - 1u;  // no bit: one op
             if (A.single_pass && (cell == kNoCell || d == kNoId - 1u)) {
+                left = true;
                 // key 0 or a key with one op: resolved by the one-pass kernel;
                 // a set's upsize policy counts the insert of a key with one op
                 // as an upsert of its table
@@ -537,6 +539,8 @@ __global__ void __launch_bounds__(256) k_apply_scatter(const __grid_constant__ A
         // i0 is a multiple of 256: a warp's 32 ops are one word of bits
         const unsigned hits = __ballot_sync(kFull, hit);
         if (bits_out && (threadIdx.x & 31) == 0 && i < n) bits_out[i >> 5] = hits;
+        const unsigned lefts = __ballot_sync(kFull, left);
+        if (A.single_pass && (threadIdx.x & 31) == 0 && i < n) A.single[i >> 5] = lefts;
         uint32_t got[2];
         block_alloc<2, 32>(A.ctr, slots, (unsigned long long)up | ((unsigned long long)er << 32),
                            got);
@@ -888,15 +892,15 @@ __global__ void __launch_bounds__(256) k_apply_unique(
     const __grid_constant__ Desc D, const __grid_constant__ Scratch S,
     const uint8_t *__restrict__ ops, const void *__restrict__ keys,
     const void *__restrict__ vals, uint32_t vb, void *__restrict__ vals_out,
-    uint32_t *__restrict__ bits_out, uint64_t n, Counters *ctr, const uint32_t *op_cell,
-    const void *cells, const unsigned long long *gate) {
+    uint32_t *__restrict__ bits_out, uint64_t n, Counters *ctr, const uint32_t *single,
+    const unsigned long long *gate) {
     using T = SlotT<KB>;
     using Sl = typename T::S;
     using Gm = Geo<KB, SB>;
-    // no key repeated in the chunk (the grouping's flag): every op is ours,
-    // and the cell words need not be read
-    if (cells != nullptr && gate != nullptr && *gate == 0ull) cells = nullptr;
-    const bool all_ops = cells == nullptr;
+    // no key repeated in the chunk (the grouping's flag): every op is ours
+    // (the scatter did not run, so the bitmap is not written)
+    if (single != nullptr && gate != nullptr && *gate == 0ull) single = nullptr;
+    const bool all_ops = single == nullptr;
     __shared__ __align__(128) unsigned char s_stage[SB >= 64 ? kWarpsPerBlock : 1][32 * SB];
     unsigned char *stage = s_stage[SB >= 64 ? (threadIdx.x >> 5) : 0];
     const uint32_t lane = threadIdx.x & 31;
@@ -909,10 +913,7 @@ __global__ void __launch_bounds__(256) k_apply_unique(
         uint8_t op = kOpFind;
         Sl e = T::empty();
         bool mine = i < n;  // this kernel resolves op i
-        if (mine && cells != nullptr) {  // after a grouping: keys with one op, and key 0
-            const uint32_t c = op_cell[i];
-            mine = c == kNoCell || (*cell_word<KB>(const_cast<void *>(cells), c) & kIdBit) == 0u;
-        }
+        if (mine && !all_ops) mine = (single[i >> 5] >> (i & 31)) & 1u;  // one op, or key 0
         if (mine) {
             k = load_key<KB>(keys, i);
             op = ops[i];

@@ -125,6 +125,9 @@ struct ApplyScratch {
     // so the find of the distinct keys, the scatter, the replays and the
     // mutation see those alone.
     uint32_t single_pass;
+    // single_pass batches: bit i set when op i is left to the one-pass
+    // kernel (written by the scatter, one word per warp, cap_ops / 32 + 1)
+    uint32_t *single;
 };
 
 // Cell words after compaction: kIdBit | distinct id. A word without the bit
@@ -271,14 +274,14 @@ template <int KB> struct Ops {
     static cudaError_t apply_group(const LaunchCtx &L, const ApplyScratch &A, const void *keys,
                                   uint64_t n);
     // a mixed batch whose keys are all distinct, in one probe pass (ops left
-    // without a slot go to S.list_a, counted in ctr->pending). With cells
-    // (a single_pass batch after its grouping), only the ops whose key has
-    // no other op in the batch, and key-0 ops; their hit bits are ORed in.
+    // without a slot go to S.list_a, counted in ctr->pending). With a single
+    // bitmap (a single_pass batch after its grouping and scatter), only the
+    // ops whose bit is set, and their hit bits are ORed in; all ops when
+    // *gate is 0 (no key repeated, so the scatter did not run).
     static cudaError_t apply_unique(const LaunchCtx &L, const Desc &D, int sb, const Scratch &S,
                                     const uint8_t *ops, const void *keys, const void *vals,
                                     uint32_t vb, void *vals_out, uint32_t *bits_out, uint64_t n,
-                                    Counters *ctr, const uint32_t *op_cell = nullptr,
-                                    const void *cells = nullptr,
+                                    Counters *ctr, const uint32_t *single = nullptr,
                                     const unsigned long long *gate = nullptr);
     // *count += the INSERT ops among ops[0..n)
     static cudaError_t count_inserts(const LaunchCtx &L, const uint8_t *ops, uint64_t n,

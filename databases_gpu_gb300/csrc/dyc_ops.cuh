@@ -156,13 +156,13 @@ template <int KB>
 cudaError_t Ops<KB>::apply_unique(const LaunchCtx &L, const Desc &D, int sb, const Scratch &S,
                                   const uint8_t *ops, const void *keys, const void *vals,
                                   uint32_t vb, void *vals_out, uint32_t *bits_out, uint64_t n,
-                                  Counters *ctr, const uint32_t *op_cell, const void *cells,
+                                  Counters *ctr, const uint32_t *single,
                                   const unsigned long long *gate) {
     if (n == 0) return cudaSuccess;
     DYC_SB_DISPATCH(sb, {
         auto k = D.l2_keep ? k_apply_unique<KB, SB, true> : k_apply_unique<KB, SB, false>;
         k<<<tile_grid(L, n), 256, 0, L.stream>>>(D, S, ops, keys, vals, vb, vals_out, bits_out, n,
-                                                  ctr, op_cell, cells, gate);
+                                                  ctr, single, gate);
     });
     return cudaGetLastError();
 }

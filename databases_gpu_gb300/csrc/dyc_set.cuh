@@ -298,17 +298,8 @@ __global__ void __launch_bounds__(256) k_set_unique(
     uint32_t n_ins = 0, n_upd = 0, n_del = 0;
     for (uint64_t base = warp_base(); base < n; base += step) {
         const uint64_t i = base + lane;
-        bool mine = i < n;
+        bool mine = i < n && ((A.single[i >> 5] >> (i & 31)) & 1u);  // the scatter's bitmap
         uint32_t tb = 0u;
-        if (mine) {
-            const uint32_t c = A.op_cell[i];
-            if (c != kNoCell && c >= A.cap_cells) {
-                note_bad(A);
-                mine = false;
-            } else if (c != kNoCell) {
-                mine = (*cell_word<KB>(A.cells, c) & kIdBit) == 0u;
-            }
-        }
         typename T::K k = 0;
         uint8_t op = kOpFind;
         Sl e = T::empty();

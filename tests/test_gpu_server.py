@@ -104,6 +104,11 @@ def test_server_results_same_alone_and_in_the_mix():
 
 def test_server_admission_rejects_what_can_never_fit():
     srv = _dg().DyCuckooServer([1024] * 4, max_step_ops=1 << 13)
+    # after one step: the set's first round allocates every member's upsize
+    # target (spare), which counts against the cap from then on
+    st, _, _, _ = srv.wait(srv.submit(0, np.zeros(1, np.uint8), np.ones(1, np.uint64),
+                                      np.zeros(1, np.uint32)))
+    assert st == 0
     base = srv.stats()["device_bytes"]
     srv.close()
     # room for the growth of about 1000 inserts (40 bytes each with headroom)
