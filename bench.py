@@ -385,7 +385,7 @@ def run_reference_per_table(w, rnd, torch):
 
 
 def run_small_table(args, dev, torch, dg):
-    """Config 1, the reference's own test scale: 2^20 unique u32 keys
+    """The reference's own test scale: 2^20 unique u32 keys
     (values 1..2^20, below 2^31) in a table sized for load factor 0.85
     (hashAPI(2^20 / 0.85)). The library and the reference's own kernels
     (cuckoo_insert / cuckoo_search / cuckoo_delete) on its own table run the
@@ -449,7 +449,8 @@ def run_small_table(args, dev, torch, dg):
             uins.append(timed(lambda: insert_unique(k2, v2)))
         return median(ins), fnd, median(ers), median(uins)
 
-    res = {"workload": "config 1: 2^20 unique u32 keys at load factor 0.85 (hashAPI(2^20/0.85)), "
+    res = {"workload": "the reference's test scale: 2^20 unique u32 keys at load factor 0.85 "
+                       "(hashAPI(2^20/0.85)), "
                        "insert of 2^19 keys into the half-full table, 2^20 finds (50 %% hits), "
                        "erase of 2^19 present keys, their re-insert; ~10 MB table; median of "
                        "%d cycles per step" % REPS}

@@ -67,7 +67,7 @@ typedef enum dyc_status {
     DYC_EOVERFLOW = 3, /* eviction overflow persisted after repeated upsizes */
     DYC_ETIMEOUT = 4,  /* a bounded device-side wait gave up */
     DYC_ECUDA = 5,     /* a CUDA runtime call failed */
-    DYC_ENOTSUP = 6    /* valid request this build does not support */
+    DYC_ENOTSUP = 6    /* valid request this library does not support */
 } dyc_status;
 
 typedef struct dyc_table dyc_table;

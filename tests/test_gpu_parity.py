@@ -26,7 +26,7 @@ def _bits_np(bits, n):
     return _dg().unpack_bits(bits, n)
 
 
-# ---------------------------------------------------------------- config 1
+# ------------------------------------- the reference test scale (2^20 keys)
 def test_config1_insert_find_erase_refind():
     """2^20 unique u32 keys at load factor 0.85, 2^20 finds (50% hits),
     2^19 erases, re-find; contents checked after every batch."""
