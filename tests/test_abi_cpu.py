@@ -97,6 +97,9 @@ def test_null_arguments_rejected():
     assert L.dyc_find(None, None, None, None, 1, None) == _lib.DYC_EINVAL
     assert L.dyc_erase(None, None, 1, None, None, 0, None) == _lib.DYC_EINVAL
     assert L.dyc_destroy(None) == _lib.DYC_OK
+    assert L.dyc_apply(None, None, None, None, 1, None, None, 0, None) == _lib.DYC_EINVAL
+    assert L.dyc_set_spare_cache(None, 0) == _lib.DYC_EINVAL
+    assert L.dyc_set_spare_bytes(None, None) == _lib.DYC_EINVAL
     assert L.dyc_status_string(_lib.DYC_EOVERFLOW) == b"eviction overflow"
 
 
