@@ -163,6 +163,55 @@ def test_set_u64_keys_and_growth():
     S.close()
 
 
+@pytest.mark.parametrize("key_bytes", [4, 8])
+def test_set_rounds_of_mostly_single_op_keys(key_bytes):
+    """Rounds in which most keys have one op (resolved by the one-pass
+    kernel in phase B) and some tables have repeats (through the per-key
+    passes), in the same round: per table, distinct keys for finds, upserts
+    and erases of present keys, inserts of new keys that fill buckets and
+    need eviction walks and upsizes, finds and erases of absent keys, and
+    key 0; every third table also repeats a few of its keys. Every op's
+    value and bit and every table's size equal its oracle's."""
+    import torch
+    rng = np.random.default_rng(71 + key_bytes)
+    nt = 64
+    sizes = np.round(2.0 ** (6 + 6 * rng.random(nt))).astype(np.int64)
+    S = _dg().DyCuckooSet(sizes, key_bytes=key_bytes, value_bytes=key_bytes)
+    maps = [O.Map() for _ in range(nt)]
+    npk, tdt = (np.uint32, np.int32) if key_bytes == 4 else (np.uint64, np.int64)
+    top = (1 << 31) if key_bytes == 4 else (1 << 62)
+    for r in range(4):
+        parts = []
+        for t in range(nt):
+            present = maps[t].export()[0].astype(npk)
+            m = int(rng.integers(0, 2 * sizes[t] + 2))
+            old = rng.choice(present, min(present.size, m // 3), replace=False) \
+                if present.size else np.zeros(0, npk)
+            new = np.unique(rng.integers(1, top, m - old.size, dtype=np.int64).astype(npk))
+            k = np.concatenate([old, new])
+            k = k[~np.isin(k, np.zeros(1, npk))]
+            if t % 3 == 0 and k.size:  # a few repeats in this table
+                k = np.concatenate([k, rng.choice(k, min(k.size, 5))])
+            if t % 5 == 0:
+                k = np.concatenate([k, np.zeros(1, npk)])  # key 0
+            parts.append(k[rng.permutation(k.size)])
+        off = np.zeros(nt + 1, np.uint32)
+        off[1:] = np.cumsum([p.size for p in parts])
+        keys = np.concatenate(parts).astype(npk)
+        n = keys.size
+        ops = rng.choice(np.array([0, 1, 2], np.uint8), size=n, p=[0.35, 0.45, 0.2])
+        vals = rng.integers(1, top, n, dtype=np.int64).astype(npk)
+        dk = torch.from_numpy(keys.view(tdt)).cuda()
+        dv = torch.from_numpy(vals.view(tdt)).cuda()
+        do = torch.from_numpy(ops).cuda()
+        doff = torch.from_numpy(off.view(np.int32)).cuda()
+        out, bits = S.apply(doff, do, dk, dv, h_offsets=off, graph=(r % 2 == 1))
+        _check_round(S, maps, off, do, dk, dv, out, bits, "single-op round %d" % r)
+    for t in range(nt):
+        assert_same_contents(S.table(t), maps[t], "table %d after the rounds" % t)
+    S.close()
+
+
 def test_tuner_picks_a_measured_candidate():
     from databases_gpu_gb300 import tune
     space = {"bucket_bytes": (64, 128), "num_subtables": (2, 4), "max_evictions": (16, 64)}
